@@ -1,0 +1,415 @@
+"""Benchmark: mode-0 MTTKRP over the skewed 100M-nonzero 3-mode CSF tensor, rank 32.
+
+Workload (the configuration the headline metric is quoted on): dims 200,000 x
+100,000 x 2,000,000, 100M nonzeros, fiber lengths round(lognormal(1.5, 1.8))
+clipped to [1, 2M] with 3 fibers forced above 1M nonzeros, values U(0,1), factors
+N(0,1) with per-column scales, rank 32.  Seeded synthetic data (seed 3); the
+reference's FROSTT tensors are not available.
+
+One step = one MTTKRP call on device-resident inputs: partition + output clear
++ walk kernel.  L2 is flushed (512 MB write) between timed steps, outside the
+per-step CUDA events.  ``value`` is GFLOP/s with the reference's flop count
+(3 * nnz * R); ``e2e`` is the same metric through the one-shot host API
+(tt_mttkrp_host: host buffers in, host result out, every copy inside the timed
+region).  ``roofline`` relates the walk kernel's compulsory HBM bytes to its
+CUDA-event duration and the measured copy bandwidth.
+
+``--impl reference`` times the reference's CPU TACO MTTKRP3 algorithm
+(tensor_kernels/mttkrp3_csf_cpu_taco.h, as restated in oracle/tt_oracle.c)
+on the host cores, on a bounded row sample of the same tensor.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DIMS = (200_000, 100_000, 2_000_000)
+NNZ = 100_000_000
+RANK = 32
+SEED = 3
+WORKLOAD = "mttkrp3_skewed_100M_r32"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--prec", default="bf16", choices=["fp32", "bf16", "bf16f"])
+    ap.add_argument("--select", default="model", choices=["default", "model", "sweep"])
+    ap.add_argument("--nnz", type=int, default=NNZ, help="smaller nonzero count for quick checks")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        return rank, world, dist
+    return rank, world, None
+
+
+def barrier(d):
+    if d is not None:
+        d.barrier()
+
+
+def allmax(d, v: float) -> float:
+    if d is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64)
+    d.all_reduce(t, op=d.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_workload(nnz):
+    import tentaco_gb300 as tt
+
+    B = tt.gen_lognormal_fibers(DIMS, nnz, 1.5, 1.8, 3, 1_000_000, SEED)
+    C = tt.gen_dense(DIMS[1], RANK, 1, SEED * 10 + 1)
+    D = tt.gen_dense(DIMS[2], RANK, 1, SEED * 10 + 2)
+    return B, C, D
+
+
+def compulsory_bytes(B, s_v, s_f):
+    """Compulsory HBM bytes of one MTTKRP3 call (index int32, values s_v, factors s_f bytes)."""
+    nnz = B.nnz
+    F = B.count(1)
+    I = B.dims[0]
+    U1 = int(np.count_nonzero(np.bincount(B.crd(1), minlength=B.dims[1])))
+    U2 = int(np.count_nonzero(np.bincount(B.crd(2), minlength=B.dims[2])))
+    return nnz * (4 + s_v) + F * 8 + (I + 1) * 4 + (U1 + U2) * RANK * s_f + I * RANK * 4, U1, U2
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.fh.close()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        try:
+            rows = [l.split(",") for l in open(self.path) if l.strip()]
+        except Exception:
+            return out
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if sm:
+            out["sm_mhz"] = statistics.median(sm)
+            out["sm_max_mhz"] = max(mx)
+            out["samples"] = len(sm)
+        out["reasons"] = sorted(reasons)
+        return out
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(prec):
+    """Per-launch DRAM bytes of the walk kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"walk_kernel_{WORKLOAD}_{prec}.json")
+    try:
+        with open(path) as fh:
+            return json.load(fh).get("dram_bytes_per_launch")
+    except Exception:
+        return None
+
+
+def sample_errors(B, C, D, A, rows):
+    from oracle import oracle as O
+
+    Oc = O.Csf(3, B.dims, [None, B.pos(1).astype(np.int64), B.pos(2).astype(np.int64)],
+               [None, B.crd(1).astype(np.int64), B.crd(2).astype(np.int64)], B.vals.astype(np.float64))
+    ref = O.mttkrp(Oc, [C, D], rows=rows)
+    got = A[rows].astype(np.float64)
+    amax = float(np.abs(ref).max())
+    rn = np.linalg.norm(ref, axis=1)
+    m = rn > 0
+    tau = 1e-6 * amax
+    e = np.abs(got - ref) / np.maximum(np.abs(ref), tau)
+    return {"rows_checked": int(len(rows)), "normwise_max": float(np.abs(got - ref).max() / amax),
+            "row_max": float((np.linalg.norm(got - ref, axis=1)[m] / rn[m]).max()),
+            "fro": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+            "elem_max": float(e.max()), "elem_mean": float(e.mean())}
+
+
+def check_rows(B, n=4096):
+    rng = np.random.default_rng(0)
+    pos1 = B.pos(1)
+    nz_rows = np.flatnonzero(np.diff(pos1))
+    sel = rng.choice(nz_rows, size=min(n, nz_rows.size), replace=False)
+    # include the rows holding the longest fibers (cross-block merges)
+    lens = np.diff(B.pos(2))
+    top = np.argsort(lens)[-8:]
+    rows_of_top = np.searchsorted(pos1, top, side="right") - 1
+    return np.unique(np.concatenate([sel, rows_of_top]))
+
+
+def run_gpu_arm(args, rank, world, d):
+    import tentaco_gb300 as tt
+
+    t0 = time.time()
+    B, C, D = make_workload(args.nnz)
+    gen_s = time.time() - t0
+    sel = {"default": tt.SELECT_DEFAULT, "model": tt.SELECT_MODEL, "sweep": tt.SELECT_SWEEP}[args.select]
+    flops = 3.0 * B.nnz * RANK
+
+    def timed_plan(prec, select):
+        plan = tt.Plan(B, rank=RANK, prec=prec, select=select)
+        if select == tt.SELECT_MODEL and plan.selected_by != 1:
+            plan = tt.Plan(B, rank=RANK, prec=prec, select=tt.SELECT_SWEEP)
+        bufs = [tt.DeviceBuffer.from_array(C), tt.DeviceBuffer.from_array(D)]
+        plan.set_factors(bufs)
+        A = tt.DeviceBuffer(B.dims[0] * RANK * 4)
+        plan.set_timing(True)
+        for _ in range(args.warmup):
+            tt.l2_flush()
+            plan.mttkrp(A)
+        tt.synchronize()
+        step_ms, kern_ms = [], []
+        barrier(d)
+        tt.synchronize()
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            tt.l2_flush()
+            plan.mttkrp(A)
+            step_ms.append(plan.last_ms())
+            kern_ms.append(plan.last_kernel_ms())
+        tt.synchronize()
+        barrier(d)
+        wall = time.perf_counter() - wall0
+        return plan, A, bufs, step_ms, kern_ms, wall
+
+    with Clocks(os.path.join(ROOT, "gpurun_out", "bench_clocks.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
+                else "/tmp/tt_bench_clocks.csv") as clk:
+        plan, A, bufs, step_ms, kern_ms, wall = timed_plan(args.prec, sel)
+    clocks = clk.summary()
+    ms = float(np.mean(step_ms))
+    ms_max = allmax(d, ms)
+    kern = float(np.mean(kern_ms))
+    value = world * flops / (ms_max * 1e-3) / 1e9
+
+    # plain FP32 kernel on the same tensor, for the BF16-vs-FP32 ratio
+    fp32_info = None
+    if args.prec != "fp32":
+        p32, A32, b32, s32, k32, _ = timed_plan("fp32", tt.SELECT_SWEEP)
+        fp32_info = {"ms_per_step": float(np.mean(s32)), "kernel_ms": float(np.mean(k32)),
+                     "gflops": flops / (np.mean(s32) * 1e-3) / 1e9, "variant": p32.variant}
+        Af32 = A32.to_array((B.dims[0], RANK))
+        del p32, A32, b32
+
+    s_v = 2 if args.prec == "bf16" else 4
+    s_f = 2 if args.prec in ("bf16", "bf16f") else 4
+    cbytes, U1, U2 = compulsory_bytes(B, s_v, s_f)
+    peak, peak_kind = peaks()
+    achieved = cbytes / (kern * 1e-3) / 1e9
+    traffic = ncu_traffic(args.prec)
+
+    out = {
+        "metric": f"MTTKRP3 GFLOP/s (3*nnz*R), {WORKLOAD}, {args.prec} storage, FP32 accumulate",
+        "value": round(value, 2), "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_max, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": args.prec if args.prec != "bf16f" else "bf16+fp32",
+        "data": "synthetic (seeded lognormal-fiber tensor; FROSTT data absent)",
+        "config": {"workload": WORKLOAD, "dims": list(DIMS), "nnz": B.nnz, "fibers": B.count(1), "rank": RANK,
+                   "precision": args.prec, "select": args.select, "variant": plan.variant,
+                   "selected_by": ["heuristic", "model", "sweep"][plan.selected_by],
+                   "l2": "flushed between steps (512 MB write)", "parallelism": f"replicas{world}",
+                   "gen_s": round(gen_s, 1)},
+        "gbs_compulsory": round(cbytes / (ms * 1e-3) / 1e9, 1),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "peak_source": f"{peak_kind} hbm_gbs", "kernel_ms": round(kern, 4),
+                     "compulsory_bytes": int(cbytes), "U1": U1, "U2": U2},
+        "clocks": clocks,
+        "gpu_launches": args.steps * 3,  # per step: partition, output clear (memset), walk kernel
+    }
+    if fp32_info:
+        out["fp32_plain"] = fp32_info
+        out["speedup_vs_fp32"] = round(fp32_info["ms_per_step"] / ms, 3)
+
+    Ah = A.to_array((B.dims[0], RANK))
+    rows = check_rows(B)
+    out["error_vs_fp64"] = sample_errors(B, C, D, Ah, rows)
+    if fp32_info:
+        out["fp32_plain"]["error_vs_fp64"] = sample_errors(B, C, D, Af32, rows)
+
+    if not args.no_e2e:
+        prec_map = {"fp32": 0, "bf16": 1, "bf16f": 2}
+        e2e_ms = []
+        for i in range(max(1, min(args.steps, 3)) + 1):
+            t = time.perf_counter()
+            Ahost = tt.mttkrp_host(B, [C, D], prec=prec_map[args.prec], select=tt.SELECT_FIXED,
+                                   variant=plan.variant)
+            if i > 0:
+                e2e_ms.append((time.perf_counter() - t) * 1e3)
+        h2d = B.nnz * 8 + (B.dims[0] + 1 + 2 * B.count(1) + 1) * 4 + (C.size + D.size) * 4
+        out["e2e"] = {"value": round(flops / (np.mean(e2e_ms) * 1e-3) / 1e9, 2), "unit": "GFLOP/s",
+                      "ms_per_step": round(float(np.mean(e2e_ms)), 2), "h2d_bytes_per_step": int(h2d),
+                      "d2h_bytes_per_step": int(Ahost.nbytes),
+                      "api": "tt_mttkrp_host (plan create + upload + factor conversion + run + download)"}
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(B, C, D, budget_s=15.0)
+    return out
+
+
+def cpu_rows_sample(B, budget_nnz):
+    """A contiguous row range from the middle holding about budget_nnz nonzeros."""
+    pos1 = B.pos(1)
+    pos2 = B.pos(2)
+    row_nnz_end = pos2[pos1]
+    start = int(np.searchsorted(row_nnz_end, B.nnz // 3))
+    end = int(np.searchsorted(row_nnz_end, row_nnz_end[start] + budget_nnz))
+    end = max(min(end, B.dims[0]), start + 1)
+    return start, end, int(row_nnz_end[end] - row_nnz_end[start])
+
+
+def cpu_baseline(B, C, D, budget_s=15.0, steps=1):
+    """The reference CPU algorithm (oracle port of mttkrp3_csf_cpu_taco) on a bounded row range."""
+    from oracle import oracle as O
+
+    threads = O.max_threads()
+    pos1 = B.pos(1).astype(np.int64)
+    Cd, Dd = C.astype(np.float64), D.astype(np.float64)
+    # calibrate on a small range, then size the sample to the budget
+    s, e, nz = cpu_rows_sample(B, 2_000_000)
+    sub = _subtensor(B, pos1, s, e)
+    t = O.now_ms()
+    O.mttkrp(sub, [Cd, Dd])
+    per_nnz = (O.now_ms() - t) * 1e-3 / max(nz, 1)
+    target = int(min(B.nnz, max(nz, budget_s / max(per_nnz, 1e-12) / max(steps, 1))))
+    s, e, nz = cpu_rows_sample(B, target)
+    sub = _subtensor(B, pos1, s, e)
+    times = []
+    for _ in range(steps):
+        t = O.now_ms()
+        O.mttkrp(sub, [Cd, Dd])
+        times.append((O.now_ms() - t) * 1e-3)
+    sec = float(np.mean(times))
+    return {"value": round(3.0 * nz * RANK / sec / 1e9, 3), "unit": "GFLOP/s", "cores": threads,
+            "kind": "port", "seconds": round(sec, 2),
+            "sample": f"rows {s}..{e} ({nz} nonzeros, {100.0 * nz / B.nnz:.1f}% of the tensor), FP64, "
+                      f"reference loop order and OpenMP schedule"}
+
+
+def _subtensor(B, pos1, s, e):
+    from oracle import oracle as O
+
+    pos2 = B.pos(2).astype(np.int64)
+    f0, f1 = int(pos1[s]), int(pos1[e])
+    n0, n1 = int(pos2[f0]), int(pos2[f1])
+    p1 = pos1[s:e + 1] - f0
+    p2 = pos2[f0:f1 + 1] - n0
+    return O.Csf(3, (e - s, B.dims[1], B.dims[2]), [None, p1, p2],
+                 [None, B.crd(1)[f0:f1].astype(np.int64), B.crd(2)[n0:n1].astype(np.int64)],
+                 B.vals[n0:n1].astype(np.float64))
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return None
+    import tentaco_gb300 as tt  # generator only; the timed work is the CPU oracle port
+
+    from oracle import oracle as O
+
+    B, C, D = make_workload(args.nnz)
+    base = cpu_baseline(B, C, D, budget_s=8.0, steps=1)
+    # steps: repeat the same bounded sample
+    pos1 = B.pos(1).astype(np.int64)
+    s, e = [int(x) for x in base["sample"].split()[1].split("..")]
+    sub = _subtensor(B, pos1, s, e)
+    Cd, Dd = C.astype(np.float64), D.astype(np.float64)
+    nz = sub.nnz
+    for _ in range(args.warmup):
+        pass  # the reference CPU kernel has no warm-up state beyond the page cache
+    times = []
+    for _ in range(args.steps):
+        t = O.now_ms()
+        O.mttkrp(sub, [Cd, Dd])
+        times.append((O.now_ms() - t) * 1e-3)
+    sec = float(np.mean(times))
+    val = 3.0 * nz * RANK / sec / 1e9
+    return {"metric": f"MTTKRP3 GFLOP/s (3*nnz*R), {WORKLOAD}, fp32 storage, FP32 accumulate",
+            "impl": "reference", "value": round(val, 3), "unit": "GFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 2),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded lognormal-fiber tensor; FROSTT data absent)",
+            "config": {"workload": WORKLOAD, "dims": list(DIMS), "nnz": B.nnz, "rank": RANK},
+            "cpu_baseline": {"value": round(val, 3), "unit": "GFLOP/s", "cores": base["cores"], "kind": "port",
+                             "sample": base["sample"]},
+            "e2e": {"value": round(val, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    rank, world, d = dist_setup(args.gpus)
+    if args.impl == "reference":
+        out = run_reference_arm(args, rank, world)
+    else:
+        out = run_gpu_arm(args, rank, world, d)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if d is not None:
+        d.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

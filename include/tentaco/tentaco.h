@@ -1,0 +1,161 @@
+/*
+ * tentaco.h -- C ABI of libtentaco_gb300: sparse MTTKRP (3- and 4-mode, mode 0)
+ * and TTV over CSF tensors on one GB300 (sm_103a).
+ *
+ * Two layers:
+ *
+ *  1. Plan API (this header).  A plan uploads a CSF tensor once, owns its
+ *     device copy and scratch, picks a kernel variant (fixed heuristic,
+ *     learned selector, or exhaustive sweep) and runs on an explicit stream.
+ *     Every call returns a tt_status; tt_last_error_string() explains the
+ *     last failure on the calling thread.  Plans are independent objects
+ *     (no process-global device state) and may be used from different host
+ *     threads as long as one plan is not used by two threads at once.
+ *
+ *  2. Reference-named entry points (gpu_kernels.cuh in this directory):
+ *     mttkrp_gpu_taco, ttv_csf_gpu_taco, every mttkrp_<R>_eb_{pr,sr}_*
+ *     variant name, and get_gpu_timer_result().  They keep the reference's
+ *     signatures and host-buffer semantics (gpu_kernels.cuh:4-73 of
+ *     zhang677/tenTACO) and are built on the plan API.
+ *
+ * All pointers in this header are plain host or device pointers; streams are
+ * passed as void* (a cudaStream_t, or NULL for the legacy default stream).
+ * No CUDA or torch types appear in any signature.
+ */
+#ifndef TENTACO_TENTACO_H
+#define TENTACO_TENTACO_H
+
+#include <stdint.h>
+#include "taco_tensor_t.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TT_ABI_VERSION 1
+#define TT_MAX_ORDER 4
+#define TT_MAX_RANK 64
+
+typedef enum tt_status {
+  TT_OK = 0,
+  TT_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad rank/order, size mismatch   */
+  TT_ERR_INVALID_CSF = 2,      /* pos not monotone, crd out of range, empty inner fiber */
+  TT_ERR_UNSUPPORTED = 3,      /* order/rank/precision combination not built    */
+  TT_ERR_CUDA = 4,             /* a CUDA runtime call failed (message has it)   */
+  TT_ERR_OUT_OF_MEMORY = 5,    /* device allocation failed                      */
+  TT_ERR_NO_DEVICE = 6,        /* no CUDA device visible                        */
+  TT_ERR_DEVICE_WAIT = 7       /* a bounded device-side wait gave up            */
+} tt_status;
+
+typedef enum tt_op {
+  TT_OP_MTTKRP = 0, /* A(i,:) = sum B(i,k,l[,m]) C(k,:) .* D(l,:) [.* E(m,:)]      */
+  TT_OP_TTV = 1     /* y(fiber) = sum_l B(i,j,l) x(l), one output per (i,j) fiber */
+} tt_op;
+
+typedef enum tt_precision {
+  TT_PREC_FP32 = 0,        /* values and factors FP32, FP32 accumulation               */
+  TT_PREC_BF16 = 1,        /* values and factors stored BF16 with power-of-two
+                              per-column scales; FP32 accumulation, FP64 cross-block merge */
+  TT_PREC_BF16_FACTORS = 2 /* values FP32, factors BF16 (per-column scales)            */
+} tt_precision;
+
+typedef enum tt_select {
+  TT_SELECT_DEFAULT = 0, /* fixed heuristic from tensor shape and rank               */
+  TT_SELECT_MODEL = 1,   /* learned selector (MLP); heuristic if no model is loaded  */
+  TT_SELECT_SWEEP = 2,   /* time every variant on this tensor and keep the fastest   */
+  TT_SELECT_FIXED = 3    /* the variant id passed to tt_plan_create                  */
+} tt_select;
+
+/* One kernel variant of the MTTKRP walk family. */
+typedef struct tt_variant_info {
+  int32_t id;
+  int32_t threads;       /* threads per block                                  */
+  int32_t cols_per_lane; /* factor columns each lane accumulates               */
+  int32_t nnz_per_team;  /* nonzeros a team walks serially (EBSR-style "g")    */
+  int32_t rank_pad;      /* rank this variant is compiled for (8,16,32,64)     */
+  int32_t lanes_per_row; /* rank_pad / cols_per_lane                           */
+  int32_t nnz_per_block; /* threads / lanes_per_row * nnz_per_team             */
+  char name[40];
+} tt_variant_info;
+
+typedef struct tt_plan tt_plan;
+
+/* ---- plan lifecycle --------------------------------------------------- */
+
+/*
+ * Validate B (host CSF, see taco_tensor_t.h), upload it to the current device
+ * and choose a variant.  rank: factor columns (1..64) for MTTKRP; ignored for
+ * TTV.  variant is used only with TT_SELECT_FIXED.  stream may be NULL.
+ */
+tt_status tt_plan_create(const taco_tensor_t* B, tt_op op, int32_t rank, tt_precision prec,
+                         tt_select select, int32_t variant, void* stream, tt_plan** plan);
+tt_status tt_plan_destroy(tt_plan* plan);
+
+/*
+ * Give the plan its factor matrices: factors[m-1] is the mode-m factor,
+ * a DEVICE FP32 row-major array of dims[m] x rank, for m = 1..order-1.
+ * FP32 plans with rank in {8,16,32,64} keep the pointers (caller keeps them
+ * alive); other plans convert into plan-owned storage (BF16 + scales, or
+ * zero-padded FP32 rows).
+ */
+tt_status tt_plan_set_factors(tt_plan* plan, const float* const* factors, void* stream);
+
+/* MTTKRP with the factors last set: A is DEVICE FP32 dims[0] x rank, overwritten. */
+tt_status tt_plan_mttkrp(tt_plan* plan, float* A, void* stream);
+
+/* TTV: x DEVICE FP32 of length dims[order-1]; y DEVICE FP32, one entry per
+ * fiber of level order-2 (tt_plan_num_fibers), overwritten. */
+tt_status tt_plan_ttv(tt_plan* plan, const float* x, float* y, void* stream);
+
+/* Time every subsequent call's device work with CUDA events (default off). */
+tt_status tt_plan_set_timing(tt_plan* plan, int32_t enabled);
+/* Milliseconds of the last timed call (partition + clear + kernels); waits for it. */
+float tt_plan_last_ms(tt_plan* plan);
+
+int32_t tt_plan_variant(const tt_plan* plan);
+int64_t tt_plan_nnz(const tt_plan* plan);
+int64_t tt_plan_num_fibers(const tt_plan* plan, int32_t level);
+/* Device bytes the plan holds (CSF copy + factor storage + scratch). */
+int64_t tt_plan_device_bytes(const tt_plan* plan);
+
+/* ---- one-shot host calls (H2D, run, D2H inside) ------------------------ */
+
+/* A->vals (host, dims[0] x rank) = MTTKRP(B, factors[0..order-2]) (host dense). */
+tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
+                         const taco_tensor_t* const* factors, tt_precision prec,
+                         tt_select select, int32_t variant);
+/* y->vals (host) = TTV(B, x) over the last mode. */
+tt_status tt_ttv_host(taco_tensor_t* y, const taco_tensor_t* B, const taco_tensor_t* x);
+
+/* ---- variants ---------------------------------------------------------- */
+
+int32_t tt_num_variants(void);
+tt_status tt_variant_get(int32_t id, tt_variant_info* info);
+/* The variant the fixed heuristic picks for a shape (used by TT_SELECT_DEFAULT). */
+int32_t tt_variant_default(int32_t order, int32_t rank, tt_precision prec, int64_t nnz);
+
+/* ---- errors ------------------------------------------------------------ */
+
+const char* tt_last_error_string(void);
+const char* tt_status_string(tt_status s);
+int32_t tt_abi_version(void);
+
+/* ---- host CSF utilities ------------------------------------------------ */
+
+/*
+ * Build the canonical CSF (modes in order 0..order-1, lexicographic,
+ * duplicates summed, dense root with compressed-root arrays also filled in
+ * indices[0] for reference callers) from COO coordinates (nnz x order,
+ * row-major, int32) and FP32 values.  *out is library-owned: free it with
+ * tt_tensor_free.
+ */
+tt_status tt_csf_from_coo(int32_t order, const int32_t* dims, int64_t nnz,
+                          const int32_t* coords, const float* vals, taco_tensor_t** out);
+/* Check monotone pos, in-range crd, sorted distinct children, non-empty inner fibers. */
+tt_status tt_csf_validate(const taco_tensor_t* B);
+void tt_tensor_free(taco_tensor_t* t);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TENTACO_TENTACO_H */

@@ -1,0 +1,239 @@
+"""Test infrastructure only: numpy bindings of the CPU oracle.
+
+Two libraries sit behind this module:
+
+* ``_build/libtt_oracle.so`` -- the FP64 restatement in ``tt_oracle.c`` of the
+  reference's CPU TACO kernels (always built by ``make -C oracle``);
+* ``_ref/libtaco_ref.so`` -- the reference's own CPU kernels
+  (``tensor_kernels/*_cpu_taco.h``) compiled unmodified through ``shim/``; built
+  only where the reference sources exist.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
+import this module.  The product library never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_ORACLE_SO = os.path.join(HERE, "_build", "libtt_oracle.so")
+_REF_SO = os.path.join(HERE, "_ref", "libtaco_ref.so")
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int64
+
+
+def build(ref: bool = True) -> None:
+    """Compile the oracle (and, where the reference sources exist, _ref)."""
+    target = "all" if ref else "oracle"
+    subprocess.run(["make", "-s", "-C", HERE, target], check=True)
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(_P)
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_ORACLE_SO):
+            build(ref=False)
+        _lib = ctypes.CDLL(_ORACLE_SO)
+        _lib.oracle_compare_array.restype = ctypes.c_double
+        _lib.oracle_compare_array_my.restype = ctypes.c_double
+        _lib.oracle_build_csf.restype = ctypes.c_int64
+        _lib.oracle_now_ms.restype = ctypes.c_double
+        _lib.oracle_max_threads.restype = ctypes.c_int
+    return _lib
+
+
+def ref_lib():
+    """The reference's own kernels, or None where they could not be built."""
+    global _ref
+    if _ref is None:
+        if not os.path.exists(_REF_SO):
+            try:
+                build(ref=True)
+            except Exception:
+                return None
+        if not os.path.exists(_REF_SO):
+            return None
+        _ref = ctypes.CDLL(_REF_SO)
+        _ref.ref_last_kernel_ms.restype = ctypes.c_double
+        _ref.ref_flush_cache.restype = ctypes.c_double
+    return _ref
+
+
+@dataclass
+class Csf:
+    """A CSF tensor with a dense root, as int64 index arrays and float64 values.
+
+    ``pos[l]``/``crd[l]`` for levels l = 1..order-1 (index 0 unused);
+    ``pos[1]`` has dims[0]+1 entries.
+    """
+
+    order: int
+    dims: tuple
+    pos: list
+    crd: list
+    vals: np.ndarray
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def nnz(self) -> int:
+        return int(self.vals.shape[0])
+
+    def nfibers(self, level: int) -> int:
+        return int(self.crd[level].shape[0])
+
+
+def _c64(a):
+    return np.ascontiguousarray(a, dtype=np.int64)
+
+
+def _cf(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def build_csf(dims, coords: np.ndarray, vals: np.ndarray) -> Csf:
+    """Canonical CSF: lexicographic coordinate order, duplicates summed, dense root."""
+    coords = _c64(coords)
+    vals = _cf(vals)
+    nnz, order = coords.shape
+    pos = [None] * order
+    crd = [None] * order
+    pos[1] = np.zeros(int(dims[0]) + 1, dtype=np.int64)
+    for l in range(1, order):
+        crd[l] = np.zeros(max(nnz, 1), dtype=np.int64)
+        if l >= 2:
+            pos[l] = np.zeros(max(nnz, 1) + 1, dtype=np.int64)
+    out_vals = np.zeros(max(nnz, 1), dtype=np.float64)
+    counts = np.zeros(order, dtype=np.int64)
+    pos_ptrs = (_P * order)(*[None if p is None else p.ctypes.data for p in pos])
+    crd_ptrs = (_P * order)(*[None if c is None else c.ctypes.data for c in crd])
+    m = lib().oracle_build_csf(ctypes.c_int32(order), _I(int(dims[0])), _I(nnz), _ptr(coords),
+                               _ptr(vals), pos_ptrs, crd_ptrs, _ptr(out_vals), _ptr(counts))
+    for l in range(1, order):
+        crd[l] = crd[l][: counts[l]].copy()
+        if l >= 2:
+            pos[l] = pos[l][: counts[l - 1] + 1].copy()
+    return Csf(order, tuple(int(d) for d in dims), pos, crd, out_vals[:m].copy())
+
+
+def mttkrp(csf: Csf, factors: list, rows: np.ndarray | None = None) -> np.ndarray:
+    """Mode-0 MTTKRP in FP64; factors[m-1] is the mode-m factor (dims[m] x R)."""
+    fs = [_cf(f) for f in factors]
+    R = fs[0].shape[1]
+    L = lib()
+    p = [None] + [_c64(x) for x in csf.pos[1:]]
+    c = [None] + [_c64(x) for x in csf.crd[1:]]
+    v = _cf(csf.vals)
+    if rows is not None:
+        rows = _c64(rows)
+        out = np.zeros((rows.shape[0], R))
+        E = fs[2] if csf.order == 4 else None
+        L.oracle_mttkrp_rows(ctypes.c_int32(csf.order), _I(R), _I(rows.shape[0]), _ptr(rows),
+                             _ptr(p[1]), _ptr(c[1]), _ptr(p[2]), _ptr(c[2]),
+                             _ptr(p[3]) if csf.order == 4 else None,
+                             _ptr(c[3]) if csf.order == 4 else None,
+                             _ptr(v), _ptr(fs[0]), _ptr(fs[1]), _ptr(E), _ptr(out))
+        return out
+    A = np.zeros((csf.dims[0], R))
+    if csf.order == 3:
+        L.oracle_mttkrp3(_I(csf.dims[0]), _I(R), _ptr(p[1]), _ptr(c[1]), _ptr(p[2]), _ptr(c[2]),
+                         _ptr(v), _ptr(fs[0]), _ptr(fs[1]), _ptr(A))
+    elif csf.order == 4:
+        L.oracle_mttkrp4(_I(csf.dims[0]), _I(R), _ptr(p[1]), _ptr(c[1]), _ptr(p[2]), _ptr(c[2]),
+                         _ptr(p[3]), _ptr(c[3]), _ptr(v), _ptr(fs[0]), _ptr(fs[1]), _ptr(fs[2]),
+                         _ptr(A))
+    else:
+        raise ValueError("oracle MTTKRP supports order 3 and 4")
+    return A
+
+
+def mttkrp3_workspace(csf: Csf, C, D) -> np.ndarray:
+    C, D = _cf(C), _cf(D)
+    R = C.shape[1]
+    A = np.zeros((csf.dims[0], R))
+    p1, c1, p2, c2 = (_c64(x) for x in (csf.pos[1], csf.crd[1], csf.pos[2], csf.crd[2]))
+    lib().oracle_mttkrp3_workspace(_I(csf.dims[0]), _I(R), _ptr(p1), _ptr(c1), _ptr(p2), _ptr(c2),
+                                   _ptr(_cf(csf.vals)), _ptr(C), _ptr(D), _ptr(A))
+    return A
+
+
+def ttv(csf: Csf, c: np.ndarray) -> np.ndarray:
+    """TTV over the last mode of a 3-mode CSF: one output per level-1 fiber."""
+    c = _cf(c)
+    y = np.zeros(csf.nfibers(1))
+    p1, c1, p2, c2 = (_c64(x) for x in (csf.pos[1], csf.crd[1], csf.pos[2], csf.crd[2]))
+    lib().oracle_ttv(_I(csf.dims[0]), _ptr(p1), _ptr(c1), _ptr(p2), _ptr(c2),
+                     _ptr(_cf(csf.vals)), _ptr(c), _ptr(y))
+    return y
+
+
+def compare_array(x: np.ndarray, y: np.ndarray) -> float:
+    """Reference ds.h compare_array: max |y/x - 1| (inf if x == 0 != y)."""
+    x = np.ascontiguousarray(x, dtype=np.float32).ravel()
+    y = np.ascontiguousarray(y, dtype=np.float32).ravel()
+    return lib().oracle_compare_array(_ptr(x), _ptr(y), _I(x.size))
+
+
+def compare_array_my(x: np.ndarray, y: np.ndarray) -> float:
+    """Reference ds.h compare_array_my: count of |x-y| > 1e-3 (stops after 10)."""
+    x = np.ascontiguousarray(x, dtype=np.float32).ravel()
+    y = np.ascontiguousarray(y, dtype=np.float32).ravel()
+    return lib().oracle_compare_array_my(_ptr(x), _ptr(y), _I(x.size))
+
+
+def now_ms() -> float:
+    return lib().oracle_now_ms()
+
+
+def max_threads() -> int:
+    return lib().oracle_max_threads()
+
+
+# ---------------------------------------------------------------------------
+# The reference's own kernels (where available)
+# ---------------------------------------------------------------------------
+
+def ref_mttkrp(csf: Csf, factors: list, workspace: bool = False) -> np.ndarray:
+    r = ref_lib()
+    if r is None:
+        raise RuntimeError("reference kernels unavailable (sources absent)")
+    fs = [_cf(f) for f in factors]
+    R = fs[0].shape[1]
+    A = np.zeros((csf.dims[0], R))
+    p = [None] + [_c64(x) for x in csf.pos[1:]]
+    c = [None] + [_c64(x) for x in csf.crd[1:]]
+    v = _cf(csf.vals)
+    if csf.order == 3:
+        r.ref_mttkrp3(_I(csf.dims[0]), _I(csf.dims[1]), _I(csf.dims[2]), _I(R),
+                      _ptr(p[1]), _ptr(c[1]), _ptr(p[2]), _ptr(c[2]), _ptr(v),
+                      _ptr(fs[0]), _ptr(fs[1]), _ptr(A), ctypes.c_int(1 if workspace else 0))
+    else:
+        r.ref_mttkrp4(_I(csf.dims[0]), _I(csf.dims[1]), _I(csf.dims[2]), _I(csf.dims[3]), _I(R),
+                      _ptr(p[1]), _ptr(c[1]), _ptr(p[2]), _ptr(c[2]), _ptr(p[3]), _ptr(c[3]),
+                      _ptr(v), _ptr(fs[0]), _ptr(fs[1]), _ptr(fs[2]), _ptr(A))
+    return A
+
+
+def ref_ttv(csf: Csf, c: np.ndarray) -> np.ndarray:
+    r = ref_lib()
+    if r is None:
+        raise RuntimeError("reference kernels unavailable (sources absent)")
+    c = _cf(c)
+    y = np.zeros(csf.nfibers(1))
+    p1, c1, p2, c2 = (_c64(x) for x in (csf.pos[1], csf.crd[1], csf.pos[2], csf.crd[2]))
+    r.ref_ttv(_I(csf.dims[0]), _I(csf.dims[1]), _I(csf.dims[2]), _ptr(p1), _ptr(c1), _ptr(p2),
+              _ptr(c2), _ptr(_cf(csf.vals)), _ptr(c), _ptr(y))
+    return y

@@ -1,0 +1,431 @@
+"""tentaco_gb300 -- Python bindings of libtentaco_gb300 (sparse MTTKRP / TTV on GB300).
+
+The library is C/C++/CUDA; this module only wraps its C ABI
+(``include/tentaco/tentaco.h``, ``gpu_kernels.cuh``, ``tentaco_gen.h``) with
+ctypes and numpy.  It never computes anything itself: if the compiled library
+is missing, importing the binding raises instead of falling back to another
+implementation.  Build it with ``python -m tentaco_gb300.build``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libtentaco_gb300.so")
+
+TT_OK = 0
+TT_ERR_INVALID_ARGUMENT = 1
+TT_ERR_INVALID_CSF = 2
+TT_ERR_UNSUPPORTED = 3
+TT_ERR_CUDA = 4
+TT_ERR_OUT_OF_MEMORY = 5
+TT_ERR_NO_DEVICE = 6
+TT_ERR_DEVICE_WAIT = 7
+
+OP_MTTKRP, OP_TTV = 0, 1
+PREC_FP32, PREC_BF16, PREC_BF16_FACTORS = 0, 1, 2
+SELECT_DEFAULT, SELECT_MODEL, SELECT_SWEEP, SELECT_FIXED = 0, 1, 2, 3
+PRECISIONS = {"fp32": PREC_FP32, "bf16": PREC_BF16, "bf16f": PREC_BF16_FACTORS}
+
+
+class TacoTensor(C.Structure):
+    """Same layout as taco_tensor_t (taco_tensor_t.h:6-15 of the reference)."""
+
+    _fields_ = [
+        ("order", C.c_int32),
+        ("dimensions", C.POINTER(C.c_int32)),
+        ("csize", C.c_int32),
+        ("mode_ordering", C.POINTER(C.c_int32)),
+        ("mode_types", C.POINTER(C.c_int)),
+        ("indices", C.POINTER(C.POINTER(C.POINTER(C.c_int32)))),
+        ("vals", C.POINTER(C.c_float)),
+        ("vals_size", C.c_int32),
+    ]
+
+
+class VariantInfo(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("id", "threads", "cols_per_lane", "nnz_per_team", "rank_pad",
+                                         "lanes_per_row", "nnz_per_block")] + [("name", C.c_char * 40)]
+
+
+class TTError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(msg)
+        self.status = status
+
+
+_lib = None
+_P = C.c_void_p
+_TP = C.POINTER(TacoTensor)
+
+
+def lib():
+    """The loaded C library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is not built; run `python -m tentaco_gb300.build`")
+    L = C.CDLL(LIB_PATH)
+    S = C.c_int
+    sig = {
+        "tt_abi_version": (C.c_int32, []),
+        "tt_last_error_string": (C.c_char_p, []),
+        "tt_status_string": (C.c_char_p, [S]),
+        "tt_num_variants": (C.c_int32, []),
+        "tt_variant_get": (S, [C.c_int32, C.POINTER(VariantInfo)]),
+        "tt_variant_default": (C.c_int32, [C.c_int32, C.c_int32, S, C.c_int64]),
+        "tt_variant_valid": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, S]),
+        "tt_plan_create": (S, [_TP, S, C.c_int32, S, S, C.c_int32, _P, C.POINTER(_P)]),
+        "tt_plan_destroy": (S, [_P]),
+        "tt_plan_set_factors": (S, [_P, C.POINTER(_P), _P]),
+        "tt_plan_mttkrp": (S, [_P, _P, _P]),
+        "tt_plan_ttv": (S, [_P, _P, _P, _P]),
+        "tt_plan_set_timing": (S, [_P, C.c_int32]),
+        "tt_plan_last_ms": (C.c_float, [_P]),
+        "tt_plan_last_kernel_ms": (C.c_float, [_P]),
+        "tt_plan_variant": (C.c_int32, [_P]),
+        "tt_plan_selected_by": (C.c_int32, [_P]),
+        "tt_plan_nnz": (C.c_int64, [_P]),
+        "tt_plan_num_fibers": (C.c_int64, [_P, C.c_int32]),
+        "tt_plan_device_bytes": (C.c_int64, [_P]),
+        "tt_plan_nblocks": (C.c_int32, [_P]),
+        "tt_plan_use_variant": (S, [_P, C.c_int32]),
+        "tt_plan_sweep_times": (S, [_P, C.POINTER(C.c_float), C.c_int32]),
+        "tt_mttkrp_host": (S, [_TP, _TP, C.POINTER(_TP), S, S, C.c_int32]),
+        "tt_ttv_host": (S, [_TP, _TP, _TP]),
+        "tt_csf_from_coo": (S, [C.c_int32, C.POINTER(C.c_int32), C.c_int64, _P, _P, C.POINTER(_TP)]),
+        "tt_csf_validate": (S, [_TP]),
+        "tt_tensor_free": (None, [_TP]),
+        "tt_gen_zipf": (S, [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_int64, C.c_float,
+                            C.c_float, C.c_uint64, C.c_int32, C.POINTER(_TP)]),
+        "tt_gen_lognormal_fibers": (S, [C.POINTER(C.c_int32), C.c_int64, C.c_double, C.c_double, C.c_int64,
+                                        C.c_int64, C.c_uint64, C.POINTER(_TP)]),
+        "tt_gen_dense": (S, [C.c_int64, C.c_int64, C.c_int32, C.c_uint64, _P]),
+        "tt_csf_features": (S, [_TP, C.c_int32, C.POINTER(C.c_float)]),
+        "tt_device_malloc": (S, [C.c_int64, C.POINTER(_P)]),
+        "tt_device_free": (S, [_P]),
+        "tt_memcpy_htod": (S, [_P, _P, C.c_int64]),
+        "tt_memcpy_dtoh": (S, [_P, _P, C.c_int64]),
+        "tt_device_synchronize": (S, []),
+        "tt_device_count": (C.c_int32, []),
+        "tt_l2_flush": (S, [_P]),
+        "get_gpu_timer_result": (C.c_float, []),
+        "ttv_csf_gpu_taco": (None, [_TP, _TP, _TP]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def check(status: int) -> None:
+    if status != TT_OK:
+        raise TTError(status, lib().tt_last_error_string().decode())
+
+
+def legacy_entry(name: str):
+    """A reference-named entry point (e.g. 'mttkrp_32_eb_sr_512_4_1') from the library."""
+    f = getattr(lib(), name)
+    f.restype = None
+    f.argtypes = [_TP, _TP, _TP, _TP]
+    return f
+
+
+def legacy_names() -> list:
+    path = os.path.join(os.path.dirname(PKG), "include", "tentaco", "tt_legacy_names.def")
+    out = []
+    with open(path) as fh:
+        for line in fh:
+            if line.startswith("X("):
+                out.append(line[2:].split(",")[0].strip())
+    return out
+
+
+# ---------------------------------------------------------------------------
+# tensors
+# ---------------------------------------------------------------------------
+
+def _i32p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class Tensor:
+    """A CSF tensor owned by the library (from a generator or tt_csf_from_coo)."""
+
+    def __init__(self, ptr):
+        self.ptr = ptr
+        t = ptr.contents
+        self.order = int(t.order)
+        self.dims = tuple(int(t.dimensions[i]) for i in range(self.order))
+
+    def __del__(self):
+        if getattr(self, "ptr", None) and _lib is not None:
+            _lib.tt_tensor_free(self.ptr)
+            self.ptr = None
+
+    def count(self, level: int) -> int:
+        if level == 0:
+            return self.dims[0]
+        return int(self.pos(level)[-1])
+
+    @property
+    def nnz(self) -> int:
+        return self.count(self.order - 1)
+
+    def pos(self, level: int) -> np.ndarray:
+        n = (self.dims[0] if level == 1 else self.count(level - 1)) + 1
+        if level == 0:
+            n = 2
+        p = self.ptr.contents.indices[level][0]
+        return np.ctypeslib.as_array(p, shape=(n,))
+
+    def crd(self, level: int) -> np.ndarray:
+        n = self.dims[0] if level == 0 else self.count(level)
+        if n == 0:
+            return np.zeros(0, dtype=np.int32)
+        return np.ctypeslib.as_array(self.ptr.contents.indices[level][1], shape=(n,))
+
+    @property
+    def vals(self) -> np.ndarray:
+        n = self.nnz
+        if n == 0:
+            return np.zeros(0, dtype=np.float32)
+        return np.ctypeslib.as_array(self.ptr.contents.vals, shape=(n,))
+
+    def features(self, rank: int) -> np.ndarray:
+        f = np.zeros(12, dtype=np.float32)
+        check(lib().tt_csf_features(self.ptr, rank, f.ctypes.data_as(C.POINTER(C.c_float))))
+        return f
+
+
+def csf_from_coo(dims, coords: np.ndarray, vals: np.ndarray) -> Tensor:
+    coords = np.ascontiguousarray(coords, dtype=np.int32)
+    vals = np.ascontiguousarray(vals, dtype=np.float32)
+    d = np.ascontiguousarray(dims, dtype=np.int32)
+    out = _TP()
+    check(lib().tt_csf_from_coo(len(d), _i32p(d), coords.shape[0], coords.ctypes.data, vals.ctypes.data,
+                                C.byref(out)))
+    return Tensor(out)
+
+
+def gen_zipf(dims, zipf_s, nnz: int, seed: int, vlo=0.0, vhi=1.0, max_rounds=8) -> Tensor:
+    d = np.ascontiguousarray(dims, dtype=np.int32)
+    s = np.ascontiguousarray(zipf_s, dtype=np.float64)
+    out = _TP()
+    check(lib().tt_gen_zipf(len(d), _i32p(d), s.ctypes.data_as(C.POINTER(C.c_double)), nnz, vlo, vhi, seed,
+                            max_rounds, C.byref(out)))
+    return Tensor(out)
+
+
+def gen_lognormal_fibers(dims, nnz: int, mu: float, sigma: float, n_long: int, long_min: int,
+                         seed: int) -> Tensor:
+    d = np.ascontiguousarray(dims, dtype=np.int32)
+    out = _TP()
+    check(lib().tt_gen_lognormal_fibers(_i32p(d), nnz, mu, sigma, n_long, long_min, seed, C.byref(out)))
+    return Tensor(out)
+
+
+def gen_dense(rows: int, cols: int, dist: int, seed: int) -> np.ndarray:
+    out = np.empty((rows, cols), dtype=np.float32)
+    check(lib().tt_gen_dense(rows, cols, dist, seed, out.ctypes.data))
+    return out
+
+
+class HostTaco:
+    """A taco_tensor_t over numpy arrays (dense matrices/vectors or a CSF given as arrays)."""
+
+    def __init__(self, dims, vals=None, levels=None, dense_root=True, order=None):
+        self._keep = []
+        self.dims = np.ascontiguousarray(dims, dtype=np.int32)
+        self.t = TacoTensor()
+        self.t.order = int(order if order is not None else len(self.dims))
+        self.t.dimensions = _i32p(self.dims)
+        self._keep.append(self.dims)
+        self.t.csize = 4
+        if levels is not None:
+            n = len(levels)
+            arr = (C.POINTER(C.POINTER(C.c_int32)) * n)()
+            for l, lv in enumerate(levels):
+                pair = (C.POINTER(C.c_int32) * 2)()
+                if lv is not None:
+                    p, c = (np.ascontiguousarray(x, dtype=np.int32) for x in lv)
+                    self._keep += [p, c]
+                    pair[0] = _i32p(p)
+                    pair[1] = _i32p(c)
+                self._keep.append(pair)
+                arr[l] = C.cast(pair, C.POINTER(C.POINTER(C.c_int32)))
+            self._keep.append(arr)
+            self.t.indices = C.cast(arr, C.POINTER(C.POINTER(C.POINTER(C.c_int32))))
+            mt = np.array([0 if dense_root else 1] + [1] * (n - 1), dtype=np.int32)
+            self._keep.append(mt)
+            self.t.mode_types = mt.ctypes.data_as(C.POINTER(C.c_int))
+        if vals is not None:
+            self.vals = np.ascontiguousarray(vals, dtype=np.float32)
+            self._keep.append(self.vals)
+            self.t.vals = self.vals.ctypes.data_as(C.POINTER(C.c_float))
+            self.t.vals_size = int(self.vals.size)
+
+    @property
+    def ptr(self):
+        return C.pointer(self.t)
+
+
+def dense(mat: np.ndarray) -> HostTaco:
+    mat = np.ascontiguousarray(mat, dtype=np.float32)
+    dims = mat.shape if mat.ndim == 2 else (mat.shape[0],)
+    return HostTaco(dims, vals=mat)
+
+
+def _tensor_ptr(B):
+    return B.ptr
+
+
+def mttkrp_host(B, factors, prec="fp32", select=SELECT_DEFAULT, variant=0) -> np.ndarray:
+    """One-shot MTTKRP through tt_mttkrp_host: host in, host out."""
+    R = factors[0].shape[1]
+    A = np.zeros((B.dims[0], R), dtype=np.float32)
+    Ah = dense(A)
+    Fh = [dense(f) for f in factors]
+    arr = (_TP * len(Fh))(*[f.ptr for f in Fh])
+    check(lib().tt_mttkrp_host(Ah.ptr, _tensor_ptr(B), arr, PRECISIONS.get(prec, prec), select, variant))
+    return Ah.vals.reshape(A.shape)
+
+
+def ttv_host(B, x: np.ndarray, nfib: int) -> np.ndarray:
+    y = dense(np.zeros(nfib, dtype=np.float32))
+    xh = dense(np.ascontiguousarray(x, dtype=np.float32))
+    check(lib().tt_ttv_host(y.ptr, _tensor_ptr(B), xh.ptr))
+    return y.vals
+
+
+def gpu_timer_ms() -> float:
+    return float(lib().get_gpu_timer_result())
+
+
+# ---------------------------------------------------------------------------
+# device buffers and plans
+# ---------------------------------------------------------------------------
+
+class DeviceBuffer:
+    def __init__(self, nbytes: int):
+        self.nbytes = int(nbytes)
+        self.ptr = _P()
+        check(lib().tt_device_malloc(self.nbytes, C.byref(self.ptr)))
+
+    @classmethod
+    def from_array(cls, a: np.ndarray) -> "DeviceBuffer":
+        a = np.ascontiguousarray(a)
+        b = cls(a.nbytes)
+        check(lib().tt_memcpy_htod(b.ptr, a.ctypes.data, a.nbytes))
+        return b
+
+    def to_array(self, shape, dtype=np.float32) -> np.ndarray:
+        out = np.empty(shape, dtype=dtype)
+        check(lib().tt_memcpy_dtoh(out.ctypes.data, self.ptr, out.nbytes))
+        return out
+
+    def upload(self, a: np.ndarray) -> None:
+        a = np.ascontiguousarray(a)
+        check(lib().tt_memcpy_htod(self.ptr, a.ctypes.data, a.nbytes))
+
+    def __del__(self):
+        if getattr(self, "ptr", None) and self.ptr.value and _lib is not None:
+            _lib.tt_device_free(self.ptr)
+            self.ptr = _P()
+
+
+class Plan:
+    def __init__(self, B, op=OP_MTTKRP, rank=32, prec="fp32", select=SELECT_DEFAULT, variant=0, stream=None):
+        self.ptr = _P()
+        self.op = op
+        self.rank = rank
+        self.dims = B.dims
+        check(lib().tt_plan_create(_tensor_ptr(B), op, rank, PRECISIONS.get(prec, prec), select, variant,
+                                   stream, C.byref(self.ptr)))
+
+    def __del__(self):
+        if getattr(self, "ptr", None) and self.ptr.value and _lib is not None:
+            _lib.tt_plan_destroy(self.ptr)
+            self.ptr = _P()
+
+    def set_factors(self, bufs) -> None:
+        arr = (_P * len(bufs))(*[b.ptr.value for b in bufs])
+        check(lib().tt_plan_set_factors(self.ptr, arr, None))
+
+    def mttkrp(self, A: DeviceBuffer, stream=None) -> None:
+        check(lib().tt_plan_mttkrp(self.ptr, A.ptr, stream))
+
+    def ttv(self, x: DeviceBuffer, y: DeviceBuffer, stream=None) -> None:
+        check(lib().tt_plan_ttv(self.ptr, x.ptr, y.ptr, stream))
+
+    def set_timing(self, on: bool) -> None:
+        check(lib().tt_plan_set_timing(self.ptr, 1 if on else 0))
+
+    def last_ms(self) -> float:
+        return float(lib().tt_plan_last_ms(self.ptr))
+
+    def last_kernel_ms(self) -> float:
+        return float(lib().tt_plan_last_kernel_ms(self.ptr))
+
+    @property
+    def variant(self) -> int:
+        return int(lib().tt_plan_variant(self.ptr))
+
+    @property
+    def selected_by(self) -> int:
+        return int(lib().tt_plan_selected_by(self.ptr))
+
+    @property
+    def nblocks(self) -> int:
+        return int(lib().tt_plan_nblocks(self.ptr))
+
+    def num_fibers(self, level: int) -> int:
+        return int(lib().tt_plan_num_fibers(self.ptr, level))
+
+    def device_bytes(self) -> int:
+        return int(lib().tt_plan_device_bytes(self.ptr))
+
+    def use_variant(self, vid: int) -> None:
+        check(lib().tt_plan_use_variant(self.ptr, vid))
+
+    def sweep_times(self) -> np.ndarray:
+        n = num_variants()
+        out = np.zeros(n, dtype=np.float32)
+        check(lib().tt_plan_sweep_times(self.ptr, out.ctypes.data_as(C.POINTER(C.c_float)), n))
+        return out
+
+
+def num_variants() -> int:
+    return int(lib().tt_num_variants())
+
+
+def variant_info(vid: int) -> dict:
+    v = VariantInfo()
+    check(lib().tt_variant_get(vid, C.byref(v)))
+    return {f: getattr(v, f) for f, _ in VariantInfo._fields_ if f != "name"} | {"name": v.name.decode()}
+
+
+def variant_valid(vid: int, order: int, rank: int, prec="fp32") -> bool:
+    return bool(lib().tt_variant_valid(vid, order, rank, PRECISIONS.get(prec, prec)))
+
+
+def default_variant(order: int, rank: int, prec="fp32", nnz: int = 0) -> int:
+    return int(lib().tt_variant_default(order, rank, PRECISIONS.get(prec, prec), nnz))
+
+
+def device_count() -> int:
+    return int(lib().tt_device_count())
+
+
+def synchronize() -> None:
+    check(lib().tt_device_synchronize())
+
+
+def l2_flush(stream=None) -> None:
+    check(lib().tt_l2_flush(stream))

@@ -1,0 +1,151 @@
+// tt_common.cuh -- device helpers shared by the sm_103a kernels of libtentaco_gb300.
+//
+// Memory access discipline on GB300 (HBM3e, 129 MB L2 over two dies):
+//  * CSF streams (crd, vals) are read once per call: 128-bit loads that do not
+//    allocate in L1 and are marked evict_first in L2, so they do not push the
+//    factor matrices out of L2.
+//  * Factor-row gathers are marked evict_last in L2: the factors are the only
+//    data re-read across the call, and keeping them L2-resident is what bounds
+//    the random-gather cost.
+#pragma once
+#include <cstdint>
+#include <type_traits>
+#include <cuda_runtime.h>
+
+namespace tt {
+
+enum Prec : int { kFP32 = 0, kBF16 = 1, kBF16F = 2 };
+
+// ---------------------------------------------------------------------------
+// L2 cache policies (createpolicy, sm_80+).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+// ---------------------------------------------------------------------------
+// Streaming loads (read-only, no L1 allocation, L2 evict_first).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int4 ld_stream_i4(const int32_t* p, uint64_t pol) {
+  int4 r;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.s32 {%0,%1,%2,%3}, [%4], %5;"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "l"(p), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ float4 ld_stream_f4(const float* p, uint64_t pol) {
+  float4 r;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0,%1,%2,%3}, [%4], %5;"
+               : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+               : "l"(p), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ uint2 ld_stream_u2(const void* p, uint64_t pol) {
+  uint2 r;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0,%1}, [%2], %3;"
+               : "=r"(r.x), "=r"(r.y)
+               : "l"(p), "l"(pol));
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// Gather loads (read-only, L2 evict_last).  Widths 2..16 bytes.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 ld_gather_16(const void* p, uint64_t pol) {
+  uint4 r;
+  asm volatile("ld.global.nc.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "l"(p), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ uint2 ld_gather_8(const void* p, uint64_t pol) {
+  uint2 r;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.u32 {%0,%1}, [%2], %3;"
+               : "=r"(r.x), "=r"(r.y)
+               : "l"(p), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ uint32_t ld_gather_4(const void* p, uint64_t pol) {
+  uint32_t r;
+  asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ uint32_t ld_gather_2(const void* p, uint64_t pol) {
+  unsigned short r;
+  asm volatile("ld.global.nc.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(r) : "l"(p), "l"(pol));
+  return (uint32_t)r;
+}
+
+// BF16 -> FP32 is exact: the bf16 bits are the high half of the fp32 bits.
+__device__ __forceinline__ float bf16lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf16hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
+
+// Load CPT consecutive factor entries starting at element offset `off` of a
+// row-major factor stored as FP32 (FT=float) or BF16 (FT=uint16_t), as floats.
+template <typename FT, int CPT>
+struct RowLoad;
+
+template <int CPT>
+struct RowLoad<float, CPT> {
+  static __device__ __forceinline__ void load(const float* base, int64_t off, uint64_t pol,
+                                              float (&v)[CPT]) {
+    const float* p = base + off;
+    if constexpr (CPT == 8) {
+      uint4 a = ld_gather_16(p, pol), b = ld_gather_16(p + 4, pol);
+      v[0] = __uint_as_float(a.x); v[1] = __uint_as_float(a.y);
+      v[2] = __uint_as_float(a.z); v[3] = __uint_as_float(a.w);
+      v[4] = __uint_as_float(b.x); v[5] = __uint_as_float(b.y);
+      v[6] = __uint_as_float(b.z); v[7] = __uint_as_float(b.w);
+    } else if constexpr (CPT == 4) {
+      uint4 a = ld_gather_16(p, pol);
+      v[0] = __uint_as_float(a.x); v[1] = __uint_as_float(a.y);
+      v[2] = __uint_as_float(a.z); v[3] = __uint_as_float(a.w);
+    } else if constexpr (CPT == 2) {
+      uint2 a = ld_gather_8(p, pol);
+      v[0] = __uint_as_float(a.x); v[1] = __uint_as_float(a.y);
+    } else {
+      v[0] = __uint_as_float(ld_gather_4(p, pol));
+    }
+  }
+};
+
+template <int CPT>
+struct RowLoad<uint16_t, CPT> {
+  static __device__ __forceinline__ void load(const uint16_t* base, int64_t off, uint64_t pol,
+                                              float (&v)[CPT]) {
+    const uint16_t* p = base + off;
+    if constexpr (CPT == 8) {
+      uint4 a = ld_gather_16(p, pol);
+      v[0] = bf16lo(a.x); v[1] = bf16hi(a.x); v[2] = bf16lo(a.y); v[3] = bf16hi(a.y);
+      v[4] = bf16lo(a.z); v[5] = bf16hi(a.z); v[6] = bf16lo(a.w); v[7] = bf16hi(a.w);
+    } else if constexpr (CPT == 4) {
+      uint2 a = ld_gather_8(p, pol);
+      v[0] = bf16lo(a.x); v[1] = bf16hi(a.x); v[2] = bf16lo(a.y); v[3] = bf16hi(a.y);
+    } else if constexpr (CPT == 2) {
+      uint32_t a = ld_gather_4(p, pol);
+      v[0] = bf16lo(a); v[1] = bf16hi(a);
+    } else {
+      v[0] = bf16lo(ld_gather_2(p, pol));
+    }
+  }
+};
+
+// Largest x in [lo, hi] with a[x] <= t, given a[lo] <= t (a non-decreasing).
+template <typename IdxT>
+__device__ __forceinline__ int64_t search_le(const IdxT* a, int64_t lo, int64_t hi, int64_t t) {
+  while (lo < hi) {
+    int64_t mid = lo + ((hi - lo + 1) >> 1);
+    if ((int64_t)a[mid] <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+}  // namespace tt

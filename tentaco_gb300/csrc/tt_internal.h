@@ -1,0 +1,69 @@
+// tt_internal.h -- host-side internals shared by the translation units of libtentaco_gb300.
+#pragma once
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+#include "../../include/tentaco/tentaco.h"
+
+#define TT_EXPORT extern "C" __attribute__((visibility("default")))
+
+namespace tt {
+
+// Per-thread last error, reported by tt_last_error_string().
+tt_status set_error(tt_status s, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+void clear_error();
+const char* g_last_error_cstr();
+
+// A library-owned taco_tensor_t with its arrays.  `t` is the first member so the
+// public pointer converts back to the owner.
+struct OwnedTensor {
+  taco_tensor_t t;
+  uint32_t magic;
+  int32_t dims[TT_MAX_ORDER];
+  int32_t mode_ordering[TT_MAX_ORDER];
+  taco_mode_t mode_types[TT_MAX_ORDER];
+  int32_t** levels[TT_MAX_ORDER];
+  int32_t* slots[2 * TT_MAX_ORDER];
+  std::vector<int32_t> pos[TT_MAX_ORDER];
+  std::vector<int32_t> crd[TT_MAX_ORDER];
+  std::vector<float> vals;
+  static constexpr uint32_t kMagic = 0x7474c5f1u;
+  OwnedTensor();
+  // Point the taco_tensor_t fields at the vectors (call after filling them).
+  void publish(int order, const int32_t* d);
+};
+
+// Number of entries at level l of a (validated) CSF: level 0 = root positions.
+struct CsfView {
+  int order = 0;
+  int32_t dims[TT_MAX_ORDER] = {0, 0, 0, 0};
+  bool dense_root = true;
+  const int32_t* root_crd = nullptr;  // compressed root ids (nullptr: dense)
+  int64_t nroot = 0;                  // root positions
+  const int32_t* pos[TT_MAX_ORDER] = {nullptr, nullptr, nullptr, nullptr};
+  const int32_t* crd[TT_MAX_ORDER] = {nullptr, nullptr, nullptr, nullptr};
+  int64_t count[TT_MAX_ORDER] = {0, 0, 0, 0};  // entries per level (count[order-1] = nnz)
+  const float* vals = nullptr;
+  int64_t nnz = 0;
+};
+
+// Read the CSF arrays of B (no validation).
+tt_status csf_view(const taco_tensor_t* B, CsfView* v);
+// Full validation (monotone pos, sorted distinct crd in range, non-empty inner fibers).
+tt_status csf_check(const CsfView& v);
+
+// Stable parallel LSD radix sort of 64-bit keys with a 32-bit payload, on the
+// low `bits` bits.
+void radix_sort_pairs(std::vector<uint64_t>& keys, std::vector<uint32_t>& payload, int bits);
+
+// Deterministic RNG: splitmix64-seeded xoshiro256**.
+struct Rng {
+  uint64_t s[4];
+  explicit Rng(uint64_t seed, uint64_t stream = 0);
+  uint64_t next();
+  double uniform();  // [0,1), 53 bits
+  double normal();   // Box-Muller
+};
+
+}  // namespace tt

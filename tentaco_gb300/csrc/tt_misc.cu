@@ -1,0 +1,154 @@
+// tt_misc.cu -- partition, TTV and storage-conversion kernels of libtentaco_gb300.
+#include <cuda_bf16.h>
+#include "tt_kernels.h"
+#include "tt_mttkrp.cuh"
+#include "tt_ttv.cuh"
+
+namespace tt {
+
+WalkLauncher walk_launcher(int order, int prec, int cpt, int lpr) {
+  if (order == 3) {
+    if (prec == kFP32) return walk_launcher_o3_fp32(cpt, lpr);
+    if (prec == kBF16) return walk_launcher_o3_bf16(cpt, lpr);
+    if (prec == kBF16F) return walk_launcher_o3_bf16f(cpt, lpr);
+  } else if (order == 4) {
+    if (prec == kFP32) return walk_launcher_o4_fp32(cpt, lpr);
+    if (prec == kBF16) return walk_launcher_o4_bf16(cpt, lpr);
+    if (prec == kBF16F) return walk_launcher_o4_bf16f(cpt, lpr);
+  }
+  return nullptr;
+}
+
+cudaError_t launch_partition(int order, const WalkArgs& a, cudaStream_t s) {
+  const int n = a.nblocks + 1;
+  const int tb = 256, grid = (n + tb - 1) / tb;
+  if (order == 3) partition_kernel<3><<<grid, tb, 0, s>>>(a);
+  else partition_kernel<4><<<grid, tb, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ttv(const TtvArgs& a, int grid, int tb, size_t smem, cudaStream_t s) {
+  static size_t configured = 48 * 1024;
+  if (smem > configured) {
+    cudaError_t e = cudaFuncSetAttribute(ttv_walk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = smem;
+  }
+  ttv_walk_kernel<<<grid, tb, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ttv_partition(const TtvArgs& a, cudaStream_t s) {
+  const int n = a.nblocks + 1;
+  ttv_partition_kernel<<<(n + 255) / 256, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// storage conversion (factors to BF16 with power-of-two column scales)
+// ---------------------------------------------------------------------------
+__global__ void colmax_kernel(const float* __restrict__ x, int64_t rows, int cols, float* colmax) {
+  // one thread per (row-slab, column); |x| >= 0 so unsigned compare of the bits orders it
+  const int j = threadIdx.x % cols;
+  const int lanes = blockDim.x / cols;
+  float m = 0.f;
+  for (int64_t r = (int64_t)blockIdx.x * lanes + threadIdx.x / cols; r < rows; r += (int64_t)gridDim.x * lanes) {
+    const float v = fabsf(x[r * cols + j]);
+    m = v > m ? v : m;  // NaN ignored
+  }
+  if (threadIdx.x < lanes * cols) atomicMax(reinterpret_cast<unsigned int*>(colmax) + j, __float_as_uint(m));
+}
+
+cudaError_t launch_colmax(const float* x, int64_t rows, int cols, float* colmax, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(colmax, 0, sizeof(float) * (size_t)cols, s);
+  if (e != cudaSuccess) return e;
+  if (rows == 0) return cudaSuccess;
+  const int lanes = 256 / cols > 0 ? 256 / cols : 1;
+  const int tb = lanes * cols;
+  int64_t grid = (rows + lanes * 32 - 1) / (lanes * 32);
+  if (grid > 4096) grid = 4096;
+  colmax_kernel<<<(int)grid, tb, 0, s>>>(x, rows, cols, colmax);
+  return cudaGetLastError();
+}
+
+__global__ void pow2_scales_kernel(const float* colmax, int cols, float* scale, float* inv) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= cols) return;
+  const uint32_t bits = __float_as_uint(colmax[j]);
+  const int ex = (int)((bits >> 23) & 0xff);  // biased exponent of the column max
+  float sc = 1.f, iv = 1.f;
+  if (ex != 0 && ex != 0xff) {
+    // column max in [2^E, 2^(E+1)), E = ex - 127: scale = 2^-E puts it in [1, 2),
+    // inv = 2^E undoes it.  Both are exact powers of two in FP32.
+    const int es = 254 - ex;  // biased exponent of 2^-E
+    if (es >= 1 && es <= 254) {
+      sc = __uint_as_float((uint32_t)es << 23);
+      iv = __uint_as_float((uint32_t)ex << 23);
+    }
+  }
+  scale[j] = sc;
+  inv[j] = iv;
+}
+
+cudaError_t launch_pow2_scales(const float* colmax, int cols, float* scale, float* inv, cudaStream_t s) {
+  pow2_scales_kernel<<<(cols + 63) / 64, 64, 0, s>>>(colmax, cols, scale, inv);
+  return cudaGetLastError();
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ src, int64_t rows, int cols, int rp,
+                               const float* __restrict__ scale, __nv_bfloat16* __restrict__ dst) {
+  const int64_t n = rows * rp;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / rp;
+    const int j = (int)(i - r * rp);
+    const float v = j < cols ? src[r * cols + j] * (scale ? scale[j] : 1.f) : 0.f;
+    dst[i] = __float2bfloat16_rn(v);
+  }
+}
+
+cudaError_t launch_to_bf16(const float* src, int64_t rows, int cols, int rp, const float* scale,
+                           uint16_t* dst, cudaStream_t s) {
+  const int64_t n = rows * rp;
+  if (n == 0) return cudaSuccess;
+  int64_t grid = (n + 255) / 256;
+  if (grid > 152 * 32) grid = 152 * 32;
+  to_bf16_kernel<<<(int)grid, 256, 0, s>>>(src, rows, cols, rp, scale, reinterpret_cast<__nv_bfloat16*>(dst));
+  return cudaGetLastError();
+}
+
+__global__ void pad_fp32_kernel(const float* __restrict__ src, int64_t rows, int cols, int rp, float* __restrict__ dst) {
+  const int64_t n = rows * rp;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / rp;
+    const int j = (int)(i - r * rp);
+    dst[i] = j < cols ? src[r * cols + j] : 0.f;
+  }
+}
+
+cudaError_t launch_pad_fp32(const float* src, int64_t rows, int cols, int rp, float* dst, cudaStream_t s) {
+  const int64_t n = rows * rp;
+  if (n == 0) return cudaSuccess;
+  int64_t grid = (n + 255) / 256;
+  if (grid > 152 * 32) grid = 152 * 32;
+  pad_fp32_kernel<<<(int)grid, 256, 0, s>>>(src, rows, cols, rp, dst);
+  return cudaGetLastError();
+}
+
+struct InvPtrs { const float* p[4]; };
+
+__global__ void scale_product_kernel(InvPtrs inv, int nm, int rp, float vinv, float* out) {
+  const int j = threadIdx.x;
+  if (j >= rp) return;
+  float v = vinv;
+  for (int m = 0; m < nm; m++) v *= inv.p[m] ? inv.p[m][j] : 1.f;
+  out[j] = v;
+}
+
+cudaError_t launch_scale_product(const float* const* inv, int nm, int rp, float vinv, float* out, cudaStream_t s) {
+  InvPtrs ip{};
+  for (int m = 0; m < nm && m < 4; m++) ip.p[m] = inv[m];
+  scale_product_kernel<<<1, 64, 0, s>>>(ip, nm, rp, vinv, out);
+  return cudaGetLastError();
+}
+
+}  // namespace tt

@@ -1,0 +1,744 @@
+// tt_plan.cu -- plan API of libtentaco_gb300 (see include/tentaco/tentaco.h).
+//
+// A plan replaces the reference's per-call staging (copy_to_device_mttkrp /
+// copy_from_device_mttkrp / free_tensors_mttkrp, gpu_library.h:780-945, which
+// cudaMalloc and upload every array on every call and publish the pointers in
+// process-global __device__ symbols).  Here the CSF is uploaded once, into
+// plan-owned buffers padded for 128-bit loads; per call only the partition
+// (inside the timed region, as the reference's TIME_GPU does), the output clear
+// and the walk kernel run, on the caller's stream.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+#include "tt_internal.h"
+#include "tt_kernels.h"
+#define TT_ARGS_ONLY
+#include "tt_mttkrp.cuh"
+#include "tt_ttv.cuh"
+#include "tt_plan.h"
+
+using namespace tt;
+
+namespace tt {
+
+// ---------------------------------------------------------------------------
+// variant table: threads {256,512} x nnz per team {4..64} x columns per lane {8,4,2,1}
+// ---------------------------------------------------------------------------
+static const int kTB[2] = {256, 512};
+static const int kG[5] = {4, 8, 16, 32, 64};
+static const int kCPT[4] = {8, 4, 2, 1};
+constexpr int kNumVariants = 2 * 5 * 4;
+
+VariantSpec variant_spec(int id) {
+  VariantSpec v{};
+  if (id < 0 || id >= kNumVariants) return v;
+  v.id = id;
+  v.cpt = kCPT[id % 4];
+  v.G = kG[(id / 4) % 5];
+  v.tb = kTB[id / 20];
+  return v;
+}
+
+int variant_id(int tb, int G, int cpt) {
+  int ti = tb == 512 ? 1 : 0, gi = 0, ci = 0;
+  for (int i = 0; i < 5; i++) if (kG[i] == G) gi = i;
+  for (int i = 0; i < 4; i++) if (kCPT[i] == cpt) ci = i;
+  return (ti * 5 + gi) * 4 + ci;
+}
+
+int rank_pad(int R) {
+  if (R <= 8) return 8;
+  if (R <= 16) return 16;
+  if (R <= 32) return 32;
+  return 64;
+}
+
+bool variant_valid(int id, int order, int rank, int prec) {
+  VariantSpec v = variant_spec(id);
+  if (v.tb == 0) return false;
+  const int rp = rank_pad(rank);
+  if (rp % v.cpt) return false;
+  const int lpr = rp / v.cpt;
+  if (lpr < 1 || lpr > 32) return false;
+  // the block's fiber window and merge scratch must fit the 227 KB opt-in shared memory
+  const int P = (v.tb / lpr) * v.G;
+  if (walk_smem_bytes(P, v.tb, rp) > (size_t)227 * 1024) return false;
+  return walk_launcher(order, prec, v.cpt, lpr) != nullptr;
+}
+
+int default_variant(int order, int rank, int prec, int64_t nnz) {
+  (void)nnz;
+  // one 16-byte factor load per lane: 4 FP32 or 8 BF16 columns
+  const int rp = rank_pad(rank);
+  int cpt = prec == kFP32 ? 4 : 8;
+  while (cpt > 1 && rp / cpt < 1) cpt >>= 1;
+  while (rp / cpt > 32) cpt <<= 1;
+  int id = variant_id(256, 16, cpt);
+  if (!variant_valid(id, order, rank, prec)) {
+    for (int i = 0; i < kNumVariants; i++)
+      if (variant_valid(i, order, rank, prec)) return i;
+    return -1;
+  }
+  return id;
+}
+
+}  // namespace tt
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+#define CK(expr)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (expr);                                                              \
+    if (e_ != cudaSuccess) {                                                              \
+      return set_error(e_ == cudaErrorMemoryAllocation ? TT_ERR_OUT_OF_MEMORY : TT_ERR_CUDA, \
+                       "%s: %s", #expr, cudaGetErrorString(e_));                         \
+    }                                                                                     \
+  } while (0)
+
+namespace {
+
+std::atomic<float> g_legacy_ms{-1.0f};
+
+template <typename T>
+tt_status dev_alloc(tt_plan* p, T** ptr, size_t count) {
+  *ptr = nullptr;
+  if (count == 0) count = 1;
+  CK(cudaMalloc((void**)ptr, count * sizeof(T)));
+  p->allocs.push_back((void*)*ptr);
+  p->device_bytes += (int64_t)(count * sizeof(T));
+  return TT_OK;
+}
+
+void dev_free(tt_plan* p, void* ptr) {
+  if (!ptr) return;
+  auto it = std::find(p->allocs.begin(), p->allocs.end(), ptr);
+  if (it != p->allocs.end()) p->allocs.erase(it);
+  cudaFree(ptr);
+}
+
+inline uint16_t f32_to_bf16_rne(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40);  // NaN stays NaN
+  u += 0x7fffu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
+}
+
+// 2^-floor(log2(m)) for m > 0 finite, else 1.
+float pow2_scale_for(float m) {
+  if (!(m > 0.f) || !std::isfinite(m)) return 1.f;
+  int e;
+  std::frexp(m, &e);  // m = f * 2^e, f in [0.5, 1)
+  return std::ldexp(1.f, -(e - 1));
+}
+
+int64_t pad16(int64_t n) { return ((n + 15) / 16) * 16 + 16; }
+
+tt_status alloc_walk_scratch(tt_plan* p, int P) {
+  const int64_t nb = (p->nnz + P - 1) / P;
+  if (nb > p->scratch_blocks) {
+    dev_free(p, p->d_part);
+    dev_free(p, p->d_carry);
+    p->d_part = nullptr;
+    p->d_carry = nullptr;
+    tt_status s = dev_alloc(p, &p->d_part, (size_t)(nb + 1) * (size_t)(p->order - 1));
+    if (s != TT_OK) return s;
+    s = dev_alloc(p, &p->d_carry, (size_t)(2 * nb) * (size_t)p->rp);
+    if (s != TT_OK) return s;
+    p->scratch_blocks = nb;
+  }
+  return TT_OK;
+}
+
+tt_status use_variant(tt_plan* p, int id) {
+  VariantSpec v = variant_spec(id);
+  p->variant = id;
+  p->tb = v.tb;
+  p->cpt = v.cpt;
+  p->lpr = p->rp / v.cpt;
+  p->G = v.G;
+  p->P = (v.tb / p->lpr) * v.G;
+  p->nblocks = (int)((p->nnz + p->P - 1) / p->P);
+  p->launcher = walk_launcher(p->order, p->prec, p->cpt, p->lpr);
+  if (!p->launcher) return set_error(TT_ERR_UNSUPPORTED, "variant %d not compiled for this shape", id);
+  return alloc_walk_scratch(p, p->P);
+}
+
+WalkArgs walk_args(const tt_plan* p, float* A) {
+  WalkArgs a{};
+  for (int l = 0; l < TT_MAX_ORDER; l++) { a.pos[l] = p->d_pos[l]; a.crd[l] = p->d_crd[l]; }
+  a.crd[0] = p->dense_root ? nullptr : p->d_crd[0];
+  a.vals = p->d_vals;
+  for (int m = 0; m < 3; m++) a.fac[m] = p->fac[m];
+  a.colscale = p->d_colscale;
+  a.out = A;
+  a.part = p->d_part;
+  a.carry = p->d_carry;
+  a.tickets = p->d_tickets;
+  a.nnz = p->nnz;
+  a.nrows = (int32_t)p->nroot;
+  a.R = p->rank;
+  a.ldo = p->rank;
+  a.P = p->P;
+  a.G = p->G;
+  a.nblocks = p->nblocks;
+  return a;
+}
+
+tt_status run_mttkrp(tt_plan* p, float* A, cudaStream_t st) {
+  const size_t outbytes = (size_t)p->dims[0] * (size_t)p->rank * sizeof(float);
+  CK(cudaMemsetAsync(A, 0, outbytes, st));
+  if (p->nnz == 0) return TT_OK;
+  WalkArgs a = walk_args(p, A);
+  CK(launch_partition(p->order, a, st));
+  const size_t smem = walk_smem_bytes(p->P, p->tb, p->rp);
+  if (p->timing) CK(cudaEventRecord(p->evk0, st));
+  CK(p->launcher(a, p->nblocks, p->tb, smem, st));
+  if (p->timing) CK(cudaEventRecord(p->evk1, st));
+  return TT_OK;
+}
+
+tt_status run_ttv(tt_plan* p, const float* x, float* y, cudaStream_t st) {
+  if (p->nnz == 0) {
+    if (p->nfib_last > 0) CK(cudaMemsetAsync(y, 0, sizeof(float) * (size_t)p->nfib_last, st));
+    return TT_OK;
+  }
+  TtvArgs a{};
+  a.pos = p->d_pos[p->order - 1];
+  a.crd = p->d_crd[p->order - 1];
+  a.vals = p->d_vals;
+  a.x = x;
+  a.y = y;
+  a.part = p->d_part;
+  a.carry = p->d_carry;
+  a.tickets = p->d_tickets;
+  a.vscale = p->prec == kBF16 ? p->vinv : 1.f;
+  a.nnz = p->nnz;
+  a.nfib = p->nfib_last;
+  a.P = p->P;
+  a.NPT = p->G;
+  a.nblocks = p->nblocks;
+  a.vals_bf16 = p->prec == kBF16;
+  CK(launch_ttv_partition(a, st));
+  if (p->timing) CK(cudaEventRecord(p->evk0, st));
+  CK(launch_ttv(a, p->nblocks, p->tb, ttv_smem_bytes(p->P, p->tb), st));
+  if (p->timing) CK(cudaEventRecord(p->evk1, st));
+  return TT_OK;
+}
+
+tt_status sweep_variants(tt_plan* p, cudaStream_t st);
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// public API
+// ---------------------------------------------------------------------------
+TT_EXPORT const char* tt_status_string(tt_status s) {
+  switch (s) {
+    case TT_OK: return "TT_OK";
+    case TT_ERR_INVALID_ARGUMENT: return "TT_ERR_INVALID_ARGUMENT";
+    case TT_ERR_INVALID_CSF: return "TT_ERR_INVALID_CSF";
+    case TT_ERR_UNSUPPORTED: return "TT_ERR_UNSUPPORTED";
+    case TT_ERR_CUDA: return "TT_ERR_CUDA";
+    case TT_ERR_OUT_OF_MEMORY: return "TT_ERR_OUT_OF_MEMORY";
+    case TT_ERR_NO_DEVICE: return "TT_ERR_NO_DEVICE";
+    case TT_ERR_DEVICE_WAIT: return "TT_ERR_DEVICE_WAIT";
+  }
+  return "TT_ERR_UNKNOWN";
+}
+
+TT_EXPORT int32_t tt_abi_version(void) { return TT_ABI_VERSION; }
+TT_EXPORT int32_t tt_num_variants(void) { return kNumVariants; }
+
+TT_EXPORT tt_status tt_variant_get(int32_t id, tt_variant_info* info) {
+  clear_error();
+  if (!info || id < 0 || id >= kNumVariants) return set_error(TT_ERR_INVALID_ARGUMENT, "variant %d", id);
+  VariantSpec v = variant_spec(id);
+  std::memset(info, 0, sizeof(*info));
+  info->id = id;
+  info->threads = v.tb;
+  info->cols_per_lane = v.cpt;
+  info->nnz_per_team = v.G;
+  info->rank_pad = 32;
+  info->lanes_per_row = 32 / v.cpt;
+  info->nnz_per_block = v.tb / info->lanes_per_row * v.G;
+  std::snprintf(info->name, sizeof(info->name), "walk_t%d_g%d_c%d", v.tb, v.G, v.cpt);
+  return TT_OK;
+}
+
+TT_EXPORT int32_t tt_variant_default(int32_t order, int32_t rank, tt_precision prec, int64_t nnz) {
+  return default_variant(order, rank, (int)prec, nnz);
+}
+
+TT_EXPORT int32_t tt_variant_valid(int32_t id, int32_t order, int32_t rank, tt_precision prec) {
+  return variant_valid(id, order, rank, (int)prec) ? 1 : 0;
+}
+
+TT_EXPORT tt_status tt_plan_create(const taco_tensor_t* B, tt_op op, int32_t rank, tt_precision prec,
+                                   tt_select select, int32_t variant, void* stream, tt_plan** out) {
+  clear_error();
+  if (!out) return set_error(TT_ERR_INVALID_ARGUMENT, "null plan pointer");
+  *out = nullptr;
+  CsfView v;
+  tt_status s = csf_view(B, &v);
+  if (s != TT_OK) return s;
+  if ((s = csf_check(v)) != TT_OK) return s;
+  if (op == TT_OP_MTTKRP) {
+    if (v.order != 3 && v.order != 4) return set_error(TT_ERR_UNSUPPORTED, "MTTKRP needs order 3 or 4 (got %d)", v.order);
+    if (rank < 1 || rank > TT_MAX_RANK) return set_error(TT_ERR_UNSUPPORTED, "rank %d (supported 1..%d)", rank, TT_MAX_RANK);
+  } else if (op != TT_OP_TTV) {
+    return set_error(TT_ERR_INVALID_ARGUMENT, "op %d", (int)op);
+  }
+  if (prec != TT_PREC_FP32 && prec != TT_PREC_BF16 && prec != TT_PREC_BF16_FACTORS)
+    return set_error(TT_ERR_INVALID_ARGUMENT, "precision %d", (int)prec);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return set_error(TT_ERR_NO_DEVICE, "no CUDA device visible");
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+
+  auto* p = new tt_plan();
+  cudaGetDevice(&p->device);
+  p->op = op;
+  p->order = v.order;
+  for (int i = 0; i < v.order; i++) p->dims[i] = v.dims[i];
+  p->nnz = v.nnz;
+  p->nroot = v.nroot;
+  p->dense_root = v.dense_root;
+  p->rank = op == TT_OP_MTTKRP ? rank : 1;
+  p->rp = op == TT_OP_MTTKRP ? rank_pad(rank) : 1;
+  p->prec = (int)prec;
+  p->stream = st;
+  for (int l = 0; l < v.order; l++) p->count[l] = v.count[l];
+  p->nfib_last = v.count[v.order - 2];
+
+  auto fail = [&](tt_status st2) { tt_plan_destroy(p); return st2; };
+
+  // upload the CSF (inner pos/crd exact size; nonzero-level crd and vals padded)
+  for (int l = 1; l < v.order; l++) {
+    if ((s = dev_alloc(p, &p->d_pos[l], (size_t)v.count[l - 1] + 1)) != TT_OK) return fail(s);
+    if (cudaMemcpyAsync(p->d_pos[l], v.pos[l], sizeof(int32_t) * ((size_t)v.count[l - 1] + 1),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return fail(set_error(TT_ERR_CUDA, "upload pos[%d]", l));
+    const bool last = l == v.order - 1;
+    const size_t n = last ? (size_t)pad16(v.count[l]) : (size_t)v.count[l];
+    if ((s = dev_alloc(p, &p->d_crd[l], n)) != TT_OK) return fail(s);
+    if (last && cudaMemsetAsync(p->d_crd[l], 0, n * sizeof(int32_t), st) != cudaSuccess)
+      return fail(set_error(TT_ERR_CUDA, "clear crd pad"));
+    if (v.count[l] > 0 &&
+        cudaMemcpyAsync(p->d_crd[l], v.crd[l], sizeof(int32_t) * (size_t)v.count[l], cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return fail(set_error(TT_ERR_CUDA, "upload crd[%d]", l));
+  }
+  if (!v.dense_root) {
+    if ((s = dev_alloc(p, &p->d_crd[0], (size_t)v.nroot)) != TT_OK) return fail(s);
+    if (v.nroot > 0 && cudaMemcpyAsync(p->d_crd[0], v.root_crd, sizeof(int32_t) * (size_t)v.nroot,
+                                       cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return fail(set_error(TT_ERR_CUDA, "upload root crd"));
+  }
+  {
+    const size_t n = (size_t)pad16(v.nnz);
+    if (prec == TT_PREC_BF16) {
+      // values: power-of-two global scale, BF16 round-to-nearest-even
+      float vmax = 0.f;
+      for (int64_t i = 0; i < v.nnz; i++) vmax = std::max(vmax, std::fabs(v.vals[i]));
+      const float sc = pow2_scale_for(vmax);
+      p->vinv = 1.f / sc;
+      p->h_vals16.assign(n, 0);
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < v.nnz; i++) p->h_vals16[(size_t)i] = f32_to_bf16_rne(v.vals[i] * sc);
+      uint16_t* d = nullptr;
+      if ((s = dev_alloc(p, &d, n)) != TT_OK) return fail(s);
+      p->d_vals = d;
+      if (cudaMemcpyAsync(d, p->h_vals16.data(), n * 2, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return fail(set_error(TT_ERR_CUDA, "upload vals"));
+    } else {
+      float* d = nullptr;
+      if ((s = dev_alloc(p, &d, n)) != TT_OK) return fail(s);
+      p->d_vals = d;
+      if (cudaMemsetAsync(d, 0, n * 4, st) != cudaSuccess) return fail(set_error(TT_ERR_CUDA, "clear vals"));
+      if (v.nnz > 0 && cudaMemcpyAsync(d, v.vals, (size_t)v.nnz * 4, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return fail(set_error(TT_ERR_CUDA, "upload vals"));
+    }
+  }
+  // tickets: one per root position (MTTKRP) or per block (TTV), zero once here
+  if (op == TT_OP_MTTKRP) {
+    if ((s = dev_alloc(p, &p->d_tickets, (size_t)std::max<int64_t>(1, v.nroot))) != TT_OK) return fail(s);
+    if (cudaMemsetAsync(p->d_tickets, 0, sizeof(int32_t) * (size_t)std::max<int64_t>(1, v.nroot), st) != cudaSuccess)
+      return fail(set_error(TT_ERR_CUDA, "clear tickets"));
+    int id = -1;
+    if (select == TT_SELECT_FIXED) {
+      if (!variant_valid(variant, p->order, rank, p->prec))
+        return fail(set_error(TT_ERR_INVALID_ARGUMENT, "variant %d not valid for order %d rank %d", variant, p->order, rank));
+      id = variant;
+    } else if (select == TT_SELECT_MODEL) {
+      id = selector_pick(p, B);
+      p->selected_by = 1;
+      if (id < 0) { id = default_variant(p->order, rank, p->prec, p->nnz); p->selected_by = 0; }
+    } else {
+      id = default_variant(p->order, rank, p->prec, p->nnz);
+    }
+    if (id < 0) return fail(set_error(TT_ERR_UNSUPPORTED, "no variant for order %d rank %d", p->order, rank));
+    if ((s = use_variant(p, id)) != TT_OK) return fail(s);
+    if (select == TT_SELECT_SWEEP) {
+      if ((s = sweep_variants(p, st)) != TT_OK) return fail(s);
+      p->selected_by = 2;
+    }
+  } else {
+    p->tb = 256;
+    p->G = 16;  // nonzeros per thread
+    p->P = p->tb * p->G;
+    p->nblocks = (int)((p->nnz + p->P - 1) / p->P);
+    if ((s = dev_alloc(p, &p->d_part, (size_t)p->nblocks + 1)) != TT_OK) return fail(s);
+    if ((s = dev_alloc(p, &p->d_carry, (size_t)2 * p->nblocks)) != TT_OK) return fail(s);
+    if ((s = dev_alloc(p, &p->d_tickets, (size_t)p->nblocks + 1)) != TT_OK) return fail(s);
+    if (cudaMemsetAsync(p->d_tickets, 0, sizeof(int32_t) * ((size_t)p->nblocks + 1), st) != cudaSuccess)
+      return fail(set_error(TT_ERR_CUDA, "clear tickets"));
+  }
+  if (cudaStreamSynchronize(st) != cudaSuccess) return fail(set_error(TT_ERR_CUDA, "plan upload: %s", cudaGetErrorString(cudaGetLastError())));
+  p->h_vals16.clear();
+  p->h_vals16.shrink_to_fit();
+  *out = p;
+  return TT_OK;
+}
+
+TT_EXPORT tt_status tt_plan_destroy(tt_plan* p) {
+  if (!p) return TT_OK;
+  if (p->ev0) cudaEventDestroy(p->ev0);
+  if (p->ev1) cudaEventDestroy(p->ev1);
+  if (p->evk0) cudaEventDestroy(p->evk0);
+  if (p->evk1) cudaEventDestroy(p->evk1);
+  for (void* a : p->allocs) cudaFree(a);
+  delete p;
+  return TT_OK;
+}
+
+TT_EXPORT tt_status tt_plan_set_factors(tt_plan* p, const float* const* factors, void* stream) {
+  clear_error();
+  if (!p || !factors) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
+  if (p->op != TT_OP_MTTKRP) return set_error(TT_ERR_INVALID_ARGUMENT, "plan is not an MTTKRP plan");
+  cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+  const int nm = p->order - 1;
+  for (int m = 0; m < nm; m++)
+    if (!factors[m]) return set_error(TT_ERR_INVALID_ARGUMENT, "factor %d is null", m + 1);
+  tt_status s;
+  if (p->prec == kFP32) {
+    for (int m = 0; m < nm; m++) {
+      if (p->rank == p->rp) {
+        p->fac[m] = factors[m];
+      } else {
+        const int64_t rows = p->dims[m + 1];
+        if (!p->fac_own[m]) {
+          float* d = nullptr;
+          if ((s = dev_alloc(p, &d, (size_t)rows * p->rp)) != TT_OK) return s;
+          p->fac_own[m] = d;
+        }
+        CK(launch_pad_fp32(factors[m], rows, p->rank, p->rp, (float*)p->fac_own[m], st));
+        p->fac[m] = p->fac_own[m];
+      }
+    }
+    p->d_colscale = nullptr;
+  } else {
+    if (!p->d_scales) {
+      if ((s = dev_alloc(p, &p->d_scales, (size_t)(3 * nm + 1) * p->rp)) != TT_OK) return s;
+    }
+    const float* inv[3] = {nullptr, nullptr, nullptr};
+    for (int m = 0; m < nm; m++) {
+      const int64_t rows = p->dims[m + 1];
+      float* cmax = p->d_scales + (size_t)(3 * m) * p->rp;
+      float* scl = cmax + p->rp;
+      float* iv = scl + p->rp;
+      CK(cudaMemsetAsync(cmax, 0, sizeof(float) * p->rp, st));
+      CK(launch_colmax(factors[m], rows, p->rank, cmax, st));
+      CK(launch_pow2_scales(cmax, p->rp, scl, iv, st));
+      if (!p->fac_own[m]) {
+        uint16_t* d = nullptr;
+        if ((s = dev_alloc(p, &d, (size_t)rows * p->rp)) != TT_OK) return s;
+        p->fac_own[m] = d;
+      }
+      CK(launch_to_bf16(factors[m], rows, p->rank, p->rp, scl, (uint16_t*)p->fac_own[m], st));
+      p->fac[m] = p->fac_own[m];
+      inv[m] = iv;
+    }
+    p->d_colscale = p->d_scales + (size_t)(3 * nm) * p->rp;
+    CK(launch_scale_product(inv, nm, p->rp, p->prec == kBF16 ? p->vinv : 1.f, p->d_colscale, st));
+  }
+  p->factors_set = true;
+  return TT_OK;
+}
+
+static tt_status timed_begin(tt_plan* p, cudaStream_t st) {
+  if (!p->timing) return TT_OK;
+  if (!p->ev0) {
+    CK(cudaEventCreate(&p->ev0));
+    CK(cudaEventCreate(&p->ev1));
+    CK(cudaEventCreate(&p->evk0));
+    CK(cudaEventCreate(&p->evk1));
+  }
+  CK(cudaEventRecord(p->ev0, st));
+  return TT_OK;
+}
+static tt_status timed_end(tt_plan* p, cudaStream_t st) {
+  if (!p->timing) return TT_OK;
+  CK(cudaEventRecord(p->ev1, st));
+  p->timed_pending = true;
+  return TT_OK;
+}
+
+TT_EXPORT tt_status tt_plan_mttkrp(tt_plan* p, float* A, void* stream) {
+  clear_error();
+  if (!p || !A) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
+  if (p->op != TT_OP_MTTKRP) return set_error(TT_ERR_INVALID_ARGUMENT, "plan is not an MTTKRP plan");
+  if (!p->factors_set) return set_error(TT_ERR_INVALID_ARGUMENT, "factors not set (tt_plan_set_factors)");
+  cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+  tt_status s;
+  if ((s = timed_begin(p, st)) != TT_OK) return s;
+  if ((s = run_mttkrp(p, A, st)) != TT_OK) return s;
+  return timed_end(p, st);
+}
+
+TT_EXPORT tt_status tt_plan_ttv(tt_plan* p, const float* x, float* y, void* stream) {
+  clear_error();
+  if (!p || !x || !y) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
+  if (p->op != TT_OP_TTV) return set_error(TT_ERR_INVALID_ARGUMENT, "plan is not a TTV plan");
+  cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+  tt_status s;
+  if ((s = timed_begin(p, st)) != TT_OK) return s;
+  if ((s = run_ttv(p, x, y, st)) != TT_OK) return s;
+  return timed_end(p, st);
+}
+
+TT_EXPORT tt_status tt_plan_set_timing(tt_plan* p, int32_t enabled) {
+  if (!p) return set_error(TT_ERR_INVALID_ARGUMENT, "null plan");
+  p->timing = enabled != 0;
+  return TT_OK;
+}
+
+TT_EXPORT float tt_plan_last_ms(tt_plan* p) {
+  if (!p || !p->timed_pending) return -1.f;
+  if (cudaEventSynchronize(p->ev1) != cudaSuccess) return -1.f;
+  float ms = -1.f;
+  cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+  return ms;
+}
+
+TT_EXPORT int32_t tt_plan_variant(const tt_plan* p) { return p ? p->variant : -1; }
+TT_EXPORT int32_t tt_plan_selected_by(const tt_plan* p) { return p ? p->selected_by : -1; }
+TT_EXPORT int64_t tt_plan_nnz(const tt_plan* p) { return p ? p->nnz : -1; }
+TT_EXPORT int64_t tt_plan_num_fibers(const tt_plan* p, int32_t level) {
+  if (!p || level < 0 || level >= p->order) return -1;
+  return p->count[level];
+}
+TT_EXPORT int64_t tt_plan_device_bytes(const tt_plan* p) { return p ? p->device_bytes : -1; }
+TT_EXPORT int32_t tt_plan_nblocks(const tt_plan* p) { return p ? p->nblocks : -1; }
+
+// Switch an existing plan to another variant (scratch grows as needed).
+TT_EXPORT tt_status tt_plan_use_variant(tt_plan* p, int32_t id) {
+  clear_error();
+  if (!p || p->op != TT_OP_MTTKRP) return set_error(TT_ERR_INVALID_ARGUMENT, "need an MTTKRP plan");
+  if (!variant_valid(id, p->order, p->rank, p->prec)) return set_error(TT_ERR_INVALID_ARGUMENT, "variant %d invalid here", id);
+  return use_variant(p, id);
+}
+
+namespace {
+// Time every valid variant (3 runs each after one warm-up) with placeholder
+// factors and keep the fastest.  Timing does not depend on factor values.
+tt_status sweep_variants(tt_plan* p, cudaStream_t st) {
+  const int nm = p->order - 1;
+  std::vector<void*> tmp;
+  const void* saved[3] = {p->fac[0], p->fac[1], p->fac[2]};
+  float* saved_scale = p->d_colscale;
+  const size_t esz = p->prec == kFP32 ? 4 : 2;
+  for (int m = 0; m < nm; m++) {
+    void* d = nullptr;
+    CK(cudaMalloc(&d, (size_t)p->dims[m + 1] * p->rp * esz));
+    CK(cudaMemsetAsync(d, 0, (size_t)p->dims[m + 1] * p->rp * esz, st));
+    tmp.push_back(d);
+    p->fac[m] = d;
+  }
+  p->d_colscale = nullptr;
+  float* A = nullptr;
+  CK(cudaMalloc(&A, (size_t)p->dims[0] * p->rank * sizeof(float)));
+  tmp.push_back(A);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  int best = p->variant;
+  float best_ms = 1e30f;
+  tt_status s = TT_OK;
+  for (int id = 0; id < kNumVariants && s == TT_OK; id++) {
+    if (!variant_valid(id, p->order, p->rank, p->prec)) continue;
+    if ((s = use_variant(p, id)) != TT_OK) break;
+    if ((s = run_mttkrp(p, A, st)) != TT_OK) break;
+    float tot = 0.f;
+    for (int r = 0; r < 3; r++) {
+      cudaEventRecord(e0, st);
+      if ((s = run_mttkrp(p, A, st)) != TT_OK) break;
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      tot += ms;
+    }
+    p->sweep_ms[id] = tot / 3.f;
+    if (tot / 3.f < best_ms) { best_ms = tot / 3.f; best = id; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamSynchronize(st);
+  for (void* d : tmp) cudaFree(d);
+  for (int m = 0; m < 3; m++) p->fac[m] = saved[m];
+  p->d_colscale = saved_scale;
+  if (s != TT_OK) return s;
+  return use_variant(p, best);
+}
+}  // namespace
+
+// Per-variant mean ms measured by the last TT_SELECT_SWEEP (negative: not timed).
+TT_EXPORT tt_status tt_plan_sweep_times(const tt_plan* p, float* ms, int32_t n) {
+  if (!p || !ms) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
+  for (int i = 0; i < n && i < kNumVariants; i++) ms[i] = p->sweep_ms[i];
+  return TT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// one-shot host calls
+// ---------------------------------------------------------------------------
+TT_EXPORT tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
+                                   const taco_tensor_t* const* factors, tt_precision prec,
+                                   tt_select select, int32_t variant) {
+  clear_error();
+  if (!A || !B || !factors || !A->vals || !A->dimensions) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
+  const int order = B->order;
+  const int rank = A->dimensions[1];
+  if (A->dimensions[0] != B->dimensions[0]) return set_error(TT_ERR_INVALID_ARGUMENT, "A rows %d != B dims[0] %d", A->dimensions[0], B->dimensions[0]);
+  for (int m = 0; m < order - 1; m++) {
+    const taco_tensor_t* F = factors[m];
+    if (!F || !F->vals || !F->dimensions) return set_error(TT_ERR_INVALID_ARGUMENT, "factor %d missing", m + 1);
+    if (F->dimensions[1] != rank || F->dimensions[0] != B->dimensions[m + 1])
+      return set_error(TT_ERR_INVALID_ARGUMENT, "factor %d is %dx%d, expected %dx%d", m + 1, F->dimensions[0], F->dimensions[1], B->dimensions[m + 1], rank);
+  }
+  tt_plan* p = nullptr;
+  tt_status s = tt_plan_create(B, TT_OP_MTTKRP, rank, prec, select, variant, nullptr, &p);
+  if (s != TT_OK) return s;
+  std::vector<float*> dfac(order - 1, nullptr);
+  float* dA = nullptr;
+  auto cleanup = [&]() {
+    for (float* d : dfac) cudaFree(d);
+    cudaFree(dA);
+    tt_plan_destroy(p);
+  };
+  for (int m = 0; m < order - 1; m++) {
+    const size_t bytes = (size_t)factors[m]->dimensions[0] * rank * sizeof(float);
+    if (cudaMalloc((void**)&dfac[m], bytes) != cudaSuccess) { cleanup(); return set_error(TT_ERR_OUT_OF_MEMORY, "factor %d", m + 1); }
+    if (cudaMemcpy(dfac[m], factors[m]->vals, bytes, cudaMemcpyHostToDevice) != cudaSuccess) { cleanup(); return set_error(TT_ERR_CUDA, "upload factor %d", m + 1); }
+  }
+  const size_t abytes = (size_t)A->dimensions[0] * rank * sizeof(float);
+  if (cudaMalloc((void**)&dA, abytes) != cudaSuccess) { cleanup(); return set_error(TT_ERR_OUT_OF_MEMORY, "output"); }
+  tt_plan_set_timing(p, 1);
+  if ((s = tt_plan_set_factors(p, (const float* const*)dfac.data(), nullptr)) != TT_OK) { cleanup(); return s; }
+  if ((s = tt_plan_mttkrp(p, dA, nullptr)) != TT_OK) { cleanup(); return s; }
+  g_legacy_ms.store(tt_plan_last_ms(p));
+  if (cudaMemcpy(A->vals, dA, abytes, cudaMemcpyDeviceToHost) != cudaSuccess) {
+    tt_status e = set_error(TT_ERR_CUDA, "download A: %s", cudaGetErrorString(cudaGetLastError()));
+    cleanup();
+    return e;
+  }
+  cleanup();
+  return TT_OK;
+}
+
+TT_EXPORT tt_status tt_ttv_host(taco_tensor_t* y, const taco_tensor_t* B, const taco_tensor_t* x) {
+  clear_error();
+  if (!y || !B || !x || !y->vals || !x->vals) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
+  tt_plan* p = nullptr;
+  tt_status s = tt_plan_create(B, TT_OP_TTV, 1, TT_PREC_FP32, TT_SELECT_DEFAULT, 0, nullptr, &p);
+  if (s != TT_OK) return s;
+  const int64_t nx = B->dimensions[B->order - 1];
+  const int64_t ny = p->nfib_last;
+  if (y->dimensions && y->dimensions[0] < ny) { tt_plan_destroy(p); return set_error(TT_ERR_INVALID_ARGUMENT, "y has %d entries, need %lld", y->dimensions[0], (long long)ny); }
+  float *dx = nullptr, *dy = nullptr;
+  auto cleanup = [&]() { cudaFree(dx); cudaFree(dy); tt_plan_destroy(p); };
+  if (cudaMalloc((void**)&dx, sizeof(float) * (size_t)std::max<int64_t>(1, nx)) != cudaSuccess ||
+      cudaMalloc((void**)&dy, sizeof(float) * (size_t)std::max<int64_t>(1, ny)) != cudaSuccess) {
+    cleanup();
+    return set_error(TT_ERR_OUT_OF_MEMORY, "ttv buffers");
+  }
+  if (cudaMemcpy(dx, x->vals, sizeof(float) * (size_t)nx, cudaMemcpyHostToDevice) != cudaSuccess) { cleanup(); return set_error(TT_ERR_CUDA, "upload x"); }
+  tt_plan_set_timing(p, 1);
+  if ((s = tt_plan_ttv(p, dx, dy, nullptr)) != TT_OK) { cleanup(); return s; }
+  g_legacy_ms.store(tt_plan_last_ms(p));
+  if (cudaMemcpy(y->vals, dy, sizeof(float) * (size_t)ny, cudaMemcpyDeviceToHost) != cudaSuccess) { cleanup(); return set_error(TT_ERR_CUDA, "download y"); }
+  cleanup();
+  return TT_OK;
+}
+
+namespace tt {
+float legacy_last_ms() { return g_legacy_ms.load(); }
+}  // namespace tt
+
+TT_EXPORT const char* tt_last_error_string(void) { return tt::g_last_error_cstr(); }
+
+// ---------------------------------------------------------------------------
+// device buffers and timing for callers without CUDA bindings (ctypes, cgo)
+// ---------------------------------------------------------------------------
+TT_EXPORT tt_status tt_device_malloc(int64_t bytes, void** ptr) {
+  clear_error();
+  if (!ptr || bytes < 0) return set_error(TT_ERR_INVALID_ARGUMENT, "bad allocation request");
+  *ptr = nullptr;
+  CK(cudaMalloc(ptr, (size_t)std::max<int64_t>(bytes, 1)));
+  return TT_OK;
+}
+TT_EXPORT tt_status tt_device_free(void* ptr) {
+  clear_error();
+  CK(cudaFree(ptr));
+  return TT_OK;
+}
+TT_EXPORT tt_status tt_memcpy_htod(void* dst, const void* src, int64_t bytes) {
+  clear_error();
+  CK(cudaMemcpy(dst, src, (size_t)bytes, cudaMemcpyHostToDevice));
+  return TT_OK;
+}
+TT_EXPORT tt_status tt_memcpy_dtoh(void* dst, const void* src, int64_t bytes) {
+  clear_error();
+  CK(cudaMemcpy(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost));
+  return TT_OK;
+}
+TT_EXPORT tt_status tt_device_synchronize(void) {
+  clear_error();
+  CK(cudaDeviceSynchronize());
+  return TT_OK;
+}
+TT_EXPORT int32_t tt_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) { cudaGetLastError(); return 0; }
+  return n;
+}
+
+// Evict L2 between timed steps: write a buffer larger than the 129 MB L2.
+TT_EXPORT tt_status tt_l2_flush(void* stream) {
+  clear_error();
+  static void* buf = nullptr;
+  static const size_t bytes = (size_t)512 << 20;
+  static std::mutex mu;
+  {
+    std::lock_guard<std::mutex> g(mu);
+    if (!buf) CK(cudaMalloc(&buf, bytes));
+  }
+  CK(cudaMemsetAsync(buf, 0x5a, bytes, (cudaStream_t)stream));
+  return TT_OK;
+}
+
+// Milliseconds of the walk kernel alone in the last timed call (no partition, no clear).
+TT_EXPORT float tt_plan_last_kernel_ms(tt_plan* p) {
+  if (!p || !p->timed_pending || !p->evk0) return -1.f;
+  if (cudaEventSynchronize(p->ev1) != cudaSuccess) return -1.f;
+  float ms = -1.f;
+  cudaEventElapsedTime(&ms, p->evk0, p->evk1);
+  return ms;
+}

@@ -1,0 +1,66 @@
+// tt_plan.h -- the plan object behind the C ABI (host-only definitions).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <vector>
+#include "tt_internal.h"
+#include "tt_kernels.h"
+
+namespace tt {
+
+struct VariantSpec {
+  int id, tb, cpt, G;
+};
+VariantSpec variant_spec(int id);
+int variant_id(int tb, int G, int cpt);
+int rank_pad(int R);
+bool variant_valid(int id, int order, int rank, int prec);
+int default_variant(int order, int rank, int prec, int64_t nnz);
+float legacy_last_ms();
+
+}  // namespace tt
+
+struct tt_plan {
+  int device = 0;
+  tt_op op = TT_OP_MTTKRP;
+  int order = 0;
+  int32_t dims[TT_MAX_ORDER] = {0, 0, 0, 0};
+  int64_t count[TT_MAX_ORDER] = {0, 0, 0, 0};
+  int64_t nnz = 0, nroot = 0, nfib_last = 0;
+  bool dense_root = true;
+  int rank = 0, rp = 0, prec = 0;
+  cudaStream_t stream = nullptr;
+  // device CSF
+  int32_t* d_pos[TT_MAX_ORDER] = {nullptr, nullptr, nullptr, nullptr};
+  int32_t* d_crd[TT_MAX_ORDER] = {nullptr, nullptr, nullptr, nullptr};
+  void* d_vals = nullptr;
+  float vinv = 1.f;  // BF16 values: stored = value * (1/vinv)
+  std::vector<uint16_t> h_vals16;
+  // factors in storage precision
+  const void* fac[3] = {nullptr, nullptr, nullptr};
+  void* fac_own[3] = {nullptr, nullptr, nullptr};
+  float* d_scales = nullptr;    // per factor: colmax, scale, inv (rp each); then the output scale
+  float* d_colscale = nullptr;
+  bool factors_set = false;
+  // variant and scratch
+  int variant = -1, selected_by = 0;  // 0 heuristic/fixed, 1 model, 2 sweep
+  int tb = 0, cpt = 0, lpr = 0, G = 0, P = 0, nblocks = 0;
+  tt::WalkLauncher launcher = nullptr;
+  int32_t* d_part = nullptr;
+  float* d_carry = nullptr;
+  int32_t* d_tickets = nullptr;
+  int64_t scratch_blocks = 0;
+  float sweep_ms[64] = {};
+  // timing
+  bool timing = false, timed_pending = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
+  // bookkeeping
+  std::vector<void*> allocs;
+  int64_t device_bytes = 0;
+  tt_plan() { for (auto& m : sweep_ms) m = -1.f; }
+};
+
+namespace tt {
+// Learned selector: the variant the loaded model prefers for this plan, or -1.
+int selector_pick(const tt_plan* p, const taco_tensor_t* B);
+}

@@ -1,0 +1,33 @@
+// tt_walk_inst.cuh -- explicit instantiations of the MTTKRP walk kernel for one
+// (order, precision), included by tt_walk_o{3,4}_{fp32,bf16,bf16f}.cu with
+// TT_ORDER, TT_PREC and TT_LOOKUP defined.  The (columns per lane, lanes per row)
+// pairs cover factor ranks 8, 16, 32 and 64.
+#include "tt_mttkrp.cuh"
+#include "tt_kernels.h"
+
+namespace tt {
+namespace {
+template <int CPT, int LPR>
+cudaError_t launch_walk(const WalkArgs& a, int grid, int tb, size_t smem, cudaStream_t s) {
+  auto k = mttkrp_walk_kernel<TT_ORDER, TT_PREC, CPT, LPR>;
+  static size_t configured = 48 * 1024;
+  if (smem > configured) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = smem;
+  }
+  k<<<grid, tb, smem, s>>>(a);
+  return cudaGetLastError();
+}
+}  // namespace
+
+WalkLauncher TT_LOOKUP(int cpt, int lpr) {
+#define TT_CASE(C, L) if (cpt == C && lpr == L) return &launch_walk<C, L>;
+  TT_CASE(1, 8) TT_CASE(2, 4) TT_CASE(4, 2) TT_CASE(8, 1)     // rank 8
+  TT_CASE(1, 16) TT_CASE(2, 8) TT_CASE(4, 4) TT_CASE(8, 2)    // rank 16
+  TT_CASE(1, 32) TT_CASE(2, 16) TT_CASE(4, 8) TT_CASE(8, 4)   // rank 32
+  TT_CASE(2, 32) TT_CASE(4, 16) TT_CASE(8, 8)                 // rank 64
+#undef TT_CASE
+  return nullptr;
+}
+}  // namespace tt

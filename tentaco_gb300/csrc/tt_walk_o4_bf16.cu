@@ -1,0 +1,5 @@
+// MTTKRP walk kernels, order 4, storage bf16.
+#define TT_ORDER 4
+#define TT_PREC kBF16
+#define TT_LOOKUP walk_launcher_o4_bf16
+#include "tt_walk_inst.cuh"

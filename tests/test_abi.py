@@ -1,0 +1,97 @@
+"""The C-ABI library loads and exports every symbol its headers declare.
+
+No compute calls here: this runs on hosts without a GPU.
+"""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import tentaco_gb300 as tt
+
+INC = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "tentaco")
+
+
+def declared_functions():
+    names = set()
+    for h in ("tentaco.h", "tentaco_gen.h"):
+        src = open(os.path.join(INC, h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"\b(tt_[a-z0-9_]+)\s*\(", src))
+    names |= {"get_gpu_timer_result", "ttv_csf_gpu_taco"}
+    names |= set(tt.legacy_names())
+    return sorted(names)
+
+
+def exported():
+    out = subprocess.run(["nm", "-D", "--defined-only", tt.LIB_PATH], capture_output=True, text=True, check=True)
+    return {line.split()[-1] for line in out.stdout.splitlines() if " T " in line}
+
+
+def test_library_loads():
+    assert tt.lib().tt_abi_version() == 1
+
+
+def test_every_declared_symbol_is_exported():
+    syms = exported()
+    missing = [n for n in declared_functions() if n not in syms]
+    assert not missing, missing
+
+
+def test_reference_cxx_linkage_names_are_exported():
+    # objects compiled against the reference's gpu_kernels.cuh link to mangled names
+    syms = exported()
+    for name in ["mttkrp_gpu_taco", "mttkrp_32_eb_sr_512_4_1", "mttkrp_32_eb_pr_256_64_32_manual"]:
+        mangled = f"_Z{len(name)}{name}P13taco_tensor_tS0_S0_S0_"
+        assert mangled in syms, mangled
+    assert "_Z16ttv_csf_gpu_tacoP13taco_tensor_tS0_S0_" in syms
+    assert "_Z20get_gpu_timer_resultv" in syms
+
+
+def test_legacy_names_cover_reference_header():
+    # every unique entry point of gpu_kernels.cuh:4-73 (67 MTTKRP names)
+    names = tt.legacy_names()
+    assert len(names) == len(set(names)) == 67
+    assert "mttkrp_gpu_taco" in names and "mttkrp_64_eb_pr_256_32_32" in names
+
+
+def test_status_strings():
+    L = tt.lib()
+    assert L.tt_status_string(0) == b"TT_OK"
+    assert L.tt_status_string(2) == b"TT_ERR_INVALID_CSF"
+
+
+def test_variant_table():
+    assert tt.num_variants() == 40
+    for order in (3, 4):
+        for rank in (1, 8, 10, 16, 20, 32, 40, 64):
+            for prec in ("fp32", "bf16", "bf16f"):
+                v = tt.default_variant(order, rank, prec)
+                assert v >= 0 and tt.variant_valid(v, order, rank, prec)
+    info = tt.variant_info(tt.default_variant(3, 32, "fp32"))
+    assert info["threads"] in (256, 512) and info["cols_per_lane"] == 4
+
+
+def test_invalid_csf_rejected_before_device_use():
+    # pos not monotone: rejected by validation, whether or not a GPU exists
+    lv = [None, (np.array([0, 2, 1], np.int32), np.array([0, 1], np.int32)),
+          (np.array([0, 1, 2], np.int32), np.array([0, 1], np.int32))]
+    B = tt.HostTaco((2, 2, 2), vals=np.ones(2, np.float32), levels=lv)
+    with pytest.raises(tt.TTError) as e:
+        tt.Plan(B, rank=8)
+    assert e.value.status == tt.TT_ERR_INVALID_CSF
+
+
+@pytest.mark.skipif(tt.device_count() > 0, reason="host has a GPU")
+def test_no_device_is_an_error_not_a_fallback():
+    lv = [None, (np.array([0, 1, 1], np.int32), np.array([0], np.int32)),
+          (np.array([0, 1], np.int32), np.array([1], np.int32))]
+    B = tt.HostTaco((2, 2, 2), vals=np.ones(1, np.float32), levels=lv)
+    with pytest.raises(tt.TTError) as e:
+        tt.Plan(B, rank=8)
+    assert e.value.status == tt.TT_ERR_NO_DEVICE
+    A = np.zeros((2, 8), np.float32)
+    with pytest.raises(tt.TTError):
+        tt.mttkrp_host(B, [np.ones((2, 8), np.float32), np.ones((2, 8), np.float32)])

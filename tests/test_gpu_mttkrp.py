@@ -1,0 +1,200 @@
+"""GPU parity of MTTKRP (3- and 4-mode) against the FP64 oracle and the golden vectors.
+
+Tolerances (stated per precision, against the FP64 oracle on the same
+FP32-representable inputs):
+  FP32 storage:  max|x-y| <= 2e-5 * max|y|  and  ||x-y||_F <= 1e-5 * ||y||_F
+  BF16 storage (values and/or factors rounded to 8-bit significands):
+                 ||x-y||_F <= 8e-3 * ||y||_F   and  max|x-y| <= 2e-2 * max|y|
+Index work (CSF, partition, row placement) is exact: an error there shows up
+as whole wrong rows, far outside these bounds.
+"""
+import numpy as np
+import pytest
+
+import tentaco_gb300 as tt
+from helpers import golden_csf, golden_files, host_taco, rel_errors, to_oracle
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FP32_MAX, FP32_FRO = 2e-5, 1e-5
+BF16_MAX, BF16_FRO = 2e-2, 8e-3
+
+
+def close(got, ref, prec="fp32"):
+    mx, fr = (FP32_MAX, FP32_FRO) if prec == "fp32" else (BF16_MAX, BF16_FRO)
+    amax = np.abs(ref).max() if ref.size else 0.0
+    err = np.abs(got.astype(np.float64) - ref).max() if ref.size else 0.0
+    e = rel_errors(got, ref)
+    assert err <= mx * max(amax, 1e-30) + 1e-30, (err, amax, e)
+    assert e["fro"] <= fr or np.linalg.norm(ref) == 0, e
+    return e
+
+
+def run_plan(B, factors, prec="fp32", select=tt.SELECT_DEFAULT, variant=0, reps=1):
+    R = factors[0].shape[1]
+    plan = tt.Plan(B, rank=R, prec=prec, select=select, variant=variant)
+    bufs = [tt.DeviceBuffer.from_array(f.astype(np.float32)) for f in factors]
+    plan.set_factors(bufs)
+    A = tt.DeviceBuffer(B.dims[0] * R * 4)
+    outs = []
+    for _ in range(reps):
+        plan.mttkrp(A)
+        outs.append(A.to_array((B.dims[0], R)))
+    return outs if reps > 1 else outs[0], plan
+
+
+@pytest.mark.parametrize("path", golden_files("mttkrp"), ids=lambda p: p.split("/")[-1])
+def test_golden_vectors(path):
+    z = np.load(path)
+    csf = golden_csf(z)
+    facs = [z[f"F{m}"].astype(np.float32) for m in range(1, int(z["order"]))]
+    B = host_taco(csf)
+    got, _ = run_plan(B, facs)
+    close(got, z["A"])
+    got2 = tt.mttkrp_host(B, facs)
+    close(got2, z["A"])
+    assert np.array_equal(got, got2)
+
+
+@pytest.fixture(scope="module")
+def c1():
+    """Config-1 shape: 1024^3, 1,000,000 distinct uniform coordinates, U(0,1), R=32 U(0,1)."""
+    B = tt.gen_zipf((1024, 1024, 1024), (0, 0, 0), 1_000_000, seed=1)
+    C = tt.gen_dense(1024, 32, 0, 11)
+    D = tt.gen_dense(1024, 32, 0, 12)
+    ref = O.mttkrp(to_oracle(B), [C, D])
+    return B, [C, D], ref
+
+
+def test_c1_every_variant(c1):
+    B, facs, ref = c1
+    nvalid = 0
+    for v in range(tt.num_variants()):
+        if not tt.variant_valid(v, 3, 32, "fp32"):
+            continue
+        nvalid += 1
+        got, plan = run_plan(B, facs, select=tt.SELECT_FIXED, variant=v)
+        assert plan.variant == v
+        close(got, ref)
+    assert nvalid >= 30
+
+
+def test_c1_deterministic_and_tickets_reset(c1):
+    B, facs, ref = c1
+    outs, _ = run_plan(B, facs, reps=4)
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+    close(outs[-1], ref)
+
+
+@pytest.mark.parametrize("prec", ["bf16", "bf16f"])
+def test_c1_bf16_storage(c1, prec):
+    B, facs, ref = c1
+    got, _ = run_plan(B, facs, prec=prec)
+    e = close(got, ref, prec)
+    print(prec, e)
+
+
+@pytest.fixture(scope="module")
+def skewed():
+    """Zipf rows and fibers with empty slices; N(0,1) factors with per-column scales."""
+    B = tt.gen_zipf((3000, 2000, 5000), (1.2, 1.1, 0), 300_000, seed=21)
+    return B, to_oracle(B)
+
+
+@pytest.mark.parametrize("R", [1, 8, 10, 16, 20, 32, 40, 64])
+def test_ranks(skewed, R):
+    B, Oc = skewed
+    facs = [tt.gen_dense(2000, R, 1, 30 + R), tt.gen_dense(5000, R, 1, 60 + R)]
+    ref = O.mttkrp(Oc, facs)
+    for v in {tt.default_variant(3, R, "fp32"), tt.variant_valid(39, 3, R) and 39 or 0}:
+        if tt.variant_valid(v, 3, R):
+            got, _ = run_plan(B, facs, select=tt.SELECT_FIXED, variant=v)
+            close(got, ref)
+    got, _ = run_plan(B, facs, prec="bf16")
+    close(got, ref, "bf16")
+
+
+def test_long_fiber_spans_many_blocks():
+    # one fiber of 200k nonzeros (hundreds of blocks) between short rows
+    L = 200_000
+    rng = np.random.default_rng(4)
+    co = [np.array([[5, 3, l] for l in range(L)])]
+    co.append(np.stack([rng.integers(0, 20, 500), rng.integers(0, 10, 500), rng.integers(0, L, 500)], 1))
+    co = np.concatenate(co).astype(np.int32)
+    B = tt.csf_from_coo((20, 10, L), co, rng.random(len(co)).astype(np.float32))
+    facs = [tt.gen_dense(10, 32, 1, 1), tt.gen_dense(L, 32, 1, 2)]
+    ref = O.mttkrp(to_oracle(B), facs)
+    for v in (0, 17, 39):
+        got, _ = run_plan(B, facs, select=tt.SELECT_FIXED, variant=v)
+        close(got, ref)
+
+
+def test_edge_cases():
+    facs = [np.ones((4, 8), np.float32), np.ones((4, 8), np.float32)]
+    # empty tensor: all-zero output
+    B0 = tt.csf_from_coo((6, 4, 4), np.zeros((0, 3), np.int32), np.zeros(0, np.float32))
+    got, _ = run_plan(B0, facs)
+    assert np.array_equal(got, np.zeros((6, 8), np.float32))
+    # one nonzero in the last row
+    B1 = tt.csf_from_coo((6, 4, 4), np.array([[5, 2, 3]], np.int32), np.array([2.5], np.float32))
+    got, _ = run_plan(B1, facs)
+    exp = np.zeros((6, 8), np.float32)
+    exp[5] = 2.5
+    assert np.array_equal(got, exp)
+    # a single row holding everything, and empty leading/trailing rows
+    rng = np.random.default_rng(8)
+    co = np.stack([np.full(3000, 7), rng.integers(0, 50, 3000), rng.integers(0, 60, 3000)], 1).astype(np.int32)
+    B2 = tt.csf_from_coo((15, 50, 60), co, rng.random(3000).astype(np.float32))
+    f2 = [tt.gen_dense(50, 16, 0, 3), tt.gen_dense(60, 16, 0, 4)]
+    got, _ = run_plan(B2, f2)
+    close(got, O.mttkrp(to_oracle(B2), f2))
+
+
+def test_compressed_root_with_gaps():
+    # root listed as {pos=[0,3], crd=[2,5,9]} of 12 rows: unlisted rows stay zero
+    rng = np.random.default_rng(12)
+    dims = (12, 30, 40)
+    co = np.stack([rng.choice([2, 5, 9], 900), rng.integers(0, 30, 900), rng.integers(0, 40, 900)], 1)
+    Oc = O.build_csf(dims, co, rng.random(900))
+    facs = [tt.gen_dense(30, 32, 0, 5), tt.gen_dense(40, 32, 0, 6)]
+    ref = O.mttkrp(Oc, facs)
+    rows = np.array([2, 5, 9], np.int32)
+    p1 = np.concatenate([[0], np.cumsum(np.diff(Oc.pos[1])[rows])]).astype(np.int32)
+    lv = [(np.array([0, 3], np.int32), rows), (p1, Oc.crd[1].astype(np.int32)),
+          (Oc.pos[2].astype(np.int32), Oc.crd[2].astype(np.int32))]
+    B = tt.HostTaco(dims, vals=Oc.vals.astype(np.float32), levels=lv, dense_root=False)
+    got, _ = run_plan(B, facs)
+    close(got, ref)
+
+
+@pytest.fixture(scope="module")
+def c5_small():
+    """Config-5 shape family scaled to 2M nonzeros: 4-mode, Zipf(1.2) on modes 0 and 3."""
+    B = tt.gen_zipf((5000, 3000, 2000, 100000), (1.2, 0, 0, 1.2), 2_000_000, seed=5)
+    facs = [tt.gen_dense(d, 32, 1, 50 + m) for m, d in enumerate((3000, 2000, 100000))]
+    return B, facs, O.mttkrp(to_oracle(B), facs)
+
+
+def test_mttkrp4_variants(c5_small):
+    B, facs, ref = c5_small
+    for v in range(tt.num_variants()):
+        if tt.variant_valid(v, 4, 32, "fp32") and v % 3 == 0:
+            got, _ = run_plan(B, facs, select=tt.SELECT_FIXED, variant=v)
+            close(got, ref)
+    got, _ = run_plan(B, facs)
+    close(got, ref)
+    for prec in ("bf16", "bf16f"):
+        got, _ = run_plan(B, facs, prec=prec)
+        print(prec, close(got, ref, prec))
+
+
+def test_sweep_selects_a_timed_variant(c1):
+    B, facs, ref = c1
+    got, plan = run_plan(B, facs, select=tt.SELECT_SWEEP)
+    times = plan.sweep_times()
+    assert plan.selected_by == 2
+    timed = times[times > 0]
+    assert len(timed) >= 30 and times[plan.variant] == timed.min()
+    close(got, ref)
