@@ -46,11 +46,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--prec", default="bf16", choices=["fp32", "bf16", "bf16f"])
+    ap.add_argument("--prec", default="bf16", choices=["fp32", "bf16", "bf16f", "fp16"])
+    ap.add_argument("--compare", default="fp32,fp16",
+                    help="other storage precisions timed on the same tensor (comma list, '' for none)")
     ap.add_argument("--select", default="model", choices=["default", "model", "sweep"])
     ap.add_argument("--nnz", type=int, default=NNZ, help="smaller nonzero count for quick checks")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-errors", action="store_true")
     return ap.parse_args()
 
 
@@ -246,17 +249,17 @@ def run_gpu_arm(args, rank, world, d):
     kern = float(np.mean(kern_ms))
     value = world * flops / (ms_max * 1e-3) / 1e9
 
-    # plain FP32 kernel on the same tensor, for the BF16-vs-FP32 ratio
-    fp32_info = None
-    if args.prec != "fp32":
-        p32, A32, b32, s32, k32, _ = timed_plan("fp32", tt.SELECT_SWEEP)
-        fp32_info = {"ms_per_step": float(np.mean(s32)), "kernel_ms": float(np.mean(k32)),
-                     "gflops": flops / (np.mean(s32) * 1e-3) / 1e9, "variant": p32.variant}
-        Af32 = A32.to_array((B.dims[0], RANK))
-        del p32, A32, b32
+    # other storage precisions on the same tensor (plain FP32 gives the 16-bit speed-up)
+    others = {}
+    for prec in [x for x in args.compare.split(",") if x and x != args.prec]:
+        po, Ao, bo, so, ko, _ = timed_plan(prec, tt.SELECT_SWEEP if args.select != "default" else tt.SELECT_DEFAULT)
+        others[prec] = {"ms_per_step": float(np.mean(so)), "kernel_ms": float(np.mean(ko)),
+                        "gflops": flops / (np.mean(so) * 1e-3) / 1e9, "variant": po.variant,
+                        "_A": Ao.to_array((B.dims[0], RANK))}
+        del po, Ao, bo
 
-    s_v = 2 if args.prec == "bf16" else 4
-    s_f = 2 if args.prec in ("bf16", "bf16f") else 4
+    s_v = 2 if args.prec in ("bf16", "fp16") else 4
+    s_f = 2 if args.prec in ("bf16", "bf16f", "fp16") else 4
     cbytes, U1, U2 = compulsory_bytes(B, s_v, s_f)
     peak, peak_kind = peaks()
     achieved = cbytes / (kern * 1e-3) / 1e9
@@ -281,18 +284,20 @@ def run_gpu_arm(args, rank, world, d):
         "clocks": clocks,
         "gpu_launches": args.steps * 3,  # per step: partition, output clear (memset), walk kernel
     }
-    if fp32_info:
-        out["fp32_plain"] = fp32_info
-        out["speedup_vs_fp32"] = round(fp32_info["ms_per_step"] / ms, 3)
-
-    Ah = A.to_array((B.dims[0], RANK))
-    rows = check_rows(B)
-    out["error_vs_fp64"] = sample_errors(B, C, D, Ah, rows)
-    if fp32_info:
-        out["fp32_plain"]["error_vs_fp64"] = sample_errors(B, C, D, Af32, rows)
+    if "fp32" in others:
+        out["speedup_vs_fp32"] = round(others["fp32"]["ms_per_step"] / ms, 3)
+    if not args.no_errors:
+        Ah = A.to_array((B.dims[0], RANK))
+        rows = check_rows(B)
+        out["error_vs_fp64"] = sample_errors(B, C, D, Ah, rows)
+        for k, o in others.items():
+            o["error_vs_fp64"] = sample_errors(B, C, D, o["_A"], rows)
+    for o in others.values():
+        o.pop("_A", None)
+    out["compare"] = others
 
     if not args.no_e2e:
-        prec_map = {"fp32": 0, "bf16": 1, "bf16f": 2}
+        prec_map = {"fp32": 0, "bf16": 1, "bf16f": 2, "fp16": 3}
         e2e_ms = []
         for i in range(max(1, min(args.steps, 3)) + 1):
             t = time.perf_counter()
@@ -312,10 +317,12 @@ def run_gpu_arm(args, rank, world, d):
 
 
 def cpu_rows_sample(B, budget_nnz):
-    """A contiguous row range from the middle holding about budget_nnz nonzeros."""
+    """A contiguous row range holding about budget_nnz nonzeros (all rows if that covers the tensor)."""
     pos1 = B.pos(1)
     pos2 = B.pos(2)
     row_nnz_end = pos2[pos1]
+    if budget_nnz >= B.nnz:
+        return 0, B.dims[0], B.nnz
     start = int(np.searchsorted(row_nnz_end, B.nnz // 3))
     end = int(np.searchsorted(row_nnz_end, row_nnz_end[start] + budget_nnz))
     end = max(min(end, B.dims[0]), start + 1)
@@ -336,6 +343,8 @@ def cpu_baseline(B, C, D, budget_s=15.0, steps=1):
     O.mttkrp(sub, [Cd, Dd])
     per_nnz = (O.now_ms() - t) * 1e-3 / max(nz, 1)
     target = int(min(B.nnz, max(nz, budget_s / max(per_nnz, 1e-12) / max(steps, 1))))
+    if target >= 0.8 * B.nnz:
+        target = B.nnz
     s, e, nz = cpu_rows_sample(B, target)
     sub = _subtensor(B, pos1, s, e)
     times = []

@@ -56,7 +56,10 @@ typedef enum tt_precision {
   TT_PREC_FP32 = 0,        /* values and factors FP32, FP32 accumulation               */
   TT_PREC_BF16 = 1,        /* values and factors stored BF16 with power-of-two
                               per-column scales; FP32 accumulation, FP64 cross-block merge */
-  TT_PREC_BF16_FACTORS = 2 /* values FP32, factors BF16 (per-column scales)            */
+  TT_PREC_BF16_FACTORS = 2, /* values FP32, factors BF16 (per-column scales)           */
+  TT_PREC_FP16 = 3          /* values and factors stored FP16 with power-of-two per-column
+                               scales (column max in [2^14, 2^15)); FP32 accumulation.
+                               Same bytes as BF16 with an 11-bit significand.            */
 } tt_precision;
 
 typedef enum tt_select {

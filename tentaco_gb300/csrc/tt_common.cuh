@@ -11,10 +11,22 @@
 #include <cstdint>
 #include <type_traits>
 #include <cuda_runtime.h>
+#include <cuda_fp16.h>
 
 namespace tt {
 
-enum Prec : int { kFP32 = 0, kBF16 = 1, kBF16F = 2 };
+// Storage precisions: which of values / factors are held in 16 bits.
+//   kFP32  values FP32, factors FP32
+//   kBF16  values BF16, factors BF16 (power-of-two per-column scales)
+//   kBF16F values FP32, factors BF16
+//   kFP16  values FP16, factors FP16 (power-of-two per-column scales that put
+//          each column's max in [2^14, 2^15), so the 11-bit significand is used
+//          over the whole column and nothing overflows)
+enum Prec : int { kFP32 = 0, kBF16 = 1, kBF16F = 2, kFP16 = 3 };
+// Element kinds of one stored array.
+enum Kind : int { kF32 = 0, kB16 = 1, kH16 = 2 };
+__host__ __device__ constexpr int fac_kind(int prec) { return prec == kFP32 ? kF32 : (prec == kFP16 ? kH16 : kB16); }
+__host__ __device__ constexpr int val_kind(int prec) { return prec == kBF16 ? kB16 : (prec == kFP16 ? kH16 : kF32); }
 
 // ---------------------------------------------------------------------------
 // L2 cache policies (createpolicy, sm_80+).
@@ -87,55 +99,50 @@ __device__ __forceinline__ uint32_t ld_gather_2(const void* p, uint64_t pol) {
 __device__ __forceinline__ float bf16lo(uint32_t w) { return __uint_as_float(w << 16); }
 __device__ __forceinline__ float bf16hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
 
-// Load CPT consecutive factor entries starting at element offset `off` of a
-// row-major factor stored as FP32 (FT=float) or BF16 (FT=uint16_t), as floats.
-template <typename FT, int CPT>
-struct RowLoad;
+__device__ __forceinline__ float h16lo(uint32_t w) { return __half2float(__ushort_as_half((unsigned short)(w & 0xffffu))); }
+__device__ __forceinline__ float h16hi(uint32_t w) { return __half2float(__ushort_as_half((unsigned short)(w >> 16))); }
 
-template <int CPT>
-struct RowLoad<float, CPT> {
-  static __device__ __forceinline__ void load(const float* base, int64_t off, uint64_t pol,
-                                              float (&v)[CPT]) {
-    const float* p = base + off;
+template <int KIND>
+__device__ __forceinline__ float lo16(uint32_t w) { return KIND == kB16 ? bf16lo(w) : h16lo(w); }
+template <int KIND>
+__device__ __forceinline__ float hi16(uint32_t w) { return KIND == kB16 ? bf16hi(w) : h16hi(w); }
+
+// Load CPT consecutive entries starting at element offset `off` of a row-major
+// array stored as KIND, as floats (gather path: L2 evict_last).
+template <int KIND, int CPT>
+__device__ __forceinline__ void row_load(const void* base, int64_t off, uint64_t pol, float (&v)[CPT]) {
+  if constexpr (KIND == kF32) {
+    const float* p = static_cast<const float*>(base) + off;
     if constexpr (CPT == 8) {
       uint4 a = ld_gather_16(p, pol), b = ld_gather_16(p + 4, pol);
-      v[0] = __uint_as_float(a.x); v[1] = __uint_as_float(a.y);
-      v[2] = __uint_as_float(a.z); v[3] = __uint_as_float(a.w);
-      v[4] = __uint_as_float(b.x); v[5] = __uint_as_float(b.y);
-      v[6] = __uint_as_float(b.z); v[7] = __uint_as_float(b.w);
+      v[0] = __uint_as_float(a.x); v[1] = __uint_as_float(a.y); v[2] = __uint_as_float(a.z); v[3] = __uint_as_float(a.w);
+      v[4] = __uint_as_float(b.x); v[5] = __uint_as_float(b.y); v[6] = __uint_as_float(b.z); v[7] = __uint_as_float(b.w);
     } else if constexpr (CPT == 4) {
       uint4 a = ld_gather_16(p, pol);
-      v[0] = __uint_as_float(a.x); v[1] = __uint_as_float(a.y);
-      v[2] = __uint_as_float(a.z); v[3] = __uint_as_float(a.w);
+      v[0] = __uint_as_float(a.x); v[1] = __uint_as_float(a.y); v[2] = __uint_as_float(a.z); v[3] = __uint_as_float(a.w);
     } else if constexpr (CPT == 2) {
       uint2 a = ld_gather_8(p, pol);
       v[0] = __uint_as_float(a.x); v[1] = __uint_as_float(a.y);
     } else {
       v[0] = __uint_as_float(ld_gather_4(p, pol));
     }
-  }
-};
-
-template <int CPT>
-struct RowLoad<uint16_t, CPT> {
-  static __device__ __forceinline__ void load(const uint16_t* base, int64_t off, uint64_t pol,
-                                              float (&v)[CPT]) {
-    const uint16_t* p = base + off;
+  } else {
+    const uint16_t* p = static_cast<const uint16_t*>(base) + off;
     if constexpr (CPT == 8) {
       uint4 a = ld_gather_16(p, pol);
-      v[0] = bf16lo(a.x); v[1] = bf16hi(a.x); v[2] = bf16lo(a.y); v[3] = bf16hi(a.y);
-      v[4] = bf16lo(a.z); v[5] = bf16hi(a.z); v[6] = bf16lo(a.w); v[7] = bf16hi(a.w);
+      v[0] = lo16<KIND>(a.x); v[1] = hi16<KIND>(a.x); v[2] = lo16<KIND>(a.y); v[3] = hi16<KIND>(a.y);
+      v[4] = lo16<KIND>(a.z); v[5] = hi16<KIND>(a.z); v[6] = lo16<KIND>(a.w); v[7] = hi16<KIND>(a.w);
     } else if constexpr (CPT == 4) {
       uint2 a = ld_gather_8(p, pol);
-      v[0] = bf16lo(a.x); v[1] = bf16hi(a.x); v[2] = bf16lo(a.y); v[3] = bf16hi(a.y);
+      v[0] = lo16<KIND>(a.x); v[1] = hi16<KIND>(a.x); v[2] = lo16<KIND>(a.y); v[3] = hi16<KIND>(a.y);
     } else if constexpr (CPT == 2) {
       uint32_t a = ld_gather_4(p, pol);
-      v[0] = bf16lo(a); v[1] = bf16hi(a);
+      v[0] = lo16<KIND>(a); v[1] = hi16<KIND>(a);
     } else {
-      v[0] = bf16lo(ld_gather_2(p, pol));
+      v[0] = lo16<KIND>(ld_gather_2(p, pol));
     }
   }
-};
+}
 
 // Largest x in [lo, hi] with a[x] <= t, given a[lo] <= t (a non-decreasing).
 template <typename IdxT>

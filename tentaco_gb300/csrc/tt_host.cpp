@@ -93,11 +93,11 @@ tt_status csf_view(const taco_tensor_t* B, CsfView* v) {
   }
   v->count[0] = v->nroot;
   for (int l = 1; l < v->order; l++) {
-    if (!B->indices[l] || !B->indices[l][0] || (!B->indices[l][1] && v->count[l - 1] > 0))
-      return set_error(TT_ERR_INVALID_CSF, "level %d arrays missing", l);
+    if (!B->indices[l] || !B->indices[l][0]) return set_error(TT_ERR_INVALID_CSF, "level %d pos missing", l);
     v->pos[l] = B->indices[l][0];
     v->crd[l] = B->indices[l][1];
     v->count[l] = v->pos[l][v->count[l - 1]];
+    if (v->count[l] > 0 && !v->crd[l]) return set_error(TT_ERR_INVALID_CSF, "level %d crd missing", l);
   }
   v->nnz = v->count[v->order - 1];
   v->vals = B->vals;

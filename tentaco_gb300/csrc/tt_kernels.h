@@ -19,6 +19,8 @@ WalkLauncher walk_launcher_o3_bf16f(int cpt, int lpr);
 WalkLauncher walk_launcher_o4_fp32(int cpt, int lpr);
 WalkLauncher walk_launcher_o4_bf16(int cpt, int lpr);
 WalkLauncher walk_launcher_o4_bf16f(int cpt, int lpr);
+WalkLauncher walk_launcher_o3_fp16(int cpt, int lpr);
+WalkLauncher walk_launcher_o4_fp16(int cpt, int lpr);
 
 cudaError_t launch_partition(int order, const WalkArgs& a, cudaStream_t s);
 cudaError_t launch_ttv(const TtvArgs& a, int grid, int tb, size_t smem, cudaStream_t s);
@@ -26,11 +28,14 @@ cudaError_t launch_ttv_partition(const TtvArgs& a, cudaStream_t s);
 
 // Column max |x| of a rows x cols FP32 row-major matrix into colmax (cols floats, zeroed here).
 cudaError_t launch_colmax(const float* x, int64_t rows, int cols, float* colmax, cudaStream_t s);
-// scale[j] = 2^-floor(log2(colmax[j])) (1 where colmax is 0 or not finite); inv[j] = 1/scale[j].
-cudaError_t launch_pow2_scales(const float* colmax, int cols, float* scale, float* inv, cudaStream_t s);
-// dst (rows x rp, BF16 RNE) = src (rows x cols) * scale[col], zero for cols <= j < rp.
-cudaError_t launch_to_bf16(const float* src, int64_t rows, int cols, int rp, const float* scale,
-                           uint16_t* dst, cudaStream_t s);
+// scale[j] = 2^(target_exp - floor(log2(colmax[j]))) (1 where colmax is 0 or not finite);
+// inv[j] = 1/scale[j].  Both exact powers of two.
+cudaError_t launch_pow2_scales(const float* colmax, int cols, int target_exp, float* scale, float* inv,
+                               cudaStream_t s);
+// dst (rows x rp, 16-bit kind: 1 = BF16, 2 = FP16, round to nearest even) =
+// src (rows x cols) * scale[col], zero for cols <= j < rp.
+cudaError_t launch_to_16(const float* src, int64_t rows, int cols, int rp, const float* scale, int kind,
+                         uint16_t* dst, cudaStream_t s);
 // dst (rows x rp, FP32) = src (rows x cols), zero padded.
 cudaError_t launch_pad_fp32(const float* src, int64_t rows, int cols, int rp, float* dst, cudaStream_t s);
 // out[j] = prod_m inv_m[j] * vinv   (nm factor inverse-scale arrays, rp entries each)

@@ -1,5 +1,6 @@
 // tt_misc.cu -- partition, TTV and storage-conversion kernels of libtentaco_gb300.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include "tt_kernels.h"
 #include "tt_mttkrp.cuh"
 #include "tt_ttv.cuh"
@@ -11,10 +12,12 @@ WalkLauncher walk_launcher(int order, int prec, int cpt, int lpr) {
     if (prec == kFP32) return walk_launcher_o3_fp32(cpt, lpr);
     if (prec == kBF16) return walk_launcher_o3_bf16(cpt, lpr);
     if (prec == kBF16F) return walk_launcher_o3_bf16f(cpt, lpr);
+    if (prec == kFP16) return walk_launcher_o3_fp16(cpt, lpr);
   } else if (order == 4) {
     if (prec == kFP32) return walk_launcher_o4_fp32(cpt, lpr);
     if (prec == kBF16) return walk_launcher_o4_bf16(cpt, lpr);
     if (prec == kBF16F) return walk_launcher_o4_bf16f(cpt, lpr);
+    if (prec == kFP16) return walk_launcher_o4_fp16(cpt, lpr);
   }
   return nullptr;
 }
@@ -71,48 +74,50 @@ cudaError_t launch_colmax(const float* x, int64_t rows, int cols, float* colmax,
   return cudaGetLastError();
 }
 
-__global__ void pow2_scales_kernel(const float* colmax, int cols, float* scale, float* inv) {
+__global__ void pow2_scales_kernel(const float* colmax, int cols, int target_exp, float* scale, float* inv) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= cols) return;
   const uint32_t bits = __float_as_uint(colmax[j]);
   const int ex = (int)((bits >> 23) & 0xff);  // biased exponent of the column max
   float sc = 1.f, iv = 1.f;
   if (ex != 0 && ex != 0xff) {
-    // column max in [2^E, 2^(E+1)), E = ex - 127: scale = 2^-E puts it in [1, 2),
-    // inv = 2^E undoes it.  Both are exact powers of two in FP32.
-    const int es = 254 - ex;  // biased exponent of 2^-E
-    if (es >= 1 && es <= 254) {
+    // column max in [2^E, 2^(E+1)), E = ex - 127: scale = 2^(T-E) puts it in
+    // [2^T, 2^(T+1)), inv = 2^(E-T) undoes it.  Both exact powers of two in FP32.
+    const int es = 127 + target_exp - (ex - 127);  // biased exponent of 2^(T-E)
+    const int ei = ex - target_exp;                 // biased exponent of 2^(E-T)
+    if (es >= 1 && es <= 254 && ei >= 1 && ei <= 254) {
       sc = __uint_as_float((uint32_t)es << 23);
-      iv = __uint_as_float((uint32_t)ex << 23);
+      iv = __uint_as_float((uint32_t)ei << 23);
     }
   }
   scale[j] = sc;
   inv[j] = iv;
 }
 
-cudaError_t launch_pow2_scales(const float* colmax, int cols, float* scale, float* inv, cudaStream_t s) {
-  pow2_scales_kernel<<<(cols + 63) / 64, 64, 0, s>>>(colmax, cols, scale, inv);
+cudaError_t launch_pow2_scales(const float* colmax, int cols, int target_exp, float* scale, float* inv,
+                               cudaStream_t s) {
+  pow2_scales_kernel<<<(cols + 63) / 64, 64, 0, s>>>(colmax, cols, target_exp, scale, inv);
   return cudaGetLastError();
 }
 
-__global__ void to_bf16_kernel(const float* __restrict__ src, int64_t rows, int cols, int rp,
-                               const float* __restrict__ scale, __nv_bfloat16* __restrict__ dst) {
+__global__ void to_16_kernel(const float* __restrict__ src, int64_t rows, int cols, int rp,
+                             const float* __restrict__ scale, int kind, uint16_t* __restrict__ dst) {
   const int64_t n = rows * rp;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = i / rp;
     const int j = (int)(i - r * rp);
     const float v = j < cols ? src[r * cols + j] * (scale ? scale[j] : 1.f) : 0.f;
-    dst[i] = __float2bfloat16_rn(v);
+    dst[i] = kind == 2 ? __half_as_ushort(__float2half_rn(v)) : __bfloat16_as_ushort(__float2bfloat16_rn(v));
   }
 }
 
-cudaError_t launch_to_bf16(const float* src, int64_t rows, int cols, int rp, const float* scale,
-                           uint16_t* dst, cudaStream_t s) {
+cudaError_t launch_to_16(const float* src, int64_t rows, int cols, int rp, const float* scale, int kind,
+                         uint16_t* dst, cudaStream_t s) {
   const int64_t n = rows * rp;
   if (n == 0) return cudaSuccess;
   int64_t grid = (n + 255) / 256;
   if (grid > 152 * 32) grid = 152 * 32;
-  to_bf16_kernel<<<(int)grid, 256, 0, s>>>(src, rows, cols, rp, scale, reinterpret_cast<__nv_bfloat16*>(dst));
+  to_16_kernel<<<(int)grid, 256, 0, s>>>(src, rows, cols, rp, scale, kind, dst);
   return cudaGetLastError();
 }
 

@@ -26,8 +26,12 @@
 // Data layout in HBM (owned by the plan): int32 pos/crd per level, values FP32 or
 // BF16, factors row-major with RP = CPT*LPR entries per row (FP32 or BF16), every
 // stream padded with zeros to a multiple of 16 entries so 128-bit loads never read
-// past the end.  Dynamic shared memory holds the block's window of last-level
-// fiber boundaries (staged with coalesced loads) and the merge scratch.
+// past the end.  Dynamic shared memory holds the block's tile of coordinates and
+// values and its window of last-level fiber boundaries, both staged with
+// coalesced 128-bit loads (evict_first in L2), and the merge scratch.  The walk
+// then reads only shared memory and the factor rows; the factor-row gathers of
+// the next four nonzeros are issued before the current four are consumed, and
+// the next fiber's factor row is requested when the current fiber starts.
 #pragma once
 #include "tt_common.cuh"
 
@@ -62,9 +66,13 @@ struct Summ {
 };
 
 // Bytes of dynamic shared memory a launch needs.
-__host__ __device__ inline size_t walk_smem_bytes(int P, int tb, int rp) {
+__host__ __device__ inline size_t walk_tile_bytes(int P, int vbytes) {
+  return (size_t)P * 4 + (((size_t)P * vbytes + 15) & ~(size_t)15);  // crd + vals tile
+}
+__host__ __device__ inline size_t walk_smem_bytes(int P, int tb, int rp, int vbytes) {
   size_t nw = (size_t)tb / 32;
-  size_t b = (size_t)(2 * P + 4) * sizeof(int32_t);   // fiber window
+  size_t b = walk_tile_bytes(P, vbytes);
+  b += (size_t)(2 * P + 4) * sizeof(int32_t);         // fiber window
   b += nw * 2 * sizeof(int32_t);                      // warp summary rows
   b += nw * 2 * (size_t)rp * sizeof(float);           // warp summary accs
   b = (b + 15) & ~(size_t)15;
@@ -76,8 +84,11 @@ __host__ __device__ inline size_t walk_smem_bytes(int P, int tb, int rp) {
 template <int ORDER, int PREC, int CPT, int LPR>
 struct Walk {
   static constexpr int RP = CPT * LPR;
-  using FT = typename std::conditional<PREC == kFP32, float, uint16_t>::type;
-  using VT = typename std::conditional<PREC == kBF16, uint16_t, float>::type;
+  static constexpr int FK = fac_kind(PREC);
+  static constexpr int VK = val_kind(PREC);
+  static constexpr int VB = VK == kF32 ? 4 : 2;  // bytes per stored value
+  // gathers of the next chunk in flight while the current one is consumed
+  static constexpr bool PIPE = CPT <= 4;
 
   const WalkArgs& a;
   int q;
@@ -104,18 +115,28 @@ struct Walk {
     }
   }
 
-  __device__ __forceinline__ void load_vals4(int64_t p, uint64_t pol, float (&v)[4]) const {
-    if constexpr (PREC == kBF16) {
-      uint2 w = ld_stream_u2(static_cast<const uint16_t*>(a.vals) + p, pol);
-      v[0] = bf16lo(w.x); v[1] = bf16hi(w.x); v[2] = bf16lo(w.y); v[3] = bf16hi(w.y);
-    } else {
-      float4 w = ld_stream_f4(static_cast<const float*>(a.vals) + p, pol);
+  // Four coordinates and values of the staged tile (offset i, a multiple of 4).
+  __device__ __forceinline__ void tile4(const int32_t* s_lc, const unsigned char* s_val, int i,
+                                        int4& l4, float (&v)[4]) const {
+    l4 = *reinterpret_cast<const int4*>(s_lc + i);
+    if constexpr (VK == kF32) {
+      const float4 w = *reinterpret_cast<const float4*>(reinterpret_cast<const float*>(s_val) + i);
       v[0] = w.x; v[1] = w.y; v[2] = w.z; v[3] = w.w;
+    } else {
+      const uint2 w = *reinterpret_cast<const uint2*>(reinterpret_cast<const uint16_t*>(s_val) + i);
+      v[0] = lo16<VK>(w.x); v[1] = hi16<VK>(w.x); v[2] = lo16<VK>(w.y); v[3] = hi16<VK>(w.y);
     }
   }
 
   __device__ __forceinline__ void frow(int m, int64_t row, uint64_t pol, float (&v)[CPT]) const {
-    RowLoad<FT, CPT>::load(static_cast<const FT*>(a.fac[m]), row * RP + q * CPT, pol, v);
+    row_load<FK, CPT>(a.fac[m], row * RP + q * CPT, pol, v);
+  }
+
+  __device__ __forceinline__ void gather4(const int4& l4, uint64_t pol, float (&g)[4][CPT]) const {
+    frow(ORDER - 2, l4.x, pol, g[0]);
+    frow(ORDER - 2, l4.y, pol, g[1]);
+    frow(ORDER - 2, l4.z, pol, g[2]);
+    frow(ORDER - 2, l4.w, pol, g[3]);
   }
 
   // Combine summary Y (to the right) into X, storing rows that become complete.
@@ -160,101 +181,6 @@ struct Walk {
     }
   }
 
-  // Serial walk of nonzeros [s, e) of this block by one team.
-  __device__ __forceinline__ void walk(int64_t s, int64_t e, const int32_t* s_pos,
-                                       const int32_t* s_crd, int W, int64_t fs,
-                                       const int32_t* pb, const int32_t* pn,
-                                       Summ<CPT>& X) const {
-    const uint64_t polF = policy_evict_first();
-    const uint64_t polL = policy_evict_last();
-    const int32_t* pos1 = a.pos[1];
-    const int32_t* nzcrd = a.crd[ORDER - 1];
-
-    int x = (int)search_le(s_pos, 0, W - 1, s);
-    int64_t fend = s_pos[x + 1];
-    int64_t f1 = 0, kend = 0;  // order 4: level-1 fiber and its end (in level-2 fibers)
-    int ip;
-    float crow[CPT], drow[CPT];
-    if constexpr (ORDER == 3) {
-      ip = (int)search_le(pos1, pb[0], pn[0], fs + x);
-      frow(0, s_crd[x], polL, crow);
-    } else {
-      f1 = search_le(a.pos[2], pb[1], pn[1], fs + x);
-      kend = a.pos[2][f1 + 1];
-      ip = (int)search_le(pos1, pb[0], pn[0], f1);
-      frow(0, a.crd[1][f1], polL, crow);
-      frow(1, s_crd[x], polL, drow);
-    }
-    int64_t rend = pos1[ip + 1];
-
-    float f3[CPT], f2[CPT], ra[CPT];
-#pragma unroll
-    for (int c = 0; c < CPT; c++) { f3[c] = 0.f; f2[c] = 0.f; ra[c] = 0.f; }
-    bool flushed = false;
-
-    for (int64_t p = s; p < e; p += 4) {
-      const int4 l4 = ld_stream_i4(nzcrd + p, polF);
-      float v4[4];
-      load_vals4(p, polF, v4);
-      float g[4][CPT];
-      frow(ORDER - 2, l4.x, polL, g[0]);
-      frow(ORDER - 2, l4.y, polL, g[1]);
-      frow(ORDER - 2, l4.z, polL, g[2]);
-      frow(ORDER - 2, l4.w, polL, g[3]);
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const int64_t pp = p + u;
-        if (pp < e) {
-          while (pp >= fend) {
-            // the last-level fiber ended: fold it into its parent
-            if constexpr (ORDER == 3) {
-#pragma unroll
-              for (int c = 0; c < CPT; c++) { ra[c] = fmaf(f3[c], crow[c], ra[c]); f3[c] = 0.f; }
-            } else {
-#pragma unroll
-              for (int c = 0; c < CPT; c++) { f2[c] = fmaf(f3[c], drow[c], f2[c]); f3[c] = 0.f; }
-            }
-            x++;
-            fend = s_pos[x + 1];
-            const int64_t fg = fs + x;
-            if constexpr (ORDER == 4) {
-              while (fg >= kend) {
-#pragma unroll
-                for (int c = 0; c < CPT; c++) { ra[c] = fmaf(f2[c], crow[c], ra[c]); f2[c] = 0.f; }
-                f1++;
-                kend = a.pos[2][f1 + 1];
-                while (f1 >= rend) { flush(ip, ra, flushed, X); ip++; rend = pos1[ip + 1]; }
-                frow(0, a.crd[1][f1], polL, crow);
-              }
-              frow(1, s_crd[x], polL, drow);
-            } else {
-              while (fg >= rend) { flush(ip, ra, flushed, X); ip++; rend = pos1[ip + 1]; }
-              frow(0, s_crd[x], polL, crow);
-            }
-          }
-#pragma unroll
-          for (int c = 0; c < CPT; c++) f3[c] = fmaf(v4[u], g[u][c], f3[c]);
-        }
-      }
-    }
-    if constexpr (ORDER == 3) {
-#pragma unroll
-      for (int c = 0; c < CPT; c++) ra[c] = fmaf(f3[c], crow[c], ra[c]);
-    } else {
-#pragma unroll
-      for (int c = 0; c < CPT; c++) { f2[c] = fmaf(f3[c], drow[c], f2[c]); ra[c] = fmaf(f2[c], crow[c], ra[c]); }
-    }
-    if (!flushed) {
-      X.h = ip; X.t = kNone;
-#pragma unroll
-      for (int c = 0; c < CPT; c++) X.ha[c] = ra[c];
-    } else {
-      X.t = ip;
-#pragma unroll
-      for (int c = 0; c < CPT; c++) X.ta[c] = ra[c];
-    }
-  }
-
   // A row ended inside the walk: the first one is the team's head (maybe
   // partial), later ones started and ended inside the team's range.
   __device__ __forceinline__ void flush(int ip, float (&ra)[CPT], bool& flushed, Summ<CPT>& X) const {
@@ -268,6 +194,120 @@ struct Walk {
     }
 #pragma unroll
     for (int c = 0; c < CPT; c++) ra[c] = 0.f;
+  }
+
+  // Serial walk of nonzeros [s, e) of the block (tile offsets relative to bstart).
+  __device__ __forceinline__ void walk(int64_t s, int64_t e, int64_t bstart, const int32_t* s_lc,
+                                       const unsigned char* s_val, const int32_t* s_pos,
+                                       const int32_t* s_fcrd, int W, int64_t fs, const int32_t* pb,
+                                       const int32_t* pn, Summ<CPT>& X) const {
+    const uint64_t polL = policy_evict_last();
+    const int32_t* pos1 = a.pos[1];
+
+    int x = (int)search_le(s_pos, 0, W - 1, s);
+    int64_t fend = s_pos[x + 1];
+    int64_t f1 = 0, kend = 0;  // order 4: level-1 fiber and its end (in level-2 fibers)
+    int ip;
+    // cur: factor row of the current window fiber; nxt: of the next one (prefetched)
+    float cur[CPT], nxt[CPT], crow[CPT];
+    if constexpr (ORDER == 3) {
+      ip = (int)search_le(pos1, pb[0], pn[0], fs + x);
+    } else {
+      f1 = search_le(a.pos[2], pb[1], pn[1], fs + x);
+      kend = a.pos[2][f1 + 1];
+      ip = (int)search_le(pos1, pb[0], pn[0], f1);
+      frow(0, a.crd[1][f1], polL, crow);
+    }
+    frow(ORDER == 3 ? 0 : 1, s_fcrd[x], polL, cur);
+    if (x + 1 < W) frow(ORDER == 3 ? 0 : 1, s_fcrd[x + 1], polL, nxt);
+    int64_t rend = pos1[ip + 1];
+
+    float f3[CPT], f2[CPT], ra[CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; c++) { f3[c] = 0.f; f2[c] = 0.f; ra[c] = 0.f; }
+    bool flushed = false;
+
+    int4 l4;
+    float v4[4];
+    float g[4][CPT];
+    tile4(s_lc, s_val, (int)(s - bstart), l4, v4);
+    gather4(l4, polL, g);
+    for (int64_t p = s; p < e; p += 4) {
+      int4 ln;
+      float vn[4];
+      float gn[PIPE ? 4 : 1][CPT];
+      if constexpr (PIPE) {
+        if (p + 4 < e) {
+          tile4(s_lc, s_val, (int)(p + 4 - bstart), ln, vn);
+          gather4(ln, polL, gn);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int64_t pp = p + u;
+        if (pp < e) {
+          while (pp >= fend) {
+            // the last-level fiber ended: fold it into its parent
+            if constexpr (ORDER == 3) {
+#pragma unroll
+              for (int c = 0; c < CPT; c++) { ra[c] = fmaf(f3[c], cur[c], ra[c]); f3[c] = 0.f; }
+            } else {
+#pragma unroll
+              for (int c = 0; c < CPT; c++) { f2[c] = fmaf(f3[c], cur[c], f2[c]); f3[c] = 0.f; }
+            }
+            x++;
+            fend = s_pos[x + 1];
+            const int64_t fg = fs + x;
+            if constexpr (ORDER == 4) {
+              while (fg >= kend) {
+#pragma unroll
+                for (int c = 0; c < CPT; c++) { ra[c] = fmaf(f2[c], crow[c], ra[c]); f2[c] = 0.f; }
+                f1++;
+                kend = a.pos[2][f1 + 1];
+                while (f1 >= rend) { flush(ip, ra, flushed, X); ip++; rend = pos1[ip + 1]; }
+                frow(0, a.crd[1][f1], polL, crow);
+              }
+            } else {
+              while (fg >= rend) { flush(ip, ra, flushed, X); ip++; rend = pos1[ip + 1]; }
+            }
+#pragma unroll
+            for (int c = 0; c < CPT; c++) cur[c] = nxt[c];
+            if (x + 1 < W) frow(ORDER == 3 ? 0 : 1, s_fcrd[x + 1], polL, nxt);
+          }
+#pragma unroll
+          for (int c = 0; c < CPT; c++) f3[c] = fmaf(v4[u], g[u][c], f3[c]);
+        }
+      }
+      if constexpr (PIPE) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          v4[u] = vn[u];
+#pragma unroll
+          for (int c = 0; c < CPT; c++) g[u][c] = gn[u][c];
+        }
+      } else {
+        if (p + 4 < e) {
+          tile4(s_lc, s_val, (int)(p + 4 - bstart), l4, v4);
+          gather4(l4, polL, g);
+        }
+      }
+    }
+    if constexpr (ORDER == 3) {
+#pragma unroll
+      for (int c = 0; c < CPT; c++) ra[c] = fmaf(f3[c], cur[c], ra[c]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < CPT; c++) { f2[c] = fmaf(f3[c], cur[c], f2[c]); ra[c] = fmaf(f2[c], crow[c], ra[c]); }
+    }
+    if (!flushed) {
+      X.h = ip; X.t = kNone;
+#pragma unroll
+      for (int c = 0; c < CPT; c++) X.ha[c] = ra[c];
+    } else {
+      X.t = ip;
+#pragma unroll
+      for (int c = 0; c < CPT; c++) X.ta[c] = ra[c];
+    }
   }
 
   // First and one-past-last nonzero of root position r.
@@ -284,6 +324,7 @@ template <int ORDER, int PREC, int CPT, int LPR>
 __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant__ WalkArgs a) {
   using WK = Walk<ORDER, PREC, CPT, LPR>;
   constexpr int RP = WK::RP;
+  constexpr int VB = WK::VB;
   constexpr int TW = 32 / LPR;  // teams per warp
   extern __shared__ __align__(16) unsigned char smem[];
 
@@ -291,13 +332,15 @@ __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant_
   const int nw = tb / 32;
   const int b = blockIdx.x;
   const int P = a.P;
-  int32_t* s_pos = reinterpret_cast<int32_t*>(smem);
-  int32_t* s_crd = s_pos + (P + 2);
-  int32_t* s_wh = s_crd + (P + 2);
+  int32_t* s_lc = reinterpret_cast<int32_t*>(smem);
+  unsigned char* s_val = smem + (size_t)P * 4;
+  int32_t* s_pos = reinterpret_cast<int32_t*>(smem + walk_tile_bytes(P, VB));
+  int32_t* s_fcrd = s_pos + (P + 2);
+  int32_t* s_wh = s_fcrd + (P + 2);
   int32_t* s_wt = s_wh + nw;
   float* s_wha = reinterpret_cast<float*>(s_wt + nw);
   float* s_wta = s_wha + nw * RP;
-  size_t off = (size_t)(2 * P + 4) * 4 + (size_t)nw * 8 + (size_t)nw * 2 * RP * 4;
+  size_t off = walk_tile_bytes(P, VB) + (size_t)(2 * P + 4) * 4 + (size_t)nw * 8 + (size_t)nw * 2 * RP * 4;
   off = (off + 15) & ~(size_t)15;
   double* s_dbl = reinterpret_cast<double*>(smem + off);
   int32_t* s_ctl = reinterpret_cast<int32_t*>(s_dbl + tb);
@@ -307,14 +350,30 @@ __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant_
   const int64_t bstart = (int64_t)b * P;
   const int64_t bend = min(bstart + (int64_t)P, a.nnz);
 
-  // Stage the block's window of last-level fibers: boundaries and coordinates.
+  // Stage the block's coordinates and values (128-bit streaming loads; the
+  // arrays are padded so the rounded-up tail stays in bounds) and its window of
+  // last-level fibers.
   const int64_t fs = pb[ORDER - 2];
   const int W = (int)(pn[ORDER - 2] - fs + 1);
   {
+    const uint64_t polF = policy_evict_first();
+    const int n4 = (int)((bend - bstart + 3) >> 2);
+    const int32_t* gl = a.crd[ORDER - 1] + bstart;
+    for (int i = threadIdx.x; i < n4; i += tb)
+      reinterpret_cast<int4*>(s_lc)[i] = ld_stream_i4(gl + 4 * i, polF);
+    if constexpr (VB == 4) {
+      const float* gv = static_cast<const float*>(a.vals) + bstart;
+      for (int i = threadIdx.x; i < n4; i += tb)
+        reinterpret_cast<float4*>(s_val)[i] = ld_stream_f4(gv + 4 * i, polF);
+    } else {
+      const uint16_t* gv = static_cast<const uint16_t*>(a.vals) + bstart;
+      for (int i = threadIdx.x; i < n4; i += tb)
+        reinterpret_cast<uint2*>(s_val)[i] = ld_stream_u2(gv + 4 * i, polF);
+    }
     const int32_t* gpos = a.pos[ORDER - 1] + fs;
     const int32_t* gcrd = a.crd[ORDER - 2] + fs;
     for (int x = threadIdx.x; x <= W; x += tb) s_pos[x] = gpos[x];
-    for (int x = threadIdx.x; x < W; x += tb) s_crd[x] = gcrd[x];
+    for (int x = threadIdx.x; x < W; x += tb) s_fcrd[x] = gcrd[x];
   }
   __syncthreads();
 
@@ -328,7 +387,8 @@ __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant_
   X.h = kEmpty;
   X.t = kNone;
   const int64_t s = bstart + (int64_t)team * a.G;
-  if (s < bend) wk.walk(s, min(s + (int64_t)a.G, bend), s_pos, s_crd, W, fs, pb, pn, X);
+  if (s < bend)
+    wk.walk(s, min(s + (int64_t)a.G, bend), bstart, s_lc, s_val, s_pos, s_fcrd, W, fs, pb, pn, X);
 
   // Warp-level merge of team summaries (tree over teams, keyed by row).
 #pragma unroll

@@ -50,6 +50,8 @@ int variant_id(int tb, int G, int cpt) {
   return (ti * 5 + gi) * 4 + ci;
 }
 
+int val_bytes(int prec) { return val_kind(prec) == kF32 ? 4 : 2; }
+
 int rank_pad(int R) {
   if (R <= 8) return 8;
   if (R <= 16) return 16;
@@ -66,7 +68,7 @@ bool variant_valid(int id, int order, int rank, int prec) {
   if (lpr < 1 || lpr > 32) return false;
   // the block's fiber window and merge scratch must fit the 227 KB opt-in shared memory
   const int P = (v.tb / lpr) * v.G;
-  if (walk_smem_bytes(P, v.tb, rp) > (size_t)227 * 1024) return false;
+  if (walk_smem_bytes(P, v.tb, rp, val_bytes(prec)) > (size_t)227 * 1024) return false;
   return walk_launcher(order, prec, v.cpt, lpr) != nullptr;
 }
 
@@ -121,13 +123,6 @@ void dev_free(tt_plan* p, void* ptr) {
   cudaFree(ptr);
 }
 
-inline uint16_t f32_to_bf16_rne(float f) {
-  uint32_t u;
-  std::memcpy(&u, &f, 4);
-  if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40);  // NaN stays NaN
-  u += 0x7fffu + ((u >> 16) & 1u);
-  return (uint16_t)(u >> 16);
-}
 
 // 2^-floor(log2(m)) for m > 0 finite, else 1.
 float pow2_scale_for(float m) {
@@ -196,7 +191,7 @@ tt_status run_mttkrp(tt_plan* p, float* A, cudaStream_t st) {
   if (p->nnz == 0) return TT_OK;
   WalkArgs a = walk_args(p, A);
   CK(launch_partition(p->order, a, st));
-  const size_t smem = walk_smem_bytes(p->P, p->tb, p->rp);
+  const size_t smem = walk_smem_bytes(p->P, p->tb, p->rp, val_bytes(p->prec));
   if (p->timing) CK(cudaEventRecord(p->evk0, st));
   CK(p->launcher(a, p->nblocks, p->tb, smem, st));
   if (p->timing) CK(cudaEventRecord(p->evk1, st));
@@ -217,13 +212,13 @@ tt_status run_ttv(tt_plan* p, const float* x, float* y, cudaStream_t st) {
   a.part = p->d_part;
   a.carry = p->d_carry;
   a.tickets = p->d_tickets;
-  a.vscale = p->prec == kBF16 ? p->vinv : 1.f;
+  a.vscale = val_kind(p->prec) != kF32 ? p->vinv : 1.f;
   a.nnz = p->nnz;
   a.nfib = p->nfib_last;
   a.P = p->P;
   a.NPT = p->G;
   a.nblocks = p->nblocks;
-  a.vals_bf16 = p->prec == kBF16;
+  a.vals_kind = val_kind(p->prec);
   CK(launch_ttv_partition(a, st));
   if (p->timing) CK(cudaEventRecord(p->evk0, st));
   CK(launch_ttv(a, p->nblocks, p->tb, ttv_smem_bytes(p->P, p->tb), st));
@@ -294,7 +289,7 @@ TT_EXPORT tt_status tt_plan_create(const taco_tensor_t* B, tt_op op, int32_t ran
   } else if (op != TT_OP_TTV) {
     return set_error(TT_ERR_INVALID_ARGUMENT, "op %d", (int)op);
   }
-  if (prec != TT_PREC_FP32 && prec != TT_PREC_BF16 && prec != TT_PREC_BF16_FACTORS)
+  if (prec != TT_PREC_FP32 && prec != TT_PREC_BF16 && prec != TT_PREC_BF16_FACTORS && prec != TT_PREC_FP16)
     return set_error(TT_ERR_INVALID_ARGUMENT, "precision %d", (int)prec);
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -343,20 +338,32 @@ TT_EXPORT tt_status tt_plan_create(const taco_tensor_t* B, tt_op op, int32_t ran
   }
   {
     const size_t n = (size_t)pad16(v.nnz);
-    if (prec == TT_PREC_BF16) {
-      // values: power-of-two global scale, BF16 round-to-nearest-even
+    if (val_kind(p->prec) != kF32) {
+      // values: one power-of-two scale (max in [1,2) for BF16, [2^14,2^15) for FP16),
+      // converted on the device with round-to-nearest-even
       float vmax = 0.f;
+#pragma omp parallel for reduction(max : vmax)
       for (int64_t i = 0; i < v.nnz; i++) vmax = std::max(vmax, std::fabs(v.vals[i]));
-      const float sc = pow2_scale_for(vmax);
+      const float sc = pow2_scale_for(vmax) * (p->prec == kFP16 ? 16384.f : 1.f);
       p->vinv = 1.f / sc;
-      p->h_vals16.assign(n, 0);
-#pragma omp parallel for schedule(static)
-      for (int64_t i = 0; i < v.nnz; i++) p->h_vals16[(size_t)i] = f32_to_bf16_rne(v.vals[i] * sc);
       uint16_t* d = nullptr;
       if ((s = dev_alloc(p, &d, n)) != TT_OK) return fail(s);
       p->d_vals = d;
-      if (cudaMemcpyAsync(d, p->h_vals16.data(), n * 2, cudaMemcpyHostToDevice, st) != cudaSuccess)
-        return fail(set_error(TT_ERR_CUDA, "upload vals"));
+      if (cudaMemsetAsync(d, 0, n * 2, st) != cudaSuccess) return fail(set_error(TT_ERR_CUDA, "clear vals"));
+      if (v.nnz > 0) {
+        float* tmp = nullptr;
+        if (cudaMalloc((void**)&tmp, (size_t)v.nnz * 4 + 16) != cudaSuccess)
+          return fail(set_error(TT_ERR_OUT_OF_MEMORY, "value staging"));
+        float* dsc = reinterpret_cast<float*>(reinterpret_cast<char*>(tmp) + (size_t)v.nnz * 4);
+        dsc = reinterpret_cast<float*>(((uintptr_t)dsc + 3) & ~(uintptr_t)3);
+        cudaError_t e1 = cudaMemcpyAsync(tmp, v.vals, (size_t)v.nnz * 4, cudaMemcpyHostToDevice, st);
+        cudaError_t e2 = e1 == cudaSuccess ? cudaMemcpyAsync(dsc, &sc, 4, cudaMemcpyHostToDevice, st) : e1;
+        cudaError_t e3 = e2 == cudaSuccess ? launch_to_16(tmp, v.nnz, 1, 1, dsc, fac_kind(p->prec) == kH16 ? 2 : 1, d, st) : e2;
+        cudaError_t e4 = cudaStreamSynchronize(st);
+        cudaFree(tmp);
+        if (e3 != cudaSuccess || e4 != cudaSuccess)
+          return fail(set_error(TT_ERR_CUDA, "value conversion: %s", cudaGetErrorString(e3 != cudaSuccess ? e3 : e4)));
+      }
     } else {
       float* d = nullptr;
       if ((s = dev_alloc(p, &d, n)) != TT_OK) return fail(s);
@@ -401,8 +408,6 @@ TT_EXPORT tt_status tt_plan_create(const taco_tensor_t* B, tt_op op, int32_t ran
       return fail(set_error(TT_ERR_CUDA, "clear tickets"));
   }
   if (cudaStreamSynchronize(st) != cudaSuccess) return fail(set_error(TT_ERR_CUDA, "plan upload: %s", cudaGetErrorString(cudaGetLastError())));
-  p->h_vals16.clear();
-  p->h_vals16.shrink_to_fit();
   *out = p;
   return TT_OK;
 }
@@ -455,18 +460,19 @@ TT_EXPORT tt_status tt_plan_set_factors(tt_plan* p, const float* const* factors,
       float* iv = scl + p->rp;
       CK(cudaMemsetAsync(cmax, 0, sizeof(float) * p->rp, st));
       CK(launch_colmax(factors[m], rows, p->rank, cmax, st));
-      CK(launch_pow2_scales(cmax, p->rp, scl, iv, st));
+      const bool h16 = fac_kind(p->prec) == kH16;
+      CK(launch_pow2_scales(cmax, p->rp, h16 ? 14 : 0, scl, iv, st));
       if (!p->fac_own[m]) {
         uint16_t* d = nullptr;
         if ((s = dev_alloc(p, &d, (size_t)rows * p->rp)) != TT_OK) return s;
         p->fac_own[m] = d;
       }
-      CK(launch_to_bf16(factors[m], rows, p->rank, p->rp, scl, (uint16_t*)p->fac_own[m], st));
+      CK(launch_to_16(factors[m], rows, p->rank, p->rp, scl, h16 ? 2 : 1, (uint16_t*)p->fac_own[m], st));
       p->fac[m] = p->fac_own[m];
       inv[m] = iv;
     }
     p->d_colscale = p->d_scales + (size_t)(3 * nm) * p->rp;
-    CK(launch_scale_product(inv, nm, p->rp, p->prec == kBF16 ? p->vinv : 1.f, p->d_colscale, st));
+    CK(launch_scale_product(inv, nm, p->rp, val_kind(p->prec) != kF32 ? p->vinv : 1.f, p->d_colscale, st));
   }
   p->factors_set = true;
   return TT_OK;

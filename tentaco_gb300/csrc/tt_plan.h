@@ -14,6 +14,7 @@ struct VariantSpec {
 VariantSpec variant_spec(int id);
 int variant_id(int tb, int G, int cpt);
 int rank_pad(int R);
+int val_bytes(int prec);
 bool variant_valid(int id, int order, int rank, int prec);
 int default_variant(int order, int rank, int prec, int64_t nnz);
 float legacy_last_ms();
@@ -34,8 +35,7 @@ struct tt_plan {
   int32_t* d_pos[TT_MAX_ORDER] = {nullptr, nullptr, nullptr, nullptr};
   int32_t* d_crd[TT_MAX_ORDER] = {nullptr, nullptr, nullptr, nullptr};
   void* d_vals = nullptr;
-  float vinv = 1.f;  // BF16 values: stored = value * (1/vinv)
-  std::vector<uint16_t> h_vals16;
+  float vinv = 1.f;  // 16-bit values: stored = value * (1/vinv)
   // factors in storage precision
   const void* fac[3] = {nullptr, nullptr, nullptr};
   void* fac_own[3] = {nullptr, nullptr, nullptr};

@@ -37,7 +37,7 @@ struct TtvArgs {
   int32_t P;
   int32_t NPT;          // nonzeros per thread, multiple of 4
   int32_t nblocks;
-  int32_t vals_bf16;
+  int32_t vals_kind;    // kF32, kB16 or kH16
 };
 
 struct TSumm {
@@ -107,10 +107,14 @@ __global__ void __launch_bounds__(512) ttv_walk_kernel(const __grid_constant__ T
     for (int64_t p = s; p < e; p += 4) {
       const int4 l4 = ld_stream_i4(a.crd + p, polF);
       float v[4];
-      if (a.vals_bf16) {
+      if (a.vals_kind == kB16) {
         uint2 w = ld_stream_u2(static_cast<const uint16_t*>(a.vals) + p, polF);
         v[0] = bf16lo(w.x) * a.vscale; v[1] = bf16hi(w.x) * a.vscale;
         v[2] = bf16lo(w.y) * a.vscale; v[3] = bf16hi(w.y) * a.vscale;
+      } else if (a.vals_kind == kH16) {
+        uint2 w = ld_stream_u2(static_cast<const uint16_t*>(a.vals) + p, polF);
+        v[0] = h16lo(w.x) * a.vscale; v[1] = h16hi(w.x) * a.vscale;
+        v[2] = h16lo(w.y) * a.vscale; v[3] = h16hi(w.y) * a.vscale;
       } else {
         float4 w = ld_stream_f4(static_cast<const float*>(a.vals) + p, polF);
         v[0] = w.x; v[1] = w.y; v[2] = w.z; v[3] = w.w;

@@ -5,6 +5,8 @@ FP32-representable inputs):
   FP32 storage:  max|x-y| <= 2e-5 * max|y|  and  ||x-y||_F <= 1e-5 * ||y||_F
   BF16 storage (values and/or factors rounded to 8-bit significands):
                  ||x-y||_F <= 8e-3 * ||y||_F   and  max|x-y| <= 2e-2 * max|y|
+  FP16 storage with power-of-two column scales (11-bit significands):
+                 ||x-y||_F <= 1e-3 * ||y||_F   and  max|x-y| <= 3e-3 * max|y|
 Index work (CSF, partition, row placement) is exact: an error there shows up
 as whole wrong rows, far outside these bounds.
 """
@@ -19,10 +21,11 @@ pytestmark = pytest.mark.gpu
 
 FP32_MAX, FP32_FRO = 2e-5, 1e-5
 BF16_MAX, BF16_FRO = 2e-2, 8e-3
+FP16_MAX, FP16_FRO = 3e-3, 1e-3
 
 
 def close(got, ref, prec="fp32"):
-    mx, fr = (FP32_MAX, FP32_FRO) if prec == "fp32" else (BF16_MAX, BF16_FRO)
+    mx, fr = {"fp32": (FP32_MAX, FP32_FRO), "fp16": (FP16_MAX, FP16_FRO)}.get(prec, (BF16_MAX, BF16_FRO))
     amax = np.abs(ref).max() if ref.size else 0.0
     err = np.abs(got.astype(np.float64) - ref).max() if ref.size else 0.0
     e = rel_errors(got, ref)
@@ -88,8 +91,8 @@ def test_c1_deterministic_and_tickets_reset(c1):
     close(outs[-1], ref)
 
 
-@pytest.mark.parametrize("prec", ["bf16", "bf16f"])
-def test_c1_bf16_storage(c1, prec):
+@pytest.mark.parametrize("prec", ["bf16", "bf16f", "fp16"])
+def test_c1_16bit_storage(c1, prec):
     B, facs, ref = c1
     got, _ = run_plan(B, facs, prec=prec)
     e = close(got, ref, prec)
@@ -112,8 +115,9 @@ def test_ranks(skewed, R):
         if tt.variant_valid(v, 3, R):
             got, _ = run_plan(B, facs, select=tt.SELECT_FIXED, variant=v)
             close(got, ref)
-    got, _ = run_plan(B, facs, prec="bf16")
-    close(got, ref, "bf16")
+    for prec in ("bf16", "fp16"):
+        got, _ = run_plan(B, facs, prec=prec)
+        close(got, ref, prec)
 
 
 def test_long_fiber_spans_many_blocks():
@@ -185,7 +189,7 @@ def test_mttkrp4_variants(c5_small):
             close(got, ref)
     got, _ = run_plan(B, facs)
     close(got, ref)
-    for prec in ("bf16", "bf16f"):
+    for prec in ("bf16", "bf16f", "fp16"):
         got, _ = run_plan(B, facs, prec=prec)
         print(prec, close(got, ref, prec))
 

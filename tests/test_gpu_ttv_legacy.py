@@ -57,6 +57,8 @@ def test_ttv_c2_small(c2_small):
     assert np.array_equal(got, got2)
     e = close(run_ttv(B, x, prec="bf16"), ref, mx=2e-2, fr=8e-3)
     print("ttv bf16", e)
+    e = close(run_ttv(B, x, prec="fp16"), ref, mx=3e-3, fr=1e-3)
+    print("ttv fp16", e)
 
 
 def test_ttv_long_fiber():
