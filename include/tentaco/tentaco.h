@@ -130,6 +130,34 @@ tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
 /* y->vals (host) = TTV(B, x) over the last mode. */
 tt_status tt_ttv_host(taco_tensor_t* y, const taco_tensor_t* B, const taco_tensor_t* x);
 
+/* ---- allocation-free MTTKRP -------------------------------------------- */
+
+/*
+ * 3-mode mode-0 MTTKRP for callers that cannot allocate device memory (code
+ * inside a memory pool or arena it does not own, loops that must never enter
+ * the driver's allocator).  No counterpart in the reference: its entry points
+ * allocate and free device buffers on every call.
+ *
+ * Everything is a DEVICE pointer the caller owns: a dense-root CSF (pos1 has
+ * nrows+1 entries; pos2/crd1 one per level-1 fiber; crd2/vals nnz entries, no
+ * padding needed), FP32 factors C (dims[1] x rank) and D (dims[2] x rank), and
+ * the FP32 output A (nrows x rank, overwritten).  crd2, vals, C, D and A must
+ * be 16-byte aligned; the CSF must be valid (tt_csf_validate on the host copy).
+ * rank must be 8, 16, 32 or 64.  Limits: nrows <= 524,288 and
+ * nnz <= 16,777,216; larger inputs return TT_ERR_INVALID_ARGUMENT (use the
+ * plan API).  The call allocates nothing: its scratch is a fixed 6.3 MB device
+ * array that every GPU loading this library holds until the process exits.
+ * The first call on each device looks that array's address up (make it before
+ * any stream capture).  All calls share the array, so calls whose work
+ * overlaps on the GPU (different streams, or several host threads) race and
+ * must be serialised by the caller.
+ */
+tt_status tt_mttkrp3_noalloc(int32_t nrows, int64_t nnz, int32_t rank,
+                             const int32_t* pos1, const int32_t* crd1,
+                             const int32_t* pos2, const int32_t* crd2,
+                             const float* vals, const float* C, const float* D,
+                             float* A, void* stream);
+
 /* ---- variants ---------------------------------------------------------- */
 
 int32_t tt_num_variants(void);

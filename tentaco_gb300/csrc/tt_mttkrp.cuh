@@ -320,11 +320,15 @@ struct Walk {
 };
 
 #ifndef TT_ARGS_ONLY
-template <int ORDER, int PREC, int CPT, int LPR>
+// EXACT = true: the nonzero-level crd/vals arrays are read only up to nnz (the
+// caller's own unpadded arrays); false: the plan's padded copies are read in
+// whole 128-bit words.
+template <int ORDER, int PREC, int CPT, int LPR, bool EXACT = false>
 __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant__ WalkArgs a) {
   using WK = Walk<ORDER, PREC, CPT, LPR>;
   constexpr int RP = WK::RP;
   constexpr int VB = WK::VB;
+  static_assert(!EXACT || VB == 4, "exact-length staging is built for FP32 values");
   constexpr int TW = 32 / LPR;  // teams per warp
   extern __shared__ __align__(16) unsigned char smem[];
 
@@ -359,6 +363,22 @@ __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant_
     const uint64_t polF = policy_evict_first();
     const int n4 = (int)((bend - bstart + 3) >> 2);
     const int32_t* gl = a.crd[ORDER - 1] + bstart;
+    if constexpr (EXACT) {
+      // whole words below nnz, element loads (zero filled) for the ragged end
+      const int nt = (int)(bend - bstart);
+      for (int i = threadIdx.x; i < n4; i += tb) {
+        if (4 * i + 4 <= nt) {
+          reinterpret_cast<int4*>(s_lc)[i] = ld_stream_i4(gl + 4 * i, polF);
+          reinterpret_cast<float4*>(s_val)[i] = ld_stream_f4(static_cast<const float*>(a.vals) + bstart + 4 * i, polF);
+        } else {
+          for (int k = 0; k < 4; k++) {
+            const bool in = 4 * i + k < nt;
+            s_lc[4 * i + k] = in ? gl[4 * i + k] : 0;
+            reinterpret_cast<float*>(s_val)[4 * i + k] = in ? static_cast<const float*>(a.vals)[bstart + 4 * i + k] : 0.f;
+          }
+        }
+      }
+    } else {
     for (int i = threadIdx.x; i < n4; i += tb)
       reinterpret_cast<int4*>(s_lc)[i] = ld_stream_i4(gl + 4 * i, polF);
     if constexpr (VB == 4) {
@@ -369,6 +389,7 @@ __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant_
       const uint16_t* gv = static_cast<const uint16_t*>(a.vals) + bstart;
       for (int i = threadIdx.x; i < n4; i += tb)
         reinterpret_cast<uint2*>(s_val)[i] = ld_stream_u2(gv + 4 * i, polF);
+    }
     }
     const int32_t* gpos = a.pos[ORDER - 1] + fs;
     const int32_t* gcrd = a.crd[ORDER - 2] + fs;
