@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--compare", default="fp32,fp16",
                     help="other storage precisions timed on the same tensor (comma list, '' for none)")
     ap.add_argument("--select", default="model", choices=["default", "model", "sweep"])
+    ap.add_argument("--variant", type=int, default=-1, help="run this variant id (overrides --select)")
     ap.add_argument("--nnz", type=int, default=NNZ, help="smaller nonzero count for quick checks")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -212,10 +213,12 @@ def run_gpu_arm(args, rank, world, d):
     B, C, D = make_workload(args.nnz)
     gen_s = time.time() - t0
     sel = {"default": tt.SELECT_DEFAULT, "model": tt.SELECT_MODEL, "sweep": tt.SELECT_SWEEP}[args.select]
+    if args.variant >= 0:
+        sel = tt.SELECT_FIXED
     flops = 3.0 * B.nnz * RANK
 
     def timed_plan(prec, select):
-        plan = tt.Plan(B, rank=RANK, prec=prec, select=select)
+        plan = tt.Plan(B, rank=RANK, prec=prec, select=select, variant=max(args.variant, 0))
         if select == tt.SELECT_MODEL and plan.selected_by != 1:
             plan = tt.Plan(B, rank=RANK, prec=prec, select=tt.SELECT_SWEEP)
         bufs = [tt.DeviceBuffer.from_array(C), tt.DeviceBuffer.from_array(D)]
@@ -273,7 +276,7 @@ def run_gpu_arm(args, rank, world, d):
         "data": "synthetic (seeded lognormal-fiber tensor; FROSTT data absent)",
         "config": {"workload": WORKLOAD, "dims": list(DIMS), "nnz": B.nnz, "fibers": B.count(1), "rank": RANK,
                    "precision": args.prec, "select": args.select, "variant": plan.variant,
-                   "selected_by": ["heuristic", "model", "sweep"][plan.selected_by],
+                   "selected_by": "fixed" if args.variant >= 0 else ["heuristic", "model", "sweep"][plan.selected_by],
                    "l2": "flushed between steps (512 MB write)", "parallelism": f"replicas{world}",
                    "gen_s": round(gen_s, 1)},
         "gbs_compulsory": round(cbytes / (ms * 1e-3) / 1e9, 1),

@@ -78,6 +78,11 @@ typedef struct tt_variant_info {
   int32_t rank_pad;      /* rank this variant is compiled for (8,16,32,64)     */
   int32_t lanes_per_row; /* rank_pad / cols_per_lane                           */
   int32_t nnz_per_block; /* threads / lanes_per_row * nnz_per_team             */
+  int32_t staged;        /* 0: factor rows gathered into registers as the team
+                            walks; 1: every row of the block's tile gathered into
+                            shared memory (cp.async) before the walk; 2: each
+                            lane's factor-row pieces copied (cp.async) into its
+                            own shared-memory ring 8 nonzeros ahead of use     */
   char name[40];
 } tt_variant_info;
 
@@ -145,7 +150,7 @@ tt_status tt_ttv_host(taco_tensor_t* y, const taco_tensor_t* B, const taco_tenso
  * be 16-byte aligned; the CSF must be valid (tt_csf_validate on the host copy).
  * rank must be 8, 16, 32 or 64.  Limits: nrows <= 524,288 and
  * nnz <= 16,777,216; larger inputs return TT_ERR_INVALID_ARGUMENT (use the
- * plan API).  The call allocates nothing: its scratch is a fixed 6.3 MB device
+ * plan API).  The call allocates nothing: its scratch is a fixed 4.2 MB device
  * array that every GPU loading this library holds until the process exits.
  * The first call on each device looks that array's address up (make it before
  * any stream capture).  All calls share the array, so calls whose work

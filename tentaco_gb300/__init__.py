@@ -48,7 +48,7 @@ class TacoTensor(C.Structure):
 
 class VariantInfo(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("id", "threads", "cols_per_lane", "nnz_per_team", "rank_pad",
-                                         "lanes_per_row", "nnz_per_block")] + [("name", C.c_char * 40)]
+                                         "lanes_per_row", "nnz_per_block", "staged")] + [("name", C.c_char * 40)]
 
 
 class TTError(RuntimeError):
@@ -93,6 +93,7 @@ def lib():
         "tt_plan_num_fibers": (C.c_int64, [_P, C.c_int32]),
         "tt_plan_device_bytes": (C.c_int64, [_P]),
         "tt_plan_nblocks": (C.c_int32, [_P]),
+        "tt_plan_device_error": (C.c_int32, [_P]),
         "tt_plan_use_variant": (S, [_P, C.c_int32]),
         "tt_plan_sweep_times": (S, [_P, C.POINTER(C.c_float), C.c_int32]),
         "tt_mttkrp_host": (S, [_TP, _TP, C.POINTER(_TP), S, S, C.c_int32]),
@@ -380,6 +381,9 @@ class Plan:
     @property
     def selected_by(self) -> int:
         return int(lib().tt_plan_selected_by(self.ptr))
+
+    def device_error(self) -> int:
+        return int(lib().tt_plan_device_error(self.ptr))
 
     @property
     def nblocks(self) -> int:

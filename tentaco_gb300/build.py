@@ -29,6 +29,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
                      "-Xcompiler", "-fPIC,-fopenmp,-fvisibility=hidden", "-I" + INCLUDE]
+# TT_CHECKED=1: device-side bounds checks on the ring kernels' copies (debug builds)
+if os.environ.get("TT_CHECKED") == "1":
+    NVCC_FLAGS = NVCC_FLAGS + ["-DTT_CHECKED"]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-fvisibility=hidden", "-Wall",
              "-Wno-unused-function", "-I" + INCLUDE, "-I" + os.path.join(CUDA_HOME, "include")]
 
@@ -79,6 +82,9 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         futs = [ex.submit(_compile, s, _obj(s, hdr, NVCC_FLAGS if s.endswith(".cu") else CXX_FLAGS), verbose)
                 for s in srcs]
         objs = [f.result() for f in futs]
+    for stale in glob.glob(os.path.join(BUILD, "*.o")):
+        if stale not in objs:
+            os.remove(stale)
     tmp = LIB + ".tmp"
     cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-Xcompiler", "-fopenmp", "-lgomp"]
     r = subprocess.run(cmd, capture_output=True, text=True)

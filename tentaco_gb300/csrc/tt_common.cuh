@@ -95,6 +95,29 @@ __device__ __forceinline__ uint32_t ld_gather_2(const void* p, uint64_t pol) {
   return (uint32_t)r;
 }
 
+// ---------------------------------------------------------------------------
+// Asynchronous global -> shared copies (cp.async, 16 bytes, L2 only).  Nothing is
+// held in registers while a copy is in flight, so a block can have thousands of
+// row gathers outstanding.  src_bytes < 16 reads only that many bytes and
+// zero-fills the rest (ragged ends of caller-owned arrays).
+// ---------------------------------------------------------------------------
+// (No L2 cache-policy operand: in cp.async's operand list a lone fourth operand
+// is the source size, so only the plain and the 32-bit source-size forms are used.)
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* src, uint64_t pol) {
+  (void)pol;
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async16_part(void* smem_dst, const void* src, int src_bytes) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// CPT consecutive entries of a row held in shared memory, stored as KIND, as floats.
+template <int KIND, int CPT>
+__device__ __forceinline__ void smem_row(const unsigned char* row, int q, float (&v)[CPT]);
+
 // BF16 -> FP32 is exact: the bf16 bits are the high half of the fp32 bits.
 __device__ __forceinline__ float bf16lo(uint32_t w) { return __uint_as_float(w << 16); }
 __device__ __forceinline__ float bf16hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
@@ -140,6 +163,40 @@ __device__ __forceinline__ void row_load(const void* base, int64_t off, uint64_t
       v[0] = lo16<KIND>(a); v[1] = hi16<KIND>(a);
     } else {
       v[0] = lo16<KIND>(ld_gather_2(p, pol));
+    }
+  }
+}
+
+template <int KIND, int CPT>
+__device__ __forceinline__ void smem_row(const unsigned char* row, int q, float (&v)[CPT]) {
+  if constexpr (KIND == kF32) {
+    const float* p = reinterpret_cast<const float*>(row) + q * CPT;
+    if constexpr (CPT == 8) {
+      const float4 a = reinterpret_cast<const float4*>(p)[0], b = reinterpret_cast<const float4*>(p)[1];
+      v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    } else if constexpr (CPT == 4) {
+      const float4 a = *reinterpret_cast<const float4*>(p);
+      v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    } else if constexpr (CPT == 2) {
+      const float2 a = *reinterpret_cast<const float2*>(p);
+      v[0] = a.x; v[1] = a.y;
+    } else {
+      v[0] = p[0];
+    }
+  } else {
+    const uint16_t* p = reinterpret_cast<const uint16_t*>(row) + q * CPT;
+    if constexpr (CPT == 8) {
+      const uint4 a = *reinterpret_cast<const uint4*>(p);
+      v[0] = lo16<KIND>(a.x); v[1] = hi16<KIND>(a.x); v[2] = lo16<KIND>(a.y); v[3] = hi16<KIND>(a.y);
+      v[4] = lo16<KIND>(a.z); v[5] = hi16<KIND>(a.z); v[6] = lo16<KIND>(a.w); v[7] = hi16<KIND>(a.w);
+    } else if constexpr (CPT == 4) {
+      const uint2 a = *reinterpret_cast<const uint2*>(p);
+      v[0] = lo16<KIND>(a.x); v[1] = hi16<KIND>(a.x); v[2] = lo16<KIND>(a.y); v[3] = hi16<KIND>(a.y);
+    } else if constexpr (CPT == 2) {
+      const uint32_t a = *reinterpret_cast<const uint32_t*>(p);
+      v[0] = lo16<KIND>(a); v[1] = hi16<KIND>(a);
+    } else {
+      v[0] = lo16<KIND>((uint32_t)p[0]);
     }
   }
 }

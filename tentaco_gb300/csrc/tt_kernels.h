@@ -10,19 +10,25 @@ struct TtvArgs;
 
 using WalkLauncher = cudaError_t (*)(const WalkArgs& a, int grid, int tb, size_t smem, cudaStream_t s);
 
-// The MTTKRP walk kernel for (order, precision, columns per lane, lanes per row),
-// or nullptr if that combination is not compiled.
-WalkLauncher walk_launcher(int order, int prec, int cpt, int lpr);
-WalkLauncher walk_launcher_o3_fp32(int cpt, int lpr);
-WalkLauncher walk_launcher_o3_bf16(int cpt, int lpr);
-WalkLauncher walk_launcher_o3_bf16f(int cpt, int lpr);
-WalkLauncher walk_launcher_o4_fp32(int cpt, int lpr);
-WalkLauncher walk_launcher_o4_bf16(int cpt, int lpr);
-WalkLauncher walk_launcher_o4_bf16f(int cpt, int lpr);
-WalkLauncher walk_launcher_o3_fp16(int cpt, int lpr);
-WalkLauncher walk_launcher_o4_fp16(int cpt, int lpr);
+// The MTTKRP kernel for (order, precision, columns per lane, lanes per row,
+// family), or nullptr if that combination is not compiled.  family 0: register
+// walk (factor rows gathered into registers); 1: the block's rows gathered into
+// shared memory first; 2: register walk fed by a per-lane cp.async ring.
+WalkLauncher walk_launcher(int order, int prec, int cpt, int lpr, int staged);
+// Largest window (last-level fibers per block) of a computed partition -> *out (device int).
+cudaError_t launch_window_max(int order, const WalkArgs& a, int* out, cudaStream_t s);
+WalkLauncher walk_launcher_o3_fp32(int cpt, int lpr, int staged);
+WalkLauncher walk_launcher_o3_bf16(int cpt, int lpr, int staged);
+WalkLauncher walk_launcher_o3_bf16f(int cpt, int lpr, int staged);
+WalkLauncher walk_launcher_o4_fp32(int cpt, int lpr, int staged);
+WalkLauncher walk_launcher_o4_bf16(int cpt, int lpr, int staged);
+WalkLauncher walk_launcher_o4_bf16f(int cpt, int lpr, int staged);
+WalkLauncher walk_launcher_o3_fp16(int cpt, int lpr, int staged);
+WalkLauncher walk_launcher_o4_fp16(int cpt, int lpr, int staged);
 
 cudaError_t launch_partition(int order, const WalkArgs& a, cudaStream_t s);
+// FP64 merge of the rows the walk left in the carry buffer (after the walk kernel).
+cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s);
 cudaError_t launch_ttv(const TtvArgs& a, int grid, int tb, size_t smem, cudaStream_t s);
 cudaError_t launch_ttv_partition(const TtvArgs& a, cudaStream_t s);
 

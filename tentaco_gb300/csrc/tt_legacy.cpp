@@ -20,10 +20,10 @@ int legacy_variant(int kind, int rank_in_name, int tb, int p1, int p2, int rank)
   else if (kind == TT_LEG_PR) { G = 4; cpt = rank_in_name * p1 / tb; }
   else { G = 4; cpt = 1; tb = 512; }
   if (cpt < 1) cpt = 1;
-  int id = variant_id(tb, G, cpt);
+  int id = variant_id(tb, G, cpt, 0);
   // the rank passed may differ from the one in the name: keep tb and G, adjust columns per lane
-  for (int c = cpt; !variant_valid(id, 3, rank, (int)TT_PREC_FP32) && c <= 8; c <<= 1) id = variant_id(tb, G, c);
-  for (int c = cpt; !variant_valid(id, 3, rank, (int)TT_PREC_FP32) && c >= 1; c >>= 1) id = variant_id(tb, G, c);
+  for (int c = cpt; !variant_valid(id, 3, rank, (int)TT_PREC_FP32) && c <= 8; c <<= 1) id = variant_id(tb, G, c, 0);
+  for (int c = cpt; !variant_valid(id, 3, rank, (int)TT_PREC_FP32) && c >= 1; c >>= 1) id = variant_id(tb, G, c, 0);
   if (!variant_valid(id, 3, rank, (int)TT_PREC_FP32)) id = default_variant(3, rank, (int)TT_PREC_FP32, 0);
   return id;
 }

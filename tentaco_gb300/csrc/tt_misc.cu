@@ -7,17 +7,17 @@
 
 namespace tt {
 
-WalkLauncher walk_launcher(int order, int prec, int cpt, int lpr) {
+WalkLauncher walk_launcher(int order, int prec, int cpt, int lpr, int staged) {
   if (order == 3) {
-    if (prec == kFP32) return walk_launcher_o3_fp32(cpt, lpr);
-    if (prec == kBF16) return walk_launcher_o3_bf16(cpt, lpr);
-    if (prec == kBF16F) return walk_launcher_o3_bf16f(cpt, lpr);
-    if (prec == kFP16) return walk_launcher_o3_fp16(cpt, lpr);
+    if (prec == kFP32) return walk_launcher_o3_fp32(cpt, lpr, staged);
+    if (prec == kBF16) return walk_launcher_o3_bf16(cpt, lpr, staged);
+    if (prec == kBF16F) return walk_launcher_o3_bf16f(cpt, lpr, staged);
+    if (prec == kFP16) return walk_launcher_o3_fp16(cpt, lpr, staged);
   } else if (order == 4) {
-    if (prec == kFP32) return walk_launcher_o4_fp32(cpt, lpr);
-    if (prec == kBF16) return walk_launcher_o4_bf16(cpt, lpr);
-    if (prec == kBF16F) return walk_launcher_o4_bf16f(cpt, lpr);
-    if (prec == kFP16) return walk_launcher_o4_fp16(cpt, lpr);
+    if (prec == kFP32) return walk_launcher_o4_fp32(cpt, lpr, staged);
+    if (prec == kBF16) return walk_launcher_o4_bf16(cpt, lpr, staged);
+    if (prec == kBF16F) return walk_launcher_o4_bf16f(cpt, lpr, staged);
+    if (prec == kFP16) return walk_launcher_o4_fp16(cpt, lpr, staged);
   }
   return nullptr;
 }
@@ -27,6 +27,29 @@ cudaError_t launch_partition(int order, const WalkArgs& a, cudaStream_t s) {
   const int tb = 256, grid = (n + tb - 1) / tb;
   if (order == 3) partition_kernel<3><<<grid, tb, 0, s>>>(a);
   else partition_kernel<4><<<grid, tb, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+__global__ void window_max_kernel(const __grid_constant__ WalkArgs a, int lvl, int stride, int* out) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= a.nblocks) return;
+  const int w = a.part[(size_t)(b + 1) * stride + lvl] - a.part[(size_t)b * stride + lvl] + 1;
+  atomicMax(out, w);
+}
+
+cudaError_t launch_window_max(int order, const WalkArgs& a, int* out, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  if (a.nblocks == 0) return cudaSuccess;
+  window_max_kernel<<<(a.nblocks + 255) / 256, 256, 0, s>>>(a, order - 2, order - 1, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s) {
+  if (a.nblocks == 0) return cudaSuccess;
+  const int grid = (a.nblocks + 7) / 8;  // one warp per walk block
+  if (order == 3) chain_fixup_kernel<3><<<grid, 256, 0, s>>>(a);
+  else chain_fixup_kernel<4><<<grid, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

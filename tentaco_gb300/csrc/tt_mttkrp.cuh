@@ -45,15 +45,21 @@ struct WalkArgs {
   const float* colscale;  // RP output scales (nullptr: all 1)
   float* out;             // output rows (row id = crd[0][ip] or ip), ldo floats apart
   const int32_t* part;    // (nblocks+1) x (order-1): root position, then fiber ids per level
-  float* carry;           // 2 * nblocks * RP
-  int32_t* tickets;       // one per root position, zero between calls
+  float* carry;           // 2 * nblocks * RP: partial rows shared with other blocks
+  int32_t* meta;          // 4 ints per block: first row, last row, flags (see block_merge)
   int64_t nnz;
   int32_t nrows;
   int32_t R;              // columns stored (<= RP)
   int32_t ldo;
   int32_t P;              // nonzeros per block
-  int32_t G;              // nonzeros per team, multiple of 4
+  int32_t G;              // nonzeros per team, a power of two >= 4
+  int32_t lgG;            // log2(G)
   int32_t nblocks;
+  int32_t rp;             // factor row width the kernels were compiled for
+  int32_t fac_rows[3];    // rows of each factor (bounds for checked builds)
+  int32_t smem_bytes;     // dynamic shared memory of the launch (bounds for checked builds)
+  int32_t wcap;           // staged kernels: window fibers per block the shared memory holds
+  int32_t* err;           // staged kernels: set nonzero if a block's window exceeds wcap
 };
 
 constexpr int kEmpty = -2;  // summary of a team that owns no nonzeros
@@ -66,19 +72,58 @@ struct Summ {
 };
 
 // Bytes of dynamic shared memory a launch needs.
+constexpr int kRingDepth = 8;  // nonzeros of lookahead in the ring kernels
+
+__device__ __forceinline__ void cp_async8(void* smem_dst, const void* src) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem_dst, const void* src) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// Same copies addressed by a 32-bit shared-memory address.
+template <int BYTES>
+__device__ __forceinline__ void cp_async_sa(uint32_t d, const void* src) {
+  if constexpr (BYTES == 32) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d + 16), "l"(static_cast<const char*>(src) + 16) : "memory");
+  } else if constexpr (BYTES == 16) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+  } else {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(d), "l"(src), "n"(BYTES) : "memory");
+  }
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 __host__ __device__ inline size_t walk_tile_bytes(int P, int vbytes) {
   return (size_t)P * 4 + (((size_t)P * vbytes + 15) & ~(size_t)15);  // crd + vals tile
 }
-__host__ __device__ inline size_t walk_smem_bytes(int P, int tb, int rp, int vbytes) {
+// tile_elems: entries of the coordinate/value tile (P, or P plus the per-team skew
+// of the ring kernels).
+__host__ __device__ inline size_t walk_smem_bytes(int P, int tb, int rp, int vbytes, int tile_elems = -1) {
   size_t nw = (size_t)tb / 32;
-  size_t b = walk_tile_bytes(P, vbytes);
+  size_t b = walk_tile_bytes(tile_elems < 0 ? P : tile_elems, vbytes);
   b += (size_t)(2 * P + 4) * sizeof(int32_t);         // fiber window
   b += nw * 2 * sizeof(int32_t);                      // warp summary rows
   b += nw * 2 * (size_t)rp * sizeof(float);           // warp summary accs
-  b = (b + 15) & ~(size_t)15;
-  b += (size_t)tb * sizeof(double);                   // FP64 merge partials
-  b += 8 * sizeof(int32_t);                           // merge control
-  return b;
+  return (b + 15) & ~(size_t)15;
+}
+
+// Staged kernels: the tile, the gathered factor rows (one per nonzero, one per
+// window fiber) and the window, then the same merge scratch.
+__host__ __device__ inline size_t stage_off_rows(int P, int vbytes) {
+  return (walk_tile_bytes(P, vbytes) + 15) & ~(size_t)15;
+}
+__host__ __device__ inline size_t stage_smem_bytes(int P, int wcap, int tb, int rp, int vbytes, int fbytes) {
+  const size_t rb = (size_t)rp * fbytes;
+  size_t b = stage_off_rows(P, vbytes) + (size_t)P * rb + (size_t)wcap * rb;
+  b += (size_t)(2 * wcap + 4) * sizeof(int32_t);
+  const size_t nw = (size_t)tb / 32;
+  b += nw * 2 * sizeof(int32_t) + nw * 2 * (size_t)rp * sizeof(float);
+  return (b + 15) & ~(size_t)15;
 }
 
 template <int ORDER, int PREC, int CPT, int LPR>
@@ -310,6 +355,283 @@ struct Walk {
     }
   }
 
+  // Bytes of its factor row one lane loads per nonzero (its CPT columns).
+  static constexpr int LB = CPT * (FK == kF32 ? 4 : 2);
+
+  // Serial walk like walk(), but every factor row piece the lane needs is copied
+  // with cp.async into this lane's own shared-memory slots, DP nonzeros ahead of
+  // use: the nonzero-level row of each nonzero (ring of DP slots) and, in the
+  // same copy group as a fiber's first nonzero, the window-level row of that
+  // fiber (ring of DP+1 slots, by fiber ordinal).  Each lane copies exactly what
+  // it reads, so completion is its own cp.async.wait_group: no barrier, nothing
+  // held in registers while in flight, and short fibers do not stall on their
+  // factor row.  A fiber's slot is refilled only by the (DP+1)-th later fiber,
+  // whose copy is issued after this fiber's fold in program order.
+  // Positions are 32-bit (nnz < 2^31); the tile is read through the per-team
+  // skew sk(j) = j + 4*(j >> lgG), which puts the teams of a warp in different
+  // shared-memory banks.  Four nonzeros inside one fiber take a fast path.
+  //   ring / wring: this lane's first nonzero / fiber slot; slots `stride` apart.
+  template <int DP>
+  __device__ __forceinline__ void walk_ring(int s, int e, int bstart, const int32_t* s_lc,
+                                            const unsigned char* s_val, int lgG, const int32_t* s_pos,
+                                            const int32_t* s_fcrd, int W, int fs, const int32_t* pb,
+                                            const int32_t* pn, unsigned char* ring, unsigned char* wring,
+                                            int stride, Summ<CPT>& X) const {
+    static_assert((DP & (DP - 1)) == 0 && DP >= 4, "ring depth must be a power of two >= 4");
+    constexpr int WS = DP + 1;  // fiber slots
+    constexpr int RB = RP * (LB / CPT);
+    const uint64_t polL = policy_evict_last();
+    const int32_t* pos1 = a.pos[1];
+    const unsigned char* fzq = static_cast<const unsigned char*>(a.fac[ORDER - 2]) + q * LB;
+    const unsigned char* fwq = static_cast<const unsigned char*>(a.fac[ORDER == 3 ? 0 : 1]) + q * LB;
+    const uint32_t ring_sa = (uint32_t)__cvta_generic_to_shared(ring);
+    const uint32_t wring_sa = (uint32_t)__cvta_generic_to_shared(wring);
+    auto sk = [&](int j) { return j + ((j >> lgG) << 2); };
+    // lookahead state: fiber of the last issued nonzero and its ordinal
+    int xl = (int)search_le(s_pos, 0, W - 1, s);
+    int lend = s_pos[xl + 1];
+    int ordl = 0;
+#ifdef TT_CHECKED
+    // checked build: every copy's shared destination and factor row are bounds-checked;
+    // a violation is recorded in the error word and the copy is skipped
+    extern __shared__ __align__(16) unsigned char smem_chk[];
+    const uint32_t smem_sa = (uint32_t)__cvta_generic_to_shared(smem_chk);
+    auto ok = [&](uint32_t d, int row, int m, int code) {
+      const bool good = d >= smem_sa && d + LB <= smem_sa + (uint32_t)a.smem_bytes && row >= 0 && row < a.fac_rows[m] &&
+                        (d % (LB < 16 ? LB : 16)) == 0;
+      if (!good) atomicCAS(a.err, 0, code);
+      return good;
+    };
+#endif
+    auto issue_fiber = [&](int xx, int ord) {
+      const uint32_t d = wring_sa + (uint32_t)((ord % WS) * stride);
+      const int row = s_fcrd[xx];
+#ifdef TT_CHECKED
+      if (xx < 0 || xx >= W) { atomicCAS(a.err, 0, 101); return; }
+      if (!ok(d, row, ORDER == 3 ? 0 : 1, 102)) return;
+#endif
+      cp_async_sa<LB>(d, fwq + (size_t)(uint32_t)row * RB);
+    };
+    auto issue = [&](int p, int slot) {
+      while (p >= lend) {  // p opens a new window fiber: copy its row in this group
+        xl++;
+        lend = s_pos[xl + 1];
+        issue_fiber(xl, ++ordl);
+      }
+      const uint32_t d = ring_sa + (uint32_t)(slot * stride);
+      const int row = s_lc[sk(p - bstart)];
+#ifdef TT_CHECKED
+      if (p - bstart < 0 || p - bstart >= a.P) { atomicCAS(a.err, 0, 103); return; }
+      if (!ok(d, row, ORDER - 2, 104)) return;
+#endif
+      cp_async_sa<LB>(d, fzq + (size_t)(uint32_t)row * RB);
+    };
+    auto val = [&](int p) -> float {
+      const int j = sk(p - bstart);
+      if constexpr (VK == kF32) return reinterpret_cast<const float*>(s_val)[j];
+      else if constexpr (VK == kB16) return bf16lo(reinterpret_cast<const uint16_t*>(s_val)[j]);
+      else return h16lo(reinterpret_cast<const uint16_t*>(s_val)[j]);
+    };
+    auto slot_row = [&](unsigned char* base, int slot, float (&v)[CPT]) {
+      smem_row<FK, CPT>(base + slot * stride - q * LB, q, v);
+    };
+    int x = xl, ord = 0;
+    int fend = lend;
+    int f1 = 0, kend = 0;
+    int ip;
+    float crow[CPT];
+    if constexpr (ORDER == 3) {
+      ip = (int)search_le(pos1, pb[0], pn[0], fs + x);
+    } else {
+      f1 = (int)search_le(a.pos[2], pb[1], pn[1], fs + x);
+      kend = a.pos[2][f1 + 1];
+      ip = (int)search_le(pos1, pb[0], pn[0], f1);
+      frow(0, a.crd[1][f1], polL, crow);
+    }
+    int rend = pos1[ip + 1];
+    float f3[CPT], f2[CPT], ra[CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; c++) { f3[c] = 0.f; f2[c] = 0.f; ra[c] = 0.f; }
+    bool flushed = false;
+    const int n = e - s;
+    issue_fiber(x, 0);  // the fiber holding the first nonzero, in the first group
+#pragma unroll
+    for (int d = 0; d < DP; d++) {
+      if (d < n) issue(s + d, d);
+      cp_async_commit();
+    }
+    int i = 0;
+    while (i < n) {
+      const int p = s + i;
+      if (i + 4 <= n && p + 4 <= fend) {
+        // fast path: four nonzeros of the current fiber
+        cp_async_wait<DP - 4>();
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          float g[CPT];
+          slot_row(ring, (i + u) & (DP - 1), g);
+          const float v = val(p + u);
+#pragma unroll
+          for (int c = 0; c < CPT; c++) f3[c] = fmaf(v, g[c], f3[c]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          if (i + u + DP < n) issue(p + u + DP, (i + u) & (DP - 1));
+          cp_async_commit();
+        }
+        i += 4;
+        continue;
+      }
+      const int slot = i & (DP - 1);
+      cp_async_wait<DP - 1>();
+      float g[CPT];
+      slot_row(ring, slot, g);
+      const float v = val(p);
+      while (p >= fend) {
+        float cur[CPT];
+        slot_row(wring, ord % WS, cur);
+        if constexpr (ORDER == 3) {
+#pragma unroll
+          for (int c = 0; c < CPT; c++) { ra[c] = fmaf(f3[c], cur[c], ra[c]); f3[c] = 0.f; }
+        } else {
+#pragma unroll
+          for (int c = 0; c < CPT; c++) { f2[c] = fmaf(f3[c], cur[c], f2[c]); f3[c] = 0.f; }
+        }
+        x++;
+        ord++;
+        fend = s_pos[x + 1];
+        const int fg = fs + x;
+        if constexpr (ORDER == 4) {
+          while (fg >= kend) {
+#pragma unroll
+            for (int c = 0; c < CPT; c++) { ra[c] = fmaf(f2[c], crow[c], ra[c]); f2[c] = 0.f; }
+            f1++;
+            kend = a.pos[2][f1 + 1];
+            while (f1 >= rend) { flush(ip, ra, flushed, X); ip++; rend = pos1[ip + 1]; }
+            frow(0, a.crd[1][f1], polL, crow);
+          }
+        } else {
+          while (fg >= rend) { flush(ip, ra, flushed, X); ip++; rend = pos1[ip + 1]; }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < CPT; c++) f3[c] = fmaf(v, g[c], f3[c]);
+      // the slot's value is consumed: refill it DP nonzeros ahead
+      if (i + DP < n) issue(p + DP, slot);
+      cp_async_commit();
+      i++;
+    }
+    cp_async_wait<0>();
+    {
+      float cur[CPT];
+      slot_row(wring, ord % WS, cur);
+      if constexpr (ORDER == 3) {
+#pragma unroll
+        for (int c = 0; c < CPT; c++) ra[c] = fmaf(f3[c], cur[c], ra[c]);
+      } else {
+#pragma unroll
+        for (int c = 0; c < CPT; c++) { f2[c] = fmaf(f3[c], cur[c], f2[c]); ra[c] = fmaf(f2[c], crow[c], ra[c]); }
+      }
+    }
+    if (!flushed) {
+      X.h = ip; X.t = kNone;
+#pragma unroll
+      for (int c = 0; c < CPT; c++) X.ha[c] = ra[c];
+    } else {
+      X.t = ip;
+#pragma unroll
+      for (int c = 0; c < CPT; c++) X.ta[c] = ra[c];
+    }
+  }
+
+  // Serial walk of nonzeros [s, e) reading only shared memory: values and the
+  // gathered nonzero-level factor rows by tile offset, window-fiber factor rows
+  // by window offset.  Global reads remain only at row boundaries (and, for
+  // order 4, at level-1 fiber boundaries).
+  __device__ __forceinline__ void walk_staged(int64_t s, int64_t e, int64_t bstart, const unsigned char* s_val,
+                                              const unsigned char* s_rows, const unsigned char* s_wrows,
+                                              const int32_t* s_pos, int W, int64_t fs, const int32_t* pb,
+                                              const int32_t* pn, Summ<CPT>& X) const {
+    constexpr int RB = RP * (FK == kF32 ? 4 : 2);
+    const uint64_t polL = policy_evict_last();
+    const int32_t* pos1 = a.pos[1];
+    int x = (int)search_le(s_pos, 0, W - 1, s);
+    int64_t fend = s_pos[x + 1];
+    int64_t f1 = 0, kend = 0;
+    int ip;
+    float crow[CPT];
+    if constexpr (ORDER == 3) {
+      ip = (int)search_le(pos1, pb[0], pn[0], fs + x);
+    } else {
+      f1 = search_le(a.pos[2], pb[1], pn[1], fs + x);
+      kend = a.pos[2][f1 + 1];
+      ip = (int)search_le(pos1, pb[0], pn[0], f1);
+      frow(0, a.crd[1][f1], polL, crow);
+    }
+    int64_t rend = pos1[ip + 1];
+    float f3[CPT], f2[CPT], ra[CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; c++) { f3[c] = 0.f; f2[c] = 0.f; ra[c] = 0.f; }
+    bool flushed = false;
+#pragma unroll 4
+    for (int64_t p = s; p < e; p++) {
+      while (p >= fend) {
+        float cur[CPT];
+        smem_row<FK, CPT>(s_wrows + (size_t)x * RB, q, cur);
+        if constexpr (ORDER == 3) {
+#pragma unroll
+          for (int c = 0; c < CPT; c++) { ra[c] = fmaf(f3[c], cur[c], ra[c]); f3[c] = 0.f; }
+        } else {
+#pragma unroll
+          for (int c = 0; c < CPT; c++) { f2[c] = fmaf(f3[c], cur[c], f2[c]); f3[c] = 0.f; }
+        }
+        x++;
+        fend = s_pos[x + 1];
+        const int64_t fg = fs + x;
+        if constexpr (ORDER == 4) {
+          while (fg >= kend) {
+#pragma unroll
+            for (int c = 0; c < CPT; c++) { ra[c] = fmaf(f2[c], crow[c], ra[c]); f2[c] = 0.f; }
+            f1++;
+            kend = a.pos[2][f1 + 1];
+            while (f1 >= rend) { flush(ip, ra, flushed, X); ip++; rend = pos1[ip + 1]; }
+            frow(0, a.crd[1][f1], polL, crow);
+          }
+        } else {
+          while (fg >= rend) { flush(ip, ra, flushed, X); ip++; rend = pos1[ip + 1]; }
+        }
+      }
+      const int i = (int)(p - bstart);
+      float v;
+      if constexpr (VK == kF32) v = reinterpret_cast<const float*>(s_val)[i];
+      else v = VK == kB16 ? bf16lo(reinterpret_cast<const uint16_t*>(s_val)[i]) : h16lo(reinterpret_cast<const uint16_t*>(s_val)[i]);
+      float g[CPT];
+      smem_row<FK, CPT>(s_rows + (size_t)i * RB, q, g);
+#pragma unroll
+      for (int c = 0; c < CPT; c++) f3[c] = fmaf(v, g[c], f3[c]);
+    }
+    {
+      float cur[CPT];
+      smem_row<FK, CPT>(s_wrows + (size_t)x * RB, q, cur);
+      if constexpr (ORDER == 3) {
+#pragma unroll
+        for (int c = 0; c < CPT; c++) ra[c] = fmaf(f3[c], cur[c], ra[c]);
+      } else {
+#pragma unroll
+        for (int c = 0; c < CPT; c++) { f2[c] = fmaf(f3[c], cur[c], f2[c]); ra[c] = fmaf(f2[c], crow[c], ra[c]); }
+      }
+    }
+    if (!flushed) {
+      X.h = ip; X.t = kNone;
+#pragma unroll
+      for (int c = 0; c < CPT; c++) X.ha[c] = ra[c];
+    } else {
+      X.t = ip;
+#pragma unroll
+      for (int c = 0; c < CPT; c++) X.ta[c] = ra[c];
+    }
+  }
+
   // First and one-past-last nonzero of root position r.
   __device__ __forceinline__ void row_span(int r, int64_t& n0, int64_t& n1) const {
     int64_t f0 = a.pos[1][r], f1 = a.pos[1][r + 1];
@@ -320,10 +642,158 @@ struct Walk {
 };
 
 #ifndef TT_ARGS_ONLY
+// Merge the teams' summaries of one block (warp shuffle tree, then the first
+// team over the warps), then settle the block's first and last rows: a row that
+// starts and ends inside the block is stored; a row shared with a neighbouring
+// block is written to the block's carry slot (0: first row, 1: last row) for
+// chain_fixup_kernel.  No fence, atomic or second barrier: the block ends here.
+//   head_ff  first window-level fiber of the block's first row (loaded at start)
+//   meta[b]  {first row, last row, flags}: bit0 first row started before the
+//            block, bit1 last row continues after it, bit2 single-row block
+template <int ORDER, int PREC, int CPT, int LPR>
+__device__ __forceinline__ void block_merge(const WalkArgs& a, const Walk<ORDER, PREC, CPT, LPR>& wk,
+                                            Summ<CPT>& X, int32_t* s_wh, int32_t* s_wt, float* s_wha,
+                                            float* s_wta, int64_t head_ff, int64_t fs, int64_t win0,
+                                            int64_t bstart, int next_row, int b) {
+  constexpr int RP = CPT * LPR;
+  constexpr int TW = 32 / LPR;
+  const int tb = blockDim.x, nw = tb / 32;
+  const int team = threadIdx.x / LPR, q = threadIdx.x % LPR, tw = team % TW, warp = threadIdx.x / 32;
+  // Warp-level merge of team summaries (tree over teams, keyed by row).
+#pragma unroll
+  for (int d = 1; d < TW; d <<= 1) {
+    Summ<CPT> Y;
+    Y.h = __shfl_down_sync(0xffffffffu, X.h, d * LPR);
+    Y.t = __shfl_down_sync(0xffffffffu, X.t, d * LPR);
+#pragma unroll
+    for (int c = 0; c < CPT; c++) {
+      Y.ha[c] = __shfl_down_sync(0xffffffffu, X.ha[c], d * LPR);
+      Y.ta[c] = __shfl_down_sync(0xffffffffu, X.ta[c], d * LPR);
+    }
+    if ((tw & (2 * d - 1)) == 0 && tw + d < TW) wk.combine(X, Y);
+  }
+  if (tw == 0) {
+    if (q == 0) { s_wh[warp] = X.h; s_wt[warp] = X.t; }
+#pragma unroll
+    for (int c = 0; c < CPT; c++) {
+      s_wha[warp * RP + q * CPT + c] = X.ha[c];
+      s_wta[warp * RP + q * CPT + c] = X.ta[c];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < LPR) {
+    for (int w = 1; w < nw; w++) {
+      Summ<CPT> Y;
+      Y.h = s_wh[w];
+      Y.t = s_wt[w];
+  #pragma unroll
+      for (int c = 0; c < CPT; c++) {
+        Y.ha[c] = s_wha[w * RP + q * CPT + c];
+        Y.ta[c] = s_wta[w * RP + q * CPT + c];
+      }
+      wk.combine(X, Y);
+    }
+    const bool single = X.t == kNone;
+    const int last = single ? X.h : X.t;
+    const bool h_before = head_ff < fs || (head_ff == fs && win0 < bstart);
+    const bool l_after = b + 1 < a.nblocks && next_row == last;
+    float* c0 = a.carry + ((size_t)(2 * b)) * RP + q * CPT;
+    float* c1 = c0 + RP;
+    if (single) {
+      if (h_before || l_after) {
+  #pragma unroll
+        for (int c = 0; c < CPT; c++) c0[c] = X.ha[c] * wk.sc[c];
+      } else {
+        wk.store_row(X.h, X.ha);
+      }
+    } else {
+      if (h_before) {
+  #pragma unroll
+        for (int c = 0; c < CPT; c++) c0[c] = X.ha[c] * wk.sc[c];
+      } else {
+        wk.store_row(X.h, X.ha);
+      }
+      if (l_after) {
+  #pragma unroll
+        for (int c = 0; c < CPT; c++) c1[c] = X.ta[c] * wk.sc[c];
+      } else {
+        wk.store_row(X.t, X.ta);
+      }
+    }
+    if (q == 0)
+      reinterpret_cast<int4*>(a.meta)[b] =
+          make_int4(X.h, last, (h_before ? 1 : 0) | (l_after ? 2 : 0) | (single ? 4 : 0), 0);
+  }
+}
+
+// First window-level fiber of root position r (level 1 for order 3, level 2 for order 4).
+template <int ORDER>
+__device__ __forceinline__ int64_t row_first_window_fiber(const WalkArgs& a, int r) {
+  int64_t f = a.pos[1][r];
+  if constexpr (ORDER == 4) f = a.pos[2][f];
+  return f;
+}
+
+#ifndef TT_ARGS_ONLY
+// Sum every cross-block row in FP64, in a fixed order (deterministic).  One warp
+// per walk block; the warp of the block where a shared row starts owns that
+// row's chain of block partials.  Short chains: lane = column, blocks in order.
+// Long chains: lane = block stripe, every lane accumulates all columns, then a
+// fixed butterfly over lanes.
+template <int ORDER>
+__global__ void __launch_bounds__(256) chain_fixup_kernel(const __grid_constant__ WalkArgs a) {
+  constexpr int kShort = 16;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (b >= a.nblocks) return;
+  const int4 m = reinterpret_cast<const int4*>(a.meta)[b];
+  const bool h_before = m.z & 1, l_after = m.z & 2, single = m.z & 4;
+  if (!l_after || (single && h_before)) return;  // warp-uniform: no chain starts here
+  const int r = m.y;
+  int64_t f1 = a.pos[1][r + 1];
+  if constexpr (ORDER == 4) f1 = a.pos[2][f1];
+  const int64_t n1 = a.pos[ORDER - 1][f1];
+  const int b1 = (int)((n1 - 1) / a.P);
+  const int rp = a.rp;
+  const int slot0 = single ? 0 : 1;  // this block's slot; later blocks hold the row in slot 0
+  const int64_t row = a.crd[0] ? (int64_t)a.crd[0][r] : (int64_t)r;
+  float* out = a.out + row * a.ldo;
+  if (b1 - b < kShort) {
+    for (int j = lane; j < rp; j += 32) {
+      double acc = 0.0;
+      for (int bb = b; bb <= b1; bb++) acc += (double)a.carry[((size_t)(2 * bb + (bb == b ? slot0 : 0))) * rp + j];
+      if (j < a.R) out[j] = (float)acc;
+    }
+    return;
+  }
+  for (int c0 = 0; c0 < rp; c0 += 32) {  // at most 32 columns per pass
+    const int nc = rp - c0 < 32 ? rp - c0 : 32;
+    double acc[32];
+#pragma unroll
+    for (int c = 0; c < 32; c++) acc[c] = 0.0;
+    for (int bb = b + lane; bb <= b1; bb += 32) {
+      const float* src = a.carry + ((size_t)(2 * bb + (bb == b ? slot0 : 0))) * rp + c0;
+#pragma unroll
+      for (int c = 0; c < 32; c++)
+        if (c < nc) acc[c] += (double)src[c];
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+#pragma unroll
+      for (int c = 0; c < 32; c++) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], d);
+    }
+    // every lane holds the same totals; lane c writes column c0 + c
+#pragma unroll
+    for (int c = 0; c < 32; c++)
+      if (lane == c && c < nc && c0 + c < a.R) out[c0 + c] = (float)acc[c];
+  }
+}
+#endif
+
 // EXACT = true: the nonzero-level crd/vals arrays are read only up to nnz (the
 // caller's own unpadded arrays); false: the plan's padded copies are read in
 // whole 128-bit words.
-template <int ORDER, int PREC, int CPT, int LPR, bool EXACT = false>
+template <int ORDER, int PREC, int CPT, int LPR, bool EXACT = false, bool RING = false>
 __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant__ WalkArgs a) {
   using WK = Walk<ORDER, PREC, CPT, LPR>;
   constexpr int RP = WK::RP;
@@ -336,18 +806,16 @@ __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant_
   const int nw = tb / 32;
   const int b = blockIdx.x;
   const int P = a.P;
+  // ring kernels skew the tile by 4 entries per team (bank-conflict-free team reads)
+  const int TE = RING ? P + 4 * (tb / LPR) : P;
   int32_t* s_lc = reinterpret_cast<int32_t*>(smem);
-  unsigned char* s_val = smem + (size_t)P * 4;
-  int32_t* s_pos = reinterpret_cast<int32_t*>(smem + walk_tile_bytes(P, VB));
+  unsigned char* s_val = smem + (size_t)TE * 4;
+  int32_t* s_pos = reinterpret_cast<int32_t*>(smem + walk_tile_bytes(TE, VB));
   int32_t* s_fcrd = s_pos + (P + 2);
   int32_t* s_wh = s_fcrd + (P + 2);
   int32_t* s_wt = s_wh + nw;
   float* s_wha = reinterpret_cast<float*>(s_wt + nw);
   float* s_wta = s_wha + nw * RP;
-  size_t off = walk_tile_bytes(P, VB) + (size_t)(2 * P + 4) * 4 + (size_t)nw * 8 + (size_t)nw * 2 * RP * 4;
-  off = (off + 15) & ~(size_t)15;
-  double* s_dbl = reinterpret_cast<double*>(smem + off);
-  int32_t* s_ctl = reinterpret_cast<int32_t*>(s_dbl + tb);
 
   const int32_t* pb = a.part + (size_t)b * (ORDER - 1);
   const int32_t* pn = pb + (ORDER - 1);
@@ -379,16 +847,18 @@ __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant_
         }
       }
     } else {
+    // entry j lands at j + 4*(j >> lgG) in ring kernels (skew), at j otherwise
+    auto dst4 = [&](int i) { return RING ? i + ((4 * i) >> a.lgG) : i; };
     for (int i = threadIdx.x; i < n4; i += tb)
-      reinterpret_cast<int4*>(s_lc)[i] = ld_stream_i4(gl + 4 * i, polF);
+      reinterpret_cast<int4*>(s_lc)[dst4(i)] = ld_stream_i4(gl + 4 * i, polF);
     if constexpr (VB == 4) {
       const float* gv = static_cast<const float*>(a.vals) + bstart;
       for (int i = threadIdx.x; i < n4; i += tb)
-        reinterpret_cast<float4*>(s_val)[i] = ld_stream_f4(gv + 4 * i, polF);
+        reinterpret_cast<float4*>(s_val)[dst4(i)] = ld_stream_f4(gv + 4 * i, polF);
     } else {
       const uint16_t* gv = static_cast<const uint16_t*>(a.vals) + bstart;
       for (int i = threadIdx.x; i < n4; i += tb)
-        reinterpret_cast<uint2*>(s_val)[i] = ld_stream_u2(gv + 4 * i, polF);
+        reinterpret_cast<uint2*>(s_val)[dst4(i)] = ld_stream_u2(gv + 4 * i, polF);
     }
     }
     const int32_t* gpos = a.pos[ORDER - 1] + fs;
@@ -404,106 +874,123 @@ __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant_
   const int warp = threadIdx.x / 32;
   WK wk(a, q);
 
+  // the first team settles the block's rows at the end; its loads start now
+  const int64_t head_ff = threadIdx.x < LPR ? row_first_window_fiber<ORDER>(a, pb[0]) : 0;
+  Summ<CPT> X;
+  X.h = kEmpty;
+  X.t = kNone;
+  const int64_t s = bstart + (int64_t)team * a.G;
+  if (s < bend) {
+    if constexpr (RING && WK::LB >= 4) {  // (2-byte lane pieces: no ring variant is valid)
+      // rings: kRingDepth nonzero slots then kRingDepth+1 fiber slots, each of
+      // tb * LB bytes, slot-major so a warp's copies and reads are contiguous
+      const size_t roff = (walk_smem_bytes(P, tb, RP, VB, TE) + 15) & ~(size_t)15;
+      unsigned char* ring = smem + roff + (size_t)threadIdx.x * WK::LB;
+      unsigned char* wring = ring + (size_t)kRingDepth * tb * WK::LB;
+      wk.template walk_ring<kRingDepth>((int)s, (int)min(s + (int64_t)a.G, bend), (int)bstart, s_lc, s_val, a.lgG,
+                                        s_pos, s_fcrd, W, (int)fs, pb, pn, ring, wring, tb * WK::LB, X);
+    } else {
+      wk.walk(s, min(s + (int64_t)a.G, bend), bstart, s_lc, s_val, s_pos, s_fcrd, W, fs, pb, pn, X);
+    }
+  }
+
+  block_merge<ORDER, PREC, CPT, LPR>(a, wk, X, s_wh, s_wt, s_wha, s_wta, head_ff, fs, s_pos[0], bstart, pn[0], blockIdx.x);
+}
+
+// Staged kernel: every factor row the block needs is gathered into shared memory
+// with cp.async before the walk (one row per nonzero of the tile and one per
+// window fiber), so thousands of row gathers per SM are in flight at once and the
+// walk itself reads only shared memory.  Layout of the dynamic shared memory:
+//   [crd tile P][vals tile P][rows P x RB][window rows wcap x RB][window bounds]
+//   [window coords][warp summaries][FP64 merge partials][control]
+template <int ORDER, int PREC, int CPT, int LPR, bool EXACT = false>
+__global__ void __launch_bounds__(512) mttkrp_stage_kernel(const __grid_constant__ WalkArgs a) {
+  using WK = Walk<ORDER, PREC, CPT, LPR>;
+  constexpr int RP = WK::RP;
+  constexpr int VB = WK::VB;
+  constexpr int FB = WK::FK == kF32 ? 4 : 2;
+  constexpr int RB = RP * FB;    // bytes per factor row
+  constexpr int CPR = RB / 16;   // 16-byte copies per row
+  static_assert(RB % 16 == 0, "factor rows must be whole 16-byte chunks");
+  static_assert(!EXACT || VB == 4, "exact-length staging is built for FP32 values");
+  extern __shared__ __align__(16) unsigned char smem[];
+
+  const int tb = blockDim.x, nw = tb / 32, b = blockIdx.x, P = a.P, wcap = a.wcap;
+  int32_t* s_lc = reinterpret_cast<int32_t*>(smem);
+  unsigned char* s_val = smem + (size_t)P * 4;
+  unsigned char* s_rows = smem + stage_off_rows(P, VB);
+  unsigned char* s_wrows = s_rows + (size_t)P * RB;
+  int32_t* s_pos = reinterpret_cast<int32_t*>(s_wrows + (size_t)wcap * RB);
+  int32_t* s_fcrd = s_pos + (wcap + 2);
+  int32_t* s_wh = s_fcrd + (wcap + 2);
+  int32_t* s_wt = s_wh + nw;
+  float* s_wha = reinterpret_cast<float*>(s_wt + nw);
+  float* s_wta = s_wha + nw * RP;
+
+  const int32_t* pb = a.part + (size_t)b * (ORDER - 1);
+  const int32_t* pn = pb + (ORDER - 1);
+  const int64_t bstart = (int64_t)b * P;
+  const int64_t bend = min(bstart + (int64_t)P, a.nnz);
+  const int nt = (int)(bend - bstart);
+  const int64_t fs = pb[ORDER - 2];
+  const int W = (int)(pn[ORDER - 2] - fs + 1);
+  if (W > wcap) {  // the plan sized wcap from this partition; never expected
+    if (threadIdx.x == 0) atomicExch(a.err, 1);
+    return;
+  }
+  const uint64_t polF = policy_evict_first();
+  const uint64_t polL = policy_evict_last();
+  const int64_t head_ff = threadIdx.x < LPR ? row_first_window_fiber<ORDER>(a, pb[0]) : 0;
+
+  // 1. tile of coordinates and values (async), window bounds and coordinates
+  {
+    const int n4 = (nt + 3) >> 2;
+    const int32_t* gl = a.crd[ORDER - 1] + bstart;
+    const unsigned char* gv = static_cast<const unsigned char*>(a.vals) + (size_t)bstart * VB;
+    for (int i = threadIdx.x; i < n4; i += tb) {
+      if (!EXACT || 4 * i + 4 <= nt) cp_async16(s_lc + 4 * i, gl + 4 * i, polF);
+      else cp_async16_part(s_lc + 4 * i, gl + 4 * i, 4 * (nt - 4 * i));
+    }
+    const int nvb = (nt * VB + 15) >> 4;  // 16-byte chunks of values
+    for (int i = threadIdx.x; i < nvb; i += tb) {
+      if (!EXACT || 16 * i + 16 <= nt * VB) cp_async16(s_val + 16 * i, gv + 16 * i, polF);
+      else cp_async16_part(s_val + 16 * i, gv + 16 * i, nt * VB - 16 * i);
+    }
+    const int32_t* gpos = a.pos[ORDER - 1] + fs;
+    const int32_t* gcrd = a.crd[ORDER - 2] + fs;
+    for (int x = threadIdx.x; x <= W; x += tb) s_pos[x] = gpos[x];
+    for (int x = threadIdx.x; x < W; x += tb) s_fcrd[x] = gcrd[x];
+  }
+  cp_async_wait_all();
+  __syncthreads();
+
+  // 2. gather the factor rows: nonzero-level factor for each tile entry, the
+  //    window factor for each window fiber
+  {
+    const unsigned char* fz = static_cast<const unsigned char*>(a.fac[ORDER - 2]);
+    const unsigned char* fw = static_cast<const unsigned char*>(a.fac[ORDER - 3]);
+    for (int j = threadIdx.x; j < nt * CPR; j += tb) {
+      const int i = j / CPR, c = j - i * CPR;
+      cp_async16(s_rows + (size_t)i * RB + 16 * c, fz + (size_t)s_lc[i] * RB + 16 * c, polL);
+    }
+    for (int j = threadIdx.x; j < W * CPR; j += tb) {
+      const int x = j / CPR, c = j - x * CPR;
+      cp_async16(s_wrows + (size_t)x * RB + 16 * c, fw + (size_t)s_fcrd[x] * RB + 16 * c, polL);
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+
+  const int team = threadIdx.x / LPR;
+  const int q = threadIdx.x % LPR;
+  WK wk(a, q);
   Summ<CPT> X;
   X.h = kEmpty;
   X.t = kNone;
   const int64_t s = bstart + (int64_t)team * a.G;
   if (s < bend)
-    wk.walk(s, min(s + (int64_t)a.G, bend), bstart, s_lc, s_val, s_pos, s_fcrd, W, fs, pb, pn, X);
-
-  // Warp-level merge of team summaries (tree over teams, keyed by row).
-#pragma unroll
-  for (int d = 1; d < TW; d <<= 1) {
-    Summ<CPT> Y;
-    Y.h = __shfl_down_sync(0xffffffffu, X.h, d * LPR);
-    Y.t = __shfl_down_sync(0xffffffffu, X.t, d * LPR);
-#pragma unroll
-    for (int c = 0; c < CPT; c++) {
-      Y.ha[c] = __shfl_down_sync(0xffffffffu, X.ha[c], d * LPR);
-      Y.ta[c] = __shfl_down_sync(0xffffffffu, X.ta[c], d * LPR);
-    }
-    if ((tw & (2 * d - 1)) == 0 && tw + d < TW) wk.combine(X, Y);
-  }
-  if (tw == 0) {
-    if (q == 0) { s_wh[warp] = X.h; s_wt[warp] = X.t; }
-#pragma unroll
-    for (int c = 0; c < CPT; c++) {
-      s_wha[warp * RP + q * CPT + c] = X.ha[c];
-      s_wta[warp * RP + q * CPT + c] = X.ta[c];
-    }
-  }
-  __syncthreads();
-
-  // Block-level merge by the first team, then the cross-block protocol.
-  if (threadIdx.x < LPR) {
-    for (int w = 1; w < nw; w++) {
-      Summ<CPT> Y;
-      Y.h = s_wh[w];
-      Y.t = s_wt[w];
-#pragma unroll
-      for (int c = 0; c < CPT; c++) {
-        Y.ha[c] = s_wha[w * RP + q * CPT + c];
-        Y.ta[c] = s_wta[w * RP + q * CPT + c];
-      }
-      wk.combine(X, Y);
-    }
-    // Up to two boundary rows: slot 0 = the block's first row, slot 1 = its last.
-#pragma unroll
-    for (int slot = 0; slot < 2; slot++) {
-      const int r = slot == 0 ? X.h : X.t;
-      int last = -1;
-      int64_t n0 = 0, n1 = 0;
-      if (r >= 0) {
-        wk.row_span(r, n0, n1);
-        const int64_t b0 = n0 / P, b1 = (n1 - 1) / P;
-        if (b0 == b1) {
-          if (slot == 0) wk.store_row(r, X.ha); else wk.store_row(r, X.ta);
-        } else {
-          float* cp = a.carry + ((size_t)(2 * b + slot)) * RP + q * CPT;
-#pragma unroll
-          for (int c = 0; c < CPT; c++) cp[c] = (slot == 0 ? X.ha[c] : X.ta[c]) * wk.sc[c];
-          __threadfence();
-          __syncwarp((LPR == 32) ? 0xffffffffu : ((1u << LPR) - 1u));
-          int t = 0;
-          if (q == 0) {
-            t = atomicAdd(a.tickets + r, 1);
-            if (t == (int)(b1 - b0)) { a.tickets[r] = 0; __threadfence(); }
-          }
-          t = __shfl_sync((LPR == 32) ? 0xffffffffu : ((1u << LPR) - 1u), t, 0, LPR);
-          if (t == (int)(b1 - b0)) last = r;
-        }
-      }
-      if (q == 0) {
-        s_ctl[slot] = last;
-        s_ctl[2 + slot] = (int)(n0 / P);
-        s_ctl[4 + slot] = (int)((n1 - 1) / P);
-      }
-    }
-  }
-  __syncthreads();
-
-  // The last block to reach a boundary row sums its block partials in FP64, in block order.
-#pragma unroll
-  for (int slot = 0; slot < 2; slot++) {
-    const int r = s_ctl[slot];
-    if (r < 0) continue;  // uniform across the block
-    const int b0 = s_ctl[2 + slot], b1 = s_ctl[4 + slot];
-    const int j = threadIdx.x % RP;
-    const int sl = threadIdx.x / RP, ns = tb / RP;
-    double acc = 0.0;
-    for (int bb = b0 + sl; bb <= b1; bb += ns) {
-      const int sb = (a.part[(size_t)bb * (ORDER - 1)] == r) ? 0 : 1;
-      acc += (double)__ldcg(a.carry + ((size_t)(2 * bb + sb)) * RP + j);
-    }
-    s_dbl[threadIdx.x] = acc;
-    __syncthreads();
-    if (threadIdx.x < RP) {
-      double tot = 0.0;
-      for (int k = 0; k < ns; k++) tot += s_dbl[k * RP + threadIdx.x];
-      if (threadIdx.x < a.R) a.out[wk.row_id(r) * a.ldo + threadIdx.x] = (float)tot;
-    }
-    __syncthreads();
-  }
+    wk.walk_staged(s, min(s + (int64_t)a.G, bend), bstart, s_val, s_rows, s_wrows, s_pos, W, fs, pb, pn, X);
+  block_merge<ORDER, PREC, CPT, LPR>(a, wk, X, s_wh, s_wt, s_wha, s_wta, head_ff, fs, s_pos[0], bstart, pn[0], blockIdx.x);
 }
 
 // Partition: for each block boundary b in [0, nblocks], the root position and
@@ -534,6 +1021,7 @@ __global__ void partition_kernel(const __grid_constant__ WalkArgs a) {
   (void)hi;
   out[0] = (int32_t)search_le(a.pos[1], 0, a.nrows - 1, f1);
 }
+
 
 #endif  // TT_ARGS_ONLY
 }  // namespace tt

@@ -11,7 +11,8 @@
 // process exits.
 //
 // The scratch holds what the walk kernel needs besides its inputs and outputs:
-// the per-block partition, the cross-block carry rows and the per-row tickets.
+// the per-block partition, the per-block row metadata and the cross-block carry
+// rows.
 #include <cuda_runtime.h>
 #include <mutex>
 #include "tt_internal.h"
@@ -27,16 +28,16 @@ constexpr int kLPR = 8;
 constexpr int kG = 64;
 constexpr int kP = (kTB / kLPR) * kG;
 
-// Limits of the scratch array (about 6.3 MB).
-constexpr int64_t kMaxRows = 1 << 19;    // root positions (one ticket each)
+// Limits of the scratch array (about 4.2 MB).
+constexpr int64_t kMaxRows = 1 << 19;    // root positions
 constexpr int64_t kMaxBlocks = 8192;     // so nnz <= 8192 * 2048 = 16,777,216
 constexpr int kMaxRankPad = 64;
-constexpr size_t kTicketBytes = (size_t)kMaxRows * 4;
+constexpr size_t kMetaBytes = (size_t)kMaxBlocks * 16;
 constexpr size_t kPartBytes = (((size_t)(kMaxBlocks + 1) * 2 * 4) + 255) & ~(size_t)255;
 constexpr size_t kCarryBytes = (size_t)2 * kMaxBlocks * kMaxRankPad * 4;
-constexpr size_t kScratchBytes = kTicketBytes + kPartBytes + kCarryBytes;
+constexpr size_t kScratchBytes = kMetaBytes + kPartBytes + kCarryBytes;
 
-// Zero at module load; the tickets are cleared again by every call.
+// Every call writes the parts of it that it reads (partition, metadata, carry).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 std::mutex g_mu;
@@ -98,16 +99,13 @@ TT_EXPORT tt_status tt_mttkrp3_noalloc(int32_t nrows, int64_t nnz, int32_t rank,
   tt_status st = scratch_address(&scratch);
   if (st != TT_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  int32_t* tickets = static_cast<int32_t*>(scratch);
-  int32_t* part = reinterpret_cast<int32_t*>(static_cast<unsigned char*>(scratch) + kTicketBytes);
-  float* carry = reinterpret_cast<float*>(static_cast<unsigned char*>(scratch) + kTicketBytes + kPartBytes);
+  int32_t* meta = static_cast<int32_t*>(scratch);
+  int32_t* part = reinterpret_cast<int32_t*>(static_cast<unsigned char*>(scratch) + kMetaBytes);
+  float* carry = reinterpret_cast<float*>(static_cast<unsigned char*>(scratch) + kMetaBytes + kPartBytes);
 
   cudaError_t e = cudaMemsetAsync(A, 0, sizeof(float) * (size_t)nrows * (size_t)rank, s);
   if (e != cudaSuccess) return tt::set_error(TT_ERR_CUDA, "clear A: %s", cudaGetErrorString(e));
   if (nnz == 0) return TT_OK;
-  // tickets must start at zero; the array keeps whatever the previous call left
-  e = cudaMemsetAsync(tickets, 0, sizeof(int32_t) * (size_t)nrows, s);
-  if (e != cudaSuccess) return tt::set_error(TT_ERR_CUDA, "clear tickets: %s", cudaGetErrorString(e));
 
   tt::WalkArgs a{};
   a.pos[1] = pos1;
@@ -122,13 +120,15 @@ TT_EXPORT tt_status tt_mttkrp3_noalloc(int32_t nrows, int64_t nnz, int32_t rank,
   a.out = A;
   a.part = part;
   a.carry = carry;
-  a.tickets = tickets;
+  a.meta = meta;
+  a.rp = rank;
   a.nnz = nnz;
   a.nrows = nrows;
   a.R = rank;
   a.ldo = rank;
   a.P = kP;
   a.G = kG;
+  a.lgG = 6;  // log2(kG)
   a.nblocks = (int32_t)nblocks;
   e = tt::launch_partition(3, a, s);
   if (e != cudaSuccess) return tt::set_error(TT_ERR_CUDA, "partition: %s", cudaGetErrorString(e));
@@ -140,5 +140,7 @@ TT_EXPORT tt_status tt_mttkrp3_noalloc(int32_t nrows, int64_t nnz, int32_t rank,
     default: e = launch_exact<8>(a, (int)nblocks, smem, s); break;
   }
   if (e != cudaSuccess) return tt::set_error(TT_ERR_CUDA, "walk kernel: %s", cudaGetErrorString(e));
+  e = tt::launch_chain_fixup(3, a, s);
+  if (e != cudaSuccess) return tt::set_error(TT_ERR_CUDA, "chain merge: %s", cudaGetErrorString(e));
   return TT_OK;
 }

@@ -26,28 +26,45 @@ using namespace tt;
 namespace tt {
 
 // ---------------------------------------------------------------------------
-// variant table: threads {256,512} x nnz per team {4..64} x columns per lane {8,4,2,1}
+// variant table: family {register walk, staged} x threads {256,512} x nonzeros
+// per team {4..64} x columns per lane {8,4,2,1}
 // ---------------------------------------------------------------------------
 static const int kTB[2] = {256, 512};
 static const int kG[5] = {4, 8, 16, 32, 64};
 static const int kCPT[4] = {8, 4, 2, 1};
-constexpr int kNumVariants = 2 * 5 * 4;
+constexpr int kPerFamily = 2 * 5 * 4;
+constexpr int kNumVariants = 3 * kPerFamily;  // register walk, staged, ring
+constexpr size_t kSmemLimit = (size_t)227 * 1024;
 
 VariantSpec variant_spec(int id) {
   VariantSpec v{};
   if (id < 0 || id >= kNumVariants) return v;
   v.id = id;
-  v.cpt = kCPT[id % 4];
-  v.G = kG[(id / 4) % 5];
-  v.tb = kTB[id / 20];
+  v.staged = id / kPerFamily;
+  const int b = id % kPerFamily;
+  v.cpt = kCPT[b % 4];
+  v.G = kG[(b / 4) % 5];
+  v.tb = kTB[b / 20];
   return v;
 }
 
-int variant_id(int tb, int G, int cpt) {
+int variant_id(int tb, int G, int cpt, int staged) {
   int ti = tb == 512 ? 1 : 0, gi = 0, ci = 0;
   for (int i = 0; i < 5; i++) if (kG[i] == G) gi = i;
   for (int i = 0; i < 4; i++) if (kCPT[i] == cpt) ci = i;
-  return (ti * 5 + gi) * 4 + ci;
+  return staged * kPerFamily + (ti * 5 + gi) * 4 + ci;
+}
+
+int fac_bytes(int prec) { return fac_kind(prec) == kF32 ? 4 : 2; }
+
+size_t variant_smem(const VariantSpec& v, int rp, int prec, int wcap) {
+  const int lpr = rp / v.cpt;
+  const int P = (v.tb / lpr) * v.G;
+  if (v.staged == 2)  // walk + nonzero ring (kRingDepth slots) + fiber ring (kRingDepth+1 slots)
+    return ((walk_smem_bytes(P, v.tb, rp, val_bytes(prec), P + 4 * (v.tb / lpr)) + 15) & ~(size_t)15) +
+           (size_t)(2 * kRingDepth + 1) * v.tb * v.cpt * fac_bytes(prec);
+  return v.staged ? stage_smem_bytes(P, wcap, v.tb, rp, val_bytes(prec), fac_bytes(prec))
+                  : walk_smem_bytes(P, v.tb, rp, val_bytes(prec));
 }
 
 int val_bytes(int prec) { return val_kind(prec) == kF32 ? 4 : 2; }
@@ -66,21 +83,29 @@ bool variant_valid(int id, int order, int rank, int prec) {
   if (rp % v.cpt) return false;
   const int lpr = rp / v.cpt;
   if (lpr < 1 || lpr > 32) return false;
-  // the block's fiber window and merge scratch must fit the 227 KB opt-in shared memory
-  const int P = (v.tb / lpr) * v.G;
-  if (walk_smem_bytes(P, v.tb, rp, val_bytes(prec)) > (size_t)227 * 1024) return false;
-  return walk_launcher(order, prec, v.cpt, lpr) != nullptr;
+  // shared memory must fit the 227 KB opt-in limit (staged: with the smallest
+  // window; a plan checks its own tensor's largest window)
+  if (variant_smem(v, rp, prec, 1) > kSmemLimit) return false;
+  if (v.staged && (rp * fac_bytes(prec)) % 16) return false;
+  if (v.staged == 2 && v.cpt * fac_bytes(prec) < 4) return false;  // cp.async moves >= 4 bytes
+  return walk_launcher(order, prec, v.cpt, lpr, v.staged) != nullptr;
 }
 
 int default_variant(int order, int rank, int prec, int64_t nnz) {
   (void)nnz;
-  // one 16-byte factor load per lane: 4 FP32 or 8 BF16 columns
+  // staged family, 16 bytes of a factor row per lane (4 FP32 or 8 16-bit columns),
+  // about 512 nonzeros per block; fits shared memory for any window
   const int rp = rank_pad(rank);
-  int cpt = prec == kFP32 ? 4 : 8;
+  int cpt = fac_kind(prec) == kF32 ? 4 : 8;
   while (cpt > 1 && rp / cpt < 1) cpt >>= 1;
   while (rp / cpt > 32) cpt <<= 1;
-  int id = variant_id(256, 16, cpt);
-  if (!variant_valid(id, order, rank, prec)) {
+  const int lpr = rp / cpt;
+  int G = 4;
+  while (G < 64 && (256 / lpr) * G * 2 <= 512) G *= 2;
+  int id = variant_id(256, G, cpt, 1);
+  const VariantSpec v = variant_spec(id);
+  const int P = (256 / lpr) * G;
+  if (!variant_valid(id, order, rank, prec) || variant_smem(v, rp, prec, P + 1) > kSmemLimit) {
     for (int i = 0; i < kNumVariants; i++)
       if (variant_valid(i, order, rank, prec)) return i;
     return -1;
@@ -141,27 +166,50 @@ tt_status alloc_walk_scratch(tt_plan* p, int P) {
     dev_free(p, p->d_carry);
     p->d_part = nullptr;
     p->d_carry = nullptr;
+    dev_free(p, p->d_meta);
+    p->d_meta = nullptr;
     tt_status s = dev_alloc(p, &p->d_part, (size_t)(nb + 1) * (size_t)(p->order - 1));
     if (s != TT_OK) return s;
     s = dev_alloc(p, &p->d_carry, (size_t)(2 * nb) * (size_t)p->rp);
+    if (s != TT_OK) return s;
+    s = dev_alloc(p, &p->d_meta, (size_t)nb * 4);
     if (s != TT_OK) return s;
     p->scratch_blocks = nb;
   }
   return TT_OK;
 }
 
+WalkArgs walk_args(const tt_plan* p, float* A);
+
 tt_status use_variant(tt_plan* p, int id) {
   VariantSpec v = variant_spec(id);
   p->variant = id;
+  p->staged = v.staged;
   p->tb = v.tb;
   p->cpt = v.cpt;
   p->lpr = p->rp / v.cpt;
   p->G = v.G;
   p->P = (v.tb / p->lpr) * v.G;
   p->nblocks = (int)((p->nnz + p->P - 1) / p->P);
-  p->launcher = walk_launcher(p->order, p->prec, p->cpt, p->lpr);
+  p->launcher = walk_launcher(p->order, p->prec, p->cpt, p->lpr, p->staged);
   if (!p->launcher) return set_error(TT_ERR_UNSUPPORTED, "variant %d not compiled for this shape", id);
-  return alloc_walk_scratch(p, p->P);
+  tt_status s = alloc_walk_scratch(p, p->P);
+  if (s != TT_OK) return s;
+  p->wcap = 1;
+  if (p->staged == 1 && p->nnz > 0) {
+    // size the window-row region from this tensor's partition (computed once here)
+    WalkArgs a = walk_args(p, nullptr);
+    CK(launch_partition(p->order, a, p->stream));
+    CK(launch_window_max(p->order, a, p->d_err + 1, p->stream));
+    int w = 0;
+    CK(cudaMemcpyAsync(&w, p->d_err + 1, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    p->wcap = std::max(1, w);
+    const size_t need = variant_smem(v, p->rp, p->prec, p->wcap);
+    if (need > kSmemLimit)
+      return set_error(TT_ERR_UNSUPPORTED, "variant %d needs %zu bytes of shared memory for this tensor", id, need);
+  }
+  return TT_OK;
 }
 
 WalkArgs walk_args(const tt_plan* p, float* A) {
@@ -174,14 +222,20 @@ WalkArgs walk_args(const tt_plan* p, float* A) {
   a.out = A;
   a.part = p->d_part;
   a.carry = p->d_carry;
-  a.tickets = p->d_tickets;
+  a.meta = p->d_meta;
   a.nnz = p->nnz;
   a.nrows = (int32_t)p->nroot;
+  a.rp = p->rp;
   a.R = p->rank;
   a.ldo = p->rank;
   a.P = p->P;
   a.G = p->G;
+  a.lgG = 0;
+  while ((1 << a.lgG) < p->G) a.lgG++;
   a.nblocks = p->nblocks;
+  a.wcap = p->wcap;
+  a.err = p->d_err;
+  for (int m = 0; m < 3; m++) a.fac_rows[m] = m + 1 < p->order ? (int32_t)p->dims[m + 1] : 0;
   return a;
 }
 
@@ -191,10 +245,12 @@ tt_status run_mttkrp(tt_plan* p, float* A, cudaStream_t st) {
   if (p->nnz == 0) return TT_OK;
   WalkArgs a = walk_args(p, A);
   CK(launch_partition(p->order, a, st));
-  const size_t smem = walk_smem_bytes(p->P, p->tb, p->rp, val_bytes(p->prec));
+  const size_t smem = variant_smem(variant_spec(p->variant), p->rp, p->prec, p->wcap);
+  a.smem_bytes = (int32_t)smem;
   if (p->timing) CK(cudaEventRecord(p->evk0, st));
   CK(p->launcher(a, p->nblocks, p->tb, smem, st));
   if (p->timing) CK(cudaEventRecord(p->evk1, st));
+  CK(launch_chain_fixup(p->order, a, st));
   return TT_OK;
 }
 
@@ -262,7 +318,9 @@ TT_EXPORT tt_status tt_variant_get(int32_t id, tt_variant_info* info) {
   info->rank_pad = 32;
   info->lanes_per_row = 32 / v.cpt;
   info->nnz_per_block = v.tb / info->lanes_per_row * v.G;
-  std::snprintf(info->name, sizeof(info->name), "walk_t%d_g%d_c%d", v.tb, v.G, v.cpt);
+  info->staged = v.staged;
+  static const char* fam[3] = {"walk", "stage", "ring"};
+  std::snprintf(info->name, sizeof(info->name), "%s_t%d_g%d_c%d", fam[v.staged], v.tb, v.G, v.cpt);
   return TT_OK;
 }
 
@@ -373,11 +431,10 @@ TT_EXPORT tt_status tt_plan_create(const taco_tensor_t* B, tt_op op, int32_t ran
         return fail(set_error(TT_ERR_CUDA, "upload vals"));
     }
   }
-  // tickets: one per root position (MTTKRP) or per block (TTV), zero once here
+  // MTTKRP scratch is sized with the variant; TTV keeps one ticket per block, zeroed once here
   if (op == TT_OP_MTTKRP) {
-    if ((s = dev_alloc(p, &p->d_tickets, (size_t)std::max<int64_t>(1, v.nroot))) != TT_OK) return fail(s);
-    if (cudaMemsetAsync(p->d_tickets, 0, sizeof(int32_t) * (size_t)std::max<int64_t>(1, v.nroot), st) != cudaSuccess)
-      return fail(set_error(TT_ERR_CUDA, "clear tickets"));
+    if ((s = dev_alloc(p, &p->d_err, 4)) != TT_OK) return fail(s);
+    if (cudaMemsetAsync(p->d_err, 0, 4 * sizeof(int32_t), st) != cudaSuccess) return fail(set_error(TT_ERR_CUDA, "clear error word"));
     int id = -1;
     if (select == TT_SELECT_FIXED) {
       if (!variant_valid(variant, p->order, rank, p->prec))
@@ -543,6 +600,16 @@ TT_EXPORT int64_t tt_plan_num_fibers(const tt_plan* p, int32_t level) {
 TT_EXPORT int64_t tt_plan_device_bytes(const tt_plan* p) { return p ? p->device_bytes : -1; }
 TT_EXPORT int32_t tt_plan_nblocks(const tt_plan* p) { return p ? p->nblocks : -1; }
 
+// Device-side error word of the plan's kernels (0: none), read after the plan's
+// stream has finished.
+TT_EXPORT int32_t tt_plan_device_error(tt_plan* p) {
+  if (!p || !p->d_err) return 0;
+  int32_t e = 0;
+  if (cudaStreamSynchronize(p->stream) != cudaSuccess) return -1;
+  if (cudaMemcpy(&e, p->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  return e;
+}
+
 // Switch an existing plan to another variant (scratch grows as needed).
 TT_EXPORT tt_status tt_plan_use_variant(tt_plan* p, int32_t id) {
   clear_error();
@@ -579,7 +646,10 @@ tt_status sweep_variants(tt_plan* p, cudaStream_t st) {
   tt_status s = TT_OK;
   for (int id = 0; id < kNumVariants && s == TT_OK; id++) {
     if (!variant_valid(id, p->order, p->rank, p->prec)) continue;
-    if ((s = use_variant(p, id)) != TT_OK) break;
+    if ((s = use_variant(p, id)) != TT_OK) {
+      if (s == TT_ERR_UNSUPPORTED) { s = TT_OK; continue; }  // does not fit this tensor's windows
+      break;
+    }
     if ((s = run_mttkrp(p, A, st)) != TT_OK) break;
     float tot = 0.f;
     for (int r = 0; r < 3; r++) {

@@ -9,10 +9,10 @@
 namespace tt {
 
 struct VariantSpec {
-  int id, tb, cpt, G;
+  int id, tb, cpt, G, staged;
 };
 VariantSpec variant_spec(int id);
-int variant_id(int tb, int G, int cpt);
+int variant_id(int tb, int G, int cpt, int staged);
 int rank_pad(int R);
 int val_bytes(int prec);
 bool variant_valid(int id, int order, int rank, int prec);
@@ -44,13 +44,15 @@ struct tt_plan {
   bool factors_set = false;
   // variant and scratch
   int variant = -1, selected_by = 0;  // 0 heuristic/fixed, 1 model, 2 sweep
-  int tb = 0, cpt = 0, lpr = 0, G = 0, P = 0, nblocks = 0;
+  int tb = 0, cpt = 0, lpr = 0, G = 0, P = 0, nblocks = 0, staged = 0, wcap = 1;
+  int32_t* d_err = nullptr;  // [0]: kernel error word, [1]: scratch for the window size
   tt::WalkLauncher launcher = nullptr;
   int32_t* d_part = nullptr;
   float* d_carry = nullptr;
-  int32_t* d_tickets = nullptr;
+  int32_t* d_tickets = nullptr;  // TTV
+  int32_t* d_meta = nullptr;     // MTTKRP: 4 ints per block
   int64_t scratch_blocks = 0;
-  float sweep_ms[64] = {};
+  float sweep_ms[128] = {};
   // timing
   bool timing = false, timed_pending = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;

@@ -1,5 +1,6 @@
 // tt_walk_inst.cuh -- explicit instantiations of the MTTKRP walk kernel for one
-// (order, precision), included by tt_walk_o{3,4}_{fp32,bf16,bf16f}.cu with
+// (order, precision) -- register walk and shared-memory staged walk --, included
+// by tt_walk_o{3,4}_{fp32,bf16,bf16f,fp16}.cu with
 // TT_ORDER, TT_PREC and TT_LOOKUP defined.  The (columns per lane, lanes per row)
 // pairs cover factor ranks 8, 16, 32 and 64.
 #include "tt_mttkrp.cuh"
@@ -7,9 +8,12 @@
 
 namespace tt {
 namespace {
-template <int CPT, int LPR>
+// fam 0: register walk, 1: shared-memory staged, 2: register walk with a per-lane cp.async ring
+template <int CPT, int LPR, int FAM>
 cudaError_t launch_walk(const WalkArgs& a, int grid, int tb, size_t smem, cudaStream_t s) {
-  auto k = mttkrp_walk_kernel<TT_ORDER, TT_PREC, CPT, LPR>;
+  auto k = FAM == 1 ? mttkrp_stage_kernel<TT_ORDER, TT_PREC, CPT, LPR>
+         : FAM == 2 ? mttkrp_walk_kernel<TT_ORDER, TT_PREC, CPT, LPR, false, true>
+                    : mttkrp_walk_kernel<TT_ORDER, TT_PREC, CPT, LPR>;
   static size_t configured = 48 * 1024;
   if (smem > configured) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -21,8 +25,10 @@ cudaError_t launch_walk(const WalkArgs& a, int grid, int tb, size_t smem, cudaSt
 }
 }  // namespace
 
-WalkLauncher TT_LOOKUP(int cpt, int lpr) {
-#define TT_CASE(C, L) if (cpt == C && lpr == L) return &launch_walk<C, L>;
+WalkLauncher TT_LOOKUP(int cpt, int lpr, int fam) {
+#define TT_CASE(C, L)                                                        \
+  if (cpt == C && lpr == L)                                                  \
+    return fam == 2 ? &launch_walk<C, L, 2> : fam == 1 ? &launch_walk<C, L, 1> : &launch_walk<C, L, 0>;
   TT_CASE(1, 8) TT_CASE(2, 4) TT_CASE(4, 2) TT_CASE(8, 1)     // rank 8
   TT_CASE(1, 16) TT_CASE(2, 8) TT_CASE(4, 4) TT_CASE(8, 2)    // rank 16
   TT_CASE(1, 32) TT_CASE(2, 16) TT_CASE(4, 8) TT_CASE(8, 4)   // rank 32

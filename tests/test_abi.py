@@ -64,14 +64,15 @@ def test_status_strings():
 
 
 def test_variant_table():
-    assert tt.num_variants() == 40
+    assert tt.num_variants() == 120
     for order in (3, 4):
         for rank in (1, 8, 10, 16, 20, 32, 40, 64):
             for prec in ("fp32", "bf16", "bf16f"):
                 v = tt.default_variant(order, rank, prec)
                 assert v >= 0 and tt.variant_valid(v, order, rank, prec)
     info = tt.variant_info(tt.default_variant(3, 32, "fp32"))
-    assert info["threads"] in (256, 512) and info["cols_per_lane"] == 4
+    assert info["threads"] in (256, 512) and info["cols_per_lane"] == 4 and info["staged"] == 1
+    assert tt.variant_info(3)["staged"] == 0 and tt.variant_info(43)["name"].startswith("stage")
 
 
 def test_invalid_csf_rejected_before_device_use():

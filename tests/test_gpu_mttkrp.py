@@ -44,6 +44,7 @@ def run_plan(B, factors, prec="fp32", select=tt.SELECT_DEFAULT, variant=0, reps=
     for _ in range(reps):
         plan.mttkrp(A)
         outs.append(A.to_array((B.dims[0], R)))
+    assert plan.device_error() == 0
     return outs if reps > 1 else outs[0], plan
 
 
@@ -76,11 +77,17 @@ def test_c1_every_variant(c1):
     for v in range(tt.num_variants()):
         if not tt.variant_valid(v, 3, 32, "fp32"):
             continue
+        print("variant", v, tt.variant_info(v)["name"], flush=True)
+        try:
+            got, plan = run_plan(B, facs, select=tt.SELECT_FIXED, variant=v)
+        except tt.TTError as e:
+            # staged variants whose largest fiber window does not fit shared memory
+            assert e.status == tt.TT_ERR_UNSUPPORTED and tt.variant_info(v)["staged"] == 1
+            continue
         nvalid += 1
-        got, plan = run_plan(B, facs, select=tt.SELECT_FIXED, variant=v)
         assert plan.variant == v
         close(got, ref)
-    assert nvalid >= 30
+    assert nvalid >= 50
 
 
 def test_c1_deterministic_and_tickets_reset(c1):
@@ -130,9 +137,10 @@ def test_long_fiber_spans_many_blocks():
     B = tt.csf_from_coo((20, 10, L), co, rng.random(len(co)).astype(np.float32))
     facs = [tt.gen_dense(10, 32, 1, 1), tt.gen_dense(L, 32, 1, 2)]
     ref = O.mttkrp(to_oracle(B), facs)
-    for v in (0, 17, 39):
-        got, _ = run_plan(B, facs, select=tt.SELECT_FIXED, variant=v)
-        close(got, ref)
+    for v in (0, 17, 39, 41, 57, 65):
+        if tt.variant_valid(v, 3, 32):
+            got, _ = run_plan(B, facs, select=tt.SELECT_FIXED, variant=v)
+            close(got, ref)
 
 
 def test_edge_cases():
@@ -185,7 +193,11 @@ def test_mttkrp4_variants(c5_small):
     B, facs, ref = c5_small
     for v in range(tt.num_variants()):
         if tt.variant_valid(v, 4, 32, "fp32") and v % 3 == 0:
-            got, _ = run_plan(B, facs, select=tt.SELECT_FIXED, variant=v)
+            try:
+                got, _ = run_plan(B, facs, select=tt.SELECT_FIXED, variant=v)
+            except tt.TTError as e:
+                assert e.status == tt.TT_ERR_UNSUPPORTED
+                continue
             close(got, ref)
     got, _ = run_plan(B, facs)
     close(got, ref)
@@ -200,5 +212,5 @@ def test_sweep_selects_a_timed_variant(c1):
     times = plan.sweep_times()
     assert plan.selected_by == 2
     timed = times[times > 0]
-    assert len(timed) >= 30 and times[plan.variant] == timed.min()
+    assert len(timed) >= 50 and times[plan.variant] == timed.min()
     close(got, ref)
