@@ -99,6 +99,25 @@ tt_status tt_plan_create(const taco_tensor_t* B, tt_op op, int32_t rank, tt_prec
                          tt_select select, int32_t variant, void* stream, tt_plan** plan);
 tt_status tt_plan_destroy(tt_plan* plan);
 
+/* Plan options (zero-initialise; NULL means all defaults). */
+typedef struct tt_plan_options {
+  /* MTTKRP over a dense-root CSF: split the last mode's index range into this
+   * many slabs and run one walk pass per slab, each adding into A, so that one
+   * slab's rows of the last factor stay resident in L2 (about 32 MB each).
+   * 0: automatic; 1: no slabs; at most 16. */
+  int32_t slabs;
+  /* L2 policy of factor-row gathers in the lean walk: 0 automatic (evict_last
+   * without slabs, evict_normal with them), 1 evict_last, 2 evict_normal. */
+  int32_t l2_policy;
+  int32_t reserved[6];
+} tt_plan_options;
+
+tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t rank, tt_precision prec,
+                            tt_select select, int32_t variant, const tt_plan_options* options,
+                            void* stream, tt_plan** plan);
+/* Slabs the plan runs (1: none). */
+int32_t tt_plan_slabs(const tt_plan* plan);
+
 /*
  * Give the plan its factor matrices: factors[m-1] is the mode-m factor,
  * a DEVICE FP32 row-major array of dims[m] x rank, for m = 1..order-1.
@@ -150,7 +169,7 @@ tt_status tt_ttv_host(taco_tensor_t* y, const taco_tensor_t* B, const taco_tenso
  * be 16-byte aligned; the CSF must be valid (tt_csf_validate on the host copy).
  * rank must be 8, 16, 32 or 64.  Limits: nrows <= 524,288 and
  * nnz <= 16,777,216; larger inputs return TT_ERR_INVALID_ARGUMENT (use the
- * plan API).  The call allocates nothing: its scratch is a fixed 4.2 MB device
+ * plan API).  The call allocates nothing: its scratch is a fixed 4.7 MB device
  * array that every GPU loading this library holds until the process exits.
  * The first call on each device looks that array's address up (make it before
  * any stream capture).  All calls share the array, so calls whose work

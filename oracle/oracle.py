@@ -53,6 +53,10 @@ def lib():
         _lib.oracle_build_csf.restype = ctypes.c_int64
         _lib.oracle_now_ms.restype = ctypes.c_double
         _lib.oracle_max_threads.restype = ctypes.c_int
+        _lib.oracle_mlp_num_params.restype = ctypes.c_int64
+        _lib.oracle_mlp_num_params.argtypes = [ctypes.c_int]
+        _lib.oracle_mlp_forward.argtypes = [_P, ctypes.c_int, _P, ctypes.c_int, _P]
+        _lib.oracle_mlp_grad.argtypes = [_P, ctypes.c_int, _P, ctypes.c_int, _P, _P, _P, _P]
     return _lib
 
 
@@ -237,3 +241,28 @@ def ref_ttv(csf: Csf, c: np.ndarray) -> np.ndarray:
     r.ref_ttv(_I(csf.dims[0]), _I(csf.dims[1]), _I(csf.dims[2]), _ptr(p1), _ptr(c1), _ptr(p2),
               _ptr(c2), _ptr(_cf(csf.vals)), _ptr(c), _ptr(y))
     return y
+
+
+# ---------------------------------------------------------------------------
+# selector network (FP64): forward and masked-MSE gradient
+# ---------------------------------------------------------------------------
+def mlp_num_params(nout: int) -> int:
+    return int(lib().oracle_mlp_num_params(nout))
+
+
+def mlp_forward(params: np.ndarray, nout: int, X: np.ndarray) -> np.ndarray:
+    p = _cf(params)
+    x = _cf(X)
+    out = np.zeros((x.shape[0], nout), dtype=np.float64)
+    lib().oracle_mlp_forward(_ptr(p), nout, _ptr(x), x.shape[0], _ptr(out))
+    return out
+
+
+def mlp_grad(params: np.ndarray, nout: int, X: np.ndarray, T: np.ndarray, M: np.ndarray):
+    """(loss, grads) of sum M (net(X) - T)^2 / sum M."""
+    p = _cf(params)
+    x, t, m = _cf(X), _cf(T), _cf(M)
+    g = np.zeros_like(p)
+    loss = np.zeros(1, dtype=np.float64)
+    lib().oracle_mlp_grad(_ptr(p), nout, _ptr(x), x.shape[0], _ptr(t), _ptr(m), _ptr(g), _ptr(loss))
+    return float(loss[0]), g

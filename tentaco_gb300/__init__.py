@@ -80,6 +80,8 @@ def lib():
         "tt_variant_default": (C.c_int32, [C.c_int32, C.c_int32, S, C.c_int64]),
         "tt_variant_valid": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, S]),
         "tt_plan_create": (S, [_TP, S, C.c_int32, S, S, C.c_int32, _P, C.POINTER(_P)]),
+        "tt_plan_create_ex": (S, [_TP, S, C.c_int32, S, S, C.c_int32, _P, _P, C.POINTER(_P)]),
+        "tt_plan_slabs": (C.c_int32, [_P]),
         "tt_plan_destroy": (S, [_P]),
         "tt_plan_set_factors": (S, [_P, C.POINTER(_P), _P]),
         "tt_plan_mttkrp": (S, [_P, _P, _P]),
@@ -115,6 +117,15 @@ def lib():
         "tt_device_count": (C.c_int32, []),
         "tt_l2_flush": (S, [_P]),
         "get_gpu_timer_result": (C.c_float, []),
+        "tt_mlp_num_params": (C.c_int64, [C.c_int32]),
+        "tt_mlp_scratch_floats": (C.c_int64, [C.c_int32, C.c_int32]),
+        "tt_mlp_forward": (S, [_P, C.c_int32, _P, C.c_int32, _P, _P, _P]),
+        "tt_mlp_grad": (S, [_P, C.c_int32, _P, C.c_int32, _P, _P, _P, _P, _P, _P]),
+        "tt_mlp_adam": (S, [_P, _P, _P, _P, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                            C.c_int32, _P]),
+        "tt_selector_load": (S, [C.c_char_p]),
+        "tt_selector_models": (C.c_int32, []),
+        "tt_selector_scores": (S, [_TP, C.c_int32, S, C.POINTER(C.c_float), C.c_int32]),
         "ttv_csf_gpu_taco": (None, [_TP, _TP, _TP]),
     }
     for name, (res, args) in sig.items():
@@ -341,14 +352,28 @@ class DeviceBuffer:
             self.ptr = _P()
 
 
+class PlanOptions(C.Structure):
+    _fields_ = [("slabs", C.c_int32), ("l2_policy", C.c_int32), ("reserved", C.c_int32 * 6)]
+
+
 class Plan:
-    def __init__(self, B, op=OP_MTTKRP, rank=32, prec="fp32", select=SELECT_DEFAULT, variant=0, stream=None):
+    """slabs: leaf-mode slabs for MTTKRP (None/0 automatic, 1 none, up to 16)."""
+
+    def __init__(self, B, op=OP_MTTKRP, rank=32, prec="fp32", select=SELECT_DEFAULT, variant=0, stream=None,
+                 slabs=None, l2_policy=0):
         self.ptr = _P()
         self.op = op
         self.rank = rank
         self.dims = B.dims
-        check(lib().tt_plan_create(_tensor_ptr(B), op, rank, PRECISIONS.get(prec, prec), select, variant,
-                                   stream, C.byref(self.ptr)))
+        opts = PlanOptions()
+        opts.slabs = int(slabs or 0)
+        opts.l2_policy = int(l2_policy)
+        check(lib().tt_plan_create_ex(_tensor_ptr(B), op, rank, PRECISIONS.get(prec, prec), select, variant,
+                                      C.byref(opts), stream, C.byref(self.ptr)))
+
+    @property
+    def slabs(self) -> int:
+        return int(lib().tt_plan_slabs(self.ptr))
 
     def __del__(self):
         if getattr(self, "ptr", None) and self.ptr.value and _lib is not None:
@@ -433,3 +458,93 @@ def synchronize() -> None:
 
 def l2_flush(stream=None) -> None:
     check(lib().tt_l2_flush(stream))
+
+
+# ---------------------------------------------------------------------------
+# learned selector: the network's kernels and the model file
+# ---------------------------------------------------------------------------
+def mlp_num_params(nout: int) -> int:
+    return int(lib().tt_mlp_num_params(nout))
+
+
+class Mlp:
+    """The selector network (12 -> 64 -> 64 -> 64 -> nout) on the device, driven
+    through the library's forward / gradient / Adam kernels.  batch: rows per call."""
+
+    def __init__(self, nout: int, batch: int):
+        self.nout, self.batch = int(nout), int(batch)
+        self.np = mlp_num_params(nout)
+        f = 4
+        self.params = DeviceBuffer(self.np * f)
+        self.grads = DeviceBuffer(self.np * f)
+        self.m = DeviceBuffer(self.np * f)
+        self.v = DeviceBuffer(self.np * f)
+        self.X = DeviceBuffer(self.batch * 12 * f)
+        self.T = DeviceBuffer(self.batch * nout * f)
+        self.M = DeviceBuffer(self.batch * nout * f)
+        self.out = DeviceBuffer(self.batch * nout * f)
+        self.loss = DeviceBuffer(f)
+        self.scratch = DeviceBuffer(int(lib().tt_mlp_scratch_floats(self.batch, nout)) * f)
+
+    def _rows(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        if X.ndim != 2 or X.shape[1] != 12 or X.shape[0] > self.batch:
+            raise ValueError(f"X must be (<= {self.batch}) x 12")
+        return X
+
+    def forward(self, params: np.ndarray, X: np.ndarray) -> np.ndarray:
+        X = self._rows(X)
+        self.params.upload(np.ascontiguousarray(params, dtype=np.float32))
+        self.X.upload(X)
+        check(lib().tt_mlp_forward(self.params.ptr, self.nout, self.X.ptr, X.shape[0], self.scratch.ptr,
+                                   self.out.ptr, None))
+        return self.out.to_array((X.shape[0], self.nout))
+
+    def grad(self, params, X, T, M):
+        """(loss, gradient) of the masked mean squared error."""
+        X = self._rows(X)
+        self.params.upload(np.ascontiguousarray(params, dtype=np.float32))
+        self.X.upload(X)
+        self.T.upload(np.ascontiguousarray(T, dtype=np.float32))
+        self.M.upload(np.ascontiguousarray(M, dtype=np.float32))
+        check(lib().tt_mlp_grad(self.params.ptr, self.nout, self.X.ptr, X.shape[0], self.T.ptr, self.M.ptr,
+                                self.scratch.ptr, self.grads.ptr, self.loss.ptr, None))
+        return float(self.loss.to_array((1,))[0]), self.grads.to_array((self.np,))
+
+    def train(self, params, X, T, M, steps: int, lr: float, beta1=0.9, beta2=0.999, eps=1e-8,
+              weight_decay=0.0, log_every: int = 100):
+        """Full-batch Adam on the device; returns (final parameters, losses every log_every steps)."""
+        X = self._rows(X)
+        self.params.upload(np.ascontiguousarray(params, dtype=np.float32))
+        zeros = np.zeros(self.np, dtype=np.float32)
+        self.m.upload(zeros)
+        self.v.upload(zeros)
+        self.X.upload(X)
+        self.T.upload(np.ascontiguousarray(T, dtype=np.float32))
+        self.M.upload(np.ascontiguousarray(M, dtype=np.float32))
+        L = lib()
+        losses = []
+        for step in range(1, steps + 1):
+            check(L.tt_mlp_grad(self.params.ptr, self.nout, self.X.ptr, X.shape[0], self.T.ptr, self.M.ptr,
+                                self.scratch.ptr, self.grads.ptr, self.loss.ptr, None))
+            if step == 1 or step % log_every == 0 or step == steps:
+                losses.append(float(self.loss.to_array((1,))[0]))
+            check(L.tt_mlp_adam(self.params.ptr, self.grads.ptr, self.m.ptr, self.v.ptr, self.np, lr, beta1,
+                                beta2, eps, weight_decay, step, None))
+        return self.params.to_array((self.np,)), losses
+
+
+def selector_load(path=None) -> None:
+    check(lib().tt_selector_load(None if path is None else os.fsencode(path)))
+
+
+def selector_models() -> int:
+    return int(lib().tt_selector_models())
+
+
+def selector_scores(B, rank: int, prec="fp32") -> np.ndarray:
+    """The network's score for every variant on tensor B (device inference); +inf = not valid."""
+    n = num_variants()
+    out = np.zeros(n, dtype=np.float32)
+    check(lib().tt_selector_scores(_tensor_ptr(B), rank, PRECISIONS[prec], out.ctypes.data_as(C.POINTER(C.c_float)), n))
+    return out

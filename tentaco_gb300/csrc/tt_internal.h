@@ -53,6 +53,26 @@ tt_status csf_view(const taco_tensor_t* B, CsfView* v);
 // Full validation (monotone pos, sorted distinct crd in range, non-empty inner fibers).
 tt_status csf_check(const CsfView& v);
 
+// A dense-root CSF split into leaf-mode slabs (leaf coordinate c is in slab
+// c / width).  Each slab is a CSF with every row; its leaf arrays are the run
+// [leaf_off, leaf_off + nnz) of leaf_crd / leaf_vals (each run padded to a
+// multiple of 16 entries plus 16, zero filled).  pos[l] of a slab indexes its
+// own arrays (leaf positions relative to leaf_off).
+constexpr int kMaxSlabs = 16;
+struct SlabCsf {
+  struct Slab {
+    std::vector<int32_t> pos[TT_MAX_ORDER], crd[TT_MAX_ORDER];
+    int64_t count[TT_MAX_ORDER] = {0, 0, 0, 0};
+    int64_t nnz = 0, leaf_off = 0;
+  };
+  int S = 1, order = 0;
+  int64_t width = 0;
+  Slab slab[kMaxSlabs];
+  std::vector<int32_t> leaf_crd;
+  std::vector<float> leaf_vals;
+};
+tt_status build_slabs(const CsfView& v, int S, SlabCsf& out);
+
 // Stable parallel LSD radix sort of 64-bit keys with a 32-bit payload, on the
 // low `bits` bits.
 void radix_sort_pairs(std::vector<uint64_t>& keys, std::vector<uint32_t>& payload, int bits);

@@ -47,9 +47,14 @@ cudaError_t launch_window_max(int order, const WalkArgs& a, int* out, cudaStream
 
 cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s) {
   if (a.nblocks == 0) return cudaSuccess;
-  const int grid = (a.nblocks + 7) / 8;  // one warp per walk block
-  if (order == 3) chain_fixup_kernel<3><<<grid, 256, 0, s>>>(a);
-  else chain_fixup_kernel<4><<<grid, 256, 0, s>>>(a);
+  const int grid = (num_segments(a.nblocks) + 7) / 8;  // one warp per segment
+  if (order == 3) {
+    seg_fold_kernel<3><<<grid, 256, 0, s>>>(a);
+    seg_chain_kernel<3><<<grid, 256, 0, s>>>(a);
+  } else {
+    seg_fold_kernel<4><<<grid, 256, 0, s>>>(a);
+    seg_chain_kernel<4><<<grid, 256, 0, s>>>(a);
+  }
   return cudaGetLastError();
 }
 

@@ -58,6 +58,10 @@ struct WalkArgs {
   int32_t rp;             // factor row width the kernels were compiled for
   int32_t fac_rows[3];    // rows of each factor (bounds for checked builds)
   int32_t smem_bytes;     // dynamic shared memory of the launch (bounds for checked builds)
+  int32_t accum;          // 1: add rows into out (slab passes), 0: overwrite
+  int32_t gpol;           // L2 policy of the lean walk's factor-row gathers: 0 evict_last, 1 evict_normal
+  double* segcarry;       // cross-unit rows: 2 FP64 partial rows per segment of kSeg units
+  int32_t* segmeta;       // 4 ints per segment
   int32_t wcap;           // staged kernels: window fibers per block the shared memory holds
   int32_t* err;           // staged kernels: set nonzero if a block's window exceeds wcap
 };
@@ -98,6 +102,10 @@ __device__ __forceinline__ void cp_async_sa(uint32_t d, const void* src) {
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+// Work units per segment of the two-level cross-unit row merge.
+constexpr int kSeg = 32;
+__host__ __device__ inline int num_segments(int units) { return (units + kSeg - 1) / kSeg; }
+
 __host__ __device__ inline size_t walk_tile_bytes(int P, int vbytes) {
   return (size_t)P * 4 + (((size_t)P * vbytes + 15) & ~(size_t)15);  // crd + vals tile
 }
@@ -109,6 +117,16 @@ __host__ __device__ inline size_t walk_smem_bytes(int P, int tb, int rp, int vby
   b += (size_t)(2 * P + 4) * sizeof(int32_t);         // fiber window
   b += nw * 2 * sizeof(int32_t);                      // warp summary rows
   b += nw * 2 * (size_t)rp * sizeof(float);           // warp summary accs
+  return (b + 15) & ~(size_t)15;
+}
+
+// Lean kernel, shared memory of one warp: coordinate runs TW x (G+4) int32,
+// value runs TW x (G*vbytes + 16) bytes, window starts and coordinates (a
+// warp's window has at most TW*G + 1 fibers).
+__host__ __device__ inline size_t lean_warp_bytes(int G, int tw, int vbytes) {
+  const size_t pu = (size_t)tw * G;
+  size_t b = (size_t)tw * (G + 4) * 4 + (size_t)tw * ((size_t)G * vbytes + 16);
+  b += (pu + 2) * 4 * 2;
   return (b + 15) & ~(size_t)15;
 }
 
@@ -149,14 +167,21 @@ struct Walk {
   }
 
   // Store a finished output row (scaled).
+  // Store a finished output row (scaled); slab passes add into the row (each
+  // row has one writer per pass, and passes run in order on one stream).
   __device__ __forceinline__ void store_row(int ip, const float (&acc)[CPT]) const {
     float* o = a.out + row_id(ip) * a.ldo + q * CPT;
     if (CPT == 4 && a.R == RP && (a.ldo & 3) == 0) {
-      *reinterpret_cast<float4*>(o) = make_float4(acc[0] * sc[0], acc[1] * sc[1], acc[2] * sc[2], acc[3] * sc[3]);
+      float4 r = make_float4(acc[0] * sc[0], acc[1] * sc[1], acc[2] * sc[2], acc[3] * sc[3]);
+      if (a.accum) {
+        const float4 o4 = *reinterpret_cast<const float4*>(o);
+        r.x += o4.x; r.y += o4.y; r.z += o4.z; r.w += o4.w;
+      }
+      *reinterpret_cast<float4*>(o) = r;
     } else {
 #pragma unroll
       for (int c = 0; c < CPT; c++)
-        if (q * CPT + c < a.R) o[c] = acc[c] * sc[c];
+        if (q * CPT + c < a.R) o[c] = acc[c] * sc[c] + (a.accum ? o[c] : 0.f);
     }
   }
 
@@ -357,6 +382,189 @@ struct Walk {
 
   // Bytes of its factor row one lane loads per nonzero (its CPT columns).
   static constexpr int LB = CPT * (FK == kF32 ? 4 : 2);
+
+  // ---- lean walk (family 0) ------------------------------------------------
+  static constexpr int NWD = LB >= 4 ? LB / 4 : 1;  // 32-bit words of a lane's row piece
+  static constexpr int FRB = RP * (FK == kF32 ? 4 : 2);  // bytes per factor row
+
+  // The lane's piece (LB bytes) of a factor row, as raw words: the load is
+  // issued now, the conversion happens when the words are used.
+  __device__ __forceinline__ static void piece_load(const unsigned char* p, uint64_t pol, uint32_t (&w)[NWD]) {
+    if constexpr (LB == 32) {
+      const uint4 x = ld_gather_16(p, pol), y = ld_gather_16(p + 16, pol);
+      w[0] = x.x; w[1] = x.y; w[2] = x.z; w[3] = x.w; w[4] = y.x; w[5] = y.y; w[6] = y.z; w[7] = y.w;
+    } else if constexpr (LB == 16) {
+      const uint4 x = ld_gather_16(p, pol);
+      w[0] = x.x; w[1] = x.y; w[2] = x.z; w[3] = x.w;
+    } else if constexpr (LB == 8) {
+      const uint2 x = ld_gather_8(p, pol);
+      w[0] = x.x; w[1] = x.y;
+    } else if constexpr (LB == 4) {
+      w[0] = ld_gather_4(p, pol);
+    } else {
+      w[0] = ld_gather_2(p, pol);
+    }
+  }
+  __device__ __forceinline__ static void piece_cvt(const uint32_t (&w)[NWD], float (&g)[CPT]) {
+#pragma unroll
+    for (int c = 0; c < CPT; c++) {
+      if constexpr (FK == kF32) g[c] = __uint_as_float(w[c]);
+      else g[c] = (c & 1) ? hi16<FK>(w[c >> 1]) : lo16<FK>(w[c >> 1]);
+    }
+  }
+  // U consecutive stored values of a team's tile (16-byte aligned run).
+  template <int U>
+  __device__ __forceinline__ static void vals_load(const unsigned char* vt, float (&v)[U]) {
+    if constexpr (VK == kF32) {
+#pragma unroll
+      for (int k = 0; k < U / 4; k++) {
+        const float4 f = reinterpret_cast<const float4*>(vt)[k];
+        v[4 * k] = f.x; v[4 * k + 1] = f.y; v[4 * k + 2] = f.z; v[4 * k + 3] = f.w;
+      }
+    } else if constexpr (U == 8) {
+      const uint4 w = *reinterpret_cast<const uint4*>(vt);
+      v[0] = lo16<VK>(w.x); v[1] = hi16<VK>(w.x); v[2] = lo16<VK>(w.y); v[3] = hi16<VK>(w.y);
+      v[4] = lo16<VK>(w.z); v[5] = hi16<VK>(w.z); v[6] = lo16<VK>(w.w); v[7] = hi16<VK>(w.w);
+    } else {
+      static_assert(U == 4, "batches of 4 or 8 nonzeros");
+      const uint2 w = *reinterpret_cast<const uint2*>(vt);
+      v[0] = lo16<VK>(w.x); v[1] = hi16<VK>(w.x); v[2] = lo16<VK>(w.y); v[3] = hi16<VK>(w.y);
+    }
+  }
+  __device__ __forceinline__ static float val_one(const unsigned char* vt, int j) {
+    if constexpr (VK == kF32) return reinterpret_cast<const float*>(vt)[j];
+    else return lo16<VK>((uint32_t)reinterpret_cast<const uint16_t*>(vt)[j]);
+  }
+
+  // Serial walk of this team's n nonzeros starting at absolute position s.
+  //   lc, vt: the team's coordinate / value run in shared memory (entry 0 = s)
+  // Nonzero-level factor rows are gathered U nonzeros per batch into registers,
+  // one batch ahead of use (two register buffers); the window-level factor row
+  // of the next fiber is loaded when the current one starts.  The fold of a
+  // finished fiber and the row bookkeeping are the only branches.
+  template <int U>
+  __device__ __forceinline__ void walk_lean(int s, int n, const int32_t* lc, const unsigned char* vt,
+                                            const int32_t* s_pos, const int32_t* s_fcrd, int W, int fs,
+                                            const int32_t* pb, const int32_t* pn, Summ<CPT>& X) const {
+    const uint64_t pol = a.gpol == 1 ? policy_evict_normal() : policy_evict_last();
+    const int32_t* pos1 = a.pos[1];
+    const unsigned char* fz = static_cast<const unsigned char*>(a.fac[ORDER - 2]) + q * LB;
+    const unsigned char* fw = static_cast<const unsigned char*>(a.fac[ORDER == 3 ? 0 : 1]) + q * LB;
+    int x = (int)search_le(s_pos, 0, W - 1, s);
+    int fend = s_pos[x + 1];
+    int f1 = 0, kend = 0, ip;
+    float crow[CPT];
+    if constexpr (ORDER == 3) {
+      ip = (int)search_le(pos1, pb[0], pn[0], fs + x);
+    } else {
+      f1 = (int)search_le(a.pos[2], pb[1], pn[1], fs + x);
+      kend = a.pos[2][f1 + 1];
+      ip = (int)search_le(pos1, pb[0], pn[0], f1);
+      frow(0, a.crd[1][f1], pol, crow);
+    }
+    int rend = pos1[ip + 1];
+    uint32_t wc[NWD], wn[NWD];
+    piece_load(fw + (size_t)(uint32_t)s_fcrd[x] * FRB, pol, wc);
+    if (x + 1 < W) piece_load(fw + (size_t)(uint32_t)s_fcrd[x + 1] * FRB, pol, wn);
+    float f3[CPT], f2[CPT], ra[CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; c++) { f3[c] = 0.f; f2[c] = 0.f; ra[c] = 0.f; }
+    bool flushed = false;
+
+    // the current window fiber ended: fold its partial into the parent level
+    auto fold = [&]() {
+      float cw[CPT];
+      piece_cvt(wc, cw);
+      if constexpr (ORDER == 3) {
+#pragma unroll
+        for (int c = 0; c < CPT; c++) { ra[c] = fmaf(f3[c], cw[c], ra[c]); f3[c] = 0.f; }
+      } else {
+#pragma unroll
+        for (int c = 0; c < CPT; c++) { f2[c] = fmaf(f3[c], cw[c], f2[c]); f3[c] = 0.f; }
+      }
+      x++;
+      fend = s_pos[x + 1];
+#pragma unroll
+      for (int k = 0; k < NWD; k++) wc[k] = wn[k];
+      if (x + 1 < W) piece_load(fw + (size_t)(uint32_t)s_fcrd[x + 1] * FRB, pol, wn);
+      const int fg = fs + x;
+      if constexpr (ORDER == 4) {
+        while (fg >= kend) {
+#pragma unroll
+          for (int c = 0; c < CPT; c++) { ra[c] = fmaf(f2[c], crow[c], ra[c]); f2[c] = 0.f; }
+          f1++;
+          kend = a.pos[2][f1 + 1];
+          while (f1 >= rend) { flush(ip, ra, flushed, X); ip++; rend = pos1[ip + 1]; }
+          frow(0, a.crd[1][f1], pol, crow);
+        }
+      } else {
+        while (fg >= rend) { flush(ip, ra, flushed, X); ip++; rend = pos1[ip + 1]; }
+      }
+    };
+    auto load = [&](uint32_t (&g)[U][NWD], int j) {
+      int32_t l[U];
+#pragma unroll
+      for (int k = 0; k < U / 4; k++) {
+        const int4 c4 = reinterpret_cast<const int4*>(lc + j)[k];
+        l[4 * k] = c4.x; l[4 * k + 1] = c4.y; l[4 * k + 2] = c4.z; l[4 * k + 3] = c4.w;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) piece_load(fz + (size_t)(uint32_t)l[u] * FRB, pol, g[u]);
+    };
+    auto consume = [&](const uint32_t (&g)[U][NWD], int j) {
+      float v[U];
+      vals_load<U>(vt + (size_t)j * VB, v);
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        while (s + j + u >= fend) fold();
+        float d[CPT];
+        piece_cvt(g[u], d);
+#pragma unroll
+        for (int c = 0; c < CPT; c++) f3[c] = fmaf(v[u], d[c], f3[c]);
+      }
+    };
+    const int nb = n / U;
+    uint32_t gA[U][NWD], gB[U][NWD];
+    if (nb > 0) load(gA, 0);
+    for (int b = 0; b < nb; b += 2) {
+      if (b + 1 < nb) load(gB, (b + 1) * U);
+      consume(gA, b * U);
+      if (b + 1 < nb) {
+        if (b + 2 < nb) load(gA, (b + 2) * U);
+        consume(gB, (b + 1) * U);
+      }
+    }
+    for (int j = nb * U; j < n; j++) {  // ragged end (the tensor's last tile only)
+      uint32_t g[NWD];
+      piece_load(fz + (size_t)(uint32_t)lc[j] * FRB, pol, g);
+      const float v = val_one(vt, j);
+      while (s + j >= fend) fold();
+      float d[CPT];
+      piece_cvt(g, d);
+#pragma unroll
+      for (int c = 0; c < CPT; c++) f3[c] = fmaf(v, d[c], f3[c]);
+    }
+    {
+      float cw[CPT];
+      piece_cvt(wc, cw);
+      if constexpr (ORDER == 3) {
+#pragma unroll
+        for (int c = 0; c < CPT; c++) ra[c] = fmaf(f3[c], cw[c], ra[c]);
+      } else {
+#pragma unroll
+        for (int c = 0; c < CPT; c++) { f2[c] = fmaf(f3[c], cw[c], f2[c]); ra[c] = fmaf(f2[c], crow[c], ra[c]); }
+      }
+    }
+    if (!flushed) {
+      X.h = ip; X.t = kNone;
+#pragma unroll
+      for (int c = 0; c < CPT; c++) X.ha[c] = ra[c];
+    } else {
+      X.t = ip;
+#pragma unroll
+      for (int c = 0; c < CPT; c++) X.ta[c] = ra[c];
+    }
+  }
 
   // Serial walk like walk(), but every factor row piece the lane needs is copied
   // with cp.async into this lane's own shared-memory slots, DP nonzeros ahead of
@@ -646,20 +854,16 @@ struct Walk {
 // team over the warps), then settle the block's first and last rows: a row that
 // starts and ends inside the block is stored; a row shared with a neighbouring
 // block is written to the block's carry slot (0: first row, 1: last row) for
-// chain_fixup_kernel.  No fence, atomic or second barrier: the block ends here.
+// the segment fold.  No fence, atomic or second barrier: the block ends here.
 //   head_ff  first window-level fiber of the block's first row (loaded at start)
 //   meta[b]  {first row, last row, flags}: bit0 first row started before the
 //            block, bit1 last row continues after it, bit2 single-row block
+// Warp-level merge of the team summaries (tree over teams, keyed by row); the
+// result is left in the first team's lanes.
 template <int ORDER, int PREC, int CPT, int LPR>
-__device__ __forceinline__ void block_merge(const WalkArgs& a, const Walk<ORDER, PREC, CPT, LPR>& wk,
-                                            Summ<CPT>& X, int32_t* s_wh, int32_t* s_wt, float* s_wha,
-                                            float* s_wta, int64_t head_ff, int64_t fs, int64_t win0,
-                                            int64_t bstart, int next_row, int b) {
-  constexpr int RP = CPT * LPR;
+__device__ __forceinline__ void warp_tree(const Walk<ORDER, PREC, CPT, LPR>& wk, Summ<CPT>& X) {
   constexpr int TW = 32 / LPR;
-  const int tb = blockDim.x, nw = tb / 32;
-  const int team = threadIdx.x / LPR, q = threadIdx.x % LPR, tw = team % TW, warp = threadIdx.x / 32;
-  // Warp-level merge of team summaries (tree over teams, keyed by row).
+  const int tw = (threadIdx.x & 31) / LPR;
 #pragma unroll
   for (int d = 1; d < TW; d <<= 1) {
     Summ<CPT> Y;
@@ -672,6 +876,66 @@ __device__ __forceinline__ void block_merge(const WalkArgs& a, const Walk<ORDER,
     }
     if ((tw & (2 * d - 1)) == 0 && tw + d < TW) wk.combine(X, Y);
   }
+}
+
+// Settle the first and last rows of work unit b (a block, or a warp's tile in
+// the lean kernel) from its merged summary X; run by the LPR lanes holding X.
+// A row that starts and ends inside the unit is stored; a row shared with a
+// neighbouring unit is written to the unit's carry slot (0: first row, 1: last
+// row) for the segment fold (seg_fold_kernel / seg_chain_kernel).
+//   head_ff  first window-level fiber of the unit's first row
+//   meta[b]  {first row, last row, flags}: bit0 first row started before the
+//            unit, bit1 last row continues after it, bit2 single-row unit
+template <int ORDER, int PREC, int CPT, int LPR>
+__device__ __forceinline__ void settle_unit(const WalkArgs& a, const Walk<ORDER, PREC, CPT, LPR>& wk,
+                                            const Summ<CPT>& X, int64_t head_ff, int64_t fs, int64_t win0,
+                                            int64_t bstart, int next_row, int b, int q) {
+  constexpr int RP = CPT * LPR;
+  const bool single = X.t == kNone;
+  const int last = single ? X.h : X.t;
+  const bool h_before = head_ff < fs || (head_ff == fs && win0 < bstart);
+  const bool l_after = b + 1 < a.nblocks && next_row == last;
+  float* c0 = a.carry + ((size_t)(2 * b)) * RP + q * CPT;
+  float* c1 = c0 + RP;
+  if (single) {
+    if (h_before || l_after) {
+#pragma unroll
+      for (int c = 0; c < CPT; c++) c0[c] = X.ha[c] * wk.sc[c];
+    } else {
+      wk.store_row(X.h, X.ha);
+    }
+  } else {
+    if (h_before) {
+#pragma unroll
+      for (int c = 0; c < CPT; c++) c0[c] = X.ha[c] * wk.sc[c];
+    } else {
+      wk.store_row(X.h, X.ha);
+    }
+    if (l_after) {
+#pragma unroll
+      for (int c = 0; c < CPT; c++) c1[c] = X.ta[c] * wk.sc[c];
+    } else {
+      wk.store_row(X.t, X.ta);
+    }
+  }
+  if (q == 0)
+    reinterpret_cast<int4*>(a.meta)[b] =
+        make_int4(X.h, last, (h_before ? 1 : 0) | (l_after ? 2 : 0) | (single ? 4 : 0), 0);
+}
+
+// Merge the teams' summaries of one block (warp trees, then the first team over
+// the warps) and settle the block's rows.  No fence, atomic or second barrier:
+// the block ends here.
+template <int ORDER, int PREC, int CPT, int LPR>
+__device__ __forceinline__ void block_merge(const WalkArgs& a, const Walk<ORDER, PREC, CPT, LPR>& wk,
+                                            Summ<CPT>& X, int32_t* s_wh, int32_t* s_wt, float* s_wha,
+                                            float* s_wta, int64_t head_ff, int64_t fs, int64_t win0,
+                                            int64_t bstart, int next_row, int b) {
+  constexpr int RP = CPT * LPR;
+  constexpr int TW = 32 / LPR;
+  const int tb = blockDim.x, nw = tb / 32;
+  const int team = threadIdx.x / LPR, q = threadIdx.x % LPR, tw = team % TW, warp = threadIdx.x / 32;
+  warp_tree(wk, X);
   if (tw == 0) {
     if (q == 0) { s_wh[warp] = X.h; s_wt[warp] = X.t; }
 #pragma unroll
@@ -686,43 +950,14 @@ __device__ __forceinline__ void block_merge(const WalkArgs& a, const Walk<ORDER,
       Summ<CPT> Y;
       Y.h = s_wh[w];
       Y.t = s_wt[w];
-  #pragma unroll
+#pragma unroll
       for (int c = 0; c < CPT; c++) {
         Y.ha[c] = s_wha[w * RP + q * CPT + c];
         Y.ta[c] = s_wta[w * RP + q * CPT + c];
       }
       wk.combine(X, Y);
     }
-    const bool single = X.t == kNone;
-    const int last = single ? X.h : X.t;
-    const bool h_before = head_ff < fs || (head_ff == fs && win0 < bstart);
-    const bool l_after = b + 1 < a.nblocks && next_row == last;
-    float* c0 = a.carry + ((size_t)(2 * b)) * RP + q * CPT;
-    float* c1 = c0 + RP;
-    if (single) {
-      if (h_before || l_after) {
-  #pragma unroll
-        for (int c = 0; c < CPT; c++) c0[c] = X.ha[c] * wk.sc[c];
-      } else {
-        wk.store_row(X.h, X.ha);
-      }
-    } else {
-      if (h_before) {
-  #pragma unroll
-        for (int c = 0; c < CPT; c++) c0[c] = X.ha[c] * wk.sc[c];
-      } else {
-        wk.store_row(X.h, X.ha);
-      }
-      if (l_after) {
-  #pragma unroll
-        for (int c = 0; c < CPT; c++) c1[c] = X.ta[c] * wk.sc[c];
-      } else {
-        wk.store_row(X.t, X.ta);
-      }
-    }
-    if (q == 0)
-      reinterpret_cast<int4*>(a.meta)[b] =
-          make_int4(X.h, last, (h_before ? 1 : 0) | (l_after ? 2 : 0) | (single ? 4 : 0), 0);
+    settle_unit(a, wk, X, head_ff, fs, win0, bstart, next_row, b, q);
   }
 }
 
@@ -735,34 +970,123 @@ __device__ __forceinline__ int64_t row_first_window_fiber(const WalkArgs& a, int
 }
 
 #ifndef TT_ARGS_ONLY
-// Sum every cross-block row in FP64, in a fixed order (deterministic).  One warp
-// per walk block; the warp of the block where a shared row starts owns that
-// row's chain of block partials.  Short chains: lane = column, blocks in order.
-// Long chains: lane = block stripe, every lane accumulates all columns, then a
-// fixed butterfly over lanes.
+// ---------------------------------------------------------------------------
+// Cross-unit rows.  Each work unit left at most two carry entries (settle_unit):
+// a partial of its first row (it started in an earlier unit) and/or of its last
+// row (it continues in a later unit).  In unit order the entries of one row are
+// consecutive, so every shared row is a run of entries.  The runs are summed in
+// FP64 in two levels, each in a fixed order (bitwise reproducible):
+//   seg_fold_kernel   one warp per segment of kSeg units, lanes over columns:
+//                     sums each run inside the segment; a run that starts and
+//                     ends in the segment is final and written to the output,
+//                     the segment's first/last run, if it crosses the segment's
+//                     edge, goes to the segment's FP64 carry slot (same meta
+//                     layout as the units', one level up);
+//   seg_chain_kernel  one warp per segment where a crossing row starts: sums the
+//                     row's segment partials (lane = column for short chains,
+//                     lane = segment stripe plus a fixed butterfly for long ones).
+// ---------------------------------------------------------------------------
+// Final value of output row r, column j (slab passes add into the row).
+__device__ __forceinline__ void put_row_value(const WalkArgs& a, int r, int j, double v) {
+  const int64_t row = a.crd[0] ? (int64_t)a.crd[0][r] : (int64_t)r;
+  float* o = a.out + row * a.ldo + j;
+  *o = (float)(a.accum ? v + (double)*o : v);
+}
+
+template <int ORDER>  // (the fold itself does not depend on the order)
+__global__ void __launch_bounds__(256) seg_fold_kernel(const __grid_constant__ WalkArgs a) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sg = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (sg >= num_segments(a.nblocks)) return;
+  const int u0 = sg * kSeg, n = min(kSeg, a.nblocks - u0);
+  const int rp = a.rp;
+  const bool two = rp > 32;  // columns lane and lane + 32
+  int4 mine = make_int4(-1, -1, 0, 0);
+  if (lane < n) mine = reinterpret_cast<const int4*>(a.meta)[u0 + lane];
+  // the current run
+  int cur = -1;
+  bool cur_before = false, cur_after = false, first_run = true;
+  double s0 = 0.0, s1 = 0.0;
+  // the segment's summary
+  int sfirst = -1, slast = -1, sflags = 0, nruns = 0;
+  double* sc0 = a.segcarry + (size_t)(2 * sg) * rp;
+  double* sc1 = sc0 + rp;
+  auto close_run = [&]() {
+    nruns++;
+    if (!cur_before && !cur_after) {
+      if (lane < a.R) put_row_value(a, cur, lane, s0);
+      if (two && lane + 32 < a.R) put_row_value(a, cur, lane + 32, s1);
+    } else if (cur_before) {  // necessarily the segment's first run
+      sfirst = cur;
+      sflags |= 1;
+      if (cur_after) { slast = cur; sflags |= 2; }
+      if (lane < rp) sc0[lane] = s0;
+      if (two) sc0[lane + 32] = s1;
+    } else {  // cur_after only: the segment's last run
+      slast = cur;
+      sflags |= 2;
+      double* d = first_run ? sc0 : sc1;  // alone in the segment: slot 0
+      if (lane < rp) d[lane] = s0;
+      if (two) d[lane + 32] = s1;
+    }
+    if (first_run && sfirst < 0) sfirst = cur;
+    first_run = false;
+  };
+  auto entry = [&](int r, size_t slot, bool before, bool after) {
+    if (r != cur) {
+      if (cur >= 0) close_run();
+      cur = r;
+      cur_before = before;
+      s0 = s1 = 0.0;
+    }
+    const float* c = a.carry + slot * rp;
+    if (lane < rp) s0 += (double)c[lane];
+    if (two) s1 += (double)c[lane + 32];
+    cur_after = after;
+  };
+  for (int k = 0; k < n; k++) {
+    const int mx = __shfl_sync(0xffffffffu, mine.x, k);
+    const int my = __shfl_sync(0xffffffffu, mine.y, k);
+    const int mz = __shfl_sync(0xffffffffu, mine.z, k);
+    const bool hb = mz & 1, la = mz & 2, single = mz & 4;
+    const size_t u = (size_t)(u0 + k);
+    if (single) {
+      if (hb || la) entry(mx, 2 * u, hb, la);
+    } else {
+      if (hb) entry(mx, 2 * u, true, false);
+      if (la) entry(my, 2 * u + 1, false, true);
+    }
+  }
+  if (cur >= 0) close_run();
+  if (slast < 0) slast = cur;
+  if (lane == 0) {
+    // bit2: one run in the segment (its partial, if any, is in slot 0)
+    reinterpret_cast<int4*>(a.segmeta)[sg] = make_int4(sfirst, slast, sflags | (nruns == 1 ? 4 : 0), 0);
+  }
+}
+
 template <int ORDER>
-__global__ void __launch_bounds__(256) chain_fixup_kernel(const __grid_constant__ WalkArgs a) {
+__global__ void __launch_bounds__(256) seg_chain_kernel(const __grid_constant__ WalkArgs a) {
   constexpr int kShort = 16;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int b = blockIdx.x * (blockDim.x >> 5) + warp;
-  if (b >= a.nblocks) return;
-  const int4 m = reinterpret_cast<const int4*>(a.meta)[b];
-  const bool h_before = m.z & 1, l_after = m.z & 2, single = m.z & 4;
-  if (!l_after || (single && h_before)) return;  // warp-uniform: no chain starts here
+  const int sg = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (sg >= num_segments(a.nblocks)) return;
+  const int4 m = reinterpret_cast<const int4*>(a.segmeta)[sg];
+  const bool before = m.z & 1, after = m.z & 2, single = m.z & 4;
+  if (!after || (single && before)) return;  // warp-uniform: no crossing row starts here
   const int r = m.y;
   int64_t f1 = a.pos[1][r + 1];
   if constexpr (ORDER == 4) f1 = a.pos[2][f1];
   const int64_t n1 = a.pos[ORDER - 1][f1];
-  const int b1 = (int)((n1 - 1) / a.P);
+  const int s1 = (int)((n1 - 1) / a.P) / kSeg;  // segment holding the row's last nonzero
   const int rp = a.rp;
-  const int slot0 = single ? 0 : 1;  // this block's slot; later blocks hold the row in slot 0
-  const int64_t row = a.crd[0] ? (int64_t)a.crd[0][r] : (int64_t)r;
-  float* out = a.out + row * a.ldo;
-  if (b1 - b < kShort) {
+  const int slot0 = single ? 0 : 1;  // this segment's slot; later segments hold the row in slot 0
+  auto src = [&](int sgi) { return a.segcarry + (size_t)(2 * sgi + (sgi == sg ? slot0 : 0)) * rp; };
+  if (s1 - sg < kShort) {
     for (int j = lane; j < rp; j += 32) {
       double acc = 0.0;
-      for (int bb = b; bb <= b1; bb++) acc += (double)a.carry[((size_t)(2 * bb + (bb == b ? slot0 : 0))) * rp + j];
-      if (j < a.R) out[j] = (float)acc;
+      for (int t = sg; t <= s1; t++) acc += src(t)[j];
+      if (j < a.R) put_row_value(a, r, j, acc);
     }
     return;
   }
@@ -771,11 +1095,11 @@ __global__ void __launch_bounds__(256) chain_fixup_kernel(const __grid_constant_
     double acc[32];
 #pragma unroll
     for (int c = 0; c < 32; c++) acc[c] = 0.0;
-    for (int bb = b + lane; bb <= b1; bb += 32) {
-      const float* src = a.carry + ((size_t)(2 * bb + (bb == b ? slot0 : 0))) * rp + c0;
+    for (int t = sg + lane; t <= s1; t += 32) {
+      const double* v = src(t) + c0;
 #pragma unroll
       for (int c = 0; c < 32; c++)
-        if (c < nc) acc[c] += (double)src[c];
+        if (c < nc) acc[c] += v[c];
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
@@ -785,10 +1109,11 @@ __global__ void __launch_bounds__(256) chain_fixup_kernel(const __grid_constant_
     // every lane holds the same totals; lane c writes column c0 + c
 #pragma unroll
     for (int c = 0; c < 32; c++)
-      if (lane == c && c < nc && c0 + c < a.R) out[c0 + c] = (float)acc[c];
+      if (lane == c && c < nc && c0 + c < a.R) put_row_value(a, r, c0 + c, acc[c]);
   }
 }
-#endif
+
+#endif  // TT_ARGS_ONLY
 
 // EXACT = true: the nonzero-level crd/vals arrays are read only up to nnz (the
 // caller's own unpadded arrays); false: the plan's padded copies are read in
@@ -895,6 +1220,79 @@ __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant_
   }
 
   block_merge<ORDER, PREC, CPT, LPR>(a, wk, X, s_wh, s_wt, s_wha, s_wta, head_ff, fs, s_pos[0], bstart, pn[0], blockIdx.x);
+}
+
+// Lean kernel (family 0): every warp owns a tile of TW*G consecutive nonzeros
+// (TW = 32/LPR teams of G), which is the unit of the partition, of the carry
+// slots and of chain_fixup_kernel.  A warp stages its own tile and window with
+// 128-bit loads, walks it (walk_lean) and settles its rows: no block barrier,
+// so a warp waiting on its gathers never holds up another.
+template <int ORDER, int PREC, int CPT, int LPR, bool EXACT = false>
+__global__ void __launch_bounds__(512) mttkrp_lean_kernel(const __grid_constant__ WalkArgs a) {
+  using WK = Walk<ORDER, PREC, CPT, LPR>;
+  constexpr int VB = WK::VB;
+  constexpr int TW = 32 / LPR;
+  constexpr int U = WK::LB >= 32 ? 4 : 8;
+  static_assert(!EXACT || VB == 4, "exact-length staging is built for FP32 values");
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int u = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (u >= a.nblocks) return;  // whole warp: nothing below synchronises the block
+  const int G = a.G, PU = a.P;
+  unsigned char* ws = smem + (size_t)warp * lean_warp_bytes(G, TW, VB);
+  int32_t* s_lc = reinterpret_cast<int32_t*>(ws);
+  unsigned char* s_val = ws + (size_t)TW * (G + 4) * 4;
+  int32_t* s_pos = reinterpret_cast<int32_t*>(s_val + (size_t)TW * (G * VB + 16));
+  int32_t* s_fcrd = s_pos + (PU + 2);
+
+  const int32_t* pb = a.part + (size_t)u * (ORDER - 1);
+  const int32_t* pn = pb + (ORDER - 1);
+  const int64_t ustart64 = (int64_t)u * PU;
+  const int ustart = (int)ustart64;
+  const int cnt = (int)min((int64_t)PU, a.nnz - ustart64);
+  const int fs = pb[ORDER - 2];
+  const int W = pn[ORDER - 2] - fs + 1;
+  {
+    // chunk c (entries 4c..4c+3) belongs to team 4c >> lgG; each team's runs of
+    // coordinates and values are followed by 16 bytes of padding (bank skew)
+    const uint64_t polF = policy_evict_first();
+    const int n4 = (cnt + 3) >> 2;
+    const int32_t* gl = a.crd[ORDER - 1] + ustart64;
+    for (int c = lane; c < n4; c += 32) {
+      const int t = (4 * c) >> a.lgG;
+      if (!EXACT || 4 * c + 4 <= cnt) {
+        reinterpret_cast<int4*>(s_lc)[c + t] = ld_stream_i4(gl + 4 * c, polF);
+        if constexpr (VB == 4)
+          reinterpret_cast<float4*>(s_val)[c + t] = ld_stream_f4(static_cast<const float*>(a.vals) + ustart64 + 4 * c, polF);
+        else
+          reinterpret_cast<uint2*>(s_val)[c + 2 * t] = ld_stream_u2(static_cast<const uint16_t*>(a.vals) + ustart64 + 4 * c, polF);
+      } else {
+        for (int k = 0; k < 4; k++) {
+          const bool in = 4 * c + k < cnt;
+          s_lc[4 * (c + t) + k] = in ? gl[4 * c + k] : 0;
+          reinterpret_cast<float*>(s_val)[4 * (c + t) + k] = in ? static_cast<const float*>(a.vals)[ustart64 + 4 * c + k] : 0.f;
+        }
+      }
+    }
+    const int32_t* gpos = a.pos[ORDER - 1] + fs;
+    const int32_t* gcrd = a.crd[ORDER - 2] + fs;
+    for (int x = lane; x <= W; x += 32) s_pos[x] = gpos[x];
+    for (int x = lane; x < W; x += 32) s_fcrd[x] = gcrd[x];
+  }
+  __syncwarp();
+
+  const int team = lane / LPR, q = lane % LPR;
+  WK wk(a, q);
+  const int64_t head_ff = lane < LPR ? row_first_window_fiber<ORDER>(a, pb[0]) : 0;
+  Summ<CPT> X;
+  X.h = kEmpty;
+  X.t = kNone;
+  const int s = ustart + team * G;
+  if (s < ustart + cnt)
+    wk.template walk_lean<U>(s, min(G, ustart + cnt - s), s_lc + team * (G + 4), s_val + (size_t)team * (G * VB + 16),
+                             s_pos, s_fcrd, W, fs, pb, pn, X);
+  warp_tree(wk, X);
+  if (lane < LPR) settle_unit(a, wk, X, head_ff, fs, s_pos[0], ustart64, pn[0], u, q);
 }
 
 // Staged kernel: every factor row the block needs is gathered into shared memory

@@ -11,8 +11,8 @@
 // process exits.
 //
 // The scratch holds what the walk kernel needs besides its inputs and outputs:
-// the per-block partition, the per-block row metadata and the cross-block carry
-// rows.
+// the per-block partition, the per-block row metadata, the cross-block carry
+// rows and the FP64 partials of the two-level cross-block merge.
 #include <cuda_runtime.h>
 #include <mutex>
 #include "tt_internal.h"
@@ -28,16 +28,19 @@ constexpr int kLPR = 8;
 constexpr int kG = 64;
 constexpr int kP = (kTB / kLPR) * kG;
 
-// Limits of the scratch array (about 4.2 MB).
+// Limits of the scratch array (about 4.7 MB).
 constexpr int64_t kMaxRows = 1 << 19;    // root positions
 constexpr int64_t kMaxBlocks = 8192;     // so nnz <= 8192 * 2048 = 16,777,216
 constexpr int kMaxRankPad = 64;
 constexpr size_t kMetaBytes = (size_t)kMaxBlocks * 16;
 constexpr size_t kPartBytes = (((size_t)(kMaxBlocks + 1) * 2 * 4) + 255) & ~(size_t)255;
 constexpr size_t kCarryBytes = (size_t)2 * kMaxBlocks * kMaxRankPad * 4;
-constexpr size_t kScratchBytes = kMetaBytes + kPartBytes + kCarryBytes;
+constexpr size_t kMaxSegs = (kMaxBlocks + tt::kSeg - 1) / tt::kSeg;
+constexpr size_t kSegMetaBytes = kMaxSegs * 16;
+constexpr size_t kSegCarryBytes = 2 * kMaxSegs * kMaxRankPad * 8;
+constexpr size_t kScratchBytes = kMetaBytes + kPartBytes + kCarryBytes + kSegMetaBytes + kSegCarryBytes;
 
-// Every call writes the parts of it that it reads (partition, metadata, carry).
+// Every call writes the parts of it that it reads (partition, metadata, carries).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 std::mutex g_mu;
@@ -102,6 +105,8 @@ TT_EXPORT tt_status tt_mttkrp3_noalloc(int32_t nrows, int64_t nnz, int32_t rank,
   int32_t* meta = static_cast<int32_t*>(scratch);
   int32_t* part = reinterpret_cast<int32_t*>(static_cast<unsigned char*>(scratch) + kMetaBytes);
   float* carry = reinterpret_cast<float*>(static_cast<unsigned char*>(scratch) + kMetaBytes + kPartBytes);
+  int32_t* segmeta = reinterpret_cast<int32_t*>(reinterpret_cast<unsigned char*>(carry) + kCarryBytes);
+  double* segcarry = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(segmeta) + kSegMetaBytes);
 
   cudaError_t e = cudaMemsetAsync(A, 0, sizeof(float) * (size_t)nrows * (size_t)rank, s);
   if (e != cudaSuccess) return tt::set_error(TT_ERR_CUDA, "clear A: %s", cudaGetErrorString(e));
@@ -121,6 +126,8 @@ TT_EXPORT tt_status tt_mttkrp3_noalloc(int32_t nrows, int64_t nnz, int32_t rank,
   a.part = part;
   a.carry = carry;
   a.meta = meta;
+  a.segmeta = segmeta;
+  a.segcarry = segcarry;
   a.rp = rank;
   a.nnz = nnz;
   a.nrows = nrows;

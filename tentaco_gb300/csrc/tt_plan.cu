@@ -26,15 +26,16 @@ using namespace tt;
 namespace tt {
 
 // ---------------------------------------------------------------------------
-// variant table: family {register walk, staged} x threads {256,512} x nonzeros
-// per team {4..64} x columns per lane {8,4,2,1}
+// variant table: family {lean warp tile, staged, ring} x threads {256,512} x
+// nonzeros per team (5 values per family) x columns per lane {8,4,2,1}
 // ---------------------------------------------------------------------------
 static const int kTB[2] = {256, 512};
-static const int kG[5] = {4, 8, 16, 32, 64};
+static const int kGF[3][5] = {{16, 32, 64, 128, 256}, {4, 8, 16, 32, 64}, {4, 8, 16, 32, 64}};
 static const int kCPT[4] = {8, 4, 2, 1};
 constexpr int kPerFamily = 2 * 5 * 4;
-constexpr int kNumVariants = 3 * kPerFamily;  // register walk, staged, ring
+constexpr int kNumVariants = 3 * kPerFamily;  // lean, staged, ring
 constexpr size_t kSmemLimit = (size_t)227 * 1024;
+constexpr int64_t kSlabBytes = (int64_t)32 << 20;
 
 VariantSpec variant_spec(int id) {
   VariantSpec v{};
@@ -43,16 +44,23 @@ VariantSpec variant_spec(int id) {
   v.staged = id / kPerFamily;
   const int b = id % kPerFamily;
   v.cpt = kCPT[b % 4];
-  v.G = kG[(b / 4) % 5];
+  v.G = kGF[v.staged][(b / 4) % 5];
   v.tb = kTB[b / 20];
   return v;
 }
 
+// Nearest table entry for (tb, G, cpt) in a family (G rounded to the family's list).
 int variant_id(int tb, int G, int cpt, int staged) {
   int ti = tb == 512 ? 1 : 0, gi = 0, ci = 0;
-  for (int i = 0; i < 5; i++) if (kG[i] == G) gi = i;
+  for (int i = 0; i < 5; i++) if (kGF[staged][i] <= G) gi = i;
   for (int i = 0; i < 4; i++) if (kCPT[i] == cpt) ci = i;
   return staged * kPerFamily + (ti * 5 + gi) * 4 + ci;
+}
+
+// Nonzeros of one work unit: a warp's tile for the lean family, a block's tile otherwise.
+int variant_unit(const VariantSpec& v, int rp) {
+  const int lpr = rp / v.cpt;
+  return (v.staged == 0 ? 32 / lpr : v.tb / lpr) * v.G;
 }
 
 int fac_bytes(int prec) { return fac_kind(prec) == kF32 ? 4 : 2; }
@@ -60,6 +68,7 @@ int fac_bytes(int prec) { return fac_kind(prec) == kF32 ? 4 : 2; }
 size_t variant_smem(const VariantSpec& v, int rp, int prec, int wcap) {
   const int lpr = rp / v.cpt;
   const int P = (v.tb / lpr) * v.G;
+  if (v.staged == 0) return (size_t)(v.tb / 32) * lean_warp_bytes(v.G, 32 / lpr, val_bytes(prec));
   if (v.staged == 2)  // walk + nonzero ring (kRingDepth slots) + fiber ring (kRingDepth+1 slots)
     return ((walk_smem_bytes(P, v.tb, rp, val_bytes(prec), P + 4 * (v.tb / lpr)) + 15) & ~(size_t)15) +
            (size_t)(2 * kRingDepth + 1) * v.tb * v.cpt * fac_bytes(prec);
@@ -111,6 +120,16 @@ int default_variant(int order, int rank, int prec, int64_t nnz) {
     return -1;
   }
   return id;
+}
+
+// Leaf-mode slabs for a plan: enough that one slab's rows of the leaf factor
+// (dims[leaf] / S rows of rp columns) stay within kSlabBytes, which keeps them
+// L2-resident next to the streamed nonzeros.
+int auto_slabs(int order, int64_t leaf_dim, int rp, int prec) {
+  (void)order;
+  const int64_t bytes = leaf_dim * (int64_t)rp * fac_bytes(prec);
+  int S = (int)((bytes + kSlabBytes - 1) / kSlabBytes);
+  return std::max(1, std::min(S, kMaxSlabs));
 }
 
 }  // namespace tt
@@ -168,18 +187,27 @@ tt_status alloc_walk_scratch(tt_plan* p, int P) {
     p->d_carry = nullptr;
     dev_free(p, p->d_meta);
     p->d_meta = nullptr;
+    dev_free(p, p->d_segcarry);
+    p->d_segcarry = nullptr;
+    dev_free(p, p->d_segmeta);
+    p->d_segmeta = nullptr;
     tt_status s = dev_alloc(p, &p->d_part, (size_t)(nb + 1) * (size_t)(p->order - 1));
     if (s != TT_OK) return s;
     s = dev_alloc(p, &p->d_carry, (size_t)(2 * nb) * (size_t)p->rp);
     if (s != TT_OK) return s;
     s = dev_alloc(p, &p->d_meta, (size_t)nb * 4);
     if (s != TT_OK) return s;
+    const int64_t ns = num_segments((int)nb);
+    s = dev_alloc(p, &p->d_segcarry, (size_t)(2 * ns) * (size_t)p->rp);
+    if (s != TT_OK) return s;
+    s = dev_alloc(p, &p->d_segmeta, (size_t)ns * 4);
+    if (s != TT_OK) return s;
     p->scratch_blocks = nb;
   }
   return TT_OK;
 }
 
-WalkArgs walk_args(const tt_plan* p, float* A);
+WalkArgs walk_args(const tt_plan* p, float* A, int q);
 
 tt_status use_variant(tt_plan* p, int id) {
   VariantSpec v = variant_spec(id);
@@ -189,7 +217,7 @@ tt_status use_variant(tt_plan* p, int id) {
   p->cpt = v.cpt;
   p->lpr = p->rp / v.cpt;
   p->G = v.G;
-  p->P = (v.tb / p->lpr) * v.G;
+  p->P = variant_unit(v, p->rp);
   p->nblocks = (int)((p->nnz + p->P - 1) / p->P);
   p->launcher = walk_launcher(p->order, p->prec, p->cpt, p->lpr, p->staged);
   if (!p->launcher) return set_error(TT_ERR_UNSUPPORTED, "variant %d not compiled for this shape", id);
@@ -198,13 +226,18 @@ tt_status use_variant(tt_plan* p, int id) {
   p->wcap = 1;
   if (p->staged == 1 && p->nnz > 0) {
     // size the window-row region from this tensor's partition (computed once here)
-    WalkArgs a = walk_args(p, nullptr);
-    CK(launch_partition(p->order, a, p->stream));
-    CK(launch_window_max(p->order, a, p->d_err + 1, p->stream));
-    int w = 0;
-    CK(cudaMemcpyAsync(&w, p->d_err + 1, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
-    CK(cudaStreamSynchronize(p->stream));
-    p->wcap = std::max(1, w);
+    int wmax = 1;
+    for (int q = 0; q < p->slabs; q++) {
+      if (p->slab[q].nnz == 0) continue;
+      WalkArgs a = walk_args(p, nullptr, q);
+      CK(launch_partition(p->order, a, p->stream));
+      CK(launch_window_max(p->order, a, p->d_err + 1, p->stream));
+      int w = 0;
+      CK(cudaMemcpyAsync(&w, p->d_err + 1, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+      CK(cudaStreamSynchronize(p->stream));
+      wmax = std::max(wmax, w);
+    }
+    p->wcap = wmax;
     const size_t need = variant_smem(v, p->rp, p->prec, p->wcap);
     if (need > kSmemLimit)
       return set_error(TT_ERR_UNSUPPORTED, "variant %d needs %zu bytes of shared memory for this tensor", id, need);
@@ -212,18 +245,24 @@ tt_status use_variant(tt_plan* p, int id) {
   return TT_OK;
 }
 
-WalkArgs walk_args(const tt_plan* p, float* A) {
+// Arguments of one walk pass over slab q (the whole tensor when slabs == 1).
+WalkArgs walk_args(const tt_plan* p, float* A, int q) {
   WalkArgs a{};
-  for (int l = 0; l < TT_MAX_ORDER; l++) { a.pos[l] = p->d_pos[l]; a.crd[l] = p->d_crd[l]; }
+  const tt_plan::SlabDev& sl = p->slab[q];
+  for (int l = 0; l < TT_MAX_ORDER; l++) { a.pos[l] = sl.pos[l]; a.crd[l] = sl.crd[l]; }
   a.crd[0] = p->dense_root ? nullptr : p->d_crd[0];
-  a.vals = p->d_vals;
+  a.vals = static_cast<const unsigned char*>(p->d_vals) + (size_t)sl.off * (size_t)val_bytes(p->prec);
+  a.accum = p->slabs > 1 ? 1 : 0;
+  a.gpol = p->gpol;
   for (int m = 0; m < 3; m++) a.fac[m] = p->fac[m];
   a.colscale = p->d_colscale;
   a.out = A;
   a.part = p->d_part;
   a.carry = p->d_carry;
   a.meta = p->d_meta;
-  a.nnz = p->nnz;
+  a.segcarry = p->d_segcarry;
+  a.segmeta = p->d_segmeta;
+  a.nnz = sl.nnz;
   a.nrows = (int32_t)p->nroot;
   a.rp = p->rp;
   a.R = p->rank;
@@ -232,7 +271,7 @@ WalkArgs walk_args(const tt_plan* p, float* A) {
   a.G = p->G;
   a.lgG = 0;
   while ((1 << a.lgG) < p->G) a.lgG++;
-  a.nblocks = p->nblocks;
+  a.nblocks = (int)((sl.nnz + p->P - 1) / p->P);
   a.wcap = p->wcap;
   a.err = p->d_err;
   for (int m = 0; m < 3; m++) a.fac_rows[m] = m + 1 < p->order ? (int32_t)p->dims[m + 1] : 0;
@@ -243,14 +282,22 @@ tt_status run_mttkrp(tt_plan* p, float* A, cudaStream_t st) {
   const size_t outbytes = (size_t)p->dims[0] * (size_t)p->rank * sizeof(float);
   CK(cudaMemsetAsync(A, 0, outbytes, st));
   if (p->nnz == 0) return TT_OK;
-  WalkArgs a = walk_args(p, A);
-  CK(launch_partition(p->order, a, st));
+  // one pass per slab, in slab order, each adding its rows into A; the kernel
+  // timer spans the first pass's walk to the last one's
   const size_t smem = variant_smem(variant_spec(p->variant), p->rp, p->prec, p->wcap);
-  a.smem_bytes = (int32_t)smem;
-  if (p->timing) CK(cudaEventRecord(p->evk0, st));
-  CK(p->launcher(a, p->nblocks, p->tb, smem, st));
-  if (p->timing) CK(cudaEventRecord(p->evk1, st));
-  CK(launch_chain_fixup(p->order, a, st));
+  int first = -1, last = -1;
+  for (int q = 0; q < p->slabs; q++)
+    if (p->slab[q].nnz > 0) { if (first < 0) first = q; last = q; }
+  for (int q = first; q >= 0 && q <= last; q++) {
+    WalkArgs a = walk_args(p, A, q);
+    if (a.nnz == 0) continue;
+    a.smem_bytes = (int32_t)smem;
+    CK(launch_partition(p->order, a, st));
+    if (p->timing && q == first) CK(cudaEventRecord(p->evk0, st));
+    CK(p->launcher(a, a.nblocks, p->tb, smem, st));
+    if (p->timing && q == last) CK(cudaEventRecord(p->evk1, st));
+    CK(launch_chain_fixup(p->order, a, st));
+  }
   return TT_OK;
 }
 
@@ -319,7 +366,7 @@ TT_EXPORT tt_status tt_variant_get(int32_t id, tt_variant_info* info) {
   info->lanes_per_row = 32 / v.cpt;
   info->nnz_per_block = v.tb / info->lanes_per_row * v.G;
   info->staged = v.staged;
-  static const char* fam[3] = {"walk", "stage", "ring"};
+  static const char* fam[3] = {"lean", "stage", "ring"};
   std::snprintf(info->name, sizeof(info->name), "%s_t%d_g%d_c%d", fam[v.staged], v.tb, v.G, v.cpt);
   return TT_OK;
 }
@@ -334,7 +381,15 @@ TT_EXPORT int32_t tt_variant_valid(int32_t id, int32_t order, int32_t rank, tt_p
 
 TT_EXPORT tt_status tt_plan_create(const taco_tensor_t* B, tt_op op, int32_t rank, tt_precision prec,
                                    tt_select select, int32_t variant, void* stream, tt_plan** out) {
+  return tt_plan_create_ex(B, op, rank, prec, select, variant, nullptr, stream, out);
+}
+
+TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t rank, tt_precision prec,
+                                      tt_select select, int32_t variant, const tt_plan_options* opts,
+                                      void* stream, tt_plan** out) {
   clear_error();
+  if (opts && (opts->slabs < 0 || opts->slabs > kMaxSlabs))
+    return set_error(TT_ERR_INVALID_ARGUMENT, "slabs %d (0 = automatic, at most %d)", opts->slabs, kMaxSlabs);
   if (!out) return set_error(TT_ERR_INVALID_ARGUMENT, "null plan pointer");
   *out = nullptr;
   CsfView v;
@@ -373,50 +428,95 @@ TT_EXPORT tt_status tt_plan_create(const taco_tensor_t* B, tt_op op, int32_t ran
 
   auto fail = [&](tt_status st2) { tt_plan_destroy(p); return st2; };
 
-  // upload the CSF (inner pos/crd exact size; nonzero-level crd and vals padded)
-  for (int l = 1; l < v.order; l++) {
-    if ((s = dev_alloc(p, &p->d_pos[l], (size_t)v.count[l - 1] + 1)) != TT_OK) return fail(s);
-    if (cudaMemcpyAsync(p->d_pos[l], v.pos[l], sizeof(int32_t) * ((size_t)v.count[l - 1] + 1),
-                        cudaMemcpyHostToDevice, st) != cudaSuccess)
-      return fail(set_error(TT_ERR_CUDA, "upload pos[%d]", l));
-    const bool last = l == v.order - 1;
-    const size_t n = last ? (size_t)pad16(v.count[l]) : (size_t)v.count[l];
-    if ((s = dev_alloc(p, &p->d_crd[l], n)) != TT_OK) return fail(s);
-    if (last && cudaMemsetAsync(p->d_crd[l], 0, n * sizeof(int32_t), st) != cudaSuccess)
-      return fail(set_error(TT_ERR_CUDA, "clear crd pad"));
-    if (v.count[l] > 0 &&
-        cudaMemcpyAsync(p->d_crd[l], v.crd[l], sizeof(int32_t) * (size_t)v.count[l], cudaMemcpyHostToDevice, st) != cudaSuccess)
-      return fail(set_error(TT_ERR_CUDA, "upload crd[%d]", l));
+  // leaf-mode slabs: the plan stores the slab-major CSF instead of the original
+  SlabCsf sc;
+  int S = 1;
+  if (op == TT_OP_MTTKRP && v.dense_root && v.nnz > 0) {
+    const int req = opts ? opts->slabs : 0;
+    S = req > 0 ? req : auto_slabs(v.order, v.dims[v.order - 1], p->rp, (int)prec);
+    if (S > kMaxSlabs) return fail(set_error(TT_ERR_INVALID_ARGUMENT, "slabs %d (at most %d)", S, kMaxSlabs));
+    if (S > 1 && (s = build_slabs(v, S, sc)) != TT_OK) return fail(s);
+  } else if (opts && opts->slabs > 1) {
+    return fail(set_error(TT_ERR_UNSUPPORTED, "slabs need an MTTKRP plan over a dense-root CSF"));
+  }
+  p->slabs = S;
+  {
+    const int pol = opts ? opts->l2_policy : 0;
+    if (pol < 0 || pol > 2) return fail(set_error(TT_ERR_INVALID_ARGUMENT, "l2_policy %d", pol));
+    p->gpol = pol == 1 ? 0 : pol == 2 ? 1 : (S > 1 ? 1 : 0);
+  }
+  const int L = v.order - 1;
+  auto upload = [&](int32_t** d, const int32_t* h, int64_t n, size_t alloc, const char* what) -> tt_status {
+    tt_status s2 = dev_alloc(p, d, alloc);
+    if (s2 != TT_OK) return s2;
+    if (alloc > (size_t)n && cudaMemsetAsync(*d, 0, alloc * sizeof(int32_t), st) != cudaSuccess)
+      return set_error(TT_ERR_CUDA, "clear %s", what);
+    if (n > 0 && cudaMemcpyAsync(*d, h, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return set_error(TT_ERR_CUDA, "upload %s", what);
+    return TT_OK;
+  };
+  const float* hvals = v.vals;
+  int64_t nvals = v.nnz;
+  size_t nvals_alloc = (size_t)pad16(v.nnz);
+  if (S == 1) {
+    // inner pos/crd exact size; nonzero-level crd and vals padded for 128-bit loads
+    for (int l = 1; l < v.order; l++) {
+      if ((s = upload(&p->d_pos[l], v.pos[l], v.count[l - 1] + 1, (size_t)v.count[l - 1] + 1, "pos")) != TT_OK) return fail(s);
+      const bool last = l == L;
+      if ((s = upload(&p->d_crd[l], v.crd[l], v.count[l], last ? (size_t)pad16(v.count[l]) : (size_t)v.count[l], "crd")) != TT_OK)
+        return fail(s);
+    }
+    for (int l = 0; l < TT_MAX_ORDER; l++) { p->slab[0].pos[l] = p->d_pos[l]; p->slab[0].crd[l] = p->d_crd[l]; }
+    p->slab[0].nnz = v.nnz;
+    p->slab[0].off = 0;
+  } else {
+    for (int q = 0; q < S; q++) {
+      const SlabCsf::Slab& h = sc.slab[q];
+      tt_plan::SlabDev& d = p->slab[q];
+      for (int l = 1; l <= L; l++)
+        if ((s = upload(&d.pos[l], h.pos[l].data(), h.count[l - 1] + 1, (size_t)h.count[l - 1] + 1, "slab pos")) != TT_OK) return fail(s);
+      for (int l = 1; l < L; l++)
+        if ((s = upload(&d.crd[l], h.crd[l].data(), h.count[l], (size_t)h.count[l], "slab crd")) != TT_OK) return fail(s);
+      d.nnz = h.nnz;
+      d.off = h.leaf_off;
+    }
+    if ((s = upload(&p->d_crd[L], sc.leaf_crd.data(), (int64_t)sc.leaf_crd.size(), sc.leaf_crd.size(), "slab leaf crd")) != TT_OK)
+      return fail(s);
+    for (int q = 0; q < S; q++) p->slab[q].crd[L] = p->d_crd[L] + p->slab[q].off;
+    hvals = sc.leaf_vals.data();
+    nvals = (int64_t)sc.leaf_vals.size();
+    nvals_alloc = sc.leaf_vals.size();
   }
   if (!v.dense_root) {
     if ((s = dev_alloc(p, &p->d_crd[0], (size_t)v.nroot)) != TT_OK) return fail(s);
     if (v.nroot > 0 && cudaMemcpyAsync(p->d_crd[0], v.root_crd, sizeof(int32_t) * (size_t)v.nroot,
                                        cudaMemcpyHostToDevice, st) != cudaSuccess)
       return fail(set_error(TT_ERR_CUDA, "upload root crd"));
+    p->slab[0].crd[0] = p->d_crd[0];
   }
   {
-    const size_t n = (size_t)pad16(v.nnz);
+    const size_t n = nvals_alloc;
     if (val_kind(p->prec) != kF32) {
       // values: one power-of-two scale (max in [1,2) for BF16, [2^14,2^15) for FP16),
       // converted on the device with round-to-nearest-even
       float vmax = 0.f;
 #pragma omp parallel for reduction(max : vmax)
       for (int64_t i = 0; i < v.nnz; i++) vmax = std::max(vmax, std::fabs(v.vals[i]));
-      const float sc = pow2_scale_for(vmax) * (p->prec == kFP16 ? 16384.f : 1.f);
-      p->vinv = 1.f / sc;
+      const float sc16 = pow2_scale_for(vmax) * (p->prec == kFP16 ? 16384.f : 1.f);
+      p->vinv = 1.f / sc16;
       uint16_t* d = nullptr;
       if ((s = dev_alloc(p, &d, n)) != TT_OK) return fail(s);
       p->d_vals = d;
       if (cudaMemsetAsync(d, 0, n * 2, st) != cudaSuccess) return fail(set_error(TT_ERR_CUDA, "clear vals"));
-      if (v.nnz > 0) {
+      if (nvals > 0) {
         float* tmp = nullptr;
-        if (cudaMalloc((void**)&tmp, (size_t)v.nnz * 4 + 16) != cudaSuccess)
+        if (cudaMalloc((void**)&tmp, (size_t)nvals * 4 + 16) != cudaSuccess)
           return fail(set_error(TT_ERR_OUT_OF_MEMORY, "value staging"));
-        float* dsc = reinterpret_cast<float*>(reinterpret_cast<char*>(tmp) + (size_t)v.nnz * 4);
+        float* dsc = reinterpret_cast<float*>(reinterpret_cast<char*>(tmp) + (size_t)nvals * 4);
         dsc = reinterpret_cast<float*>(((uintptr_t)dsc + 3) & ~(uintptr_t)3);
-        cudaError_t e1 = cudaMemcpyAsync(tmp, v.vals, (size_t)v.nnz * 4, cudaMemcpyHostToDevice, st);
-        cudaError_t e2 = e1 == cudaSuccess ? cudaMemcpyAsync(dsc, &sc, 4, cudaMemcpyHostToDevice, st) : e1;
-        cudaError_t e3 = e2 == cudaSuccess ? launch_to_16(tmp, v.nnz, 1, 1, dsc, fac_kind(p->prec) == kH16 ? 2 : 1, d, st) : e2;
+        cudaError_t e1 = cudaMemcpyAsync(tmp, hvals, (size_t)nvals * 4, cudaMemcpyHostToDevice, st);
+        cudaError_t e2 = e1 == cudaSuccess ? cudaMemcpyAsync(dsc, &sc16, 4, cudaMemcpyHostToDevice, st) : e1;
+        cudaError_t e3 = e2 == cudaSuccess ? launch_to_16(tmp, nvals, 1, 1, dsc, fac_kind(p->prec) == kH16 ? 2 : 1, d, st) : e2;
         cudaError_t e4 = cudaStreamSynchronize(st);
         cudaFree(tmp);
         if (e3 != cudaSuccess || e4 != cudaSuccess)
@@ -427,7 +527,7 @@ TT_EXPORT tt_status tt_plan_create(const taco_tensor_t* B, tt_op op, int32_t ran
       if ((s = dev_alloc(p, &d, n)) != TT_OK) return fail(s);
       p->d_vals = d;
       if (cudaMemsetAsync(d, 0, n * 4, st) != cudaSuccess) return fail(set_error(TT_ERR_CUDA, "clear vals"));
-      if (v.nnz > 0 && cudaMemcpyAsync(d, v.vals, (size_t)v.nnz * 4, cudaMemcpyHostToDevice, st) != cudaSuccess)
+      if (nvals > 0 && cudaMemcpyAsync(d, hvals, (size_t)nvals * 4, cudaMemcpyHostToDevice, st) != cudaSuccess)
         return fail(set_error(TT_ERR_CUDA, "upload vals"));
     }
   }
@@ -436,19 +536,28 @@ TT_EXPORT tt_status tt_plan_create(const taco_tensor_t* B, tt_op op, int32_t ran
     if ((s = dev_alloc(p, &p->d_err, 4)) != TT_OK) return fail(s);
     if (cudaMemsetAsync(p->d_err, 0, 4 * sizeof(int32_t), st) != cudaSuccess) return fail(set_error(TT_ERR_CUDA, "clear error word"));
     int id = -1;
+    bool placed = false;
     if (select == TT_SELECT_FIXED) {
       if (!variant_valid(variant, p->order, rank, p->prec))
         return fail(set_error(TT_ERR_INVALID_ARGUMENT, "variant %d not valid for order %d rank %d", variant, p->order, rank));
       id = variant;
     } else if (select == TT_SELECT_MODEL) {
-      id = selector_pick(p, B);
-      p->selected_by = 1;
-      if (id < 0) { id = default_variant(p->order, rank, p->prec, p->nnz); p->selected_by = 0; }
+      // the network's ranking; a staged variant whose window does not fit is skipped
+      std::vector<int> ranked;
+      if (selector_rank(p, B, ranked) == TT_OK) {
+        for (int cand : ranked) {
+          s = use_variant(p, cand);
+          if (s == TT_OK) { id = cand; placed = true; p->selected_by = 1; break; }
+          if (s != TT_ERR_UNSUPPORTED) return fail(s);
+        }
+      }
+      clear_error();
+      if (!placed) id = default_variant(p->order, rank, p->prec, p->nnz);
     } else {
       id = default_variant(p->order, rank, p->prec, p->nnz);
     }
     if (id < 0) return fail(set_error(TT_ERR_UNSUPPORTED, "no variant for order %d rank %d", p->order, rank));
-    if ((s = use_variant(p, id)) != TT_OK) return fail(s);
+    if (!placed && (s = use_variant(p, id)) != TT_OK) return fail(s);
     if (select == TT_SELECT_SWEEP) {
       if ((s = sweep_variants(p, st)) != TT_OK) return fail(s);
       p->selected_by = 2;
@@ -592,6 +701,7 @@ TT_EXPORT float tt_plan_last_ms(tt_plan* p) {
 
 TT_EXPORT int32_t tt_plan_variant(const tt_plan* p) { return p ? p->variant : -1; }
 TT_EXPORT int32_t tt_plan_selected_by(const tt_plan* p) { return p ? p->selected_by : -1; }
+TT_EXPORT int32_t tt_plan_slabs(const tt_plan* p) { return p ? p->slabs : -1; }
 TT_EXPORT int64_t tt_plan_nnz(const tt_plan* p) { return p ? p->nnz : -1; }
 TT_EXPORT int64_t tt_plan_num_fibers(const tt_plan* p, int32_t level) {
   if (!p || level < 0 || level >= p->order) return -1;

@@ -50,9 +50,21 @@ struct tt_plan {
   int32_t* d_part = nullptr;
   float* d_carry = nullptr;
   int32_t* d_tickets = nullptr;  // TTV
-  int32_t* d_meta = nullptr;     // MTTKRP: 4 ints per block
+  int32_t* d_meta = nullptr;     // MTTKRP: 4 ints per work unit
+  double* d_segcarry = nullptr;  // MTTKRP: 2 FP64 rows per segment of work units
+  int32_t* d_segmeta = nullptr;  // MTTKRP: 4 ints per segment
   int64_t scratch_blocks = 0;
   float sweep_ms[128] = {};
+  // leaf-mode slabs: one walk pass per slab, adding into the output (slabs == 1:
+  // slab[0] is the whole tensor)
+  struct SlabDev {
+    int32_t* pos[TT_MAX_ORDER] = {nullptr, nullptr, nullptr, nullptr};
+    int32_t* crd[TT_MAX_ORDER] = {nullptr, nullptr, nullptr, nullptr};
+    int64_t nnz = 0, off = 0;
+  };
+  int slabs = 1;
+  int gpol = 0;  // WalkArgs::gpol
+  SlabDev slab[tt::kMaxSlabs];
   // timing
   bool timing = false, timed_pending = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
@@ -64,5 +76,7 @@ struct tt_plan {
 
 namespace tt {
 // Learned selector: the variant the loaded model prefers for this plan, or -1.
-int selector_pick(const tt_plan* p, const taco_tensor_t* B);
+// Valid variants for the plan's shape, ordered by the selector network's
+// predicted time; TT_ERR_UNSUPPORTED when no loaded model covers the shape.
+tt_status selector_rank(const tt_plan* p, const taco_tensor_t* B, std::vector<int>& ranked);
 }

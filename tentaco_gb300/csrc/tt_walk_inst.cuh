@@ -1,19 +1,22 @@
-// tt_walk_inst.cuh -- explicit instantiations of the MTTKRP walk kernel for one
-// (order, precision) -- register walk and shared-memory staged walk --, included
-// by tt_walk_o{3,4}_{fp32,bf16,bf16f,fp16}.cu with
-// TT_ORDER, TT_PREC and TT_LOOKUP defined.  The (columns per lane, lanes per row)
+// tt_walk_inst.cuh -- explicit instantiations of the MTTKRP walk kernels for one
+// (order, precision) -- lean warp-tile walk, shared-memory staged walk and ring
+// walk --, included by tt_walk_o{3,4}_{fp32,bf16,bf16f,fp16}.cu with TT_ORDER,
+// TT_PREC and TT_LOOKUP defined.  The (columns per lane, lanes per row)
 // pairs cover factor ranks 8, 16, 32 and 64.
 #include "tt_mttkrp.cuh"
 #include "tt_kernels.h"
 
 namespace tt {
 namespace {
-// fam 0: register walk, 1: shared-memory staged, 2: register walk with a per-lane cp.async ring
+// fam 0: lean warp-tile walk, 1: shared-memory staged, 2: register walk with a
+// per-lane cp.async ring.  units: work units of the partition (warp tiles for
+// fam 0, blocks otherwise).
 template <int CPT, int LPR, int FAM>
-cudaError_t launch_walk(const WalkArgs& a, int grid, int tb, size_t smem, cudaStream_t s) {
+cudaError_t launch_walk(const WalkArgs& a, int units, int tb, size_t smem, cudaStream_t s) {
   auto k = FAM == 1 ? mttkrp_stage_kernel<TT_ORDER, TT_PREC, CPT, LPR>
          : FAM == 2 ? mttkrp_walk_kernel<TT_ORDER, TT_PREC, CPT, LPR, false, true>
-                    : mttkrp_walk_kernel<TT_ORDER, TT_PREC, CPT, LPR>;
+                    : mttkrp_lean_kernel<TT_ORDER, TT_PREC, CPT, LPR>;
+  const int grid = FAM == 0 ? (units + tb / 32 - 1) / (tb / 32) : units;
   static size_t configured = 48 * 1024;
   if (smem > configured) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -34,9 +34,9 @@ def close(got, ref, prec="fp32"):
     return e
 
 
-def run_plan(B, factors, prec="fp32", select=tt.SELECT_DEFAULT, variant=0, reps=1):
+def run_plan(B, factors, prec="fp32", select=tt.SELECT_DEFAULT, variant=0, reps=1, slabs=None):
     R = factors[0].shape[1]
-    plan = tt.Plan(B, rank=R, prec=prec, select=select, variant=variant)
+    plan = tt.Plan(B, rank=R, prec=prec, select=select, variant=variant, slabs=slabs)
     bufs = [tt.DeviceBuffer.from_array(f.astype(np.float32)) for f in factors]
     plan.set_factors(bufs)
     A = tt.DeviceBuffer(B.dims[0] * R * 4)
@@ -213,4 +213,61 @@ def test_sweep_selects_a_timed_variant(c1):
     assert plan.selected_by == 2
     timed = times[times > 0]
     assert len(timed) >= 50 and times[plan.variant] == timed.min()
+    close(got, ref)
+
+
+@pytest.mark.parametrize("slabs", [2, 3, 16])
+def test_slabs_parity(skewed, slabs):
+    """Leaf-mode slabs: one pass per slab adding into A, for every family."""
+    B, Oc = skewed
+    facs = [tt.gen_dense(2000, 32, 1, 71), tt.gen_dense(5000, 32, 1, 72)]
+    ref = O.mttkrp(Oc, facs)
+    for prec in ("fp32", "fp16"):
+        got, plan = run_plan(B, facs, prec=prec, slabs=slabs)
+        assert plan.slabs == slabs
+        close(got, ref, prec)
+        for v in (8, 13, 18, 49, 54, 97):
+            if tt.variant_valid(v, 3, 32, prec):
+                try:
+                    outs, _ = run_plan(B, facs, prec=prec, select=tt.SELECT_FIXED, variant=v, slabs=slabs, reps=2)
+                except tt.TTError as e:
+                    assert e.status == tt.TT_ERR_UNSUPPORTED
+                    continue
+                assert np.array_equal(outs[0], outs[1])  # passes add in a fixed order
+                close(outs[0], ref, prec)
+
+
+def test_slabs_long_fiber_and_order4(c5_small):
+    # a fiber crossing every slab, rows spanning many warp tiles
+    L = 200_000
+    rng = np.random.default_rng(9)
+    co = np.concatenate([np.array([[5, 3, l] for l in range(0, L, 2)]),
+                         np.stack([rng.integers(0, 20, 800), rng.integers(0, 10, 800), rng.integers(0, L, 800)], 1)])
+    B = tt.csf_from_coo((20, 10, L), co.astype(np.int32), rng.random(len(co)).astype(np.float32))
+    facs = [tt.gen_dense(10, 32, 1, 1), tt.gen_dense(L, 32, 1, 2)]
+    ref = O.mttkrp(to_oracle(B), facs)
+    for slabs in (4, 7):
+        got, _ = run_plan(B, facs, slabs=slabs)
+        close(got, ref)
+    B4, facs4, ref4 = c5_small
+    for slabs in (2, 5):
+        for prec in ("fp32", "fp16"):
+            got, plan = run_plan(B4, facs4, prec=prec, slabs=slabs)
+            assert plan.slabs == slabs
+            close(got, ref4, prec)
+
+
+def test_auto_slabs_for_large_leaf_factor():
+    # leaf factor 2M x 32 FP32 = 256 MB: automatic slabs keep each pass's rows near 32 MB
+    B = tt.gen_zipf((1000, 800, 2_000_000), (0.5, 0, 0), 300_000, seed=31)
+    facs = [tt.gen_dense(800, 32, 1, 3), tt.gen_dense(2_000_000, 32, 1, 4)]
+    ref = O.mttkrp(to_oracle(B), facs)
+    got, plan = run_plan(B, facs)
+    assert plan.slabs == 8
+    close(got, ref)
+    got, plan = run_plan(B, facs, prec="fp16")
+    assert plan.slabs == 4
+    close(got, ref, "fp16")
+    got, plan = run_plan(B, facs, slabs=1)
+    assert plan.slabs == 1
     close(got, ref)

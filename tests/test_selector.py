@@ -1,0 +1,140 @@
+"""Learned variant selector: the network's training kernels against the FP64
+oracle, the committed model file, and what the model gains over the heuristic.
+
+CPU tests check the oracle gradient by finite differences and the committed
+corpus/model files; GPU tests check the library's forward/backward/Adam
+kernels against the oracle and the product's inference path (TT_SELECT_MODEL)
+against the committed sweep timings of the held-out tensors.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import tentaco_gb300 as tt
+from oracle import oracle as orc
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(tt.__file__)
+CORPUS = os.path.join(PKG, "selector_corpus.jsonl")
+MODEL = os.path.join(PKG, "selector_model.bin")
+NOUT = 120
+
+
+def _rand_problem(seed, B=24, nout=NOUT):
+    rng = np.random.default_rng(seed)
+    n = orc.mlp_num_params(nout)
+    params = rng.normal(0, 0.2, n)
+    X = rng.normal(0, 1, (B, 12))
+    T = rng.normal(0, 1, (B, nout))
+    M = (rng.random((B, nout)) < 0.7).astype(np.float64)
+    return params, X, T, M
+
+
+def test_oracle_grad_matches_finite_differences():
+    params, X, T, M = _rand_problem(1, B=6, nout=10)
+    loss, g = orc.mlp_grad(params, 10, X, T, M)
+    rng = np.random.default_rng(2)
+    idx = rng.choice(params.size, 40, replace=False)
+    h = 1e-6
+    for i in idx:
+        p1 = params.copy(); p1[i] += h
+        p0 = params.copy(); p0[i] -= h
+        fd = (orc.mlp_grad(p1, 10, X, T, M)[0] - orc.mlp_grad(p0, 10, X, T, M)[0]) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-6 + 1e-5 * abs(fd), (i, fd, g[i])
+    out = orc.mlp_forward(params, 10, X)
+    assert abs(loss - float(((out - T) ** 2 * M).sum() / M.sum())) < 1e-12
+
+
+def test_param_count_agrees():
+    assert tt.mlp_num_params(NOUT) == orc.mlp_num_params(NOUT) == 12 * 64 + 64 + 2 * (64 * 64 + 64) + 64 * NOUT + NOUT
+
+
+def _corpus():
+    if not os.path.exists(CORPUS):
+        pytest.skip("no committed selector corpus")
+    with open(CORPUS) as f:
+        return [json.loads(l) for l in f if l.strip()]
+
+
+def test_corpus_and_model_files():
+    recs = _corpus()
+    assert len(recs) >= 300
+    for r in recs[:20]:
+        assert len(r["features"]) == 12 and len(r["ms"]) == NOUT
+        assert r["best"] == int(np.argmin([t if t > 0 else np.inf for t in r["ms"]]))
+    assert os.path.exists(MODEL)
+    from tentaco_gb300 import selector
+    models = selector.read_model(MODEL)
+    assert {m["storage"] for m in models} == {0, 1}
+    for m in models:
+        assert m["params"].size == orc.mlp_num_params(NOUT)
+
+
+def test_model_beats_heuristic_on_held_out():
+    """Regret of the committed model on the held-out tensors (FP64 oracle forward,
+    same weights the library loads) vs the fixed heuristic, from the committed
+    sweep timings."""
+    from tentaco_gb300 import selector
+    recs = _corpus()
+    models = {m["storage"]: m for m in selector.read_model(MODEL)}
+    rep = selector.evaluate(recs, models, forward=lambda p, X: orc.mlp_forward(p, NOUT, X), split="test")
+    for storage, r in rep.items():
+        assert r["n"] >= 20
+        assert r["model_mean_regret"] <= 0.10, r
+        assert r["model_mean_regret"] < r["heuristic_mean_regret"], r
+
+
+@pytest.mark.gpu
+def test_gpu_grad_matches_oracle():
+    params, X, T, M = _rand_problem(3)
+    B = X.shape[0]
+    loss_ref, g_ref = orc.mlp_grad(params, NOUT, X, T, M)
+    net = tt.Mlp(NOUT, B)
+    loss, g = net.grad(params.astype(np.float32), X.astype(np.float32), T.astype(np.float32), M.astype(np.float32))
+    assert abs(loss - loss_ref) <= 1e-5 * abs(loss_ref) + 1e-7
+    err = np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref)
+    assert err < 1e-5, err
+    out = net.forward(params.astype(np.float32), X.astype(np.float32))
+    ref = orc.mlp_forward(params, NOUT, X)
+    assert np.abs(out - ref).max() <= 1e-5 * (1 + np.abs(ref).max())
+
+
+@pytest.mark.gpu
+def test_gpu_training_is_deterministic_and_learns():
+    params, X, T, M = _rand_problem(4, B=64)
+    runs = []
+    for _ in range(2):
+        net = tt.Mlp(NOUT, X.shape[0])
+        p, losses = net.train(params.astype(np.float32), X.astype(np.float32), T.astype(np.float32),
+                              M.astype(np.float32), steps=200, lr=3e-3)
+        runs.append((p, losses))
+    assert np.array_equal(runs[0][0], runs[1][0])
+    assert runs[0][1][-1] < 0.5 * runs[0][1][0]
+
+
+@pytest.mark.gpu
+def test_product_selector_regret_on_held_out():
+    """TT_SELECT_MODEL through the library (device inference) on regenerated
+    held-out tensors picks variants whose recorded sweep time is within 10% of
+    the best on average, and beats the heuristic."""
+    from tentaco_gb300 import selector
+    recs = [r for r in _corpus() if selector.split_of(r["t"]) == "test"]
+    tt.selector_load(MODEL)
+    small = sorted(recs, key=lambda r: r["nnz"])[:24]
+    reg_m, reg_h = [], []
+    for r in small:
+        B = selector.corpus_tensor(r)
+        scores = tt.selector_scores(B, r["rank"], r["prec"])
+        pick = int(np.argmin(scores))
+        ms = np.array(r["ms"])
+        best = ms[r["best"]]
+        if ms[pick] > 0:
+            reg_m.append(ms[pick] / best - 1)
+        d = r["default"]
+        if ms[d] > 0:
+            reg_h.append(ms[d] / best - 1)
+    assert len(reg_m) >= 16
+    assert np.mean(reg_m) <= 0.10
+    assert np.mean(reg_m) < np.mean(reg_h)
