@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--select", default="model", choices=["default", "model", "sweep"])
     ap.add_argument("--variant", type=int, default=-1, help="run this variant id (overrides --select)")
     ap.add_argument("--nnz", type=int, default=NNZ, help="smaller nonzero count for quick checks")
+    ap.add_argument("--slabs", type=int, default=0, help="leaf-mode slabs (0: the plan's automatic choice)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-errors", action="store_true")
@@ -218,9 +219,9 @@ def run_gpu_arm(args, rank, world, d):
     flops = 3.0 * B.nnz * RANK
 
     def timed_plan(prec, select):
-        plan = tt.Plan(B, rank=RANK, prec=prec, select=select, variant=max(args.variant, 0))
+        plan = tt.Plan(B, rank=RANK, prec=prec, select=select, variant=max(args.variant, 0), slabs=args.slabs)
         if select == tt.SELECT_MODEL and plan.selected_by != 1:
-            plan = tt.Plan(B, rank=RANK, prec=prec, select=tt.SELECT_SWEEP)
+            plan = tt.Plan(B, rank=RANK, prec=prec, select=tt.SELECT_SWEEP, slabs=args.slabs)
         bufs = [tt.DeviceBuffer.from_array(C), tt.DeviceBuffer.from_array(D)]
         plan.set_factors(bufs)
         A = tt.DeviceBuffer(B.dims[0] * RANK * 4)
@@ -275,7 +276,7 @@ def run_gpu_arm(args, rank, world, d):
         "scaling": "weak", "vs_baseline": None, "dtype": args.prec if args.prec != "bf16f" else "bf16+fp32",
         "data": "synthetic (seeded lognormal-fiber tensor; FROSTT data absent)",
         "config": {"workload": WORKLOAD, "dims": list(DIMS), "nnz": B.nnz, "fibers": B.count(1), "rank": RANK,
-                   "precision": args.prec, "select": args.select, "variant": plan.variant,
+                   "precision": args.prec, "select": args.select, "variant": plan.variant, "slabs": plan.slabs,
                    "selected_by": "fixed" if args.variant >= 0 else ["heuristic", "model", "sweep"][plan.selected_by],
                    "l2": "flushed between steps (512 MB write)", "parallelism": f"replicas{world}",
                    "gen_s": round(gen_s, 1)},

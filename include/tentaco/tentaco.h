@@ -103,8 +103,9 @@ tt_status tt_plan_destroy(tt_plan* plan);
 typedef struct tt_plan_options {
   /* MTTKRP over a dense-root CSF: split the last mode's index range into this
    * many slabs and run one walk pass per slab, each adding into A, so that one
-   * slab's rows of the last factor stay resident in L2 (about 32 MB each).
-   * 0: automatic; 1: no slabs; at most 16. */
+   * slab's rows of the last factor stay resident in L2.  0: automatic (no
+   * slabs: the walk is issue-bound, and slabs trade DRAM traffic for extra
+   * fiber work); 1: no slabs; at most 16. */
   int32_t slabs;
   /* L2 policy of factor-row gathers in the lean walk: 0 automatic (evict_last
    * without slabs, evict_normal with them), 1 evict_last, 2 evict_normal. */
@@ -144,6 +145,30 @@ int64_t tt_plan_nnz(const tt_plan* plan);
 int64_t tt_plan_num_fibers(const tt_plan* plan, int32_t level);
 /* Device bytes the plan holds (CSF copy + factor storage + scratch). */
 int64_t tt_plan_device_bytes(const tt_plan* plan);
+
+/* Walk work units of the plan's variant (blocks, or warp tiles for the lean family). */
+int32_t tt_plan_nblocks(const tt_plan* plan);
+/* Switch an MTTKRP plan to another valid variant (scratch grows as needed). */
+tt_status tt_plan_use_variant(tt_plan* plan, int32_t variant);
+/* Per-variant mean ms of the last TT_SELECT_SWEEP (negative: not timed); n entries. */
+tt_status tt_plan_sweep_times(const tt_plan* plan, float* ms, int32_t n);
+/* Milliseconds of the walk kernel(s) alone in the last timed call (first slab's
+ * walk to the last slab's), without partition, clear and row merge. */
+float tt_plan_last_kernel_ms(tt_plan* plan);
+/* Device error word of the plan's kernels (0: none; -1: could not be read);
+ * waits for the plan's stream. */
+int32_t tt_plan_device_error(tt_plan* plan);
+
+/* ---- device memory for callers without CUDA bindings ------------------ */
+
+tt_status tt_device_malloc(int64_t bytes, void** ptr);
+tt_status tt_device_free(void* ptr);
+tt_status tt_memcpy_htod(void* dst, const void* src, int64_t bytes);
+tt_status tt_memcpy_dtoh(void* dst, const void* src, int64_t bytes);
+tt_status tt_device_synchronize(void);
+int32_t tt_device_count(void);
+/* Write 512 MB on the stream (evicts L2 between timed steps). */
+tt_status tt_l2_flush(void* stream);
 
 /* ---- one-shot host calls (H2D, run, D2H inside) ------------------------ */
 
@@ -186,6 +211,8 @@ tt_status tt_mttkrp3_noalloc(int32_t nrows, int64_t nnz, int32_t rank,
 
 int32_t tt_num_variants(void);
 tt_status tt_variant_get(int32_t id, tt_variant_info* info);
+/* 1 if variant id is compiled and fits shared memory for (order, rank, prec). */
+int32_t tt_variant_valid(int32_t id, int32_t order, int32_t rank, tt_precision prec);
 /* The variant the fixed heuristic picks for a shape (used by TT_SELECT_DEFAULT). */
 int32_t tt_variant_default(int32_t order, int32_t rank, tt_precision prec, int64_t nnz);
 

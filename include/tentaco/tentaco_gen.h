@@ -49,6 +49,15 @@ tt_status tt_gen_lognormal_fibers(const int32_t* dims, int64_t nnz, double mu, d
 tt_status tt_gen_dense(int64_t rows, int64_t cols, int32_t dist, uint64_t seed, float* out);
 
 /*
+ * Read a FROSTT .tns file (one nonzero per line: `order` 1-based coordinates
+ * and a value; '#' comment lines) into the canonical CSF of tt_csf_from_coo,
+ * with dims[m] = the largest coordinate of mode m.  Replaces the reference's
+ * SPLATT loader (ds.h:351-366).  order 0: taken from the first line.
+ * Malformed lines return TT_ERR_INVALID_ARGUMENT naming the line.
+ */
+tt_status tt_read_tns(const char* path, int32_t order, taco_tensor_t** out);
+
+/*
  * Features of a CSF tensor used by the learned variant selector (12 floats):
  * log2 of dims[0..2] (0 for missing modes), log2 nnz, log2 nnz per root row,
  * log2 nnz per last-level fiber, CV of last-level fiber lengths, skewness of

@@ -109,6 +109,7 @@ def lib():
                                         C.c_int64, C.c_uint64, C.POINTER(_TP)]),
         "tt_gen_dense": (S, [C.c_int64, C.c_int64, C.c_int32, C.c_uint64, _P]),
         "tt_csf_features": (S, [_TP, C.c_int32, C.POINTER(C.c_float)]),
+        "tt_read_tns": (S, [C.c_char_p, C.c_int32, C.POINTER(_TP)]),
         "tt_device_malloc": (S, [C.c_int64, C.POINTER(_P)]),
         "tt_device_free": (S, [_P]),
         "tt_memcpy_htod": (S, [_P, _P, C.c_int64]),
@@ -232,6 +233,13 @@ def gen_zipf(dims, zipf_s, nnz: int, seed: int, vlo=0.0, vhi=1.0, max_rounds=8) 
     out = _TP()
     check(lib().tt_gen_zipf(len(d), _i32p(d), s.ctypes.data_as(C.POINTER(C.c_double)), nnz, vlo, vhi, seed,
                             max_rounds, C.byref(out)))
+    return Tensor(out)
+
+
+def read_tns(path, order: int = 0) -> Tensor:
+    """A FROSTT .tns file (1-based coordinates and a value per line) as a canonical CSF."""
+    out = _TP()
+    check(lib().tt_read_tns(os.fsencode(path), order, C.byref(out)))
     return Tensor(out)
 
 

@@ -130,6 +130,18 @@ __device__ __forceinline__ float bf16hi(uint32_t w) { return __uint_as_float(w &
 __device__ __forceinline__ float h16lo(uint32_t w) { return __half2float(__ushort_as_half((unsigned short)(w & 0xffffu))); }
 __device__ __forceinline__ float h16hi(uint32_t w) { return __half2float(__ushort_as_half((unsigned short)(w >> 16))); }
 
+// Both halves of a packed word as floats (FP16: one packed conversion, no masking).
+template <int KIND>
+__device__ __forceinline__ float2 pair16(uint32_t w) {
+  if constexpr (KIND == kB16) {
+    return make_float2(bf16lo(w), bf16hi(w));
+  } else {
+    __half2 h;
+    memcpy(&h, &w, 4);
+    return __half22float2(h);
+  }
+}
+
 template <int KIND>
 __device__ __forceinline__ float lo16(uint32_t w) { return KIND == kB16 ? bf16lo(w) : h16lo(w); }
 template <int KIND>

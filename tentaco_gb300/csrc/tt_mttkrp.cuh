@@ -155,12 +155,12 @@ struct Walk {
 
   const WalkArgs& a;
   int q;
-  float sc[CPT];
 
-  __device__ __forceinline__ Walk(const WalkArgs& args, int lane_in_team) : a(args), q(lane_in_team) {
-#pragma unroll
-    for (int c = 0; c < CPT; c++) sc[c] = a.colscale ? a.colscale[q * CPT + c] : 1.0f;
-  }
+  __device__ __forceinline__ Walk(const WalkArgs& args, int lane_in_team) : a(args), q(lane_in_team) {}
+
+  // Output scale of this lane's column c (16-bit storage), read when a row is
+  // written rather than held in registers through the walk.
+  __device__ __forceinline__ float sc(int c) const { return a.colscale ? a.colscale[q * CPT + c] : 1.0f; }
 
   __device__ __forceinline__ int64_t row_id(int ip) const {
     return a.crd[0] ? (int64_t)a.crd[0][ip] : (int64_t)ip;
@@ -172,7 +172,7 @@ struct Walk {
   __device__ __forceinline__ void store_row(int ip, const float (&acc)[CPT]) const {
     float* o = a.out + row_id(ip) * a.ldo + q * CPT;
     if (CPT == 4 && a.R == RP && (a.ldo & 3) == 0) {
-      float4 r = make_float4(acc[0] * sc[0], acc[1] * sc[1], acc[2] * sc[2], acc[3] * sc[3]);
+      float4 r = make_float4(acc[0] * sc(0), acc[1] * sc(1), acc[2] * sc(2), acc[3] * sc(3));
       if (a.accum) {
         const float4 o4 = *reinterpret_cast<const float4*>(o);
         r.x += o4.x; r.y += o4.y; r.z += o4.z; r.w += o4.w;
@@ -181,7 +181,7 @@ struct Walk {
     } else {
 #pragma unroll
       for (int c = 0; c < CPT; c++)
-        if (q * CPT + c < a.R) o[c] = acc[c] * sc[c] + (a.accum ? o[c] : 0.f);
+        if (q * CPT + c < a.R) o[c] = acc[c] * sc(c) + (a.accum ? o[c] : 0.f);
     }
   }
 
@@ -406,10 +406,18 @@ struct Walk {
     }
   }
   __device__ __forceinline__ static void piece_cvt(const uint32_t (&w)[NWD], float (&g)[CPT]) {
+    if constexpr (FK == kF32) {
 #pragma unroll
-    for (int c = 0; c < CPT; c++) {
-      if constexpr (FK == kF32) g[c] = __uint_as_float(w[c]);
-      else g[c] = (c & 1) ? hi16<FK>(w[c >> 1]) : lo16<FK>(w[c >> 1]);
+      for (int c = 0; c < CPT; c++) g[c] = __uint_as_float(w[c]);
+    } else if constexpr (CPT == 1) {
+      g[0] = lo16<FK>(w[0]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < CPT; c += 2) {
+        const float2 f = pair16<FK>(w[c >> 1]);
+        g[c] = f.x;
+        g[c + 1] = f.y;
+      }
     }
   }
   // U consecutive stored values of a team's tile (16-byte aligned run).
@@ -423,12 +431,13 @@ struct Walk {
       }
     } else if constexpr (U == 8) {
       const uint4 w = *reinterpret_cast<const uint4*>(vt);
-      v[0] = lo16<VK>(w.x); v[1] = hi16<VK>(w.x); v[2] = lo16<VK>(w.y); v[3] = hi16<VK>(w.y);
-      v[4] = lo16<VK>(w.z); v[5] = hi16<VK>(w.z); v[6] = lo16<VK>(w.w); v[7] = hi16<VK>(w.w);
+      const float2 a = pair16<VK>(w.x), b = pair16<VK>(w.y), c = pair16<VK>(w.z), d = pair16<VK>(w.w);
+      v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y; v[6] = d.x; v[7] = d.y;
     } else {
       static_assert(U == 4, "batches of 4 or 8 nonzeros");
       const uint2 w = *reinterpret_cast<const uint2*>(vt);
-      v[0] = lo16<VK>(w.x); v[1] = hi16<VK>(w.x); v[2] = lo16<VK>(w.y); v[3] = hi16<VK>(w.y);
+      const float2 a = pair16<VK>(w.x), b = pair16<VK>(w.y);
+      v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
     }
   }
   __device__ __forceinline__ static float val_one(const unsigned char* vt, int j) {
@@ -514,6 +523,17 @@ struct Walk {
     auto consume = [&](const uint32_t (&g)[U][NWD], int j) {
       float v[U];
       vals_load<U>(vt + (size_t)j * VB, v);
+      if (s + j + U <= fend) {
+        // the whole batch lies in the current fiber: no boundary checks
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          float d[CPT];
+          piece_cvt(g[u], d);
+#pragma unroll
+          for (int c = 0; c < CPT; c++) f3[c] = fmaf(v[u], d[c], f3[c]);
+        }
+        return;
+      }
 #pragma unroll
       for (int u = 0; u < U; u++) {
         while (s + j + u >= fend) fold();
@@ -900,20 +920,20 @@ __device__ __forceinline__ void settle_unit(const WalkArgs& a, const Walk<ORDER,
   if (single) {
     if (h_before || l_after) {
 #pragma unroll
-      for (int c = 0; c < CPT; c++) c0[c] = X.ha[c] * wk.sc[c];
+      for (int c = 0; c < CPT; c++) c0[c] = X.ha[c] * wk.sc(c);
     } else {
       wk.store_row(X.h, X.ha);
     }
   } else {
     if (h_before) {
 #pragma unroll
-      for (int c = 0; c < CPT; c++) c0[c] = X.ha[c] * wk.sc[c];
+      for (int c = 0; c < CPT; c++) c0[c] = X.ha[c] * wk.sc(c);
     } else {
       wk.store_row(X.h, X.ha);
     }
     if (l_after) {
 #pragma unroll
-      for (int c = 0; c < CPT; c++) c1[c] = X.ta[c] * wk.sc[c];
+      for (int c = 0; c < CPT; c++) c1[c] = X.ta[c] * wk.sc(c);
     } else {
       wk.store_row(X.t, X.ta);
     }
@@ -994,71 +1014,85 @@ __device__ __forceinline__ void put_row_value(const WalkArgs& a, int r, int j, d
 }
 
 template <int ORDER>  // (the fold itself does not depend on the order)
-__global__ void __launch_bounds__(256) seg_fold_kernel(const __grid_constant__ WalkArgs a) {
+__global__ void __launch_bounds__(256, 2) seg_fold_kernel(const __grid_constant__ WalkArgs a) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sg = blockIdx.x * (blockDim.x >> 5) + warp;
   if (sg >= num_segments(a.nblocks)) return;
   const int u0 = sg * kSeg, n = min(kSeg, a.nblocks - u0);
   const int rp = a.rp;
-  const bool two = rp > 32;  // columns lane and lane + 32
   int4 mine = make_int4(-1, -1, 0, 0);
   if (lane < n) mine = reinterpret_cast<const int4*>(a.meta)[u0 + lane];
-  // the current run
-  int cur = -1;
-  bool cur_before = false, cur_after = false, first_run = true;
-  double s0 = 0.0, s1 = 0.0;
-  // the segment's summary
-  int sfirst = -1, slast = -1, sflags = 0, nruns = 0;
   double* sc0 = a.segcarry + (size_t)(2 * sg) * rp;
   double* sc1 = sc0 + rp;
-  auto close_run = [&]() {
-    nruns++;
-    if (!cur_before && !cur_after) {
-      if (lane < a.R) put_row_value(a, cur, lane, s0);
-      if (two && lane + 32 < a.R) put_row_value(a, cur, lane + 32, s1);
-    } else if (cur_before) {  // necessarily the segment's first run
-      sfirst = cur;
-      sflags |= 1;
-      if (cur_after) { slast = cur; sflags |= 2; }
-      if (lane < rp) sc0[lane] = s0;
-      if (two) sc0[lane + 32] = s1;
-    } else {  // cur_after only: the segment's last run
-      slast = cur;
-      sflags |= 2;
-      double* d = first_run ? sc0 : sc1;  // alone in the segment: slot 0
-      if (lane < rp) d[lane] = s0;
-      if (two) d[lane + 32] = s1;
+  int sfirst = -1, slast = -1, sflags = 0, nruns = 0;
+  // one pass per 32 columns (lane = column); the run structure is the same in every pass
+  for (int c0 = 0; c0 < rp; c0 += 32) {
+    const int col = c0 + lane;
+    const bool live = col < rp;
+    int cur = -1;
+    bool cur_before = false, cur_after = false, first_run = true;
+    double acc = 0.0;
+    int runs = 0;
+    auto close_run = [&]() {
+      runs++;
+      if (!cur_before && !cur_after) {
+        if (col < a.R) put_row_value(a, cur, col, acc);
+      } else if (cur_before) {  // necessarily the segment's first run
+        if (c0 == 0) { sfirst = cur; sflags |= 1; if (cur_after) { slast = cur; sflags |= 2; } }
+        if (live) sc0[col] = acc;
+      } else {  // cur_after only: the segment's last run (slot 0 when it is the only run)
+        if (c0 == 0) { slast = cur; sflags |= 2; }
+        if (live) (first_run ? sc0 : sc1)[col] = acc;
+      }
+      if (c0 == 0 && first_run && sfirst < 0) sfirst = cur;
+      first_run = false;
+    };
+    auto entry = [&](int r, float v, bool before, bool after) {
+      if (r != cur) {
+        if (cur >= 0) close_run();
+        cur = r;
+        cur_before = before;
+        acc = 0.0;
+      }
+      acc += (double)v;
+      cur_after = after;
+    };
+    constexpr int kHalf = kSeg / 2;
+    for (int h = 0; h < kSeg; h += kHalf) {
+      // both carry slots of the next kHalf units, loaded before any is used
+      float v0[kHalf], v1[kHalf];
+#pragma unroll
+      for (int k = 0; k < kHalf; k++) {
+        v0[k] = 0.f;
+        v1[k] = 0.f;
+        if (h + k < n && live) {
+          const float* c = a.carry + (size_t)(2 * (u0 + h + k)) * rp + col;
+          v0[k] = c[0];
+          v1[k] = c[rp];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kHalf; k++) {
+        if (h + k < n) {
+          const int mx = __shfl_sync(0xffffffffu, mine.x, h + k);
+          const int my = __shfl_sync(0xffffffffu, mine.y, h + k);
+          const int mz = __shfl_sync(0xffffffffu, mine.z, h + k);
+          const bool hb = mz & 1, la = mz & 2, single = mz & 4;
+          if (single) {
+            if (hb || la) entry(mx, v0[k], hb, la);
+          } else {
+            if (hb) entry(mx, v0[k], true, false);
+            if (la) entry(my, v1[k], false, true);
+          }
+        }
+      }
     }
-    if (first_run && sfirst < 0) sfirst = cur;
-    first_run = false;
-  };
-  auto entry = [&](int r, size_t slot, bool before, bool after) {
-    if (r != cur) {
-      if (cur >= 0) close_run();
-      cur = r;
-      cur_before = before;
-      s0 = s1 = 0.0;
-    }
-    const float* c = a.carry + slot * rp;
-    if (lane < rp) s0 += (double)c[lane];
-    if (two) s1 += (double)c[lane + 32];
-    cur_after = after;
-  };
-  for (int k = 0; k < n; k++) {
-    const int mx = __shfl_sync(0xffffffffu, mine.x, k);
-    const int my = __shfl_sync(0xffffffffu, mine.y, k);
-    const int mz = __shfl_sync(0xffffffffu, mine.z, k);
-    const bool hb = mz & 1, la = mz & 2, single = mz & 4;
-    const size_t u = (size_t)(u0 + k);
-    if (single) {
-      if (hb || la) entry(mx, 2 * u, hb, la);
-    } else {
-      if (hb) entry(mx, 2 * u, true, false);
-      if (la) entry(my, 2 * u + 1, false, true);
+    if (cur >= 0) close_run();
+    if (c0 == 0) {
+      nruns = runs;
+      if (slast < 0) slast = cur;
     }
   }
-  if (cur >= 0) close_run();
-  if (slast < 0) slast = cur;
   if (lane == 0) {
     // bit2: one run in the segment (its partial, if any, is in slot 0)
     reinterpret_cast<int4*>(a.segmeta)[sg] = make_int4(sfirst, slast, sflags | (nruns == 1 ? 4 : 0), 0);
@@ -1227,12 +1261,14 @@ __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant_
 // slots and of chain_fixup_kernel.  A warp stages its own tile and window with
 // 128-bit loads, walks it (walk_lean) and settles its rows: no block barrier,
 // so a warp waiting on its gathers never holds up another.
-template <int ORDER, int PREC, int CPT, int LPR, bool EXACT = false>
-__global__ void __launch_bounds__(512) mttkrp_lean_kernel(const __grid_constant__ WalkArgs a) {
+// MINB: resident 256-thread blocks per SM the register budget is cut for
+// (2: up to 128 registers a thread, 3: 80, 4: 64).
+template <int ORDER, int PREC, int CPT, int LPR, int MINB = 2, bool EXACT = false>
+__global__ void __launch_bounds__(256, MINB) mttkrp_lean_kernel(const __grid_constant__ WalkArgs a) {
   using WK = Walk<ORDER, PREC, CPT, LPR>;
   constexpr int VB = WK::VB;
   constexpr int TW = 32 / LPR;
-  constexpr int U = WK::LB >= 32 ? 4 : 8;
+  constexpr int U = WK::LB >= 16 ? 4 : 8;  // nonzeros per gather batch (two batches in registers)
   static_assert(!EXACT || VB == 4, "exact-length staging is built for FP32 values");
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;

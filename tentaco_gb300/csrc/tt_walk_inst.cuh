@@ -9,14 +9,21 @@
 namespace tt {
 namespace {
 // fam 0: lean warp-tile walk, 1: shared-memory staged, 2: register walk with a
-// per-lane cp.async ring.  units: work units of the partition (warp tiles for
+// per-lane cp.async ring, 3: lean with the tighter register budget.  units: work units of the partition (warp tiles for
 // fam 0, blocks otherwise).
+// Resident blocks per SM the lean kernel's registers are budgeted for: the
+// variant's thread axis selects the looser (tb 256) or tighter (tb 512) budget;
+// both launch 256-thread blocks.
+constexpr int lean_minb(int cpt, bool tight) { return cpt >= 4 ? (tight ? 3 : 2) : (tight ? 4 : 3); }
+
 template <int CPT, int LPR, int FAM>
 cudaError_t launch_walk(const WalkArgs& a, int units, int tb, size_t smem, cudaStream_t s) {
+  constexpr bool kTight = FAM == 3;  // lean with the tighter register budget
   auto k = FAM == 1 ? mttkrp_stage_kernel<TT_ORDER, TT_PREC, CPT, LPR>
          : FAM == 2 ? mttkrp_walk_kernel<TT_ORDER, TT_PREC, CPT, LPR, false, true>
-                    : mttkrp_lean_kernel<TT_ORDER, TT_PREC, CPT, LPR>;
-  const int grid = FAM == 0 ? (units + tb / 32 - 1) / (tb / 32) : units;
+                    : mttkrp_lean_kernel<TT_ORDER, TT_PREC, CPT, LPR, lean_minb(CPT, kTight)>;
+  if (FAM == 0 || FAM == 3) tb = 256;
+  const int grid = (FAM == 0 || FAM == 3) ? (units + tb / 32 - 1) / (tb / 32) : units;
   static size_t configured = 48 * 1024;
   if (smem > configured) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -31,7 +38,8 @@ cudaError_t launch_walk(const WalkArgs& a, int units, int tb, size_t smem, cudaS
 WalkLauncher TT_LOOKUP(int cpt, int lpr, int fam) {
 #define TT_CASE(C, L)                                                        \
   if (cpt == C && lpr == L)                                                  \
-    return fam == 2 ? &launch_walk<C, L, 2> : fam == 1 ? &launch_walk<C, L, 1> : &launch_walk<C, L, 0>;
+    return fam == 3 ? &launch_walk<C, L, 3> : fam == 2 ? &launch_walk<C, L, 2> : fam == 1 ? &launch_walk<C, L, 1> \
+                                                                                  : &launch_walk<C, L, 0>;
   TT_CASE(1, 8) TT_CASE(2, 4) TT_CASE(4, 2) TT_CASE(8, 1)     // rank 8
   TT_CASE(1, 16) TT_CASE(2, 8) TT_CASE(4, 4) TT_CASE(8, 2)    // rank 16
   TT_CASE(1, 32) TT_CASE(2, 16) TT_CASE(4, 8) TT_CASE(8, 4)   // rank 32

@@ -257,17 +257,16 @@ def test_slabs_long_fiber_and_order4(c5_small):
             close(got, ref4, prec)
 
 
-def test_auto_slabs_for_large_leaf_factor():
-    # leaf factor 2M x 32 FP32 = 256 MB: automatic slabs keep each pass's rows near 32 MB
+def test_slabs_over_large_leaf_factor():
+    # leaf factor 2M x 32 FP32 = 256 MB, split into 32 MB (FP32) and 16 MB (FP16) slabs
     B = tt.gen_zipf((1000, 800, 2_000_000), (0.5, 0, 0), 300_000, seed=31)
     facs = [tt.gen_dense(800, 32, 1, 3), tt.gen_dense(2_000_000, 32, 1, 4)]
     ref = O.mttkrp(to_oracle(B), facs)
     got, plan = run_plan(B, facs)
+    assert plan.slabs == 1  # automatic: no slabs
+    close(got, ref)
+    got, plan = run_plan(B, facs, slabs=8)
     assert plan.slabs == 8
     close(got, ref)
-    got, plan = run_plan(B, facs, prec="fp16")
-    assert plan.slabs == 4
+    got, plan = run_plan(B, facs, prec="fp16", slabs=8)
     close(got, ref, "fp16")
-    got, plan = run_plan(B, facs, slabs=1)
-    assert plan.slabs == 1
-    close(got, ref)
