@@ -155,7 +155,7 @@ def init_params(nout: int, seed: int) -> np.ndarray:
     return np.concatenate(parts).astype(np.float32)
 
 
-def train(recs: list, storage: int, nout: int, steps: int = 4000, lr: float = 2e-3, wd: float = 1e-4,
+def train(recs: list, storage: int, nout: int, steps: int = 3000, lr: float = 1e-3, wd: float = 3e-3,
           seed: int = 0, log=sys.stdout) -> dict:
     import tentaco_gb300 as tt
     _, X, T, M = dataset(recs, storage, "train")
@@ -180,6 +180,15 @@ def pick(scores: np.ndarray, ms: np.ndarray) -> int:
     return -1
 
 
+def heuristic_pick(r: dict) -> int:
+    """The fixed heuristic's variant for a corpus record (the library's current rule)."""
+    try:
+        import tentaco_gb300 as tt
+        return int(tt.default_variant(3, r["rank"], r["prec"], r["nnz"]))
+    except Exception:  # library not built: the rule recorded with the sweep
+        return int(r["default"])
+
+
 def evaluate(recs: list, models: dict, forward, split: str = "test") -> dict:
     """Per storage class: mean/max regret of the model's pick and of the heuristic."""
     out = {}
@@ -197,7 +206,7 @@ def evaluate(recs: list, models: dict, forward, split: str = "test") -> dict:
             v = pick(sc, ms)
             reg.append(ms[v] / best - 1.0)
             within += ms[v] <= 1.10 * best
-            d = r["default"]
+            d = heuristic_pick(r)
             regh.append((ms[d] if ms[d] > 0 else np.nan) / best - 1.0)
         reg = np.array(reg)
         regh = np.array(regh)
@@ -218,8 +227,8 @@ def main(argv=None) -> int:
     t = sub.add_parser("train")
     t.add_argument("--corpus", required=True)
     t.add_argument("--out", required=True)
-    t.add_argument("--steps", type=int, default=4000)
-    t.add_argument("--lr", type=float, default=2e-3)
+    t.add_argument("--steps", type=int, default=3000)
+    t.add_argument("--lr", type=float, default=1e-3)
     t.add_argument("--report", default=None, help="write the held-out regret report (JSON) here")
     a = ap.parse_args(argv)
     if a.cmd == "corpus":
