@@ -46,8 +46,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--prec", default="bf16", choices=["fp32", "bf16", "bf16f", "fp16"])
-    ap.add_argument("--compare", default="fp32,fp16",
+    ap.add_argument("--prec", default="fp16", choices=["fp32", "bf16", "bf16f", "fp16"],
+                    help="storage precision of the headline run (fp16: the 16-bit mode within 1e-3 of FP64)")
+    ap.add_argument("--compare", default="fp32,bf16",
                     help="other storage precisions timed on the same tensor (comma list, '' for none)")
     ap.add_argument("--select", default="model", choices=["default", "model", "sweep"])
     ap.add_argument("--variant", type=int, default=-1, help="run this variant id (overrides --select)")
@@ -56,6 +57,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-errors", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the TTV (50M nonzeros) and 4-mode MTTKRP (80M nonzeros) measurements")
     return ap.parse_args()
 
 
@@ -286,7 +289,9 @@ def run_gpu_arm(args, rank, world, d):
                      "peak_source": f"{peak_kind} hbm_gbs", "kernel_ms": round(kern, 4),
                      "compulsory_bytes": int(cbytes), "U1": U1, "U2": U2},
         "clocks": clocks,
-        "gpu_launches": args.steps * 3,  # per step: partition, output clear (memset), walk kernel
+        # our kernels per step and slab: partition, walk, segment fold, segment chain (the
+        # output clear is a cudaMemsetAsync)
+        "gpu_launches": args.steps * 4 * plan.slabs,
     }
     if "fp32" in others:
         out["speedup_vs_fp32"] = round(others["fp32"]["ms_per_step"] / ms, 3)
@@ -317,7 +322,83 @@ def run_gpu_arm(args, rank, world, d):
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(B, C, D, budget_s=15.0)
+    if not args.no_secondary:
+        del B, C, D, A, bufs, plan
+        out["secondary"] = {"ttv_config2": secondary_ttv(args), "mttkrp4_config5": secondary_mttkrp4(args)}
     return out
+
+
+def _timed(call, plan, steps, warmup):
+    """Mean ms of a plan call over `steps` (L2 flushed before each), CUDA events."""
+    import tentaco_gb300 as tt
+
+    plan.set_timing(True)
+    for _ in range(warmup):
+        tt.l2_flush()
+        call()
+    ms = []
+    for _ in range(steps):
+        tt.l2_flush()
+        call()
+        ms.append(plan.last_ms())
+    return float(np.mean(ms))
+
+
+def secondary_ttv(args):
+    """TTV on config 2: 50,000 x 40,000 x 30,000, 50M nonzeros, Zipf(1.1) on modes 0 and 1,
+    uniform mode 2, values and vector U(-1,1); checked against the FP64 oracle."""
+    import tentaco_gb300 as tt
+    from oracle import oracle as O
+
+    B = tt.gen_zipf((50_000, 40_000, 30_000), (1.1, 1.1, 0.0), 50_000_000, seed=2, vlo=-1.0, vhi=1.0)
+    x = tt.gen_dense(30_000, 1, 2, 21)[:, 0].copy()
+    plan = tt.Plan(B, op=tt.OP_TTV)
+    nfib = B.count(1)
+    dx = tt.DeviceBuffer.from_array(x)
+    dy = tt.DeviceBuffer(nfib * 4)
+    ms = _timed(lambda: plan.ttv(dx, dy), plan, max(3, args.steps), args.warmup)
+    y = dy.to_array((nfib,))
+    Oc = O.Csf(3, B.dims, [None, B.pos(1).astype(np.int64), B.pos(2).astype(np.int64)],
+               [None, B.crd(1).astype(np.int64), B.crd(2).astype(np.int64)], B.vals.astype(np.float64))
+    ref = O.ttv(Oc, x.astype(np.float64))
+    U = int(np.count_nonzero(np.bincount(B.crd(2), minlength=B.dims[2])))
+    cbytes = B.nnz * 8 + nfib * 12 + (B.dims[0] + 1) * 4 + U * 4
+    return {"nnz": B.nnz, "fibers": nfib, "ms_per_step": round(ms, 4),
+            "gflops": round(2.0 * B.nnz / (ms * 1e-3) / 1e9, 2),
+            "gbs_compulsory": round(cbytes / (ms * 1e-3) / 1e9, 1),
+            "error_vs_fp64": {"normwise_max": float(np.abs(y - ref).max() / max(np.abs(ref).max(), 1e-300)),
+                              "fro": float(np.linalg.norm(y - ref) / max(np.linalg.norm(ref), 1e-300))}}
+
+
+def secondary_mttkrp4(args):
+    """MTTKRP on config 5: 4-mode 5,000 x 3,000 x 2,000 x 100,000, 80M nonzeros, Zipf(1.2) on
+    modes 0 and 3, rank 32 N(0,1) factors; FP16 storage (sweep-selected: the learned model
+    covers 3-mode tensors) against plain FP32, sampled rows checked against the FP64 oracle."""
+    import tentaco_gb300 as tt
+    from oracle import oracle as O
+
+    dims = (5_000, 3_000, 2_000, 100_000)
+    B = tt.gen_zipf(dims, (1.2, 0.0, 0.0, 1.2), 80_000_000, seed=5)
+    facs = [tt.gen_dense(d, RANK, 1, 50 + m) for m, d in enumerate(dims[1:])]
+    bufs = [tt.DeviceBuffer.from_array(f) for f in facs]
+    A = tt.DeviceBuffer(dims[0] * RANK * 4)
+    Oc = O.Csf(4, B.dims, [None] + [B.pos(l).astype(np.int64) for l in (1, 2, 3)],
+               [None] + [B.crd(l).astype(np.int64) for l in (1, 2, 3)], B.vals.astype(np.float64))
+    rows = np.random.default_rng(0).choice(np.flatnonzero(np.diff(B.pos(1))), 512, replace=False)
+    ref = O.mttkrp(Oc, facs, rows=rows)
+    res = {"nnz": B.nnz}
+    for prec in ("fp16", "fp32"):
+        plan = tt.Plan(B, rank=RANK, prec=prec, select=tt.SELECT_SWEEP)
+        plan.set_factors(bufs)
+        ms = _timed(lambda: plan.mttkrp(A), plan, max(3, args.steps // 2), args.warmup)
+        got = A.to_array((dims[0], RANK))[rows].astype(np.float64)
+        res[prec] = {"ms_per_step": round(ms, 4), "gflops": round(4.0 * B.nnz * RANK / (ms * 1e-3) / 1e9, 2),
+                     "variant": tt.variant_info(plan.variant)["name"],
+                     "error_vs_fp64": {"normwise_max": float(np.abs(got - ref).max() / np.abs(ref).max()),
+                                       "fro": float(np.linalg.norm(got - ref) / np.linalg.norm(ref))}}
+        del plan
+    res["speedup_fp16_vs_fp32"] = round(res["fp32"]["ms_per_step"] / res["fp16"]["ms_per_step"], 3)
+    return res
 
 
 def cpu_rows_sample(B, budget_nnz):
