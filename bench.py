@@ -170,12 +170,14 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(prec):
-    """Per-launch DRAM bytes of the walk kernel from the committed ncu summary, if any."""
+def ncu_traffic(prec, variant):
+    """Per-launch DRAM bytes of the walk kernel from the committed ncu capture of the
+    same workload, precision and variant (None when there is none)."""
     path = os.path.join(ROOT, "profiles", f"walk_kernel_{WORKLOAD}_{prec}.json")
     try:
         with open(path) as fh:
-            return json.load(fh).get("dram_bytes_per_launch")
+            p = json.load(fh)
+        return p.get("dram_bytes_per_launch") if p.get("variant") == variant else None
     except Exception:
         return None
 
@@ -270,7 +272,7 @@ def run_gpu_arm(args, rank, world, d):
     cbytes, U1, U2 = compulsory_bytes(B, s_v, s_f)
     peak, peak_kind = peaks()
     achieved = cbytes / (kern * 1e-3) / 1e9
-    traffic = ncu_traffic(args.prec)
+    traffic = ncu_traffic(args.prec, plan.variant) if args.nnz == NNZ else None
 
     out = {
         "metric": f"MTTKRP3 GFLOP/s (3*nnz*R), {WORKLOAD}, {args.prec} storage, FP32 accumulate",
