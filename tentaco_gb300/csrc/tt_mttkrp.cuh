@@ -429,12 +429,16 @@ struct Walk {
         const float4 f = reinterpret_cast<const float4*>(vt)[k];
         v[4 * k] = f.x; v[4 * k + 1] = f.y; v[4 * k + 2] = f.z; v[4 * k + 3] = f.w;
       }
-    } else if constexpr (U == 8) {
-      const uint4 w = *reinterpret_cast<const uint4*>(vt);
-      const float2 a = pair16<VK>(w.x), b = pair16<VK>(w.y), c = pair16<VK>(w.z), d = pair16<VK>(w.w);
-      v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y; v[6] = d.x; v[7] = d.y;
+    } else if constexpr (U % 8 == 0) {
+#pragma unroll
+      for (int k = 0; k < U / 8; k++) {
+        const uint4 w = reinterpret_cast<const uint4*>(vt)[k];
+        const float2 a = pair16<VK>(w.x), b = pair16<VK>(w.y), c = pair16<VK>(w.z), d = pair16<VK>(w.w);
+        v[8 * k] = a.x; v[8 * k + 1] = a.y; v[8 * k + 2] = b.x; v[8 * k + 3] = b.y;
+        v[8 * k + 4] = c.x; v[8 * k + 5] = c.y; v[8 * k + 6] = d.x; v[8 * k + 7] = d.y;
+      }
     } else {
-      static_assert(U == 4, "batches of 4 or 8 nonzeros");
+      static_assert(U == 4, "batches of 4, 8 or 16 nonzeros");
       const uint2 w = *reinterpret_cast<const uint2*>(vt);
       const float2 a = pair16<VK>(w.x), b = pair16<VK>(w.y);
       v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
@@ -995,9 +999,10 @@ __device__ __forceinline__ int64_t row_first_window_fiber(const WalkArgs& a, int
 // a partial of its first row (it started in an earlier unit) and/or of its last
 // row (it continues in a later unit).  In unit order the entries of one row are
 // consecutive, so every shared row is a run of entries.  The runs are summed in
-// FP64 in two levels, each in a fixed order (bitwise reproducible):
+// two levels, each in a fixed order (bitwise reproducible):
 //   seg_fold_kernel   one warp per segment of kSeg units, lanes over columns:
-//                     sums each run inside the segment; a run that starts and
+//                     sums each run inside the segment (FP32 with Kahan
+//                     compensation; at most 2*kSeg terms); a run that starts and
 //                     ends in the segment is final and written to the output,
 //                     the segment's first/last run, if it crosses the segment's
 //                     edge, goes to the segment's FP64 carry slot (same meta
@@ -1031,18 +1036,21 @@ __global__ void __launch_bounds__(256, 2) seg_fold_kernel(const __grid_constant_
     const bool live = col < rp;
     int cur = -1;
     bool cur_before = false, cur_after = false, first_run = true;
-    double acc = 0.0;
+    // the run's sum in FP32 with Kahan compensation (a run has at most 64 terms);
+    // what leaves the segment is kept in FP64
+    float acc = 0.f, comp = 0.f;
     int runs = 0;
     auto close_run = [&]() {
       runs++;
+      const double v = (double)acc + (double)comp;
       if (!cur_before && !cur_after) {
-        if (col < a.R) put_row_value(a, cur, col, acc);
+        if (col < a.R) put_row_value(a, cur, col, v);
       } else if (cur_before) {  // necessarily the segment's first run
         if (c0 == 0) { sfirst = cur; sflags |= 1; if (cur_after) { slast = cur; sflags |= 2; } }
-        if (live) sc0[col] = acc;
+        if (live) sc0[col] = v;
       } else {  // cur_after only: the segment's last run (slot 0 when it is the only run)
         if (c0 == 0) { slast = cur; sflags |= 2; }
-        if (live) (first_run ? sc0 : sc1)[col] = acc;
+        if (live) (first_run ? sc0 : sc1)[col] = v;
       }
       if (c0 == 0 && first_run && sfirst < 0) sfirst = cur;
       first_run = false;
@@ -1052,9 +1060,14 @@ __global__ void __launch_bounds__(256, 2) seg_fold_kernel(const __grid_constant_
         if (cur >= 0) close_run();
         cur = r;
         cur_before = before;
-        acc = 0.0;
+        acc = 0.f;
+        comp = 0.f;
       }
-      acc += (double)v;
+      // Kahan (1965): y = v - c; t = s + y; c = (t - s) - y; s = t  (comp holds -c)
+      const float y = v + comp;
+      const float t = acc + y;
+      comp = y - (t - acc);
+      acc = t;
       cur_after = after;
     };
     constexpr int kHalf = kSeg / 2;
