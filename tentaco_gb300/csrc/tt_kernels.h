@@ -6,7 +6,6 @@
 
 namespace tt {
 struct WalkArgs;
-struct TtvArgs;
 
 using WalkLauncher = cudaError_t (*)(const WalkArgs& a, int grid, int tb, size_t smem, cudaStream_t s);
 
@@ -29,8 +28,8 @@ WalkLauncher walk_launcher_o4_fp16(int cpt, int lpr, int staged);
 cudaError_t launch_partition(int order, const WalkArgs& a, cudaStream_t s);
 // FP64 merge of the rows the walk left in the carry buffer (after the walk kernel).
 cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s);
-cudaError_t launch_ttv(const TtvArgs& a, int grid, int tb, size_t smem, cudaStream_t s);
-cudaError_t launch_ttv_partition(const TtvArgs& a, cudaStream_t s);
+// TTV walk over units of 32 * kTtvNpt nonzeros (a: the 2-level view, see tt_ttv.cuh).
+cudaError_t launch_ttv(const WalkArgs& a, int vals_kind, cudaStream_t s);
 
 // Column max |x| of a rows x cols FP32 row-major matrix into colmax (cols floats, zeroed here).
 cudaError_t launch_colmax(const float* x, int64_t rows, int cols, float* colmax, cudaStream_t s);

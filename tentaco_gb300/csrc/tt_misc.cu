@@ -25,7 +25,8 @@ WalkLauncher walk_launcher(int order, int prec, int cpt, int lpr, int staged) {
 cudaError_t launch_partition(int order, const WalkArgs& a, cudaStream_t s) {
   const int n = a.nblocks + 1;
   const int tb = 256, grid = (n + tb - 1) / tb;
-  if (order == 3) partition_kernel<3><<<grid, tb, 0, s>>>(a);
+  if (order == 2) partition_kernel<2><<<grid, tb, 0, s>>>(a);
+  else if (order == 3) partition_kernel<3><<<grid, tb, 0, s>>>(a);
   else partition_kernel<4><<<grid, tb, 0, s>>>(a);
   return cudaGetLastError();
 }
@@ -48,7 +49,10 @@ cudaError_t launch_window_max(int order, const WalkArgs& a, int* out, cudaStream
 cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s) {
   if (a.nblocks == 0) return cudaSuccess;
   const int grid = (num_segments(a.nblocks) + 7) / 8;  // one warp per segment
-  if (order == 3) {
+  if (order == 2) {
+    seg_fold_kernel<2><<<grid, 256, 0, s>>>(a);
+    seg_chain_kernel<2><<<grid, 256, 0, s>>>(a);
+  } else if (order == 3) {
     seg_fold_kernel<3><<<grid, 256, 0, s>>>(a);
     seg_chain_kernel<3><<<grid, 256, 0, s>>>(a);
   } else {
@@ -58,21 +62,25 @@ cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_ttv(const TtvArgs& a, int grid, int tb, size_t smem, cudaStream_t s) {
+template <int VK>
+cudaError_t launch_ttv_k(const WalkArgs& a, int grid, size_t smem, cudaStream_t s) {
   static size_t configured = 48 * 1024;
   if (smem > configured) {
-    cudaError_t e = cudaFuncSetAttribute(ttv_walk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(ttv_lean_kernel<VK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     configured = smem;
   }
-  ttv_walk_kernel<<<grid, tb, smem, s>>>(a);
+  ttv_lean_kernel<VK><<<grid, 256, smem, s>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t launch_ttv_partition(const TtvArgs& a, cudaStream_t s) {
-  const int n = a.nblocks + 1;
-  ttv_partition_kernel<<<(n + 255) / 256, 256, 0, s>>>(a);
-  return cudaGetLastError();
+cudaError_t launch_ttv(const WalkArgs& a, int vals_kind, cudaStream_t s) {
+  if (a.nblocks == 0) return cudaSuccess;
+  const int grid = (a.nblocks + 7) / 8;  // one warp per unit, 8 warps per block
+  const size_t smem = (size_t)8 * ttv_warp_bytes(vals_kind == kF32 ? 4 : 2);
+  if (vals_kind == kB16) return launch_ttv_k<kB16>(a, grid, smem, s);
+  if (vals_kind == kH16) return launch_ttv_k<kH16>(a, grid, smem, s);
+  return launch_ttv_k<kF32>(a, grid, smem, s);
 }
 
 // ---------------------------------------------------------------------------

@@ -60,6 +60,7 @@ struct WalkArgs {
   int32_t smem_bytes;     // dynamic shared memory of the launch (bounds for checked builds)
   int32_t accum;          // 1: add rows into out (slab passes), 0: overwrite
   int32_t gpol;           // L2 policy of the lean walk's factor-row gathers: 0 evict_last, 1 evict_normal
+  float vscale;           // TTV: scale of the stored values (1 for FP32 values)
   double* segcarry;       // cross-unit rows: 2 FP64 partial rows per segment of kSeg units
   int32_t* segmeta;       // 4 ints per segment
   int32_t wcap;           // staged kernels: window fibers per block the shared memory holds
@@ -1122,7 +1123,8 @@ __global__ void __launch_bounds__(256) seg_chain_kernel(const __grid_constant__ 
   const bool before = m.z & 1, after = m.z & 2, single = m.z & 4;
   if (!after || (single && before)) return;  // warp-uniform: no crossing row starts here
   const int r = m.y;
-  int64_t f1 = a.pos[1][r + 1];
+  // ORDER 2: the "rows" are TTV fibers (pos[1] = fiber starts)
+  int64_t f1 = ORDER == 2 ? (int64_t)r + 1 : (int64_t)a.pos[1][r + 1];
   if constexpr (ORDER == 4) f1 = a.pos[2][f1];
   const int64_t n1 = a.pos[ORDER - 1][f1];
   const int s1 = (int)((n1 - 1) / a.P) / kSeg;  // segment holding the row's last nonzero
@@ -1450,23 +1452,24 @@ __global__ void partition_kernel(const __grid_constant__ WalkArgs a) {
   if (b > a.nblocks) return;
   const int64_t s = (b < a.nblocks) ? (int64_t)b * a.P : a.nnz - 1;
   int32_t* out = const_cast<int32_t*>(a.part) + (size_t)b * (ORDER - 1);
-  // number of fibers at level ORDER-2 = last entry index of pos[ORDER-1] minus one
-  int64_t hi = 0;
-  // fibers at level 1: pos[1][nrows]; level 2: pos[2][#level1]
-  int64_t nf1 = a.pos[1][a.nrows];
-  int64_t f1;
-  if constexpr (ORDER == 3) {
-    f1 = search_le(a.pos[2], 0, nf1 - 1, s);
-    out[1] = (int32_t)f1;
+  if constexpr (ORDER == 2) {  // TTV: the fiber holding the unit's first nonzero (nrows = fibers)
+    out[0] = (int32_t)search_le(a.pos[1], 0, a.nrows - 1, s);
   } else {
-    int64_t nf2 = a.pos[2][nf1];
-    int64_t f2 = search_le(a.pos[3], 0, nf2 - 1, s);
-    f1 = search_le(a.pos[2], 0, nf1 - 1, f2);
-    out[1] = (int32_t)f1;
-    out[2] = (int32_t)f2;
+    // fibers at level 1: pos[1][nrows]; level 2: pos[2][#level1]
+    const int64_t nf1 = a.pos[1][a.nrows];
+    int64_t f1;
+    if constexpr (ORDER == 3) {
+      f1 = search_le(a.pos[2], 0, nf1 - 1, s);
+      out[1] = (int32_t)f1;
+    } else {
+      const int64_t nf2 = a.pos[2][nf1];
+      const int64_t f2 = search_le(a.pos[3], 0, nf2 - 1, s);
+      f1 = search_le(a.pos[2], 0, nf1 - 1, f2);
+      out[1] = (int32_t)f1;
+      out[2] = (int32_t)f2;
+    }
+    out[0] = (int32_t)search_le(a.pos[1], 0, a.nrows - 1, f1);
   }
-  (void)hi;
-  out[0] = (int32_t)search_le(a.pos[1], 0, a.nrows - 1, f1);
 }
 
 

@@ -312,26 +312,32 @@ tt_status run_ttv(tt_plan* p, const float* x, float* y, cudaStream_t st) {
     if (p->nfib_last > 0) CK(cudaMemsetAsync(y, 0, sizeof(float) * (size_t)p->nfib_last, st));
     return TT_OK;
   }
-  TtvArgs a{};
-  a.pos = p->d_pos[p->order - 1];
-  a.crd = p->d_crd[p->order - 1];
+  // the last two levels as a 2-level CSF: "rows" are the fibers, one output column
+  WalkArgs a{};
+  a.pos[1] = p->d_pos[p->order - 1];
+  a.crd[1] = p->d_crd[p->order - 1];
   a.vals = p->d_vals;
-  a.x = x;
-  a.y = y;
+  a.fac[0] = x;
+  a.out = y;
   a.part = p->d_part;
   a.carry = p->d_carry;
-  a.tickets = p->d_tickets;
+  a.meta = p->d_meta;
+  a.segcarry = p->d_segcarry;
+  a.segmeta = p->d_segmeta;
   a.vscale = val_kind(p->prec) != kF32 ? p->vinv : 1.f;
   a.nnz = p->nnz;
-  a.nfib = p->nfib_last;
+  a.nrows = (int32_t)p->nfib_last;
+  a.R = 1;
+  a.rp = 1;
+  a.ldo = 1;
   a.P = p->P;
-  a.NPT = p->G;
+  a.G = kTtvNpt;
   a.nblocks = p->nblocks;
-  a.vals_kind = val_kind(p->prec);
-  CK(launch_ttv_partition(a, st));
+  CK(launch_partition(2, a, st));
   if (p->timing) CK(cudaEventRecord(p->evk0, st));
-  CK(launch_ttv(a, p->nblocks, p->tb, ttv_smem_bytes(p->P, p->tb), st));
+  CK(launch_ttv(a, val_kind(p->prec), st));
   if (p->timing) CK(cudaEventRecord(p->evk1, st));
+  CK(launch_chain_fixup(2, a, st));
   return TT_OK;
 }
 
@@ -575,15 +581,12 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
       p->selected_by = 2;
     }
   } else {
+    // TTV: one warp per 32 * kTtvNpt nonzeros
     p->tb = 256;
-    p->G = 16;  // nonzeros per thread
-    p->P = p->tb * p->G;
+    p->G = kTtvNpt;
+    p->P = 32 * kTtvNpt;
     p->nblocks = (int)((p->nnz + p->P - 1) / p->P);
-    if ((s = dev_alloc(p, &p->d_part, (size_t)p->nblocks + 1)) != TT_OK) return fail(s);
-    if ((s = dev_alloc(p, &p->d_carry, (size_t)2 * p->nblocks)) != TT_OK) return fail(s);
-    if ((s = dev_alloc(p, &p->d_tickets, (size_t)p->nblocks + 1)) != TT_OK) return fail(s);
-    if (cudaMemsetAsync(p->d_tickets, 0, sizeof(int32_t) * ((size_t)p->nblocks + 1), st) != cudaSuccess)
-      return fail(set_error(TT_ERR_CUDA, "clear tickets"));
+    if ((s = alloc_walk_scratch(p, p->P)) != TT_OK) return fail(s);
   }
   if (cudaStreamSynchronize(st) != cudaSuccess) return fail(set_error(TT_ERR_CUDA, "plan upload: %s", cudaGetErrorString(cudaGetLastError())));
   *out = p;

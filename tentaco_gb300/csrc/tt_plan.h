@@ -49,7 +49,6 @@ struct tt_plan {
   tt::WalkLauncher launcher = nullptr;
   int32_t* d_part = nullptr;
   float* d_carry = nullptr;
-  int32_t* d_tickets = nullptr;  // TTV
   int32_t* d_meta = nullptr;     // MTTKRP: 4 ints per work unit
   double* d_segcarry = nullptr;  // MTTKRP: 2 FP64 rows per segment of work units
   int32_t* d_segmeta = nullptr;  // MTTKRP: 4 ints per segment

@@ -5,203 +5,148 @@
 // Replaces the reference's ttv_kernel / ttv_csf_gpu_taco
 // (tensor_kernels/ttv_csf_gpu_taco.h:2-121).  The output is indexed by fiber
 // position, as in the reference (A_vals[j_pos] there), so only the last two CSF
-// levels are read.  Unlike the reference, every output is written exactly once
-// (no memset, no float atomics):
-//   * block b owns nonzeros [b*P, (b+1)*P); each thread walks NPT consecutive
-//     nonzeros with 128-bit streaming loads of crd and vals;
-//   * fibers complete inside a thread are stored directly; the first and last
-//     partial fibers of every thread are merged by a warp shuffle tree and
-//     across warps in shared memory;
-//   * fibers that span blocks go through a carry buffer and a per-chain ticket
-//     (indexed by the chain's first block, reset by the last arriver), and the
-//     last block sums the partials in FP64 in block order.
-// x is gathered through L1 (it is small for the reference's workloads); the
-// streams are evict_first in L2.
+// levels are read: the kernels see a 2-level CSF (WalkArgs with pos[1] = fiber
+// starts, crd[1] = last-mode coordinates, nrows = fibers, one output column).
+// Unlike the reference, every output is written exactly once (no memset, no
+// float atomics):
+//   * a warp owns kTtvNpt * 32 consecutive nonzeros (its work unit); it stages
+//     their coordinates and values with 128-bit loads into shared memory (each
+//     lane's run padded by 16 bytes against bank conflicts) and the fiber
+//     window, then every lane walks kTtvNpt nonzeros with its x gathers issued
+//     before use;
+//   * fibers complete inside a lane are stored directly; the lanes' first and
+//     last partial fibers are merged by the warp's shuffle tree, and fibers
+//     shared between warps go through the unit carry slots and the two-level
+//     merge of tt_mttkrp.cuh (FP32 Kahan inside a segment of units, FP64 across).
+// x is read through L1 (it is small for the reference's workloads); the streams
+// are evict_first in L2.
 #pragma once
-#include "tt_common.cuh"
+#include "tt_mttkrp.cuh"
 
 namespace tt {
 
-struct TtvArgs {
-  const int32_t* pos;   // nfib+1
-  const int32_t* crd;   // nnz (padded)
-  const void* vals;     // FP32 or BF16 (padded)
-  const float* x;
-  float* y;             // nfib
-  const int32_t* part;  // nblocks+1 fiber ids
-  float* carry;         // 2*nblocks
-  int32_t* tickets;     // nblocks, zero between calls
-  float vscale;         // value scale (BF16 values), 1 otherwise
-  int64_t nnz;
-  int64_t nfib;
-  int32_t P;
-  int32_t NPT;          // nonzeros per thread, multiple of 4
-  int32_t nblocks;
-  int32_t vals_kind;    // kF32, kB16 or kH16
-};
+constexpr int kTtvNpt = 16;  // nonzeros per lane
 
-struct TSumm {
-  int64_t h, t;
-  float ha, ta;
-};
-
-__host__ __device__ inline size_t ttv_smem_bytes(int P, int tb) {
-  size_t b = (size_t)(P + 2) * sizeof(int32_t);
-  b = (b + 15) & ~(size_t)15;
-  b += (size_t)(tb / 32) * (2 * sizeof(int64_t) + 2 * sizeof(float));
-  b = (b + 15) & ~(size_t)15;
-  b += (size_t)tb * sizeof(double) + 8 * sizeof(int64_t);
-  return b;
+// Shared memory of one warp: coordinate runs 32 x (kTtvNpt + 4) int32, value runs
+// 32 x (kTtvNpt * vbytes + 16) bytes, fiber window starts (at most 32*kTtvNpt + 2).
+__host__ __device__ inline size_t ttv_warp_bytes(int vbytes) {
+  const size_t pu = (size_t)32 * kTtvNpt;
+  size_t b = (size_t)32 * (kTtvNpt + 4) * 4 + (size_t)32 * ((size_t)kTtvNpt * vbytes + 16);
+  b += (pu + 2) * 4;
+  return (b + 15) & ~(size_t)15;
 }
 
 #ifndef TT_ARGS_ONLY
-__device__ __forceinline__ void ttv_combine(TSumm& X, const TSumm& Y, float* y) {
-  if (Y.h == kEmpty) return;
-  if (X.h == kEmpty) { X = Y; return; }
-  const bool xs = X.t == kNone, ys = Y.t == kNone;
-  const int64_t xl = xs ? X.h : X.t;
-  if (xl == Y.h) {
-    if (xs) { X.ha += Y.ha; if (!ys) { X.t = Y.t; X.ta = Y.ta; } }
-    else if (ys) X.ta += Y.ha;
-    else { y[X.t] = X.ta + Y.ha; X.t = Y.t; X.ta = Y.ta; }
-  } else {
-    if (!xs) y[X.t] = X.ta;
-    if (ys) { X.t = Y.h; X.ta = Y.ha; }
-    else { y[Y.h] = Y.ha; X.t = Y.t; X.ta = Y.ta; }
-  }
-}
-
-__global__ void __launch_bounds__(512) ttv_walk_kernel(const __grid_constant__ TtvArgs a) {
+template <int VK>
+__global__ void __launch_bounds__(256, 4) ttv_lean_kernel(const __grid_constant__ WalkArgs a) {
+  constexpr int VB = VK == kF32 ? 4 : 2;
+  constexpr int NPT = kTtvNpt;
+  using WK = Walk<3, kFP32, 1, 1>;  // the merge helpers for one output column
   extern __shared__ __align__(16) unsigned char smem[];
-  const int tb = blockDim.x, nw = tb / 32, warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int b = blockIdx.x;
-  const int P = a.P;
-  int32_t* s_pos = reinterpret_cast<int32_t*>(smem);
-  size_t off = ((size_t)(P + 2) * 4 + 15) & ~(size_t)15;
-  int64_t* s_wh = reinterpret_cast<int64_t*>(smem + off);
-  int64_t* s_wt = s_wh + nw;
-  float* s_wha = reinterpret_cast<float*>(s_wt + nw);
-  float* s_wta = s_wha + nw;
-  off += (size_t)nw * (2 * sizeof(int64_t) + 2 * sizeof(float));
-  off = (off + 15) & ~(size_t)15;
-  double* s_dbl = reinterpret_cast<double*>(smem + off);
-  int64_t* s_ctl = reinterpret_cast<int64_t*>(s_dbl + tb);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int u = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (u >= a.nblocks) return;  // whole warp
+  const int PU = a.P;          // 32 * NPT
+  unsigned char* ws = smem + (size_t)warp * ttv_warp_bytes(VB);
+  int32_t* s_lc = reinterpret_cast<int32_t*>(ws);
+  unsigned char* s_val = ws + (size_t)32 * (NPT + 4) * 4;
+  int32_t* s_pos = reinterpret_cast<int32_t*>(s_val + (size_t)32 * (NPT * VB + 16));
 
-  const int64_t bstart = (int64_t)b * P;
-  const int64_t bend = min(bstart + (int64_t)P, a.nnz);
-  const int64_t fs = a.part[b];
-  const int W = (int)(a.part[b + 1] - fs + 1);
-  for (int x = threadIdx.x; x <= W; x += tb) s_pos[x] = a.pos[fs + x];
-  __syncthreads();
+  const int64_t ustart64 = (int64_t)u * PU;
+  const int ustart = (int)ustart64;
+  const int cnt = (int)min((int64_t)PU, a.nnz - ustart64);
+  const int fs = a.part[u];
+  const int W = a.part[u + 1] - fs + 1;
+  {
+    // chunk c (entries 4c..4c+3) belongs to lane c / (NPT/4); the arrays are padded
+    // so the rounded-up last chunk stays in bounds
+    const uint64_t polF = policy_evict_first();
+    const int n4 = (cnt + 3) >> 2;
+    const int32_t* gl = a.crd[1] + ustart64;
+    for (int c = lane; c < n4; c += 32) {
+      const int t = c / (NPT / 4);
+      reinterpret_cast<int4*>(s_lc)[c + t] = ld_stream_i4(gl + 4 * c, polF);
+      if constexpr (VB == 4)
+        reinterpret_cast<float4*>(s_val)[c + t] = ld_stream_f4(static_cast<const float*>(a.vals) + ustart64 + 4 * c, polF);
+      else
+        reinterpret_cast<uint2*>(s_val)[c + 2 * t] = ld_stream_u2(static_cast<const uint16_t*>(a.vals) + ustart64 + 4 * c, polF);
+    }
+    const int32_t* gpos = a.pos[1] + fs;
+    for (int x = lane; x <= W; x += 32) s_pos[x] = gpos[x];
+  }
+  __syncwarp();
 
-  const uint64_t polF = policy_evict_first();
-  TSumm X;
-  X.h = kEmpty; X.t = kNone; X.ha = 0.f; X.ta = 0.f;
-  const int64_t s = bstart + (int64_t)threadIdx.x * a.NPT;
-  if (s < bend) {
-    const int64_t e = min(s + (int64_t)a.NPT, bend);
-    int xw = (int)search_le(s_pos, 0, W - 1, s);
-    int64_t fend = s_pos[xw + 1];
+  WK wk(a, 0);
+  Summ<1> X;
+  X.h = kEmpty;
+  X.t = kNone;
+  const int s = ustart + lane * NPT;
+  if (s < ustart + cnt) {
+    const int n = min(NPT, ustart + cnt - s);
+    const int32_t* lc = s_lc + lane * (NPT + 4);
+    const unsigned char* vt = s_val + lane * (NPT * VB + 16);
+    const float* xv_g = static_cast<const float*>(a.fac[0]);
+    float xv[NPT], v[NPT];
+#pragma unroll
+    for (int k = 0; k < NPT; k++) xv[k] = __ldg(xv_g + (k < n ? lc[k] : 0));
+    if constexpr (VB == 4) {
+#pragma unroll
+      for (int k = 0; k < NPT / 4; k++) {
+        const float4 f = reinterpret_cast<const float4*>(vt)[k];
+        v[4 * k] = f.x; v[4 * k + 1] = f.y; v[4 * k + 2] = f.z; v[4 * k + 3] = f.w;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < NPT / 8; k++) {
+        const uint4 w = reinterpret_cast<const uint4*>(vt)[k];
+        const float2 p0 = pair16<VK>(w.x), p1 = pair16<VK>(w.y), p2 = pair16<VK>(w.z), p3 = pair16<VK>(w.w);
+        v[8 * k] = p0.x; v[8 * k + 1] = p0.y; v[8 * k + 2] = p1.x; v[8 * k + 3] = p1.y;
+        v[8 * k + 4] = p2.x; v[8 * k + 5] = p2.y; v[8 * k + 6] = p3.x; v[8 * k + 7] = p3.y;
+      }
+#pragma unroll
+      for (int k = 0; k < NPT; k++) v[k] *= a.vscale;
+    }
+    // a nonzero ends at most one fiber (fibers are not empty): emit the fiber at
+    // its last nonzero, with a short body the compiler can predicate
+    int x = (int)search_le(s_pos, 0, W - 1, s);
+    int fend = s_pos[x + 1];
     float acc = 0.f;
-    bool flushed = false;
-    for (int64_t p = s; p < e; p += 4) {
-      const int4 l4 = ld_stream_i4(a.crd + p, polF);
-      float v[4];
-      if (a.vals_kind == kB16) {
-        uint2 w = ld_stream_u2(static_cast<const uint16_t*>(a.vals) + p, polF);
-        v[0] = bf16lo(w.x) * a.vscale; v[1] = bf16hi(w.x) * a.vscale;
-        v[2] = bf16lo(w.y) * a.vscale; v[3] = bf16hi(w.y) * a.vscale;
-      } else if (a.vals_kind == kH16) {
-        uint2 w = ld_stream_u2(static_cast<const uint16_t*>(a.vals) + p, polF);
-        v[0] = h16lo(w.x) * a.vscale; v[1] = h16hi(w.x) * a.vscale;
-        v[2] = h16lo(w.y) * a.vscale; v[3] = h16hi(w.y) * a.vscale;
-      } else {
-        float4 w = ld_stream_f4(static_cast<const float*>(a.vals) + p, polF);
-        v[0] = w.x; v[1] = w.y; v[2] = w.z; v[3] = w.w;
-      }
-      const float xv[4] = {__ldg(a.x + l4.x), __ldg(a.x + l4.y), __ldg(a.x + l4.z), __ldg(a.x + l4.w)};
+    bool flushed = false, open = false;
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const int64_t pp = p + u;
-        if (pp < e) {
-          while (pp >= fend) {
-            const int64_t f = fs + xw;
-            if (!flushed) { X.h = f; X.ha = acc; flushed = true; }
-            else a.y[f] = acc;
-            acc = 0.f;
-            xw++;
-            fend = s_pos[xw + 1];
+    for (int k = 0; k < NPT; k++) {
+      if (k < n) {
+        acc = fmaf(v[k], xv[k], acc);
+        open = true;
+        if (s + k + 1 == fend) {  // fiber fs + x ends here
+          const int f = fs + x;
+          if (flushed) {
+            a.out[f] = acc;
+          } else {
+            X.h = f;
+            X.ha[0] = acc;
           }
-          acc = fmaf(v[u], xv[u], acc);
+          flushed = true;
+          open = false;
+          acc = 0.f;
+          x++;
+          // past the window's last fiber (the tensor's last unit) there is no next end
+          fend = x < W ? s_pos[x + 1] : INT32_MAX;
         }
       }
     }
-    const int64_t f = fs + xw;
-    if (!flushed) { X.h = f; X.ha = acc; X.t = kNone; }
-    else { X.t = f; X.ta = acc; }
-  }
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    TSumm Y;
-    Y.h = __shfl_down_sync(0xffffffffu, X.h, d);
-    Y.t = __shfl_down_sync(0xffffffffu, X.t, d);
-    Y.ha = __shfl_down_sync(0xffffffffu, X.ha, d);
-    Y.ta = __shfl_down_sync(0xffffffffu, X.ta, d);
-    if ((lane & (2 * d - 1)) == 0 && lane + d < 32) ttv_combine(X, Y, a.y);
-  }
-  if (lane == 0) { s_wh[warp] = X.h; s_wt[warp] = X.t; s_wha[warp] = X.ha; s_wta[warp] = X.ta; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int w = 1; w < nw; w++) {
-      TSumm Y;
-      Y.h = s_wh[w]; Y.t = s_wt[w]; Y.ha = s_wha[w]; Y.ta = s_wta[w];
-      ttv_combine(X, Y, a.y);
-    }
-    for (int slot = 0; slot < 2; slot++) {
-      const int64_t f = slot == 0 ? X.h : X.t;
-      int64_t last = -1, b0 = 0, b1 = 0;
-      if (f >= 0) {
-        b0 = (int64_t)a.pos[f] / P;
-        b1 = ((int64_t)a.pos[f + 1] - 1) / P;
-        const float v = slot == 0 ? X.ha : X.ta;
-        if (b0 == b1) a.y[f] = v;
-        else {
-          a.carry[2 * (size_t)b + slot] = v;
-          __threadfence();
-          const int t = atomicAdd(a.tickets + b0, 1);
-          if (t == (int)(b1 - b0)) { a.tickets[b0] = 0; __threadfence(); last = f; }
-        }
+    if (open) {  // the lane's last fiber continues past it
+      if (!flushed) {
+        X.h = fs + x;
+        X.t = kNone;
+        X.ha[0] = acc;
+      } else {
+        X.t = fs + x;
+        X.ta[0] = acc;
       }
-      s_ctl[slot] = last; s_ctl[2 + slot] = b0; s_ctl[4 + slot] = b1;
-    }
+    }  // else: X.h is the first fiber and nothing is left open (X.t stays kNone)
   }
-  __syncthreads();
-  for (int slot = 0; slot < 2; slot++) {
-    const int64_t f = s_ctl[slot];
-    if (f < 0) continue;
-    const int64_t b0 = s_ctl[2 + slot], b1 = s_ctl[4 + slot];
-    double acc = 0.0;
-    for (int64_t bb = b0 + threadIdx.x; bb <= b1; bb += tb) {
-      const int sb = (a.part[bb] == f) ? 0 : 1;
-      acc += (double)__ldcg(a.carry + 2 * bb + sb);
-    }
-    s_dbl[threadIdx.x] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double tot = 0.0;
-      for (int k = 0; k < tb; k++) tot += s_dbl[k];
-      a.y[f] = (float)tot;
-    }
-    __syncthreads();
-  }
+  warp_tree(wk, X);
+  if (lane == 0) settle_unit(a, wk, X, (int64_t)fs, (int64_t)fs, (int64_t)s_pos[0], ustart64, a.part[u + 1], u, 0);
 }
-
-__global__ void ttv_partition_kernel(const __grid_constant__ TtvArgs a) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b > a.nblocks) return;
-  const int64_t s = (b < a.nblocks) ? (int64_t)b * a.P : a.nnz - 1;
-  const_cast<int32_t*>(a.part)[b] = (int32_t)search_le(a.pos, 0, a.nfib - 1, s);
-}
-
 #endif  // TT_ARGS_ONLY
 }  // namespace tt

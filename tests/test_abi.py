@@ -70,8 +70,11 @@ def test_variant_table():
             for prec in ("fp32", "bf16", "bf16f"):
                 v = tt.default_variant(order, rank, prec)
                 assert v >= 0 and tt.variant_valid(v, order, rank, prec)
+    # the fixed heuristic: lean family, 16 bytes of a factor row per lane
     info = tt.variant_info(tt.default_variant(3, 32, "fp32"))
-    assert info["threads"] in (256, 512) and info["cols_per_lane"] == 4 and info["staged"] == 1
+    assert info["threads"] == 256 and info["cols_per_lane"] == 4 and info["staged"] == 0
+    assert info["name"] == "lean_b2_g64_c4"
+    assert tt.variant_info(tt.default_variant(3, 32, "fp16"))["name"] == "lean_b2_g32_c8"
     assert tt.variant_info(3)["staged"] == 0 and tt.variant_info(43)["name"].startswith("stage")
 
 
