@@ -100,6 +100,32 @@ __device__ __forceinline__ uint32_t ld_gather_2(const void* p, uint64_t pol) {
   return (uint32_t)r;
 }
 
+// Same gathers without allocating in L1 (rows gathered once per nonzero rarely hit L1).
+__device__ __forceinline__ uint4 ld_gather_16_na(const void* p, uint64_t pol) {
+  uint4 r;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "l"(p), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ uint2 ld_gather_8_na(const void* p, uint64_t pol) {
+  uint2 r;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0,%1}, [%2], %3;"
+               : "=r"(r.x), "=r"(r.y)
+               : "l"(p), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ uint32_t ld_gather_4_na(const void* p, uint64_t pol) {
+  uint32_t r;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ uint32_t ld_gather_2_na(const void* p, uint64_t pol) {
+  unsigned short r;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(r) : "l"(p), "l"(pol));
+  return (uint32_t)r;
+}
+
 // ---------------------------------------------------------------------------
 // Asynchronous global -> shared copies (cp.async, 16 bytes, L2 only).  Nothing is
 // held in registers while a copy is in flight, so a block can have thousands of

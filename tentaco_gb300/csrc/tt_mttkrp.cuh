@@ -392,18 +392,18 @@ struct Walk {
   // issued now, the conversion happens when the words are used.
   __device__ __forceinline__ static void piece_load(const unsigned char* p, uint64_t pol, uint32_t (&w)[NWD]) {
     if constexpr (LB == 32) {
-      const uint4 x = ld_gather_16(p, pol), y = ld_gather_16(p + 16, pol);
+      const uint4 x = ld_gather_16_na(p, pol), y = ld_gather_16_na(p + 16, pol);
       w[0] = x.x; w[1] = x.y; w[2] = x.z; w[3] = x.w; w[4] = y.x; w[5] = y.y; w[6] = y.z; w[7] = y.w;
     } else if constexpr (LB == 16) {
-      const uint4 x = ld_gather_16(p, pol);
+      const uint4 x = ld_gather_16_na(p, pol);
       w[0] = x.x; w[1] = x.y; w[2] = x.z; w[3] = x.w;
     } else if constexpr (LB == 8) {
-      const uint2 x = ld_gather_8(p, pol);
+      const uint2 x = ld_gather_8_na(p, pol);
       w[0] = x.x; w[1] = x.y;
     } else if constexpr (LB == 4) {
-      w[0] = ld_gather_4(p, pol);
+      w[0] = ld_gather_4_na(p, pol);
     } else {
-      w[0] = ld_gather_2(p, pol);
+      w[0] = ld_gather_2_na(p, pol);
     }
   }
   __device__ __forceinline__ static void piece_cvt(const uint32_t (&w)[NWD], float (&g)[CPT]) {
