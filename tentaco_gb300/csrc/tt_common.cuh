@@ -127,6 +127,54 @@ __device__ __forceinline__ uint32_t ld_gather_2_na(const void* p, uint64_t pol) 
 }
 
 // ---------------------------------------------------------------------------
+// mbarrier and TMA (cp.async.bulk.tensor) helpers.  Addresses are 32-bit shared
+// addresses; the tensor map lives in kernel parameter space (__grid_constant__).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+// Make barrier initialisation visible to the async proxy (the TMA unit).
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// Order this thread's earlier shared-memory accesses before later async-proxy writes.
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// One bounded probe of the barrier's phase with the given parity (true: completed).
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Nanoseconds of the GPU's global timer (bounds every wait on a barrier).
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Wait for the barrier phase with the given parity, at most limit_ns; true: completed.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, uint64_t limit_ns) {
+  const uint64_t t0 = global_ns();
+  while (!mbar_try_wait(bar, parity))
+    if (global_ns() - t0 > limit_ns) return false;
+  return true;
+}
+// Four rows (y0..y3) of a 2-D tensor map, columns from x, into shared memory at dst
+// (contiguous, 4 x box-width elements), completing `bytes` on the barrier.
+__device__ __forceinline__ void tma_gather4(uint32_t dst, const void* tmap, int x, int y0, int y1, int y2, int y3,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cta.global.tile::gather4.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+      ::"r"(dst), "l"(tmap), "r"(x), "r"(y0), "r"(y1), "r"(y2), "r"(y3), "r"(bar)
+      : "memory");
+}
+
+// ---------------------------------------------------------------------------
 // Asynchronous global -> shared copies (cp.async, 16 bytes, L2 only).  Nothing is
 // held in registers while a copy is in flight, so a block can have thousands of
 // row gathers outstanding.  src_bytes < 16 reads only that many bytes and

@@ -33,11 +33,13 @@
 // the next four nonzeros are issued before the current four are consumed, and
 // the next fiber's factor row is requested when the current fiber starts.
 #pragma once
+#include <cuda.h>  // CUtensorMap (the TMA walk's descriptor of the leaf factor)
 #include "tt_common.cuh"
 
 namespace tt {
 
-struct WalkArgs {
+struct alignas(64) WalkArgs {
+  CUtensorMap tmap;       // TMA walk: 2-D map of the leaf factor (RP columns x rows, box RP x 1)
   const int32_t* pos[4];  // pos[l], l = 1..order-1 (pos[1] indexed by root position)
   const int32_t* crd[4];  // crd[l], l = 1..order-1; crd[0] = root ids (nullptr: dense root)
   const void* vals;       // FP32 or BF16, padded
@@ -76,37 +78,11 @@ struct Summ {
   float ha[CPT], ta[CPT];
 };
 
-// Bytes of dynamic shared memory a launch needs.
-constexpr int kRingDepth = 8;  // nonzeros of lookahead in the ring kernels
-
-__device__ __forceinline__ void cp_async8(void* smem_dst, const void* src) {
-  const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async4(void* smem_dst, const void* src) {
-  const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-// Same copies addressed by a 32-bit shared-memory address.
-template <int BYTES>
-__device__ __forceinline__ void cp_async_sa(uint32_t d, const void* src) {
-  if constexpr (BYTES == 32) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d + 16), "l"(static_cast<const char*>(src) + 16) : "memory");
-  } else if constexpr (BYTES == 16) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
-  } else {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(d), "l"(src), "n"(BYTES) : "memory");
-  }
-}
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
 // Work units per segment of the two-level cross-unit row merge.
 constexpr int kSeg = 32;
 __host__ __device__ inline int num_segments(int units) { return (units + kSeg - 1) / kSeg; }
 
+// Bytes of dynamic shared memory a launch needs.
 __host__ __device__ inline size_t walk_tile_bytes(int P, int vbytes) {
   return (size_t)P * 4 + (((size_t)P * vbytes + 15) & ~(size_t)15);  // crd + vals tile
 }
@@ -129,6 +105,17 @@ __host__ __device__ inline size_t lean_warp_bytes(int G, int tw, int vbytes) {
   size_t b = (size_t)tw * (G + 4) * 4 + (size_t)tw * ((size_t)G * vbytes + 16);
   b += (pu + 2) * 4 * 2;
   return (b + 15) & ~(size_t)15;
+}
+
+// TMA walk, shared memory of one warp: a ring of ns stages of kTmaRows factor rows
+// (rb bytes each), ns mbarriers, then the lean layout; rounded to 128 bytes so every
+// warp's ring starts 128-byte aligned.
+constexpr int kTmaRows = 32;  // factor rows per stage: 8 gather4 copies
+__host__ __device__ inline size_t tma_warp_bytes(int G, int tw, int vbytes, int rb, int ns) {
+  size_t b = (size_t)ns * kTmaRows * rb + (size_t)ns * 8;
+  b = (b + 15) & ~(size_t)15;
+  b += lean_warp_bytes(G, tw, vbytes);
+  return (b + 127) & ~(size_t)127;
 }
 
 // Staged kernels: the tile, the gathered factor rows (one per nonzero, one per
@@ -421,16 +408,16 @@ struct Walk {
       }
     }
   }
-  // U consecutive stored values of a team's tile (16-byte aligned run).
+  // U consecutive stored values of a team's run (runs of 4 or more start 16-byte aligned).
   template <int U>
   __device__ __forceinline__ static void vals_load(const unsigned char* vt, float (&v)[U]) {
-    if constexpr (VK == kF32) {
+    if constexpr (VK == kF32 && U % 4 == 0) {
 #pragma unroll
       for (int k = 0; k < U / 4; k++) {
         const float4 f = reinterpret_cast<const float4*>(vt)[k];
         v[4 * k] = f.x; v[4 * k + 1] = f.y; v[4 * k + 2] = f.z; v[4 * k + 3] = f.w;
       }
-    } else if constexpr (U % 8 == 0) {
+    } else if constexpr (VK != kF32 && U % 8 == 0) {
 #pragma unroll
       for (int k = 0; k < U / 8; k++) {
         const uint4 w = reinterpret_cast<const uint4*>(vt)[k];
@@ -438,11 +425,13 @@ struct Walk {
         v[8 * k] = a.x; v[8 * k + 1] = a.y; v[8 * k + 2] = b.x; v[8 * k + 3] = b.y;
         v[8 * k + 4] = c.x; v[8 * k + 5] = c.y; v[8 * k + 6] = d.x; v[8 * k + 7] = d.y;
       }
-    } else {
-      static_assert(U == 4, "batches of 4, 8 or 16 nonzeros");
+    } else if constexpr (VK != kF32 && U == 4) {
       const uint2 w = *reinterpret_cast<const uint2*>(vt);
       const float2 a = pair16<VK>(w.x), b = pair16<VK>(w.y);
       v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+    } else {  // 1 or 2 values
+#pragma unroll
+      for (int u = 0; u < U; u++) v[u] = val_one(vt, u);
     }
   }
   __device__ __forceinline__ static float val_one(const unsigned char* vt, int j) {
@@ -591,179 +580,183 @@ struct Walk {
     }
   }
 
-  // Serial walk like walk(), but every factor row piece the lane needs is copied
-  // with cp.async into this lane's own shared-memory slots, DP nonzeros ahead of
-  // use: the nonzero-level row of each nonzero (ring of DP slots) and, in the
-  // same copy group as a fiber's first nonzero, the window-level row of that
-  // fiber (ring of DP+1 slots, by fiber ordinal).  Each lane copies exactly what
-  // it reads, so completion is its own cp.async.wait_group: no barrier, nothing
-  // held in registers while in flight, and short fibers do not stall on their
-  // factor row.  A fiber's slot is refilled only by the (DP+1)-th later fiber,
-  // whose copy is issued after this fiber's fold in program order.
-  // Positions are 32-bit (nnz < 2^31); the tile is read through the per-team
-  // skew sk(j) = j + 4*(j >> lgG), which puts the teams of a warp in different
-  // shared-memory banks.  Four nonzeros inside one fiber take a fast path.
-  //   ring / wring: this lane's first nonzero / fiber slot; slots `stride` apart.
-  template <int DP>
-  __device__ __forceinline__ void walk_ring(int s, int e, int bstart, const int32_t* s_lc,
-                                            const unsigned char* s_val, int lgG, const int32_t* s_pos,
-                                            const int32_t* s_fcrd, int W, int fs, const int32_t* pb,
-                                            const int32_t* pn, unsigned char* ring, unsigned char* wring,
-                                            int stride, Summ<CPT>& X) const {
-    static_assert((DP & (DP - 1)) == 0 && DP >= 4, "ring depth must be a power of two >= 4");
-    constexpr int WS = DP + 1;  // fiber slots
-    constexpr int RB = RP * (LB / CPT);
-    const uint64_t polL = policy_evict_last();
-    const int32_t* pos1 = a.pos[1];
-    const unsigned char* fzq = static_cast<const unsigned char*>(a.fac[ORDER - 2]) + q * LB;
-    const unsigned char* fwq = static_cast<const unsigned char*>(a.fac[ORDER == 3 ? 0 : 1]) + q * LB;
+  // Walk like walk_lean, but the nonzero-level factor rows arrive by TMA: for
+  // every stage k of the warp (U nonzeros of each of its TW teams, kTmaRows rows),
+  // lanes 0..7 issue one tile::gather4 copy each into ring slot k % NS, completing
+  // on that slot's mbarrier; NS stages are in flight.  All lanes of the warp call
+  // this (teams without nonzeros pass n = 0) because the stage loop is warp-wide.
+  //   s_lcw: the warp's coordinate runs (team t at t * (G + 4)); cnt: the warp
+  //   tile's nonzeros; nst: stages (ceil(min(G, cnt) / U)); ring/bar_sa: the warp's
+  //   ring and barriers.  A barrier that does not complete within a bounded number
+  //   of probes sets the error word (301) and the warp stops walking.
+  template <int U, int NS>
+  __device__ __forceinline__ void walk_tma(int s, int n, int team, int nst, const int32_t* s_lcw, int G, int cnt,
+                                           const unsigned char* vt, const int32_t* s_pos,
+                                           const int32_t* s_fcrd, int W, int fs, const int32_t* pb,
+                                           const int32_t* pn, const unsigned char* ring, uint32_t bar_sa,
+                                           Summ<CPT>& X) const {
+    constexpr int TW = 32 / LPR;
+    constexpr int SR = kTmaRows;
+    static_assert(U * TW == SR, "a stage holds U nonzeros of every team");
+    const int lane = threadIdx.x & 31;
     const uint32_t ring_sa = (uint32_t)__cvta_generic_to_shared(ring);
-    const uint32_t wring_sa = (uint32_t)__cvta_generic_to_shared(wring);
-    auto sk = [&](int j) { return j + ((j >> lgG) << 2); };
-    // lookahead state: fiber of the last issued nonzero and its ordinal
-    int xl = (int)search_le(s_pos, 0, W - 1, s);
-    int lend = s_pos[xl + 1];
-    int ordl = 0;
-#ifdef TT_CHECKED
-    // checked build: every copy's shared destination and factor row are bounds-checked;
-    // a violation is recorded in the error word and the copy is skipped
-    extern __shared__ __align__(16) unsigned char smem_chk[];
-    const uint32_t smem_sa = (uint32_t)__cvta_generic_to_shared(smem_chk);
-    auto ok = [&](uint32_t d, int row, int m, int code) {
-      const bool good = d >= smem_sa && d + LB <= smem_sa + (uint32_t)a.smem_bytes && row >= 0 && row < a.fac_rows[m] &&
-                        (d % (LB < 16 ? LB : 16)) == 0;
-      if (!good) atomicCAS(a.err, 0, code);
-      return good;
-    };
-#endif
-    auto issue_fiber = [&](int xx, int ord) {
-      const uint32_t d = wring_sa + (uint32_t)((ord % WS) * stride);
-      const int row = s_fcrd[xx];
-#ifdef TT_CHECKED
-      if (xx < 0 || xx >= W) { atomicCAS(a.err, 0, 101); return; }
-      if (!ok(d, row, ORDER == 3 ? 0 : 1, 102)) return;
-#endif
-      cp_async_sa<LB>(d, fwq + (size_t)(uint32_t)row * RB);
-    };
-    auto issue = [&](int p, int slot) {
-      while (p >= lend) {  // p opens a new window fiber: copy its row in this group
-        xl++;
-        lend = s_pos[xl + 1];
-        issue_fiber(xl, ++ordl);
-      }
-      const uint32_t d = ring_sa + (uint32_t)(slot * stride);
-      const int row = s_lc[sk(p - bstart)];
-#ifdef TT_CHECKED
-      if (p - bstart < 0 || p - bstart >= a.P) { atomicCAS(a.err, 0, 103); return; }
-      if (!ok(d, row, ORDER - 2, 104)) return;
-#endif
-      cp_async_sa<LB>(d, fzq + (size_t)(uint32_t)row * RB);
-    };
-    auto val = [&](int p) -> float {
-      const int j = sk(p - bstart);
-      if constexpr (VK == kF32) return reinterpret_cast<const float*>(s_val)[j];
-      else if constexpr (VK == kB16) return bf16lo(reinterpret_cast<const uint16_t*>(s_val)[j]);
-      else return h16lo(reinterpret_cast<const uint16_t*>(s_val)[j]);
-    };
-    auto slot_row = [&](unsigned char* base, int slot, float (&v)[CPT]) {
-      smem_row<FK, CPT>(base + slot * stride - q * LB, q, v);
-    };
-    int x = xl, ord = 0;
-    int fend = lend;
-    int f1 = 0, kend = 0;
-    int ip;
+    const uint64_t pol = a.gpol == 1 ? policy_evict_normal() : policy_evict_last();
+    const int32_t* pos1 = a.pos[1];
+    const unsigned char* fw = static_cast<const unsigned char*>(a.fac[ORDER == 3 ? 0 : 1]) + q * LB;
+    const bool active = n > 0;
+    int x = 0, fend = 0, f1 = 0, kend = 0, ip = 0, rend = 0;
     float crow[CPT];
-    if constexpr (ORDER == 3) {
-      ip = (int)search_le(pos1, pb[0], pn[0], fs + x);
-    } else {
-      f1 = (int)search_le(a.pos[2], pb[1], pn[1], fs + x);
-      kend = a.pos[2][f1 + 1];
-      ip = (int)search_le(pos1, pb[0], pn[0], f1);
-      frow(0, a.crd[1][f1], polL, crow);
-    }
-    int rend = pos1[ip + 1];
+    uint32_t wc[NWD], wn[NWD];
     float f3[CPT], f2[CPT], ra[CPT];
 #pragma unroll
-    for (int c = 0; c < CPT; c++) { f3[c] = 0.f; f2[c] = 0.f; ra[c] = 0.f; }
+    for (int c = 0; c < CPT; c++) { f3[c] = 0.f; f2[c] = 0.f; ra[c] = 0.f; crow[c] = 0.f; }
+#pragma unroll
+    for (int k = 0; k < NWD; k++) { wc[k] = 0u; wn[k] = 0u; }
     bool flushed = false;
-    const int n = e - s;
-    issue_fiber(x, 0);  // the fiber holding the first nonzero, in the first group
-#pragma unroll
-    for (int d = 0; d < DP; d++) {
-      if (d < n) issue(s + d, d);
-      cp_async_commit();
-    }
-    int i = 0;
-    while (i < n) {
-      const int p = s + i;
-      if (i + 4 <= n && p + 4 <= fend) {
-        // fast path: four nonzeros of the current fiber
-        cp_async_wait<DP - 4>();
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-          float g[CPT];
-          slot_row(ring, (i + u) & (DP - 1), g);
-          const float v = val(p + u);
-#pragma unroll
-          for (int c = 0; c < CPT; c++) f3[c] = fmaf(v, g[c], f3[c]);
-        }
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-          if (i + u + DP < n) issue(p + u + DP, (i + u) & (DP - 1));
-          cp_async_commit();
-        }
-        i += 4;
-        continue;
+    if (active) {
+      x = (int)search_le(s_pos, 0, W - 1, s);
+      fend = s_pos[x + 1];
+      if constexpr (ORDER == 3) {
+        ip = (int)search_le(pos1, pb[0], pn[0], fs + x);
+      } else {
+        f1 = (int)search_le(a.pos[2], pb[1], pn[1], fs + x);
+        kend = a.pos[2][f1 + 1];
+        ip = (int)search_le(pos1, pb[0], pn[0], f1);
+        frow(0, a.crd[1][f1], pol, crow);
       }
-      const int slot = i & (DP - 1);
-      cp_async_wait<DP - 1>();
-      float g[CPT];
-      slot_row(ring, slot, g);
-      const float v = val(p);
-      while (p >= fend) {
-        float cur[CPT];
-        slot_row(wring, ord % WS, cur);
-        if constexpr (ORDER == 3) {
-#pragma unroll
-          for (int c = 0; c < CPT; c++) { ra[c] = fmaf(f3[c], cur[c], ra[c]); f3[c] = 0.f; }
-        } else {
-#pragma unroll
-          for (int c = 0; c < CPT; c++) { f2[c] = fmaf(f3[c], cur[c], f2[c]); f3[c] = 0.f; }
-        }
-        x++;
-        ord++;
-        fend = s_pos[x + 1];
-        const int fg = fs + x;
-        if constexpr (ORDER == 4) {
-          while (fg >= kend) {
-#pragma unroll
-            for (int c = 0; c < CPT; c++) { ra[c] = fmaf(f2[c], crow[c], ra[c]); f2[c] = 0.f; }
-            f1++;
-            kend = a.pos[2][f1 + 1];
-            while (f1 >= rend) { flush(ip, ra, flushed, X); ip++; rend = pos1[ip + 1]; }
-            frow(0, a.crd[1][f1], polL, crow);
-          }
-        } else {
-          while (fg >= rend) { flush(ip, ra, flushed, X); ip++; rend = pos1[ip + 1]; }
-        }
-      }
-#pragma unroll
-      for (int c = 0; c < CPT; c++) f3[c] = fmaf(v, g[c], f3[c]);
-      // the slot's value is consumed: refill it DP nonzeros ahead
-      if (i + DP < n) issue(p + DP, slot);
-      cp_async_commit();
-      i++;
+      rend = pos1[ip + 1];
+      piece_load(fw + (size_t)(uint32_t)s_fcrd[x] * FRB, pol, wc);
+      if (x + 1 < W) piece_load(fw + (size_t)(uint32_t)s_fcrd[x + 1] * FRB, pol, wn);
     }
-    cp_async_wait<0>();
-    {
-      float cur[CPT];
-      slot_row(wring, ord % WS, cur);
+    auto fold = [&]() {
+      float cw[CPT];
+      piece_cvt(wc, cw);
       if constexpr (ORDER == 3) {
 #pragma unroll
-        for (int c = 0; c < CPT; c++) ra[c] = fmaf(f3[c], cur[c], ra[c]);
+        for (int c = 0; c < CPT; c++) { ra[c] = fmaf(f3[c], cw[c], ra[c]); f3[c] = 0.f; }
       } else {
 #pragma unroll
-        for (int c = 0; c < CPT; c++) { f2[c] = fmaf(f3[c], cur[c], f2[c]); ra[c] = fmaf(f2[c], crow[c], ra[c]); }
+        for (int c = 0; c < CPT; c++) { f2[c] = fmaf(f3[c], cw[c], f2[c]); f3[c] = 0.f; }
+      }
+      x++;
+      fend = s_pos[x + 1];
+#pragma unroll
+      for (int k = 0; k < NWD; k++) wc[k] = wn[k];
+      if (x + 1 < W) piece_load(fw + (size_t)(uint32_t)s_fcrd[x + 1] * FRB, pol, wn);
+      const int fg = fs + x;
+      if constexpr (ORDER == 4) {
+        while (fg >= kend) {
+#pragma unroll
+          for (int c = 0; c < CPT; c++) { ra[c] = fmaf(f2[c], crow[c], ra[c]); f2[c] = 0.f; }
+          f1++;
+          kend = a.pos[2][f1 + 1];
+          while (f1 >= rend) { flush(ip, ra, flushed, X); ip++; rend = pos1[ip + 1]; }
+          frow(0, a.crd[1][f1], pol, crow);
+        }
+      } else {
+        while (fg >= rend) { flush(ip, ra, flushed, X); ip++; rend = pos1[ip + 1]; }
+      }
+    };
+    // producer: stage k into slot k % NS (lane 0 arms the barrier first)
+    auto issue = [&](int k) {
+      const int slot = k % NS;
+      const uint32_t bar = bar_sa + (uint32_t)slot * 8u;
+      if (lane == 0) mbar_arrive_expect_tx(bar, (uint32_t)(SR * FRB));
+      __syncwarp();
+      if (lane < SR / 4) {
+        int r[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const int j = 4 * lane + i;
+          const int tt = j % TW, u = j / TW;
+          const int p = k * U + u;
+          const int nt = min(max(cnt - tt * G, 0), G);
+          r[i] = p < nt ? s_lcw[tt * (G + 4) + p] : 0;
+        }
+        tma_gather4(ring_sa + (uint32_t)(slot * SR * FRB + 4 * lane * FRB), &a.tmap, 0, r[0], r[1], r[2], r[3], bar);
+      }
+    };
+    // the team's piece of row slot u of a stage
+    auto piece = [&](int slot, int u, uint32_t (&w)[NWD]) {
+      const unsigned char* p = ring + (size_t)slot * SR * FRB + (size_t)(u * TW + team) * FRB + q * LB;
+      if constexpr (LB >= 16) {
+#pragma unroll
+        for (int k = 0; k < LB / 16; k++) {
+          const uint4 v4 = reinterpret_cast<const uint4*>(p)[k];
+          w[4 * k] = v4.x; w[4 * k + 1] = v4.y; w[4 * k + 2] = v4.z; w[4 * k + 3] = v4.w;
+        }
+      } else if constexpr (LB == 8) {
+        const uint2 v2 = *reinterpret_cast<const uint2*>(p);
+        w[0] = v2.x; w[1] = v2.y;
+      } else if constexpr (LB == 4) {
+        w[0] = *reinterpret_cast<const uint32_t*>(p);
+      } else {
+        w[0] = *reinterpret_cast<const uint16_t*>(p);
+      }
+    };
+    auto consume = [&](int slot, int j) {
+      float v[U];
+      vals_load<U>(vt + (size_t)j * VB, v);
+      if (j + U <= n && s + j + U <= fend) {
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          uint32_t w[NWD];
+          piece(slot, u, w);
+          float d[CPT];
+          piece_cvt(w, d);
+#pragma unroll
+          for (int c = 0; c < CPT; c++) f3[c] = fmaf(v[u], d[c], f3[c]);
+        }
+        return;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        if (j + u < n) {
+          while (s + j + u >= fend) fold();
+          uint32_t w[NWD];
+          piece(slot, u, w);
+          float d[CPT];
+          piece_cvt(w, d);
+#pragma unroll
+          for (int c = 0; c < CPT; c++) f3[c] = fmaf(v[u], d[c], f3[c]);
+        }
+      }
+    };
+    constexpr uint64_t kWaitNs = 5000000;  // a stage normally lands within microseconds
+    bool ok = true;
+    for (int k = 0; k < NS && k < nst; k++) issue(k);
+    int k = 0;
+    for (; k < nst && ok; k++) {
+      const int slot = k % NS;
+      const uint32_t bar = bar_sa + (uint32_t)slot * 8u;
+      const uint32_t parity = (uint32_t)((k / NS) & 1);
+      const bool landed = mbar_wait_bounded(bar, parity, kWaitNs);
+      if (__any_sync(0xffffffffu, !landed)) {
+        if (lane == 0) atomicCAS(a.err, 0, 301);
+        ok = false;
+        break;
+      }
+      if (active && k * U < n) consume(slot, k * U);
+      fence_proxy_async_smem();  // this slot's reads before the TMA refills it
+      __syncwarp();
+      if (k + NS < nst) issue(k + NS);
+    }
+    if (!ok) {
+      // wait (bounded) for every copy still in flight before the warp leaves
+      for (int kk = k; kk < nst && kk < k + NS; kk++)
+        mbar_wait_bounded(bar_sa + (uint32_t)(kk % NS) * 8u, (uint32_t)((kk / NS) & 1), kWaitNs);
+      return;
+    }
+    if (!active) return;
+    {
+      float cw[CPT];
+      piece_cvt(wc, cw);
+      if constexpr (ORDER == 3) {
+#pragma unroll
+        for (int c = 0; c < CPT; c++) ra[c] = fmaf(f3[c], cw[c], ra[c]);
+      } else {
+#pragma unroll
+        for (int c = 0; c < CPT; c++) { f2[c] = fmaf(f3[c], cw[c], f2[c]); ra[c] = fmaf(f2[c], crow[c], ra[c]); }
       }
     }
     if (!flushed) {
@@ -1167,7 +1160,7 @@ __global__ void __launch_bounds__(256) seg_chain_kernel(const __grid_constant__ 
 // EXACT = true: the nonzero-level crd/vals arrays are read only up to nnz (the
 // caller's own unpadded arrays); false: the plan's padded copies are read in
 // whole 128-bit words.
-template <int ORDER, int PREC, int CPT, int LPR, bool EXACT = false, bool RING = false>
+template <int ORDER, int PREC, int CPT, int LPR, bool EXACT = false>
 __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant__ WalkArgs a) {
   using WK = Walk<ORDER, PREC, CPT, LPR>;
   constexpr int RP = WK::RP;
@@ -1180,8 +1173,7 @@ __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant_
   const int nw = tb / 32;
   const int b = blockIdx.x;
   const int P = a.P;
-  // ring kernels skew the tile by 4 entries per team (bank-conflict-free team reads)
-  const int TE = RING ? P + 4 * (tb / LPR) : P;
+  const int TE = P;
   int32_t* s_lc = reinterpret_cast<int32_t*>(smem);
   unsigned char* s_val = smem + (size_t)TE * 4;
   int32_t* s_pos = reinterpret_cast<int32_t*>(smem + walk_tile_bytes(TE, VB));
@@ -1221,8 +1213,7 @@ __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant_
         }
       }
     } else {
-    // entry j lands at j + 4*(j >> lgG) in ring kernels (skew), at j otherwise
-    auto dst4 = [&](int i) { return RING ? i + ((4 * i) >> a.lgG) : i; };
+    auto dst4 = [&](int i) { return i; };
     for (int i = threadIdx.x; i < n4; i += tb)
       reinterpret_cast<int4*>(s_lc)[dst4(i)] = ld_stream_i4(gl + 4 * i, polF);
     if constexpr (VB == 4) {
@@ -1255,17 +1246,7 @@ __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant_
   X.t = kNone;
   const int64_t s = bstart + (int64_t)team * a.G;
   if (s < bend) {
-    if constexpr (RING && WK::LB >= 4) {  // (2-byte lane pieces: no ring variant is valid)
-      // rings: kRingDepth nonzero slots then kRingDepth+1 fiber slots, each of
-      // tb * LB bytes, slot-major so a warp's copies and reads are contiguous
-      const size_t roff = (walk_smem_bytes(P, tb, RP, VB, TE) + 15) & ~(size_t)15;
-      unsigned char* ring = smem + roff + (size_t)threadIdx.x * WK::LB;
-      unsigned char* wring = ring + (size_t)kRingDepth * tb * WK::LB;
-      wk.template walk_ring<kRingDepth>((int)s, (int)min(s + (int64_t)a.G, bend), (int)bstart, s_lc, s_val, a.lgG,
-                                        s_pos, s_fcrd, W, (int)fs, pb, pn, ring, wring, tb * WK::LB, X);
-    } else {
-      wk.walk(s, min(s + (int64_t)a.G, bend), bstart, s_lc, s_val, s_pos, s_fcrd, W, fs, pb, pn, X);
-    }
+    wk.walk(s, min(s + (int64_t)a.G, bend), bstart, s_lc, s_val, s_pos, s_fcrd, W, fs, pb, pn, X);
   }
 
   block_merge<ORDER, PREC, CPT, LPR>(a, wk, X, s_wh, s_wt, s_wha, s_wta, head_ff, fs, s_pos[0], bstart, pn[0], blockIdx.x);
@@ -1342,6 +1323,76 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_lean_kernel(const __grid_con
   if (s < ustart + cnt)
     wk.template walk_lean<U>(s, min(G, ustart + cnt - s), s_lc + team * (G + 4), s_val + (size_t)team * (G * VB + 16),
                              s_pos, s_fcrd, W, fs, pb, pn, X);
+  warp_tree(wk, X);
+  if (lane < LPR) settle_unit(a, wk, X, head_ff, fs, s_pos[0], ustart64, pn[0], u, q);
+}
+
+// TMA kernel (family 2): the lean kernel's warp tiles, with the nonzero-level
+// factor rows fetched by TMA tile::gather4 into a per-warp ring (walk_tma).
+// NS: stages in flight per warp.
+template <int ORDER, int PREC, int CPT, int LPR, int NS>
+__global__ void __launch_bounds__(256, 1) mttkrp_tma_kernel(const __grid_constant__ WalkArgs a) {
+  using WK = Walk<ORDER, PREC, CPT, LPR>;
+  constexpr int VB = WK::VB;
+  constexpr int TW = 32 / LPR;
+  constexpr int U = kTmaRows / TW;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int u = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (u >= a.nblocks) return;  // whole warp
+  // after a recorded device error, later warps skip their tiles (the call fails)
+  if (*reinterpret_cast<volatile const int32_t*>(a.err) != 0) return;
+  const int G = a.G, PU = a.P;
+  unsigned char* ws = smem + (size_t)warp * tma_warp_bytes(G, TW, VB, WK::FRB, NS);
+  unsigned char* ring = ws;
+  const uint32_t bar_sa = (uint32_t)__cvta_generic_to_shared(ws + (size_t)NS * kTmaRows * WK::FRB);
+  unsigned char* lw = ws + ((((size_t)NS * kTmaRows * WK::FRB + (size_t)NS * 8) + 15) & ~(size_t)15);
+  int32_t* s_lc = reinterpret_cast<int32_t*>(lw);
+  unsigned char* s_val = lw + (size_t)TW * (G + 4) * 4;
+  int32_t* s_pos = reinterpret_cast<int32_t*>(s_val + (size_t)TW * (G * VB + 16));
+  int32_t* s_fcrd = s_pos + (PU + 2);
+
+  const int32_t* pb = a.part + (size_t)u * (ORDER - 1);
+  const int32_t* pn = pb + (ORDER - 1);
+  const int64_t ustart64 = (int64_t)u * PU;
+  const int ustart = (int)ustart64;
+  const int cnt = (int)min((int64_t)PU, a.nnz - ustart64);
+  const int fs = pb[ORDER - 2];
+  const int W = pn[ORDER - 2] - fs + 1;
+  if (lane == 0) {
+    for (int k = 0; k < NS; k++) mbar_init(bar_sa + 8u * k, 1);
+    fence_mbar_init();
+  }
+  {
+    const uint64_t polF = policy_evict_first();
+    const int n4 = (cnt + 3) >> 2;
+    const int32_t* gl = a.crd[ORDER - 1] + ustart64;
+    for (int c = lane; c < n4; c += 32) {
+      const int t = (4 * c) >> a.lgG;
+      reinterpret_cast<int4*>(s_lc)[c + t] = ld_stream_i4(gl + 4 * c, polF);
+      if constexpr (VB == 4)
+        reinterpret_cast<float4*>(s_val)[c + t] = ld_stream_f4(static_cast<const float*>(a.vals) + ustart64 + 4 * c, polF);
+      else
+        reinterpret_cast<uint2*>(s_val)[c + 2 * t] = ld_stream_u2(static_cast<const uint16_t*>(a.vals) + ustart64 + 4 * c, polF);
+    }
+    const int32_t* gpos = a.pos[ORDER - 1] + fs;
+    const int32_t* gcrd = a.crd[ORDER - 2] + fs;
+    for (int x = lane; x <= W; x += 32) s_pos[x] = gpos[x];
+    for (int x = lane; x < W; x += 32) s_fcrd[x] = gcrd[x];
+  }
+  __syncwarp();
+
+  const int team = lane / LPR, q = lane % LPR;
+  WK wk(a, q);
+  const int64_t head_ff = lane < LPR ? row_first_window_fiber<ORDER>(a, pb[0]) : 0;
+  Summ<CPT> X;
+  X.h = kEmpty;
+  X.t = kNone;
+  const int s = ustart + team * G;
+  const int n = s < ustart + cnt ? min(G, ustart + cnt - s) : 0;
+  const int nst = (min(G, cnt) + U - 1) / U;
+  wk.template walk_tma<U, NS>(s, n, team, nst, s_lc, G, cnt, s_val + (size_t)team * (G * VB + 16), s_pos, s_fcrd,
+                              W, fs, pb, pn, ring, bar_sa, X);
   warp_tree(wk, X);
   if (lane < LPR) settle_unit(a, wk, X, head_ff, fs, s_pos[0], ustart64, pn[0], u, q);
 }

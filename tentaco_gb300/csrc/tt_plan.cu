@@ -30,10 +30,10 @@ namespace tt {
 // nonzeros per team (5 values per family) x columns per lane {8,4,2,1}
 // ---------------------------------------------------------------------------
 static const int kTB[2] = {256, 512};
-static const int kGF[3][5] = {{16, 32, 64, 128, 256}, {4, 8, 16, 32, 64}, {4, 8, 16, 32, 64}};
+static const int kGF[3][5] = {{16, 32, 64, 128, 256}, {4, 8, 16, 32, 64}, {16, 32, 64, 128, 256}};
 static const int kCPT[4] = {8, 4, 2, 1};
 constexpr int kPerFamily = 2 * 5 * 4;
-constexpr int kNumVariants = 3 * kPerFamily;  // lean, staged, ring
+constexpr int kNumVariants = 3 * kPerFamily;  // lean, staged, TMA gather
 constexpr size_t kSmemLimit = (size_t)227 * 1024;
 
 VariantSpec variant_spec(int id) {
@@ -58,7 +58,13 @@ int variant_id(int tb, int G, int cpt, int staged) {
 
 // Kernel family a variant launches: the lean family's second thread value selects
 // its tighter register budget (family 3); both launch 256-thread blocks.
-int launch_family(const VariantSpec& v) { return v.staged == 0 && v.tb == 512 ? 3 : v.staged; }
+// The TMA family's second value selects 8 stages in flight per warp instead of 4 (family 5).
+int launch_family(const VariantSpec& v) {
+  if (v.staged == 0) return v.tb == 512 ? 3 : 0;
+  if (v.staged == 2) return v.tb == 512 ? 5 : 2;
+  return v.staged;
+}
+int tma_stages(const VariantSpec& v) { return v.tb == 512 ? 8 : 4; }
 
 // Resident 256-thread blocks a lean variant's registers are budgeted for.
 int lean_blocks(const VariantSpec& v) { return v.cpt >= 4 ? (v.tb == 512 ? 3 : 2) : (v.tb == 512 ? 4 : 3); }
@@ -66,7 +72,7 @@ int lean_blocks(const VariantSpec& v) { return v.cpt >= 4 ? (v.tb == 512 ? 3 : 2
 // Nonzeros of one work unit: a warp's tile for the lean family, a block's tile otherwise.
 int variant_unit(const VariantSpec& v, int rp) {
   const int lpr = rp / v.cpt;
-  return (v.staged == 0 ? 32 / lpr : v.tb / lpr) * v.G;
+  return (v.staged != 1 ? 32 / lpr : v.tb / lpr) * v.G;
 }
 
 int fac_bytes(int prec) { return fac_kind(prec) == kF32 ? 4 : 2; }
@@ -75,9 +81,8 @@ size_t variant_smem(const VariantSpec& v, int rp, int prec, int wcap) {
   const int lpr = rp / v.cpt;
   const int P = (v.tb / lpr) * v.G;
   if (v.staged == 0) return (size_t)(256 / 32) * lean_warp_bytes(v.G, 32 / lpr, val_bytes(prec));
-  if (v.staged == 2)  // walk + nonzero ring (kRingDepth slots) + fiber ring (kRingDepth+1 slots)
-    return ((walk_smem_bytes(P, v.tb, rp, val_bytes(prec), P + 4 * (v.tb / lpr)) + 15) & ~(size_t)15) +
-           (size_t)(2 * kRingDepth + 1) * v.tb * v.cpt * fac_bytes(prec);
+  if (v.staged == 2)  // TMA gather: 8 warps, each with its ring of row stages and its lean tile
+    return (size_t)(256 / 32) * tma_warp_bytes(v.G, 32 / lpr, val_bytes(prec), rp * fac_bytes(prec), tma_stages(v));
   return v.staged ? stage_smem_bytes(P, wcap, v.tb, rp, val_bytes(prec), fac_bytes(prec))
                   : walk_smem_bytes(P, v.tb, rp, val_bytes(prec));
 }
@@ -102,7 +107,9 @@ bool variant_valid(int id, int order, int rank, int prec) {
   // window; a plan checks its own tensor's largest window)
   if (variant_smem(v, rp, prec, 1) > kSmemLimit) return false;
   if (v.staged && (rp * fac_bytes(prec)) % 16) return false;
-  if (v.staged == 2 && v.cpt * fac_bytes(prec) < 4) return false;  // cp.async moves >= 4 bytes
+  // TMA gather: four rows per copy land on 128-byte boundaries (rows of 32-byte
+  // multiples), and a team's G nonzeros are whole stages of U = lanes-per-row rows
+  if (v.staged == 2 && ((rp * fac_bytes(prec)) % 32 != 0 || v.G % lpr != 0)) return false;
   return walk_launcher(order, prec, v.cpt, lpr, launch_family(v)) != nullptr;
 }
 
@@ -284,6 +291,45 @@ WalkArgs walk_args(const tt_plan* p, float* A, int q) {
   return a;
 }
 
+// The TMA walk's descriptor of the leaf factor: RP columns x dims[leaf] rows of the
+// stored type, one-row boxes (tile::gather4 fetches four rows of the box width).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = []() -> EncodeTiledFn {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    return reinterpret_cast<EncodeTiledFn>(f);
+  }();
+  return fn;
+}
+
+tt_status encode_leaf_tmap(const tt_plan* p, CUtensorMap* m) {
+  const int leaf = p->order - 1;
+  const void* base = p->fac[p->order - 2];
+  const int fb = fac_bytes(p->prec);
+  if (reinterpret_cast<uintptr_t>(base) % 16)
+    return set_error(TT_ERR_UNSUPPORTED, "TMA walk: the last factor is not 16-byte aligned");
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn) return set_error(TT_ERR_UNSUPPORTED, "TMA walk: cuTensorMapEncodeTiled is not available");
+  const cuuint64_t dims[2] = {(cuuint64_t)p->rp, (cuuint64_t)p->dims[leaf]};
+  const cuuint64_t strides[1] = {(cuuint64_t)p->rp * (cuuint64_t)fb};
+  const cuuint32_t box[2] = {(cuuint32_t)p->rp, 1u};
+  const cuuint32_t estr[2] = {1u, 1u};
+  const CUresult r = fn(m, fb == 2 ? CU_TENSOR_MAP_DATA_TYPE_UINT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                        const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(TT_ERR_UNSUPPORTED, "TMA walk: cuTensorMapEncodeTiled returned %d", (int)r);
+  return TT_OK;
+}
+
 tt_status run_mttkrp(tt_plan* p, float* A, cudaStream_t st) {
   const size_t outbytes = (size_t)p->dims[0] * (size_t)p->rank * sizeof(float);
   CK(cudaMemsetAsync(A, 0, outbytes, st));
@@ -298,6 +344,10 @@ tt_status run_mttkrp(tt_plan* p, float* A, cudaStream_t st) {
     WalkArgs a = walk_args(p, A, q);
     if (a.nnz == 0) continue;
     a.smem_bytes = (int32_t)smem;
+    if (p->staged == 2) {
+      const tt_status s2 = encode_leaf_tmap(p, &a.tmap);
+      if (s2 != TT_OK) return s2;
+    }
     CK(launch_partition(p->order, a, st));
     if (p->timing && q == first) CK(cudaEventRecord(p->evk0, st));
     CK(p->launcher(a, a.nblocks, p->tb, smem, st));
@@ -378,11 +428,15 @@ TT_EXPORT tt_status tt_variant_get(int32_t id, tt_variant_info* info) {
   info->lanes_per_row = 32 / v.cpt;
   info->nnz_per_block = v.tb / info->lanes_per_row * v.G;
   info->staged = v.staged;
-  static const char* fam[3] = {"lean", "stage", "ring"};
+  static const char* fam[3] = {"lean", "stage", "tma"};
   if (v.staged == 0) {  // lean: 256-thread blocks, register budget for b resident blocks per SM
     info->threads = 256;
     info->nnz_per_block = 256 / info->lanes_per_row * v.G;
     std::snprintf(info->name, sizeof(info->name), "lean_b%d_g%d_c%d", lean_blocks(v), v.G, v.cpt);
+  } else if (v.staged == 2) {  // TMA gather: 256-thread blocks, s stages in flight per warp
+    info->threads = 256;
+    info->nnz_per_block = 256 / info->lanes_per_row * v.G;
+    std::snprintf(info->name, sizeof(info->name), "tma_s%d_g%d_c%d", tma_stages(v), v.G, v.cpt);
   } else {
     std::snprintf(info->name, sizeof(info->name), "%s_t%d_g%d_c%d", fam[v.staged], v.tb, v.G, v.cpt);
   }
@@ -775,7 +829,10 @@ tt_status sweep_variants(tt_plan* p, cudaStream_t st) {
       if (s == TT_ERR_UNSUPPORTED) { s = TT_OK; continue; }  // does not fit this tensor's windows
       break;
     }
-    if ((s = run_mttkrp(p, A, st)) != TT_OK) break;
+    if ((s = run_mttkrp(p, A, st)) != TT_OK) {
+      if (s == TT_ERR_UNSUPPORTED) { s = TT_OK; clear_error(); continue; }  // e.g. no TMA descriptor
+      break;
+    }
     float tot = 0.f;
     for (int r = 0; r < 3; r++) {
       cudaEventRecord(e0, st);

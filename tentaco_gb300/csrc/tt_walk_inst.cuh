@@ -1,6 +1,6 @@
 // tt_walk_inst.cuh -- explicit instantiations of the MTTKRP walk kernels for one
-// (order, precision) -- lean warp-tile walk, shared-memory staged walk and ring
-// walk --, included by tt_walk_o{3,4}_{fp32,bf16,bf16f,fp16}.cu with TT_ORDER,
+// (order, precision) -- lean warp-tile walk, shared-memory staged walk and TMA
+// gather walk --, included by tt_walk_o{3,4}_{fp32,bf16,bf16f,fp16}.cu with TT_ORDER,
 // TT_PREC and TT_LOOKUP defined.  The (columns per lane, lanes per row)
 // pairs cover factor ranks 8, 16, 32 and 64.
 #include "tt_mttkrp.cuh"
@@ -8,9 +8,9 @@
 
 namespace tt {
 namespace {
-// fam 0: lean warp-tile walk, 1: shared-memory staged, 2: register walk with a
-// per-lane cp.async ring, 3: lean with the tighter register budget.  units: work units of the partition (warp tiles for
-// fam 0, blocks otherwise).
+// fam 0: lean warp-tile walk, 1: shared-memory staged, 2 / 5: TMA-gather walk with
+// 4 / 8 stages in flight per warp, 3: lean with the tighter register budget.
+// units: work units of the partition (warp tiles except for fam 1, blocks there).
 // Resident blocks per SM the lean kernel's registers are budgeted for: the
 // variant's thread axis selects the looser (tb 256) or tighter (tb 512) budget;
 // both launch 256-thread blocks.
@@ -19,11 +19,13 @@ constexpr int lean_minb(int cpt, bool tight) { return cpt >= 4 ? (tight ? 3 : 2)
 template <int CPT, int LPR, int FAM>
 cudaError_t launch_walk(const WalkArgs& a, int units, int tb, size_t smem, cudaStream_t s) {
   constexpr bool kTight = FAM == 3;  // lean with the tighter register budget
-  auto k = FAM == 1 ? mttkrp_stage_kernel<TT_ORDER, TT_PREC, CPT, LPR>
-         : FAM == 2 ? mttkrp_walk_kernel<TT_ORDER, TT_PREC, CPT, LPR, false, true>
+  auto k = FAM == 1   ? mttkrp_stage_kernel<TT_ORDER, TT_PREC, CPT, LPR>
+         : FAM == 2 ? mttkrp_tma_kernel<TT_ORDER, TT_PREC, CPT, LPR, 4>
+         : FAM == 5 ? mttkrp_tma_kernel<TT_ORDER, TT_PREC, CPT, LPR, 8>
                     : mttkrp_lean_kernel<TT_ORDER, TT_PREC, CPT, LPR, lean_minb(CPT, kTight)>;
-  if (FAM == 0 || FAM == 3) tb = 256;
-  const int grid = (FAM == 0 || FAM == 3) ? (units + tb / 32 - 1) / (tb / 32) : units;
+  const bool warp_units = FAM != 1;  // lean and TMA: one work unit per warp, 256-thread blocks
+  if (warp_units) tb = 256;
+  const int grid = warp_units ? (units + tb / 32 - 1) / (tb / 32) : units;
   static size_t configured = 48 * 1024;
   if (smem > configured) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -38,8 +40,8 @@ cudaError_t launch_walk(const WalkArgs& a, int units, int tb, size_t smem, cudaS
 WalkLauncher TT_LOOKUP(int cpt, int lpr, int fam) {
 #define TT_CASE(C, L)                                                        \
   if (cpt == C && lpr == L)                                                  \
-    return fam == 3 ? &launch_walk<C, L, 3> : fam == 2 ? &launch_walk<C, L, 2> : fam == 1 ? &launch_walk<C, L, 1> \
-                                                                                  : &launch_walk<C, L, 0>;
+    return fam == 5 ? &launch_walk<C, L, 5> : fam == 3 ? &launch_walk<C, L, 3> : fam == 2 ? &launch_walk<C, L, 2> \
+         : fam == 1 ? &launch_walk<C, L, 1> : &launch_walk<C, L, 0>;
   TT_CASE(1, 8) TT_CASE(2, 4) TT_CASE(4, 2) TT_CASE(8, 1)     // rank 8
   TT_CASE(1, 16) TT_CASE(2, 8) TT_CASE(4, 4) TT_CASE(8, 2)    // rank 16
   TT_CASE(1, 32) TT_CASE(2, 16) TT_CASE(4, 8) TT_CASE(8, 4)   // rank 32
