@@ -225,7 +225,7 @@ def run_gpu_arm(args, rank, world, d):
 
     def timed_plan(prec, select):
         plan = tt.Plan(B, rank=RANK, prec=prec, select=select, variant=max(args.variant, 0), slabs=args.slabs)
-        if select == tt.SELECT_MODEL and plan.selected_by != 1:
+        if select == tt.SELECT_MODEL and plan.selected_by not in (1, 3):
             plan = tt.Plan(B, rank=RANK, prec=prec, select=tt.SELECT_SWEEP, slabs=args.slabs)
         bufs = [tt.DeviceBuffer.from_array(C), tt.DeviceBuffer.from_array(D)]
         plan.set_factors(bufs)
@@ -282,7 +282,10 @@ def run_gpu_arm(args, rank, world, d):
         "data": "synthetic (seeded lognormal-fiber tensor; FROSTT data absent)",
         "config": {"workload": WORKLOAD, "dims": list(DIMS), "nnz": B.nnz, "fibers": B.count(1), "rank": RANK,
                    "precision": args.prec, "select": args.select, "variant": plan.variant, "slabs": plan.slabs,
-                   "selected_by": "fixed" if args.variant >= 0 else ["heuristic", "model", "sweep"][plan.selected_by],
+                   "selected_by": "fixed" if args.variant >= 0 else
+                   ["heuristic", "model", "sweep", "model top-k timed"][plan.selected_by],
+                   "candidates_ms": {str(v): round(float(t), 4) for v, t in enumerate(plan.sweep_times()) if t > 0}
+                   if plan.selected_by == 3 else None,
                    "l2": "flushed between steps (512 MB write)", "parallelism": f"replicas{world}",
                    "gen_s": round(gen_s, 1)},
         "gbs_compulsory": round(cbytes / (ms * 1e-3) / 1e9, 1),

@@ -110,7 +110,13 @@ typedef struct tt_plan_options {
   /* L2 policy of factor-row gathers in the lean walk: 0 automatic (evict_last
    * without slabs, evict_normal with them), 1 evict_last, 2 evict_normal. */
   int32_t l2_policy;
-  int32_t reserved[6];
+  /* TT_SELECT_MODEL only: time this many of the network's best-ranked variants
+   * (those that run on the tensor) and the fixed heuristic's variant at plan
+   * creation, and keep the fastest.  0: automatic -- 1 (the network's first
+   * choice, nothing timed) when every feature of the tensor lies inside the range
+   * the network was trained on, else 6; 1 to 16 as given. */
+  int32_t model_topk;
+  int32_t reserved[5];
 } tt_plan_options;
 
 tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t rank, tt_precision prec,
@@ -150,7 +156,8 @@ int64_t tt_plan_device_bytes(const tt_plan* plan);
 int32_t tt_plan_nblocks(const tt_plan* plan);
 /* Switch an MTTKRP plan to another valid variant (scratch grows as needed). */
 tt_status tt_plan_use_variant(tt_plan* plan, int32_t variant);
-/* Per-variant mean ms of the last TT_SELECT_SWEEP (negative: not timed); n entries. */
+/* Per-variant mean ms timed at plan creation by TT_SELECT_SWEEP, or by
+ * TT_SELECT_MODEL's top-k candidates (negative: not timed); n entries. */
 tt_status tt_plan_sweep_times(const tt_plan* plan, float* ms, int32_t n);
 /* Milliseconds of the walk kernel(s) alone in the last timed call (first slab's
  * walk to the last slab's), without partition, clear and row merge. */

@@ -6,7 +6,10 @@
  * by a person.  Here a small network scores every variant of the MTTKRP walk
  * table from 12 tensor features (tt_csf_features in tentaco_gen.h); plans
  * created with TT_SELECT_MODEL run the variant it ranks first (the next one if
- * a staged variant does not fit the tensor's largest fiber window).  The
+ * a staged variant does not fit the tensor's largest fiber window); for a tensor
+ * outside the feature range the network was trained on, or when asked
+ * (tt_plan_options::model_topk), they time its best-ranked few and keep the
+ * fastest.  The
  * exhaustive sweep (TT_SELECT_SWEEP) stays the fallback and produces the
  * timings the network is trained on.  Selection never changes numerics beyond
  * the summation order of the chosen variant.
@@ -74,7 +77,8 @@ int32_t tt_selector_models(void);
 tt_status tt_selector_scores(const taco_tensor_t* B, int32_t rank, tt_precision prec, float* scores,
                              int32_t n);
 
-/* How a plan's variant was chosen: 0 heuristic or fixed, 1 network, 2 sweep. */
+/* How a plan's variant was chosen: 0 heuristic or fixed, 1 network, 2 sweep,
+ * 3 fastest of the network's timed top-k candidates (tt_plan_options::model_topk). */
 int32_t tt_plan_selected_by(const tt_plan* plan);
 
 #ifdef __cplusplus

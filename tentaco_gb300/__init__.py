@@ -361,14 +361,17 @@ class DeviceBuffer:
 
 
 class PlanOptions(C.Structure):
-    _fields_ = [("slabs", C.c_int32), ("l2_policy", C.c_int32), ("reserved", C.c_int32 * 6)]
+    _fields_ = [("slabs", C.c_int32), ("l2_policy", C.c_int32), ("model_topk", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
 
 
 class Plan:
-    """slabs: leaf-mode slabs for MTTKRP (None/0 automatic, 1 none, up to 16)."""
+    """slabs: leaf-mode slabs for MTTKRP (None/0 automatic, 1 none, up to 16).
+    model_topk: with SELECT_MODEL, how many of the network's best-ranked variants
+    to time at creation (0 automatic: 1 inside the training range, else 6)."""
 
     def __init__(self, B, op=OP_MTTKRP, rank=32, prec="fp32", select=SELECT_DEFAULT, variant=0, stream=None,
-                 slabs=None, l2_policy=0):
+                 slabs=None, l2_policy=0, model_topk=0):
         self.ptr = _P()
         self.op = op
         self.rank = rank
@@ -376,6 +379,7 @@ class Plan:
         opts = PlanOptions()
         opts.slabs = int(slabs or 0)
         opts.l2_policy = int(l2_policy)
+        opts.model_topk = int(model_topk)
         check(lib().tt_plan_create_ex(_tensor_ptr(B), op, rank, PRECISIONS.get(prec, prec), select, variant,
                                       C.byref(opts), stream, C.byref(self.ptr)))
 

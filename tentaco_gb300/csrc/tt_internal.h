@@ -59,6 +59,10 @@ tt_status csf_check(const CsfView& v);
 // multiple of 16 entries plus 16, zero filled).  pos[l] of a slab indexes its
 // own arrays (leaf positions relative to leaf_off).
 constexpr int kMaxSlabs = 16;
+// TT_SELECT_MODEL: most candidates a plan may time, and how many it times when the
+// tensor lies outside the range of features the network was trained on.
+constexpr int kMaxTopk = 16;
+constexpr int kTopkOutside = 6;
 struct SlabCsf {
   struct Slab {
     std::vector<int32_t> pos[TT_MAX_ORDER], crd[TT_MAX_ORDER];

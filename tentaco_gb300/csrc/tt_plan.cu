@@ -391,7 +391,7 @@ tt_status run_ttv(tt_plan* p, const float* x, float* y, cudaStream_t st) {
   return TT_OK;
 }
 
-tt_status sweep_variants(tt_plan* p, cudaStream_t st);
+tt_status time_variants(tt_plan* p, cudaStream_t st, const std::vector<int>& cands, int max_timed, int extra);
 
 }  // namespace
 
@@ -614,13 +614,33 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
         return fail(set_error(TT_ERR_INVALID_ARGUMENT, "variant %d not valid for order %d rank %d", variant, p->order, rank));
       id = variant;
     } else if (select == TT_SELECT_MODEL) {
-      // the network's ranking; a staged variant whose window does not fit is skipped
+      // the network's ranking; a variant that does not fit this tensor is skipped.
+      // k > 1: time the k best-ranked variants that run and the fixed heuristic's
+      // variant, keep the fastest (automatic: k = 1 inside the model's training
+      // range, where its pick is trusted, else kTopkOutside)
       std::vector<int> ranked;
-      if (selector_rank(p, B, ranked) == TT_OK) {
-        for (int cand : ranked) {
-          s = use_variant(p, cand);
-          if (s == TT_OK) { id = cand; placed = true; p->selected_by = 1; break; }
-          if (s != TT_ERR_UNSUPPORTED) return fail(s);
+      bool in_range = true;
+      const int req_k = opts ? opts->model_topk : 0;
+      if (req_k < 0 || req_k > kMaxTopk)
+        return fail(set_error(TT_ERR_INVALID_ARGUMENT, "model_topk %d (0..%d)", req_k, kMaxTopk));
+      if (selector_rank(p, B, ranked, &in_range) == TT_OK && !ranked.empty()) {
+        const int k = req_k > 0 ? req_k : (in_range ? 1 : kTopkOutside);
+        if (k > 1) {
+          const int dflt = default_variant(p->order, rank, p->prec, p->nnz);
+          s = time_variants(p, st, ranked, k, dflt);
+          if (s == TT_OK) {
+            id = p->variant;
+            placed = true;
+            p->selected_by = 3;
+          } else if (s != TT_ERR_UNSUPPORTED) {
+            return fail(s);
+          }
+        } else {
+          for (int cand : ranked) {
+            s = use_variant(p, cand);
+            if (s == TT_OK) { id = cand; placed = true; p->selected_by = 1; break; }
+            if (s != TT_ERR_UNSUPPORTED) return fail(s);
+          }
         }
       }
       clear_error();
@@ -631,7 +651,10 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
     if (id < 0) return fail(set_error(TT_ERR_UNSUPPORTED, "no variant for order %d rank %d", p->order, rank));
     if (!placed && (s = use_variant(p, id)) != TT_OK) return fail(s);
     if (select == TT_SELECT_SWEEP) {
-      if ((s = sweep_variants(p, st)) != TT_OK) return fail(s);
+      std::vector<int> all;
+      for (int v = 0; v < kNumVariants; v++)
+        if (variant_valid(v, p->order, rank, p->prec)) all.push_back(v);
+      if ((s = time_variants(p, st, all, kNumVariants, -1)) != TT_OK) return fail(s);
       p->selected_by = 2;
     }
   } else {
@@ -798,9 +821,12 @@ TT_EXPORT tt_status tt_plan_use_variant(tt_plan* p, int32_t id) {
 }
 
 namespace {
-// Time every valid variant (3 runs each after one warm-up) with placeholder
-// factors and keep the fastest.  Timing does not depend on factor values.
-tt_status sweep_variants(tt_plan* p, cudaStream_t st) {
+// Time variants (3 runs each after one warm-up) with placeholder factors and keep
+// the fastest; timing does not depend on factor values.  cands are tried in order
+// until max_timed of them have run (a variant that does not fit this tensor is
+// skipped); extra (>= 0), if not timed yet, is timed as well.  The times go to
+// sweep_ms (untimed variants keep -1).
+tt_status time_variants(tt_plan* p, cudaStream_t st, const std::vector<int>& cands, int max_timed, int extra) {
   const int nm = p->order - 1;
   std::vector<void*> tmp;
   const void* saved[3] = {p->fac[0], p->fac[1], p->fac[2]};
@@ -823,7 +849,15 @@ tt_status sweep_variants(tt_plan* p, cudaStream_t st) {
   int best = p->variant;
   float best_ms = 1e30f;
   tt_status s = TT_OK;
-  for (int id = 0; id < kNumVariants && s == TT_OK; id++) {
+  std::vector<int> order;
+  order.reserve(cands.size() + 1);
+  for (int id : cands) order.push_back(id);
+  if (extra >= 0) order.push_back(extra);
+  int timed = 0;
+  for (size_t i = 0; i < order.size() && s == TT_OK; i++) {
+    const int id = order[i];
+    const bool is_extra = extra >= 0 && i + 1 == order.size();
+    if (is_extra ? p->sweep_ms[id] >= 0.f : timed >= max_timed) continue;
     if (!variant_valid(id, p->order, p->rank, p->prec)) continue;
     if ((s = use_variant(p, id)) != TT_OK) {
       if (s == TT_ERR_UNSUPPORTED) { s = TT_OK; continue; }  // does not fit this tensor's windows
@@ -843,7 +877,9 @@ tt_status sweep_variants(tt_plan* p, cudaStream_t st) {
       cudaEventElapsedTime(&ms, e0, e1);
       tot += ms;
     }
+    if (s != TT_OK) break;
     p->sweep_ms[id] = tot / 3.f;
+    timed++;
     if (tot / 3.f < best_ms) { best_ms = tot / 3.f; best = id; }
   }
   cudaEventDestroy(e0);
@@ -853,11 +889,13 @@ tt_status sweep_variants(tt_plan* p, cudaStream_t st) {
   for (int m = 0; m < 3; m++) p->fac[m] = saved[m];
   p->d_colscale = saved_scale;
   if (s != TT_OK) return s;
+  if (best < 0) return set_error(TT_ERR_UNSUPPORTED, "no candidate variant runs on this tensor");
   return use_variant(p, best);
 }
 }  // namespace
 
-// Per-variant mean ms measured by the last TT_SELECT_SWEEP (negative: not timed).
+// Per-variant mean ms measured at plan creation by TT_SELECT_SWEEP or by the
+// network's timed candidates (negative: not timed).
 TT_EXPORT tt_status tt_plan_sweep_times(const tt_plan* p, float* ms, int32_t n) {
   if (!p || !ms) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
   for (int i = 0; i < n && i < kNumVariants; i++) ms[i] = p->sweep_ms[i];

@@ -43,7 +43,7 @@ struct tt_plan {
   float* d_colscale = nullptr;
   bool factors_set = false;
   // variant and scratch
-  int variant = -1, selected_by = 0;  // 0 heuristic/fixed, 1 model, 2 sweep
+  int variant = -1, selected_by = 0;  // 0 heuristic/fixed, 1 model, 2 sweep, 3 model's top k timed
   int tb = 0, cpt = 0, lpr = 0, G = 0, P = 0, nblocks = 0, staged = 0, wcap = 1;
   int32_t* d_err = nullptr;  // [0]: kernel error word, [1]: scratch for the window size
   tt::WalkLauncher launcher = nullptr;
@@ -77,5 +77,5 @@ namespace tt {
 // Learned selector: the variant the loaded model prefers for this plan, or -1.
 // Valid variants for the plan's shape, ordered by the selector network's
 // predicted time; TT_ERR_UNSUPPORTED when no loaded model covers the shape.
-tt_status selector_rank(const tt_plan* p, const taco_tensor_t* B, std::vector<int>& ranked);
+tt_status selector_rank(const tt_plan* p, const taco_tensor_t* B, std::vector<int>& ranked, bool* in_range);
 }

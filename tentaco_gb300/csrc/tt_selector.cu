@@ -22,6 +22,7 @@ namespace {
 struct Model {
   int storage = 0;  // 0: FP32 storage plans, 1: 16-bit storage plans
   float mean[TT_MLP_IN], sd[TT_MLP_IN];
+  float lo[TT_MLP_IN], hi[TT_MLP_IN];  // feature range of the training tensors
   std::vector<float> params;
 };
 
@@ -40,6 +41,10 @@ std::string default_model_path() {
   return "selector_model.bin";
 }
 
+// File layout (little-endian): "TTSEL001", int32 {version, inputs, hidden, outputs,
+// models}, then per model: int32 storage, float mean[inputs], sd[inputs], (version
+// 2 only) lo[inputs], hi[inputs], params.  Version 1 files carry no training range
+// and count every tensor as inside it.
 tt_status load_file(const std::string& path, std::vector<Model>& out, int& nout) {
   FILE* f = std::fopen(path.c_str(), "rb");
   if (!f) return set_error(TT_ERR_INVALID_ARGUMENT, "selector model %s: cannot open", path.c_str());
@@ -47,7 +52,7 @@ tt_status load_file(const std::string& path, std::vector<Model>& out, int& nout)
   char magic[8];
   int32_t hdr[5];
   bool ok = rd(magic, 8) && std::memcmp(magic, "TTSEL001", 8) == 0 && rd(hdr, sizeof(hdr));
-  ok = ok && hdr[0] == 1 && hdr[1] == TT_MLP_IN && hdr[2] == TT_MLP_HIDDEN && hdr[3] > 0 && hdr[3] <= 4096 &&
+  ok = ok && (hdr[0] == 1 || hdr[0] == 2) && hdr[1] == TT_MLP_IN && hdr[2] == TT_MLP_HIDDEN && hdr[3] > 0 && hdr[3] <= 4096 &&
        hdr[4] > 0 && hdr[4] <= 8;
   std::vector<Model> ms;
   if (ok) {
@@ -56,8 +61,14 @@ tt_status load_file(const std::string& path, std::vector<Model>& out, int& nout)
       Model m;
       int32_t storage = 0;
       m.params.resize((size_t)np);
-      ok = rd(&storage, 4) && rd(m.mean, sizeof(m.mean)) && rd(m.sd, sizeof(m.sd)) &&
-           rd(m.params.data(), sizeof(float) * (size_t)np);
+      ok = rd(&storage, 4) && rd(m.mean, sizeof(m.mean)) && rd(m.sd, sizeof(m.sd));
+      if (hdr[0] == 2) {
+        ok = ok && rd(m.lo, sizeof(m.lo)) && rd(m.hi, sizeof(m.hi));
+      } else {
+        std::fill(m.lo, m.lo + TT_MLP_IN, -std::numeric_limits<float>::infinity());
+        std::fill(m.hi, m.hi + TT_MLP_IN, std::numeric_limits<float>::infinity());
+      }
+      ok = ok && rd(m.params.data(), sizeof(float) * (size_t)np);
       m.storage = storage;
       for (int k = 0; k < TT_MLP_IN && ok; k++) ok = std::isfinite(m.mean[k]) && m.sd[k] > 0.f;
       ms.push_back(std::move(m));
@@ -90,7 +101,9 @@ const Model* model_for(int storage, int& nout) {
 int storage_class(int prec) { return prec == (int)TT_PREC_FP32 ? 0 : 1; }
 
 // Scores of every variant for tensor B (device inference).  Invalid variants: +inf.
-tt_status scores_for(const taco_tensor_t* B, int order, int rank, int prec, std::vector<float>& scores) {
+// in_range (optional): whether every feature lies inside the training range.
+tt_status scores_for(const taco_tensor_t* B, int order, int rank, int prec, std::vector<float>& scores,
+                     bool* in_range = nullptr) {
   if (order != 3) return set_error(TT_ERR_UNSUPPORTED, "the selector covers 3-mode tensors");
   int nout = 0;
   const Model* m = model_for(storage_class(prec), nout);
@@ -98,6 +111,10 @@ tt_status scores_for(const taco_tensor_t* B, int order, int rank, int prec, std:
   float f[TT_MLP_IN];
   tt_status s = tt_csf_features(B, rank, f);
   if (s != TT_OK) return s;
+  if (in_range) {
+    *in_range = true;
+    for (int k = 0; k < TT_MLP_IN; k++) *in_range = *in_range && f[k] >= m->lo[k] && f[k] <= m->hi[k];
+  }
   for (int k = 0; k < TT_MLP_IN; k++) f[k] = (f[k] - m->mean[k]) / m->sd[k];
   const int64_t np = (int64_t)m->params.size();
   const int64_t ns = tt_mlp_scratch_floats(1, nout);
@@ -129,10 +146,11 @@ tt_status scores_for(const taco_tensor_t* B, int order, int rank, int prec, std:
 }  // namespace
 
 // Variants ordered by predicted time (valid ones only); empty when no model applies.
-tt_status selector_rank(const tt_plan* p, const taco_tensor_t* B, std::vector<int>& ranked) {
+// in_range: whether the tensor's features lie inside the model's training range.
+tt_status selector_rank(const tt_plan* p, const taco_tensor_t* B, std::vector<int>& ranked, bool* in_range) {
   ranked.clear();
   std::vector<float> sc;
-  tt_status s = scores_for(B, p->order, p->rank, p->prec, sc);
+  tt_status s = scores_for(B, p->order, p->rank, p->prec, sc, in_range);
   if (s != TT_OK) return s;
   for (int v = 0; v < (int)sc.size(); v++)
     if (std::isfinite(sc[(size_t)v])) ranked.push_back(v);

@@ -17,6 +17,10 @@ and its generator: mode sizes log-uniform in [1e3, 1e6], nnz log-uniform in
 Targets: y_v = log2(ms_v / ms_best) for every variant timed on the tensor
 (masked mean squared error; untimed variants are masked out).
 
+The model file also records each feature's range over the training tensors; a
+plan whose tensor falls outside it times the network's best few variants instead
+of trusting its first choice (tt_plan_options::model_topk).
+
 Usage (needs a GPU):
     python -m tentaco_gb300.selector corpus --out tentaco_gb300/selector_corpus.jsonl
     python -m tentaco_gb300.selector train --corpus ... --out tentaco_gb300/selector_model.bin
@@ -111,13 +115,14 @@ def dataset(recs: list, storage: int, split: str | None):
 
 
 def write_model(path: str, models: list) -> None:
+    """Version 2: per model storage, mean, sd, lo, hi (training feature range), params."""
     with open(path, "wb") as f:
         f.write(MAGIC)
-        f.write(struct.pack("<5i", 1, NIN, HIDDEN, models[0]["nout"], len(models)))
+        f.write(struct.pack("<5i", 2, NIN, HIDDEN, models[0]["nout"], len(models)))
         for m in models:
             f.write(struct.pack("<i", m["storage"]))
-            f.write(np.asarray(m["mean"], dtype="<f4").tobytes())
-            f.write(np.asarray(m["sd"], dtype="<f4").tobytes())
+            for key in ("mean", "sd", "lo", "hi"):
+                f.write(np.asarray(m[key], dtype="<f4").tobytes())
             f.write(np.asarray(m["params"], dtype="<f4").tobytes())
 
 
@@ -126,7 +131,7 @@ def read_model(path: str) -> list:
         data = f.read()
     assert data[:8] == MAGIC, "not a selector model file"
     ver, nin, hid, nout, nm = struct.unpack_from("<5i", data, 8)
-    assert ver == 1 and nin == NIN and hid == HIDDEN
+    assert ver in (1, 2) and nin == NIN and hid == HIDDEN
     np_ = NIN * HIDDEN + HIDDEN + 2 * (HIDDEN * HIDDEN + HIDDEN) + HIDDEN * nout + nout
     off = 28
     out = []
@@ -135,8 +140,15 @@ def read_model(path: str) -> list:
         off += 4
         mean = np.frombuffer(data, "<f4", NIN, off); off += 4 * NIN
         sd = np.frombuffer(data, "<f4", NIN, off); off += 4 * NIN
+        if ver == 2:
+            lo = np.frombuffer(data, "<f4", NIN, off).copy(); off += 4 * NIN
+            hi = np.frombuffer(data, "<f4", NIN, off).copy(); off += 4 * NIN
+        else:  # no recorded range: every tensor counts as inside it
+            lo = np.full(NIN, -np.inf, np.float32)
+            hi = np.full(NIN, np.inf, np.float32)
         params = np.frombuffer(data, "<f4", np_, off); off += 4 * np_
-        out.append({"storage": storage, "nout": nout, "mean": mean.copy(), "sd": sd.copy(), "params": params.copy()})
+        out.append({"storage": storage, "nout": nout, "mean": mean.copy(), "sd": sd.copy(), "lo": lo, "hi": hi,
+                    "params": params.copy()})
     assert off == len(data)
     return out
 
@@ -144,6 +156,17 @@ def read_model(path: str) -> list:
 # ---------------------------------------------------------------------------
 # training (library kernels) and evaluation
 # ---------------------------------------------------------------------------
+def feature_range(recs: list, storage: int):
+    """Per-feature min and max over the training tensors of a storage class (FP32)."""
+    _, X, _, _ = dataset(recs, storage, "train")
+    return X.min(axis=0).astype(np.float32), X.max(axis=0).astype(np.float32)
+
+
+def in_range(m: dict, feats) -> bool:
+    f = np.asarray(feats, dtype=np.float32)
+    return bool(np.all(f >= m["lo"]) and np.all(f <= m["hi"]))
+
+
 def init_params(nout: int, seed: int) -> np.ndarray:
     """He-normal weights, zero biases, in the library's flat layout."""
     rng = np.random.default_rng(seed)
@@ -167,8 +190,9 @@ def train(recs: list, storage: int, nout: int, steps: int = 3000, lr: float = 1e
     params, losses = net.train(init_params(nout, seed), Xn, T.astype(np.float32), M.astype(np.float32),
                                steps=steps, lr=lr, weight_decay=wd)
     print(f"storage {storage}: {Xn.shape[0]} tensors, loss {losses[0]:.4f} -> {losses[-1]:.4f}", file=log)
+    lo, hi = feature_range(recs, storage)
     return {"storage": storage, "nout": nout, "mean": mean.astype(np.float32), "sd": sd.astype(np.float32),
-            "params": params}
+            "lo": lo, "hi": hi, "params": params}
 
 
 def pick(scores: np.ndarray, ms: np.ndarray) -> int:

@@ -86,6 +86,50 @@ def test_model_beats_heuristic_on_held_out():
         assert r["model_mean_regret"] < r["heuristic_mean_regret"], r
 
 
+def test_model_file_ranges_and_versions(tmp_path):
+    """The committed model records the training feature range (version 2), a
+    version-1 file reads as unbounded, and the library loads both."""
+    from tentaco_gb300 import selector
+    recs = _corpus()
+    models = selector.read_model(MODEL)
+    for m in models:
+        lo, hi = selector.feature_range(recs, m["storage"])
+        assert np.array_equal(m["lo"], lo) and np.array_equal(m["hi"], hi)
+        assert np.all(np.isfinite(m["lo"])) and np.all(m["lo"] <= m["hi"])
+    train = [r for r in recs if selector.split_of(r["t"]) == "train"]
+    assert all(selector.in_range(models[0], r["features"]) for r in train[:50])
+    # a 100M-nonzero tensor with a 2M-long leaf mode lies outside the corpus
+    far = np.array(train[0]["features"], dtype=np.float32)
+    far[2], far[3] = 20.93, 26.58
+    assert not selector.in_range(models[0], far)
+    v1 = tmp_path / "v1.bin"
+    raw = open(MODEL, "rb").read()
+    import struct
+    ver, nin, hid, nout, nm = struct.unpack_from("<5i", raw, 8)
+    assert ver == 2
+    out = bytearray(raw[:8] + struct.pack("<5i", 1, nin, hid, nout, nm))
+    off = 28
+    np_ = orc.mlp_num_params(nout)
+    for _ in range(nm):
+        out += raw[off:off + 4 + 8 * nin]          # storage, mean, sd
+        off += 4 + 16 * nin                         # skip lo, hi
+        out += raw[off:off + 4 * np_]
+        off += 4 * np_
+    assert off == len(raw)
+    v1.write_bytes(bytes(out))
+    old = selector.read_model(str(v1))
+    assert all(np.all(np.isinf(m["lo"])) for m in old)
+    assert all(np.array_equal(a["params"], b["params"]) for a, b in zip(old, models))
+    tt.selector_load(str(v1))
+    assert tt.selector_models() == 2
+    tt.selector_load(MODEL)
+    assert tt.selector_models() == 2
+    bad = tmp_path / "bad.bin"
+    bad.write_bytes(raw[:-4])
+    with pytest.raises(tt.TTError):
+        tt.selector_load(str(bad))
+
+
 @pytest.mark.gpu
 def test_gpu_grad_matches_oracle():
     params, X, T, M = _rand_problem(3)
@@ -138,3 +182,32 @@ def test_product_selector_regret_on_held_out():
     assert len(reg_m) >= 30
     assert np.mean(reg_m) <= 0.10
     assert np.mean(reg_m) < np.mean(reg_h)
+
+
+@pytest.mark.gpu
+def test_model_topk_times_candidates():
+    """model_topk > 1 times the network's best-ranked variants (and the fixed
+    heuristic's) at plan creation and keeps the fastest; automatic selection
+    trusts the network inside its training range and times candidates outside it."""
+    from tentaco_gb300 import selector
+    tt.selector_load(MODEL)
+    recs = [r for r in _corpus() if selector.split_of(r["t"]) == "test"]
+    r = sorted(recs, key=lambda r: r["nnz"])[5]
+    B = selector.corpus_tensor(r)
+    auto = tt.Plan(B, rank=r["rank"], prec=r["prec"], select=tt.SELECT_MODEL)
+    assert auto.selected_by == 1
+    assert np.all(auto.sweep_times() < 0)
+    plan = tt.Plan(B, rank=r["rank"], prec=r["prec"], select=tt.SELECT_MODEL, model_topk=4)
+    assert plan.selected_by == 3
+    ms = plan.sweep_times()
+    timed = np.flatnonzero(ms > 0)
+    assert 4 <= timed.size <= 5
+    assert plan.variant == timed[np.argmin(ms[timed])]
+    assert auto.variant in timed  # the network's first runnable choice is a candidate
+    # mode sizes of 100 are below the corpus's 10^3: outside the training range
+    small = tt.gen_zipf((100, 120, 140), (0.5, 0.5, 0.5), 20_000, 7)
+    far = tt.Plan(small, rank=32, prec="fp16", select=tt.SELECT_MODEL)
+    assert far.selected_by == 3
+    assert np.count_nonzero(far.sweep_times() > 0) >= 6
+    with pytest.raises(tt.TTError):
+        tt.Plan(small, rank=32, prec="fp16", select=tt.SELECT_MODEL, model_topk=17)
