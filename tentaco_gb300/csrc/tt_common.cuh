@@ -216,6 +216,53 @@ __device__ __forceinline__ float2 pair16(uint32_t w) {
   }
 }
 
+// Mixed-precision FMA (sm_100 and later): 16-bit operands, FP32 addend and
+// result, one rounding.  The product of two FP16 (or two BF16) numbers is exact
+// in FP32, so acc = fma(a, b, acc) equals fmaf on the operands converted to FP32;
+// no conversion instructions are issued.
+//   mfma2<KIND, HV>: a0 += lo(d) * v.half[HV], a1 += hi(d) * v.half[HV]
+//   mfma1<KIND, HV>: a0 += lo(d) * v.half[HV]
+template <int KIND, int HV>
+__device__ __forceinline__ void mfma2(float& a0, float& a1, uint32_t d, uint32_t v) {
+  if constexpr (KIND == kB16) {
+    if constexpr (HV == 0)
+      asm("{\n\t.reg .b16 dl, dh, vl, vh;\n\tmov.b32 {dl, dh}, %2;\n\tmov.b32 {vl, vh}, %3;\n\t"
+          "fma.rn.f32.bf16 %0, dl, vl, %0;\n\tfma.rn.f32.bf16 %1, dh, vl, %1;\n\t}"
+          : "+f"(a0), "+f"(a1) : "r"(d), "r"(v));
+    else
+      asm("{\n\t.reg .b16 dl, dh, vl, vh;\n\tmov.b32 {dl, dh}, %2;\n\tmov.b32 {vl, vh}, %3;\n\t"
+          "fma.rn.f32.bf16 %0, dl, vh, %0;\n\tfma.rn.f32.bf16 %1, dh, vh, %1;\n\t}"
+          : "+f"(a0), "+f"(a1) : "r"(d), "r"(v));
+  } else {
+    if constexpr (HV == 0)
+      asm("{\n\t.reg .b16 dl, dh, vl, vh;\n\tmov.b32 {dl, dh}, %2;\n\tmov.b32 {vl, vh}, %3;\n\t"
+          "fma.rn.f32.f16 %0, dl, vl, %0;\n\tfma.rn.f32.f16 %1, dh, vl, %1;\n\t}"
+          : "+f"(a0), "+f"(a1) : "r"(d), "r"(v));
+    else
+      asm("{\n\t.reg .b16 dl, dh, vl, vh;\n\tmov.b32 {dl, dh}, %2;\n\tmov.b32 {vl, vh}, %3;\n\t"
+          "fma.rn.f32.f16 %0, dl, vh, %0;\n\tfma.rn.f32.f16 %1, dh, vh, %1;\n\t}"
+          : "+f"(a0), "+f"(a1) : "r"(d), "r"(v));
+  }
+}
+template <int KIND, int HV>
+__device__ __forceinline__ void mfma1(float& a0, uint32_t d, uint32_t v) {
+  if constexpr (KIND == kB16) {
+    if constexpr (HV == 0)
+      asm("{\n\t.reg .b16 dl, dh, vl, vh;\n\tmov.b32 {dl, dh}, %1;\n\tmov.b32 {vl, vh}, %2;\n\t"
+          "fma.rn.f32.bf16 %0, dl, vl, %0;\n\t}" : "+f"(a0) : "r"(d), "r"(v));
+    else
+      asm("{\n\t.reg .b16 dl, dh, vl, vh;\n\tmov.b32 {dl, dh}, %1;\n\tmov.b32 {vl, vh}, %2;\n\t"
+          "fma.rn.f32.bf16 %0, dl, vh, %0;\n\t}" : "+f"(a0) : "r"(d), "r"(v));
+  } else {
+    if constexpr (HV == 0)
+      asm("{\n\t.reg .b16 dl, dh, vl, vh;\n\tmov.b32 {dl, dh}, %1;\n\tmov.b32 {vl, vh}, %2;\n\t"
+          "fma.rn.f32.f16 %0, dl, vl, %0;\n\t}" : "+f"(a0) : "r"(d), "r"(v));
+    else
+      asm("{\n\t.reg .b16 dl, dh, vl, vh;\n\tmov.b32 {dl, dh}, %1;\n\tmov.b32 {vl, vh}, %2;\n\t"
+          "fma.rn.f32.f16 %0, dl, vh, %0;\n\t}" : "+f"(a0) : "r"(d), "r"(v));
+  }
+}
+
 template <int KIND>
 __device__ __forceinline__ float lo16(uint32_t w) { return KIND == kB16 ? bf16lo(w) : h16lo(w); }
 template <int KIND>

@@ -434,6 +434,36 @@ struct Walk {
       for (int u = 0; u < U; u++) v[u] = val_one(vt, u);
     }
   }
+  // 16-bit storage whose values and factors share a kind: the walk's products
+  // use the mixed-precision FMA on the raw 16-bit words (same result as fmaf on
+  // the converted operands, without the conversions).
+  static constexpr bool MIXED = VK == FK && VK != kF32;
+  // f3 += (half HV of value word v) * (the lane's piece w of a factor row)
+  template <int HV>
+  __device__ __forceinline__ static void acc_mixed(float (&f3)[CPT], const uint32_t (&w)[NWD], uint32_t v) {
+    if constexpr (CPT == 1) {
+      mfma1<FK, HV>(f3[0], w[0], v);
+    } else {
+#pragma unroll
+      for (int k = 0; k < CPT / 2; k++) mfma2<FK, HV>(f3[2 * k], f3[2 * k + 1], w[k], v);
+    }
+  }
+  // U consecutive stored 16-bit values as raw words, two per word (U % 4 == 0;
+  // runs of 4 or more start 16-byte aligned).
+  template <int U>
+  __device__ __forceinline__ static void vals_raw(const unsigned char* vt, uint32_t (&w)[U / 2]) {
+    static_assert(U % 4 == 0, "raw values come in 8-byte pieces");
+    if constexpr (U % 8 == 0) {
+#pragma unroll
+      for (int k = 0; k < U / 8; k++) {
+        const uint4 x = reinterpret_cast<const uint4*>(vt)[k];
+        w[4 * k] = x.x; w[4 * k + 1] = x.y; w[4 * k + 2] = x.z; w[4 * k + 3] = x.w;
+      }
+    } else {
+      const uint2 x = *reinterpret_cast<const uint2*>(vt);
+      w[0] = x.x; w[1] = x.y;
+    }
+  }
   __device__ __forceinline__ static float val_one(const unsigned char* vt, int j) {
     if constexpr (VK == kF32) return reinterpret_cast<const float*>(vt)[j];
     else return lo16<VK>((uint32_t)reinterpret_cast<const uint16_t*>(vt)[j]);
@@ -515,6 +545,26 @@ struct Walk {
       for (int u = 0; u < U; u++) piece_load(fz + (size_t)(uint32_t)l[u] * FRB, pol, g[u]);
     };
     auto consume = [&](const uint32_t (&g)[U][NWD], int j) {
+      if constexpr (MIXED) {
+        uint32_t vw[U / 2];
+        vals_raw<U>(vt + (size_t)j * VB, vw);
+        if (s + j + U <= fend) {
+#pragma unroll
+          for (int u = 0; u < U; u += 2) {
+            acc_mixed<0>(f3, g[u], vw[u >> 1]);
+            acc_mixed<1>(f3, g[u + 1], vw[u >> 1]);
+          }
+          return;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u += 2) {
+          while (s + j + u >= fend) fold();
+          acc_mixed<0>(f3, g[u], vw[u >> 1]);
+          while (s + j + u + 1 >= fend) fold();
+          acc_mixed<1>(f3, g[u + 1], vw[u >> 1]);
+        }
+        return;
+      }
       float v[U];
       vals_load<U>(vt + (size_t)j * VB, v);
       if (s + j + U <= fend) {
@@ -551,12 +601,18 @@ struct Walk {
     for (int j = nb * U; j < n; j++) {  // ragged end (the tensor's last tile only)
       uint32_t g[NWD];
       piece_load(fz + (size_t)(uint32_t)lc[j] * FRB, pol, g);
-      const float v = val_one(vt, j);
-      while (s + j >= fend) fold();
-      float d[CPT];
-      piece_cvt(g, d);
+      if constexpr (MIXED) {
+        const uint32_t vr = reinterpret_cast<const uint16_t*>(vt)[j];
+        while (s + j >= fend) fold();
+        acc_mixed<0>(f3, g, vr);
+      } else {
+        const float v = val_one(vt, j);
+        while (s + j >= fend) fold();
+        float d[CPT];
+        piece_cvt(g, d);
 #pragma unroll
-      for (int c = 0; c < CPT; c++) f3[c] = fmaf(v, d[c], f3[c]);
+        for (int c = 0; c < CPT; c++) f3[c] = fmaf(v, d[c], f3[c]);
+      }
     }
     {
       float cw[CPT];
