@@ -1308,6 +1308,87 @@ __global__ void __launch_bounds__(512) mttkrp_walk_kernel(const __grid_constant_
   block_merge<ORDER, PREC, CPT, LPR>(a, wk, X, s_wh, s_wt, s_wha, s_wta, head_ff, fs, s_pos[0], bstart, pn[0], blockIdx.x);
 }
 
+// Warp staging of a tile's coordinate and value streams into per-run shared
+// memory: 16-byte chunk c (entries 4c..4c+3) goes to run c >> lg_cpr, each run
+// followed by 16 bytes of padding (bank skew).  All loads of a round (up to
+// four chunks per lane) are issued before any store, so a lane has several
+// DRAM round trips in flight instead of one.  The streams are padded, so the
+// rounded-up last chunk stays in bounds.
+template <int VB>
+__device__ __forceinline__ void stage_runs(const int32_t* gl, const void* vals, int64_t base, int n4, int lg_cpr,
+                                           int lane, int32_t* s_lc, unsigned char* s_val, uint64_t pol) {
+  constexpr int R = 4;
+  for (int c0 = lane; c0 < n4; c0 += 32 * R) {
+    int4 li[R];
+    float4 vf[R];
+    uint2 vh[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int c = c0 + 32 * r;
+      if (c < n4) {
+        li[r] = ld_stream_i4(gl + 4 * c, pol);
+        if constexpr (VB == 4)
+          vf[r] = ld_stream_f4(static_cast<const float*>(vals) + base + 4 * c, pol);
+        else
+          vh[r] = ld_stream_u2(static_cast<const uint16_t*>(vals) + base + 4 * c, pol);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int c = c0 + 32 * r;
+      if (c < n4) {
+        const int t = c >> lg_cpr;
+        reinterpret_cast<int4*>(s_lc)[c + t] = li[r];
+        if constexpr (VB == 4)
+          reinterpret_cast<float4*>(s_val)[c + t] = vf[r];
+        else
+          reinterpret_cast<uint2*>(s_val)[c + 2 * t] = vh[r];
+      }
+    }
+  }
+}
+
+// A tile's fiber window: W + 1 fiber starts and W fiber coordinates, all loads
+// of a round issued before its stores.
+__device__ __forceinline__ void stage_window(const int32_t* gpos, const int32_t* gcrd, int W, int lane,
+                                             int32_t* s_pos, int32_t* s_fcrd) {
+  constexpr int R = 2;
+  for (int x0 = lane; x0 <= W; x0 += 32 * R) {
+    int p[R], c[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int x = x0 + 32 * r;
+      if (x <= W) p[r] = gpos[x];
+      if (x < W) c[r] = gcrd[x];
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int x = x0 + 32 * r;
+      if (x <= W) s_pos[x] = p[r];
+      if (x < W) s_fcrd[x] = c[r];
+    }
+  }
+}
+
+// n consecutive int32 from global into shared memory, four loads per lane in
+// flight per round.
+__device__ __forceinline__ void stage_ints(const int32_t* g, int n, int lane, int32_t* sdst) {
+  constexpr int R = 4;
+  for (int x0 = lane; x0 < n; x0 += 32 * R) {
+    int v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int x = x0 + 32 * r;
+      if (x < n) v[r] = g[x];
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int x = x0 + 32 * r;
+      if (x < n) sdst[x] = v[r];
+    }
+  }
+}
+
 // Lean kernel (family 0): every warp owns a tile of TW*G consecutive nonzeros
 // (TW = 32/LPR teams of G), which is the unit of the partition, of the carry
 // slots and of chain_fixup_kernel.  A warp stages its own tile and window with
@@ -1346,9 +1427,10 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_lean_kernel(const __grid_con
     const uint64_t polF = policy_evict_first();
     const int n4 = (cnt + 3) >> 2;
     const int32_t* gl = a.crd[ORDER - 1] + ustart64;
-    for (int c = lane; c < n4; c += 32) {
+    if constexpr (!EXACT) stage_runs<VB>(gl, a.vals, ustart64, n4, a.lgG - 2, lane, s_lc, s_val, polF);
+    for (int c = lane; EXACT && c < n4; c += 32) {
       const int t = (4 * c) >> a.lgG;
-      if (!EXACT || 4 * c + 4 <= cnt) {
+      if (4 * c + 4 <= cnt) {
         reinterpret_cast<int4*>(s_lc)[c + t] = ld_stream_i4(gl + 4 * c, polF);
         if constexpr (VB == 4)
           reinterpret_cast<float4*>(s_val)[c + t] = ld_stream_f4(static_cast<const float*>(a.vals) + ustart64 + 4 * c, polF);
@@ -1362,10 +1444,7 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_lean_kernel(const __grid_con
         }
       }
     }
-    const int32_t* gpos = a.pos[ORDER - 1] + fs;
-    const int32_t* gcrd = a.crd[ORDER - 2] + fs;
-    for (int x = lane; x <= W; x += 32) s_pos[x] = gpos[x];
-    for (int x = lane; x < W; x += 32) s_fcrd[x] = gcrd[x];
+    stage_window(a.pos[ORDER - 1] + fs, a.crd[ORDER - 2] + fs, W, lane, s_pos, s_fcrd);
   }
   __syncwarp();
 
@@ -1423,18 +1502,8 @@ __global__ void __launch_bounds__(256, 1) mttkrp_tma_kernel(const __grid_constan
     const uint64_t polF = policy_evict_first();
     const int n4 = (cnt + 3) >> 2;
     const int32_t* gl = a.crd[ORDER - 1] + ustart64;
-    for (int c = lane; c < n4; c += 32) {
-      const int t = (4 * c) >> a.lgG;
-      reinterpret_cast<int4*>(s_lc)[c + t] = ld_stream_i4(gl + 4 * c, polF);
-      if constexpr (VB == 4)
-        reinterpret_cast<float4*>(s_val)[c + t] = ld_stream_f4(static_cast<const float*>(a.vals) + ustart64 + 4 * c, polF);
-      else
-        reinterpret_cast<uint2*>(s_val)[c + 2 * t] = ld_stream_u2(static_cast<const uint16_t*>(a.vals) + ustart64 + 4 * c, polF);
-    }
-    const int32_t* gpos = a.pos[ORDER - 1] + fs;
-    const int32_t* gcrd = a.crd[ORDER - 2] + fs;
-    for (int x = lane; x <= W; x += 32) s_pos[x] = gpos[x];
-    for (int x = lane; x < W; x += 32) s_fcrd[x] = gcrd[x];
+    stage_runs<VB>(gl, a.vals, ustart64, n4, a.lgG - 2, lane, s_lc, s_val, polF);
+    stage_window(a.pos[ORDER - 1] + fs, a.crd[ORDER - 2] + fs, W, lane, s_pos, s_fcrd);
   }
   __syncwarp();
 

@@ -63,16 +63,8 @@ __global__ void __launch_bounds__(256, 4) ttv_lean_kernel(const __grid_constant_
     const uint64_t polF = policy_evict_first();
     const int n4 = (cnt + 3) >> 2;
     const int32_t* gl = a.crd[1] + ustart64;
-    for (int c = lane; c < n4; c += 32) {
-      const int t = c / (NPT / 4);
-      reinterpret_cast<int4*>(s_lc)[c + t] = ld_stream_i4(gl + 4 * c, polF);
-      if constexpr (VB == 4)
-        reinterpret_cast<float4*>(s_val)[c + t] = ld_stream_f4(static_cast<const float*>(a.vals) + ustart64 + 4 * c, polF);
-      else
-        reinterpret_cast<uint2*>(s_val)[c + 2 * t] = ld_stream_u2(static_cast<const uint16_t*>(a.vals) + ustart64 + 4 * c, polF);
-    }
-    const int32_t* gpos = a.pos[1] + fs;
-    for (int x = lane; x <= W; x += 32) s_pos[x] = gpos[x];
+    stage_runs<VB>(gl, a.vals, ustart64, n4, 2, lane, s_lc, s_val, polF);  // runs of NPT = 16 entries
+    stage_ints(a.pos[1] + fs, W + 1, lane, s_pos);
   }
   __syncwarp();
 
