@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--no-errors", action="store_true")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the TTV (50M nonzeros) and 4-mode MTTKRP (80M nonzeros) measurements")
+    ap.add_argument("--only", default=None, choices=["ttv", "mttkrp4"],
+                    help="run only this secondary measurement and print its JSON (for profiling)")
     return ap.parse_args()
 
 
@@ -499,6 +501,9 @@ def run_reference_arm(args, rank, world):
 
 def main():
     args = parse()
+    if args.only:
+        print(json.dumps({"ttv": secondary_ttv, "mttkrp4": secondary_mttkrp4}[args.only](args)))
+        return
     rank, world, d = dist_setup(args.gpus)
     if args.impl == "reference":
         out = run_reference_arm(args, rank, world)

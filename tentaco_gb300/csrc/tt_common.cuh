@@ -64,6 +64,15 @@ __device__ __forceinline__ float4 ld_stream_f4(const float* p, uint64_t pol) {
                : "l"(p), "l"(pol));
   return r;
 }
+// 16 bytes of a stream that the lane's neighbour reads the other half sector of
+// in its next load: L1 allocation kept, L2 evict_first.
+__device__ __forceinline__ uint4 ld_stream_l1_u4(const void* p, uint64_t pol) {
+  uint4 r;
+  asm volatile("ld.global.nc.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "l"(p), "l"(pol));
+  return r;
+}
 __device__ __forceinline__ uint2 ld_stream_u2(const void* p, uint64_t pol) {
   uint2 r;
   asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0,%1}, [%2], %3;"

@@ -62,25 +62,13 @@ cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-template <int VK>
-cudaError_t launch_ttv_k(const WalkArgs& a, int grid, size_t smem, cudaStream_t s) {
-  static size_t configured = 48 * 1024;
-  if (smem > configured) {
-    cudaError_t e = cudaFuncSetAttribute(ttv_lean_kernel<VK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = smem;
-  }
-  ttv_lean_kernel<VK><<<grid, 256, smem, s>>>(a);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_ttv(const WalkArgs& a, int vals_kind, cudaStream_t s) {
   if (a.nblocks == 0) return cudaSuccess;
   const int grid = (a.nblocks + 7) / 8;  // one warp per unit, 8 warps per block
-  const size_t smem = (size_t)8 * ttv_warp_bytes(vals_kind == kF32 ? 4 : 2);
-  if (vals_kind == kB16) return launch_ttv_k<kB16>(a, grid, smem, s);
-  if (vals_kind == kH16) return launch_ttv_k<kH16>(a, grid, smem, s);
-  return launch_ttv_k<kF32>(a, grid, smem, s);
+  if (vals_kind == kB16) ttv_stream_kernel<kB16><<<grid, 256, 0, s>>>(a);
+  else if (vals_kind == kH16) ttv_stream_kernel<kH16><<<grid, 256, 0, s>>>(a);
+  else ttv_stream_kernel<kF32><<<grid, 256, 0, s>>>(a);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

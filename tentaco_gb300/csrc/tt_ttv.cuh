@@ -5,140 +5,157 @@
 // Replaces the reference's ttv_kernel / ttv_csf_gpu_taco
 // (tensor_kernels/ttv_csf_gpu_taco.h:2-121).  The output is indexed by fiber
 // position, as in the reference (A_vals[j_pos] there), so only the last two CSF
-// levels are read: the kernels see a 2-level CSF (WalkArgs with pos[1] = fiber
+// levels are read: the kernel sees a 2-level CSF (WalkArgs with pos[1] = fiber
 // starts, crd[1] = last-mode coordinates, nrows = fibers, one output column).
 // Unlike the reference, every output is written exactly once (no memset, no
 // float atomics):
-//   * a warp owns kTtvNpt * 32 consecutive nonzeros (its work unit); it stages
-//     their coordinates and values with 128-bit loads into shared memory (each
-//     lane's run padded by 16 bytes against bank conflicts) and the fiber
-//     window, then every lane walks kTtvNpt nonzeros with its x gathers issued
-//     before use;
-//   * fibers complete inside a lane are stored directly; the lanes' first and
-//     last partial fibers are merged by the warp's shuffle tree, and fibers
-//     shared between warps go through the unit carry slots and the two-level
-//     merge of tt_mttkrp.cuh (FP32 Kahan inside a segment of units, FP64 across).
-// x is read through L1 (it is small for the reference's workloads); the streams
-// are evict_first in L2.
+//   * a warp owns kTtvNpt * 32 consecutive nonzeros (its work unit) and lane L
+//     the kTtvNpt nonzeros from 16 L; the lane loads its coordinates and values
+//     straight into registers (16-byte loads, issued first: they depend on
+//     nothing), then its x entries;
+//   * the unit's fiber ends are a bit mask (bit e: nonzero e ends a fiber), set
+//     in shared memory from the fiber starts of the unit's window; a lane's first
+//     fiber is fs + the set bits before it (a warp prefix sum of popcounts);
+//   * the per-nonzero loop has no branches: an FMA, a predicated store of a fiber
+//     that starts and ends in the lane, and selects;
+//   * the lanes' first and last partial fibers are merged by the warp's shuffle
+//     tree; fibers shared between warps go through the unit carry slots and the
+//     two-level merge of tt_mttkrp.cuh (FP32 Kahan inside a segment of units,
+//     FP64 across).
+// Fibers are never empty (canonical CSF), so a nonzero ends at most one fiber.
 #pragma once
 #include "tt_mttkrp.cuh"
 
 namespace tt {
 
-constexpr int kTtvNpt = 16;  // nonzeros per lane
-
-// Shared memory of one warp: coordinate runs 32 x (kTtvNpt + 4) int32, value runs
-// 32 x (kTtvNpt * vbytes + 16) bytes, fiber window starts (at most 32*kTtvNpt + 2).
-__host__ __device__ inline size_t ttv_warp_bytes(int vbytes) {
-  const size_t pu = (size_t)32 * kTtvNpt;
-  size_t b = (size_t)32 * (kTtvNpt + 4) * 4 + (size_t)32 * ((size_t)kTtvNpt * vbytes + 16);
-  b += (pu + 2) * 4;
-  return (b + 15) & ~(size_t)15;
-}
+constexpr int kTtvNpt = 16;  // nonzeros per lane (the mask holds 16 bits per lane)
 
 #ifndef TT_ARGS_ONLY
 template <int VK>
-__global__ void __launch_bounds__(256, 4) ttv_lean_kernel(const __grid_constant__ WalkArgs a) {
-  constexpr int VB = VK == kF32 ? 4 : 2;
+__global__ void __launch_bounds__(256, 4) ttv_stream_kernel(const __grid_constant__ WalkArgs a) {
   constexpr int NPT = kTtvNpt;
-  using WK = Walk<3, kFP32, 1, 1>;  // the merge helpers for one output column
-  extern __shared__ __align__(16) unsigned char smem[];
+  static_assert(NPT == 16, "a lane's fiber-end bits are half a mask word");
+  constexpr int NW = VK == kF32 ? NPT : NPT / 2;  // value words per lane
+  using WK = Walk<3, kFP32, 1, 1>;                // the merge helpers for one output column
+  __shared__ uint32_t s_mask[8][NPT];             // per warp: 32 * NPT bits
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int u = blockIdx.x * (blockDim.x >> 5) + warp;
   if (u >= a.nblocks) return;  // whole warp
   const int PU = a.P;          // 32 * NPT
-  unsigned char* ws = smem + (size_t)warp * ttv_warp_bytes(VB);
-  int32_t* s_lc = reinterpret_cast<int32_t*>(ws);
-  unsigned char* s_val = ws + (size_t)32 * (NPT + 4) * 4;
-  int32_t* s_pos = reinterpret_cast<int32_t*>(s_val + (size_t)32 * (NPT * VB + 16));
-
   const int64_t ustart64 = (int64_t)u * PU;
-  const int ustart = (int)ustart64;
   const int cnt = (int)min((int64_t)PU, a.nnz - ustart64);
-  const int fs = a.part[u];
-  const int W = a.part[u + 1] - fs + 1;
-  {
-    // chunk c (entries 4c..4c+3) belongs to lane c / (NPT/4); the arrays are padded
-    // so the rounded-up last chunk stays in bounds
-    const uint64_t polF = policy_evict_first();
-    const int n4 = (cnt + 3) >> 2;
-    const int32_t* gl = a.crd[1] + ustart64;
-    stage_runs<VB>(gl, a.vals, ustart64, n4, 2, lane, s_lc, s_val, polF);  // runs of NPT = 16 entries
-    stage_ints(a.pos[1] + fs, W + 1, lane, s_pos);
-  }
-  __syncwarp();
+  const int n = max(0, min(NPT, cnt - lane * NPT));
+  const int64_t s64 = ustart64 + (int64_t)lane * NPT;
 
-  WK wk(a, 0);
-  Summ<1> X;
-  X.h = kEmpty;
-  X.t = kNone;
-  const int s = ustart + lane * NPT;
-  if (s < ustart + cnt) {
-    const int n = min(NPT, ustart + cnt - s);
-    const int32_t* lc = s_lc + lane * (NPT + 4);
-    const unsigned char* vt = s_val + lane * (NPT * VB + 16);
-    const float* xv_g = static_cast<const float*>(a.fac[0]);
-    float xv[NPT], v[NPT];
-#pragma unroll
-    for (int k = 0; k < NPT; k++) xv[k] = __ldg(xv_g + (k < n ? lc[k] : 0));
-    if constexpr (VB == 4) {
+  // the lane's streams (runs start 64-byte aligned; the arrays are padded past
+  // the last 16-entry run, so a run that starts before nnz stays in bounds)
+  int32_t lc[NPT];
+  uint32_t vw[NW];
+  {
+    const uint64_t polF = policy_evict_first();
+    const int32_t* gl = a.crd[1] + s64;
+    if (n > 0) {
 #pragma unroll
       for (int k = 0; k < NPT / 4; k++) {
-        const float4 f = reinterpret_cast<const float4*>(vt)[k];
-        v[4 * k] = f.x; v[4 * k + 1] = f.y; v[4 * k + 2] = f.z; v[4 * k + 3] = f.w;
+        const uint4 c4 = ld_stream_l1_u4(gl + 4 * k, polF);
+        lc[4 * k] = (int32_t)c4.x; lc[4 * k + 1] = (int32_t)c4.y; lc[4 * k + 2] = (int32_t)c4.z; lc[4 * k + 3] = (int32_t)c4.w;
+      }
+      const unsigned char* gv = static_cast<const unsigned char*>(a.vals) + s64 * (VK == kF32 ? 4 : 2);
+#pragma unroll
+      for (int k = 0; k < NW / 4; k++) {
+        const uint4 w = ld_stream_l1_u4(gv + 16 * k, polF);
+        vw[4 * k] = w.x; vw[4 * k + 1] = w.y; vw[4 * k + 2] = w.z; vw[4 * k + 3] = w.w;
       }
     } else {
 #pragma unroll
-      for (int k = 0; k < NPT / 8; k++) {
-        const uint4 w = reinterpret_cast<const uint4*>(vt)[k];
-        const float2 p0 = pair16<VK>(w.x), p1 = pair16<VK>(w.y), p2 = pair16<VK>(w.z), p3 = pair16<VK>(w.w);
-        v[8 * k] = p0.x; v[8 * k + 1] = p0.y; v[8 * k + 2] = p1.x; v[8 * k + 3] = p1.y;
-        v[8 * k + 4] = p2.x; v[8 * k + 5] = p2.y; v[8 * k + 6] = p3.x; v[8 * k + 7] = p3.y;
-      }
+      for (int k = 0; k < NPT; k++) lc[k] = 0;
 #pragma unroll
-      for (int k = 0; k < NPT; k++) v[k] *= a.vscale;
+      for (int k = 0; k < NW; k++) vw[k] = 0u;
     }
-    // a nonzero ends at most one fiber (fibers are not empty): emit the fiber at
-    // its last nonzero, with a short body the compiler can predicate
-    int x = (int)search_le(s_pos, 0, W - 1, s);
-    int fend = s_pos[x + 1];
-    float acc = 0.f;
-    bool flushed = false, open = false;
-#pragma unroll
-    for (int k = 0; k < NPT; k++) {
-      if (k < n) {
-        acc = fmaf(v[k], xv[k], acc);
-        open = true;
-        if (s + k + 1 == fend) {  // fiber fs + x ends here
-          const int f = fs + x;
-          if (flushed) {
-            a.out[f] = acc;
-          } else {
-            X.h = f;
-            X.ha[0] = acc;
-          }
-          flushed = true;
-          open = false;
-          acc = 0.f;
-          x++;
-          // past the window's last fiber (the tensor's last unit) there is no next end
-          fend = x < W ? s_pos[x + 1] : INT32_MAX;
-        }
-      }
-    }
-    if (open) {  // the lane's last fiber continues past it
-      if (!flushed) {
-        X.h = fs + x;
-        X.t = kNone;
-        X.ha[0] = acc;
-      } else {
-        X.t = fs + x;
-        X.ta[0] = acc;
-      }
-    }  // else: X.h is the first fiber and nothing is left open (X.t stays kNone)
   }
+
+  // fiber window: fibers fs .. fs + W - 1; fiber fs + x ends at nonzero pos[fs + x + 1] - 1
+  const int fs = a.part[u];
+  const int fnext = a.part[u + 1];
+  const int W = fnext - fs + 1;
+  const int32_t* gpos = a.pos[1] + fs;
+  if (lane < NPT) s_mask[warp][lane] = 0u;
+  __syncwarp();
+  const int ustart = (int)ustart64;
+  for (int x0 = lane + 1; x0 <= W; x0 += 32 * 4) {
+    int e[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const int x = x0 + 32 * r;
+      e[r] = x <= W ? gpos[x] - 1 - ustart : -1;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+      if (e[r] >= 0 && e[r] < cnt) atomicOr(&s_mask[warp][e[r] >> 5], 1u << (e[r] & 31));
+  }
+  const int win0 = lane == 0 ? gpos[0] : 0;  // start of the unit's first fiber
+  __syncwarp();
+  const uint32_t m = (s_mask[warp][lane >> 1] >> ((lane & 1) * 16)) & 0xffffu;
+  int incl = __popc(m);
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += t;
+  }
+  const int f0 = fs + incl - __popc(m);  // fiber of the lane's first nonzero
+
+  float xv[NPT];
+  {
+    const float* xg = static_cast<const float*>(a.fac[0]);
+#pragma unroll
+    for (int k = 0; k < NPT; k++) xv[k] = __ldg(xg + lc[k]);
+  }
+  float v[NPT];
+  if constexpr (VK == kF32) {
+#pragma unroll
+    for (int k = 0; k < NPT; k++) v[k] = __uint_as_float(vw[k]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < NPT / 2; k++) {
+      const float2 p = pair16<VK>(vw[k]);
+      v[2 * k] = p.x * a.vscale;
+      v[2 * k + 1] = p.y * a.vscale;
+    }
+  }
+
+  float acc = 0.f, hacc = 0.f;
+  bool hset = false;
+  int f = f0;
+#pragma unroll
+  for (int k = 0; k < NPT; k++) {
+    if (k < n) {
+      acc = fmaf(v[k], xv[k], acc);
+      const bool e = (m >> k) & 1u;
+      if (e && hset) a.out[f] = acc;  // a fiber that started and ended in this lane
+      hacc = (e && !hset) ? acc : hacc;
+      hset = hset || e;
+      f += e ? 1 : 0;
+      acc = e ? 0.f : acc;
+    }
+  }
+  Summ<1> X;
+  X.t = kNone;
+  if (n <= 0) {
+    X.h = kEmpty;
+  } else if (!hset) {  // the lane lies inside one fiber
+    X.h = f0;
+    X.ha[0] = acc;
+  } else {
+    X.h = f0;
+    X.ha[0] = hacc;
+    if (!((m >> (n - 1)) & 1u)) {  // the lane's last fiber continues past it
+      X.t = f;
+      X.ta[0] = acc;
+    }
+  }
+  WK wk(a, 0);
   warp_tree(wk, X);
-  if (lane == 0) settle_unit(a, wk, X, (int64_t)fs, (int64_t)fs, (int64_t)s_pos[0], ustart64, a.part[u + 1], u, 0);
+  if (lane == 0) settle_unit(a, wk, X, (int64_t)fs, (int64_t)fs, (int64_t)win0, ustart64, fnext, u, 0);
 }
 #endif  // TT_ARGS_ONLY
 }  // namespace tt

@@ -69,6 +69,19 @@ def test_ttv_long_fiber():
     close(run_ttv(B, x), O.ttv(to_oracle(B), x))
 
 
+@pytest.mark.parametrize("nnz,mu", [(100_003, 0.0), (262_151, 1.0), (513, 0.5), (17, 0.0)])
+def test_ttv_short_fibers_ragged_units(nnz, mu):
+    """Many fibers of one or two nonzeros per lane, fibers crossing lanes and
+    units, and a last unit whose count is not a multiple of 16."""
+    B = tt.gen_lognormal_fibers((300, 200, 5000), nnz, mu, 1.2, 1 if nnz > 10_000 else 0, 3000, 11)
+    x = tt.gen_dense(5000, 1, 2, 5).ravel()
+    ref = O.ttv(to_oracle(B), x)
+    got = run_ttv(B, x)
+    close(got, ref)
+    assert np.array_equal(got, run_ttv(B, x))
+    close(run_ttv(B, x, prec="fp16"), ref, mx=3e-3, fr=1e-3)
+
+
 @pytest.fixture(scope="module")
 def legacy_case():
     B = tt.gen_zipf((600, 500, 700), (0.8, 0.5, 0), 60_000, seed=9)
