@@ -143,7 +143,9 @@ tt_status tt_plan_ttv(tt_plan* plan, const float* x, float* y, void* stream);
 
 /* Time every subsequent call's device work with CUDA events (default off). */
 tt_status tt_plan_set_timing(tt_plan* plan, int32_t enabled);
-/* Milliseconds of the last timed call (partition + clear + kernels); waits for it. */
+/* Milliseconds of the last timed call (clear + kernels); waits for it.  The
+ * work-unit partition of a single-slab plan depends only on the tensor and runs
+ * once, when the plan (or its variant) is set up; slab plans run it per pass. */
 float tt_plan_last_ms(tt_plan* plan);
 
 int32_t tt_plan_variant(const tt_plan* plan);

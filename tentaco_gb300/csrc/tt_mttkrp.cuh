@@ -1067,6 +1067,17 @@ __device__ __forceinline__ void put_row_value(const WalkArgs& a, int r, int j, d
   float* o = a.out + row * a.ldo + j;
   *o = (float)(a.accum ? v + (double)*o : v);
 }
+// The same for a Kahan pair (s, c) with |c| <= ulp(s): without slab accumulation
+// the FP32 sum s + c rounds the exact value once, which is what the FP64 route
+// gives (the FP64 sum of the pair is exact), and it keeps the FP64 pipe free.
+__device__ __forceinline__ void put_row_pair(const WalkArgs& a, int r, int j, float s, float c) {
+  if (a.accum) {
+    put_row_value(a, r, j, (double)s + (double)c);
+    return;
+  }
+  const int64_t row = a.crd[0] ? (int64_t)a.crd[0][r] : (int64_t)r;
+  a.out[row * a.ldo + j] = __fadd_rn(s, c);
+}
 
 template <int ORDER>  // (the fold itself does not depend on the order)
 __global__ void __launch_bounds__(256, 2) seg_fold_kernel(const __grid_constant__ WalkArgs a) {
@@ -1092,15 +1103,14 @@ __global__ void __launch_bounds__(256, 2) seg_fold_kernel(const __grid_constant_
     int runs = 0;
     auto close_run = [&]() {
       runs++;
-      const double v = (double)acc + (double)comp;
       if (!cur_before && !cur_after) {
-        if (col < a.R) put_row_value(a, cur, col, v);
+        if (col < a.R) put_row_pair(a, cur, col, acc, comp);
       } else if (cur_before) {  // necessarily the segment's first run
         if (c0 == 0) { sfirst = cur; sflags |= 1; if (cur_after) { slast = cur; sflags |= 2; } }
-        if (live) sc0[col] = v;
+        if (live) sc0[col] = (double)acc + (double)comp;
       } else {  // cur_after only: the segment's last run (slot 0 when it is the only run)
         if (c0 == 0) { slast = cur; sflags |= 2; }
-        if (live) (first_run ? sc0 : sc1)[col] = v;
+        if (live) (first_run ? sc0 : sc1)[col] = (double)acc + (double)comp;
       }
       if (c0 == 0 && first_run && sfirst < 0) sfirst = cur;
       first_run = false;

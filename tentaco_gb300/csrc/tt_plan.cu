@@ -221,6 +221,35 @@ tt_status alloc_walk_scratch(tt_plan* p, int P) {
 }
 
 WalkArgs walk_args(const tt_plan* p, float* A, int q);
+WalkArgs ttv_args(const tt_plan* p, const float* x, float* y);
+
+// Compute the work-unit partition of a single-slab plan once, on the plan's
+// stream, timed with events (the legacy timer adds it back, so that it covers
+// what the reference's per-call timer covers); later calls reuse it.
+tt_status prepare_partition(tt_plan* p) {
+  p->part_ready = false;
+  p->part_ms = 0.f;
+  if (p->slabs != 1 || p->nnz == 0) return TT_OK;
+  const WalkArgs a = p->op == TT_OP_TTV ? ttv_args(p, nullptr, nullptr) : walk_args(p, nullptr, 0);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return set_error(TT_ERR_CUDA, "partition timer");
+  }
+  cudaError_t e = cudaEventRecord(e0, p->stream);
+  if (e == cudaSuccess) e = launch_partition(p->op == TT_OP_TTV ? 2 : p->order, a, p->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, p->stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return set_error(TT_ERR_CUDA, "partition: %s", cudaGetErrorString(e));
+  p->part_ms = ms;
+  p->part_ready = true;
+  return TT_OK;
+}
 
 tt_status use_variant(tt_plan* p, int id) {
   VariantSpec v = variant_spec(id);
@@ -236,6 +265,7 @@ tt_status use_variant(tt_plan* p, int id) {
   if (!p->launcher) return set_error(TT_ERR_UNSUPPORTED, "variant %d not compiled for this shape", id);
   tt_status s = alloc_walk_scratch(p, p->P);
   if (s != TT_OK) return s;
+  p->part_ready = false;
   p->wcap = 1;
   if (p->staged == 1 && p->nnz > 0) {
     // size the window-row region from this tensor's partition (computed once here)
@@ -255,7 +285,7 @@ tt_status use_variant(tt_plan* p, int id) {
     if (need > kSmemLimit)
       return set_error(TT_ERR_UNSUPPORTED, "variant %d needs %zu bytes of shared memory for this tensor", id, need);
   }
-  return TT_OK;
+  return prepare_partition(p);
 }
 
 // Arguments of one walk pass over slab q (the whole tensor when slabs == 1).
@@ -348,7 +378,7 @@ tt_status run_mttkrp(tt_plan* p, float* A, cudaStream_t st) {
       const tt_status s2 = encode_leaf_tmap(p, &a.tmap);
       if (s2 != TT_OK) return s2;
     }
-    CK(launch_partition(p->order, a, st));
+    if (!p->part_ready) CK(launch_partition(p->order, a, st));
     if (p->timing && q == first) CK(cudaEventRecord(p->evk0, st));
     CK(p->launcher(a, a.nblocks, p->tb, smem, st));
     if (p->timing && q == last) CK(cudaEventRecord(p->evk1, st));
@@ -357,12 +387,9 @@ tt_status run_mttkrp(tt_plan* p, float* A, cudaStream_t st) {
   return TT_OK;
 }
 
-tt_status run_ttv(tt_plan* p, const float* x, float* y, cudaStream_t st) {
-  if (p->nnz == 0) {
-    if (p->nfib_last > 0) CK(cudaMemsetAsync(y, 0, sizeof(float) * (size_t)p->nfib_last, st));
-    return TT_OK;
-  }
-  // the last two levels as a 2-level CSF: "rows" are the fibers, one output column
+// TTV sees the last two levels as a 2-level CSF: "rows" are the fibers, one
+// output column.
+WalkArgs ttv_args(const tt_plan* p, const float* x, float* y) {
   WalkArgs a{};
   a.pos[1] = p->d_pos[p->order - 1];
   a.crd[1] = p->d_crd[p->order - 1];
@@ -383,7 +410,16 @@ tt_status run_ttv(tt_plan* p, const float* x, float* y, cudaStream_t st) {
   a.P = p->P;
   a.G = kTtvNpt;
   a.nblocks = p->nblocks;
-  CK(launch_partition(2, a, st));
+  return a;
+}
+
+tt_status run_ttv(tt_plan* p, const float* x, float* y, cudaStream_t st) {
+  if (p->nnz == 0) {
+    if (p->nfib_last > 0) CK(cudaMemsetAsync(y, 0, sizeof(float) * (size_t)p->nfib_last, st));
+    return TT_OK;
+  }
+  const WalkArgs a = ttv_args(p, x, y);
+  if (!p->part_ready) CK(launch_partition(2, a, st));
   if (p->timing) CK(cudaEventRecord(p->evk0, st));
   CK(launch_ttv(a, val_kind(p->prec), st));
   if (p->timing) CK(cudaEventRecord(p->evk1, st));
@@ -664,6 +700,7 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
     p->P = 32 * kTtvNpt;
     p->nblocks = (int)((p->nnz + p->P - 1) / p->P);
     if ((s = alloc_walk_scratch(p, p->P)) != TT_OK) return fail(s);
+    if ((s = prepare_partition(p)) != TT_OK) return fail(s);
   }
   if (cudaStreamSynchronize(st) != cudaSuccess) return fail(set_error(TT_ERR_CUDA, "plan upload: %s", cudaGetErrorString(cudaGetLastError())));
   *out = p;
@@ -939,7 +976,9 @@ TT_EXPORT tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
   tt_plan_set_timing(p, 1);
   if ((s = tt_plan_set_factors(p, (const float* const*)dfac.data(), nullptr)) != TT_OK) { cleanup(); return s; }
   if ((s = tt_plan_mttkrp(p, dA, nullptr)) != TT_OK) { cleanup(); return s; }
-  g_legacy_ms.store(tt_plan_last_ms(p));
+  // the reference times partition + clear + kernel per call; the plan ran its
+  // partition once at creation
+  g_legacy_ms.store(tt_plan_last_ms(p) + (p->part_ready ? p->part_ms : 0.f));
   if (cudaMemcpy(A->vals, dA, abytes, cudaMemcpyDeviceToHost) != cudaSuccess) {
     tt_status e = set_error(TT_ERR_CUDA, "download A: %s", cudaGetErrorString(cudaGetLastError()));
     cleanup();
@@ -968,7 +1007,7 @@ TT_EXPORT tt_status tt_ttv_host(taco_tensor_t* y, const taco_tensor_t* B, const 
   if (cudaMemcpy(dx, x->vals, sizeof(float) * (size_t)nx, cudaMemcpyHostToDevice) != cudaSuccess) { cleanup(); return set_error(TT_ERR_CUDA, "upload x"); }
   tt_plan_set_timing(p, 1);
   if ((s = tt_plan_ttv(p, dx, dy, nullptr)) != TT_OK) { cleanup(); return s; }
-  g_legacy_ms.store(tt_plan_last_ms(p));
+  g_legacy_ms.store(tt_plan_last_ms(p) + (p->part_ready ? p->part_ms : 0.f));
   if (cudaMemcpy(y->vals, dy, sizeof(float) * (size_t)ny, cudaMemcpyDeviceToHost) != cudaSuccess) { cleanup(); return set_error(TT_ERR_CUDA, "download y"); }
   cleanup();
   return TT_OK;

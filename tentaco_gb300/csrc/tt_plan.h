@@ -48,6 +48,10 @@ struct tt_plan {
   int32_t* d_err = nullptr;  // [0]: kernel error word, [1]: scratch for the window size
   tt::WalkLauncher launcher = nullptr;
   int32_t* d_part = nullptr;
+  // the partition depends only on the CSF and the unit size: a single-slab plan
+  // computes it once per variant (part_ready) and times it (part_ms)
+  bool part_ready = false;
+  float part_ms = 0.f;
   float* d_carry = nullptr;
   int32_t* d_meta = nullptr;     // MTTKRP: 4 ints per work unit
   double* d_segcarry = nullptr;  // MTTKRP: 2 FP64 rows per segment of work units
