@@ -1130,35 +1130,45 @@ __global__ void __launch_bounds__(256, 2) seg_fold_kernel(const __grid_constant_
       acc = t;
       cur_after = after;
     };
-    constexpr int kHalf = kSeg / 2;
-    for (int h = 0; h < kSeg; h += kHalf) {
-      // both carry slots of the next kHalf units, loaded before any is used
-      float v0[kHalf], v1[kHalf];
+    // units in groups of kG, the loop kept rolled (a small body stays in the
+    // instruction cache); the next group's carries are loaded before the current
+    // group is folded
+    constexpr int kG = 4;
+    auto load_group = [&](int g, float (&w0)[kG], float (&w1)[kG]) {
 #pragma unroll
-      for (int k = 0; k < kHalf; k++) {
-        v0[k] = 0.f;
-        v1[k] = 0.f;
-        if (h + k < n && live) {
-          const float* c = a.carry + (size_t)(2 * (u0 + h + k)) * rp + col;
-          v0[k] = c[0];
-          v1[k] = c[rp];
+      for (int k = 0; k < kG; k++) {
+        const int uu = g * kG + k;
+        w0[k] = 0.f;
+        w1[k] = 0.f;
+        if (uu < n && live) {
+          const float* c = a.carry + (size_t)(2 * (u0 + uu)) * rp + col;
+          w0[k] = c[0];
+          w1[k] = c[rp];
         }
       }
+    };
+    float c0v[kG], c1v[kG];
+    load_group(0, c0v, c1v);
+#pragma unroll 1
+    for (int g = 0; g * kG < n; g++) {
+      float n0[kG], n1[kG];
+      load_group(g + 1, n0, n1);
 #pragma unroll
-      for (int k = 0; k < kHalf; k++) {
-        if (h + k < n) {
-          const int mx = __shfl_sync(0xffffffffu, mine.x, h + k);
-          const int my = __shfl_sync(0xffffffffu, mine.y, h + k);
-          const int mz = __shfl_sync(0xffffffffu, mine.z, h + k);
+      for (int k = 0; k < kG; k++) {
+        const int uu = g * kG + k;
+        if (uu < n) {  // warp-uniform
+          const int mx = __shfl_sync(0xffffffffu, mine.x, uu);
+          const int my = __shfl_sync(0xffffffffu, mine.y, uu);
+          const int mz = __shfl_sync(0xffffffffu, mine.z, uu);
           const bool hb = mz & 1, la = mz & 2, single = mz & 4;
-          if (single) {
-            if (hb || la) entry(mx, v0[k], hb, la);
-          } else {
-            if (hb) entry(mx, v0[k], true, false);
-            if (la) entry(my, v1[k], false, true);
-          }
+          // slot 0: the unit's first row (a single-row unit's only entry); slot 1:
+          // its last row when that differs
+          if (single ? (hb || la) : hb) entry(mx, c0v[k], hb, single && la);
+          if (!single && la) entry(my, c1v[k], false, true);
         }
       }
+#pragma unroll
+      for (int k = 0; k < kG; k++) { c0v[k] = n0[k]; c1v[k] = n1[k]; }
     }
     if (cur >= 0) close_run();
     if (c0 == 0) {
