@@ -141,6 +141,11 @@ tt_status tt_plan_mttkrp(tt_plan* plan, float* A, void* stream);
  * fiber of level order-2 (tt_plan_num_fibers), overwritten. */
 tt_status tt_plan_ttv(tt_plan* plan, const float* x, float* y, void* stream);
 
+/* Plans and one-shot calls take device memory from a stream-ordered pool per
+ * device that keeps freed memory for the next plan; this returns what no live
+ * plan holds to the driver. */
+tt_status tt_release_cached_memory(void);
+
 /* Time every subsequent call's device work with CUDA events (default off). */
 tt_status tt_plan_set_timing(tt_plan* plan, int32_t enabled);
 /* Milliseconds of the last timed call (clear + kernels); waits for it.  The

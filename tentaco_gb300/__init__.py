@@ -125,6 +125,7 @@ def lib():
         "tt_mlp_adam": (S, [_P, _P, _P, _P, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
                             C.c_int32, _P]),
         "tt_selector_load": (S, [C.c_char_p]),
+        "tt_release_cached_memory": (S, []),
         "tt_selector_models": (C.c_int32, []),
         "tt_selector_scores": (S, [_TP, C.c_int32, S, C.POINTER(C.c_float), C.c_int32]),
         "ttv_csf_gpu_taco": (None, [_TP, _TP, _TP]),
@@ -544,6 +545,11 @@ class Mlp:
             check(L.tt_mlp_adam(self.params.ptr, self.grads.ptr, self.m.ptr, self.v.ptr, self.np, lr, beta1,
                                 beta2, eps, weight_decay, step, None))
         return self.params.to_array((self.np,)), losses
+
+
+def release_cached_memory() -> None:
+    """Return the device memory the library's pool keeps for later plans."""
+    check(lib().tt_release_cached_memory())
 
 
 def selector_load(path=None) -> None:

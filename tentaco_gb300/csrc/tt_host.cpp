@@ -105,7 +105,7 @@ tt_status csf_view(const taco_tensor_t* B, CsfView* v) {
   return TT_OK;
 }
 
-tt_status csf_check(const CsfView& v) {
+tt_status csf_check_root(const CsfView& v) {
   if (!v.dense_root) {
     for (int64_t r = 0; r < v.nroot; r++) {
       if (v.root_crd[r] < 0 || v.root_crd[r] >= v.dims[0])
@@ -115,6 +115,14 @@ tt_status csf_check(const CsfView& v) {
     }
   }
   if (v.nnz > 0x7fffffffLL) return set_error(TT_ERR_UNSUPPORTED, "nnz %lld exceeds int32 positions", (long long)v.nnz);
+  for (int l = 1; l < v.order; l++)
+    if (v.pos[l][0] != 0) return set_error(TT_ERR_INVALID_CSF, "level %d pos[0] = %d", l, v.pos[l][0]);
+  return TT_OK;
+}
+
+tt_status csf_check(const CsfView& v) {
+  tt_status s = csf_check_root(v);
+  if (s != TT_OK) return s;
   for (int l = 1; l < v.order; l++) {
     const int32_t* pos = v.pos[l];
     const int32_t* crd = v.crd[l];
@@ -141,6 +149,16 @@ tt_status csf_check(const CsfView& v) {
     if (bad.load()) return set_error(TT_ERR_INVALID_CSF, "level %d fiber %lld: %s", l, (long long)where.load(), why[bad.load()]);
   }
   return TT_OK;
+}
+
+tt_status csf_check_error(int level, uint64_t word) {
+  if (word == UINT64_MAX) return TT_OK;
+  const int code = (int)(word & 7u);
+  const long long at = (long long)(word >> 3);
+  const char* why[] = {"", "pos decreasing", "empty inner fiber", "crd out of range",
+                       "crd not strictly increasing in a fiber"};
+  return set_error(TT_ERR_INVALID_CSF, "level %d %s %lld: %s", level, code <= 2 ? "fiber" : "position", at,
+                   why[code >= 1 && code <= 4 ? code : 0]);
 }
 
 // ---------------------------------------------------------------------------

@@ -51,7 +51,13 @@ struct CsfView {
 // Read the CSF arrays of B (no validation).
 tt_status csf_view(const taco_tensor_t* B, CsfView* v);
 // Full validation (monotone pos, sorted distinct crd in range, non-empty inner fibers).
+// Full host check of the structure (every level, in parallel over fibers).
 tt_status csf_check(const CsfView& v);
+// What the device check (launch_csf_check) leaves to the host: the compressed
+// root's coordinates, the nnz limit, pos[0] of every level.
+tt_status csf_check_root(const CsfView& v);
+// Message for a device check result ((index << 3) | code, UINT64_MAX: none).
+tt_status csf_check_error(int level, uint64_t word);
 
 // A dense-root CSF split into leaf-mode slabs (leaf coordinate c is in slab
 // c / width).  Each slab is a CSF with every row; its leaf arrays are the run

@@ -32,6 +32,12 @@ cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s);
 cudaError_t launch_ttv(const WalkArgs& a, int vals_kind, cudaStream_t s);
 
 // Column max |x| of a rows x cols FP32 row-major matrix into colmax (cols floats, zeroed here).
+// Structure check of one CSF level on device copies: pos (nf + 1 fiber starts;
+// inner != 0: fibers must not be empty), crd (n coordinates below dim); starts:
+// scratch of n / 32 + 1 words; err[0..1]: pos / crd violation words, set to
+// UINT64_MAX by the caller (see tt_misc.cu).
+cudaError_t launch_csf_check(const int32_t* pos, int64_t nf, int inner, const int32_t* crd, int64_t n, int32_t dim,
+                             uint32_t* starts, unsigned long long* err, cudaStream_t s);
 cudaError_t launch_colmax(const float* x, int64_t rows, int cols, float* colmax, cudaStream_t s);
 // scale[j] = 2^(target_exp - floor(log2(colmax[j]))) (1 where colmax is 0 or not finite);
 // inv[j] = 1/scale[j].  Both exact powers of two.

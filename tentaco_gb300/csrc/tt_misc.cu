@@ -1,5 +1,6 @@
 // tt_misc.cu -- partition, TTV and storage-conversion kernels of libtentaco_gb300.
 #include <cuda_bf16.h>
+#include <algorithm>
 #include <cuda_fp16.h>
 #include "tt_kernels.h"
 #include "tt_mttkrp.cuh"
@@ -68,6 +69,49 @@ cudaError_t launch_ttv(const WalkArgs& a, int vals_kind, cudaStream_t s) {
   if (vals_kind == kB16) ttv_stream_kernel<kB16><<<grid, 256, 0, s>>>(a);
   else if (vals_kind == kH16) ttv_stream_kernel<kH16><<<grid, 256, 0, s>>>(a);
   else ttv_stream_kernel<kF32><<<grid, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// CSF structure check of one level on the plan's device copies (after upload;
+// the host checks the compressed root and every pos[0]).  err[0] keeps the first
+// pos violation, err[1] the first crd violation, each as (index << 3) | code
+// (atomicMin: the lowest index wins; UINT64_MAX: none):
+//   1 pos[f + 1] < pos[f]   2 empty inner fiber   (index: fiber f)
+//   3 crd outside [0, dim)  4 crd not increasing inside a fiber   (index: position p)
+// The pos pass marks every fiber start in [0, n) in a bit mask; the crd pass
+// compares crd[p] with crd[p - 1] where p starts no fiber.  Every access is in
+// bounds whatever the arrays hold.
+// ---------------------------------------------------------------------------
+__global__ void csf_pos_check_kernel(const int32_t* __restrict__ pos, int64_t nf, int64_t n, int inner,
+                                     uint32_t* __restrict__ starts, unsigned long long* __restrict__ err) {
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t a = pos[f], b = pos[f + 1];
+    if (b < a) atomicMin(err, ((unsigned long long)f << 3) | 1ull);
+    else if (inner && b == a) atomicMin(err, ((unsigned long long)f << 3) | 2ull);
+    if (a >= 0 && (int64_t)a < n) atomicOr(&starts[a >> 5], 1u << (a & 31));
+  }
+}
+
+__global__ void csf_crd_check_kernel(const int32_t* __restrict__ crd, int64_t n, int32_t dim,
+                                     const uint32_t* __restrict__ starts, unsigned long long* __restrict__ err) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t c = crd[p];
+    if (c < 0 || c >= dim) {
+      atomicMin(err, ((unsigned long long)p << 3) | 3ull);
+    } else if (p > 0 && !((starts[p >> 5] >> (p & 31)) & 1u) && c <= crd[p - 1]) {
+      atomicMin(err, ((unsigned long long)p << 3) | 4ull);
+    }
+  }
+}
+
+cudaError_t launch_csf_check(const int32_t* pos, int64_t nf, int inner, const int32_t* crd, int64_t n, int32_t dim,
+                             uint32_t* starts, unsigned long long* err, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(starts, 0, sizeof(uint32_t) * (size_t)((n + 31) / 32 + 1), s);
+  if (e != cudaSuccess) return e;
+  auto grid = [](int64_t m) { return (int)std::min<int64_t>((m + 255) / 256, 152 * 16); };
+  if (nf > 0) csf_pos_check_kernel<<<grid(nf), 256, 0, s>>>(pos, nf, n, inner, starts, err);
+  if (n > 0) csf_crd_check_kernel<<<grid(n), 256, 0, s>>>(crd, n, dim, starts, err + 1);
   return cudaGetLastError();
 }
 

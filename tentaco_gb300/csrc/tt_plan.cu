@@ -163,37 +163,78 @@ namespace {
 
 std::atomic<float> g_legacy_ms{-1.0f};
 
+// ---------------------------------------------------------------------------
+// Device memory of plans and one-shot calls comes from one stream-ordered pool
+// per device, owned by the library, that keeps freed memory for reuse (release
+// threshold unlimited): repeated calls on tensors of similar size then pay no
+// cudaMalloc / cudaFree.  tt_release_cached_memory() hands it back.
+// ---------------------------------------------------------------------------
+constexpr int kMaxDevices = 64;
+std::mutex g_pool_mu;
+cudaMemPool_t g_pool[kMaxDevices] = {};
+
+cudaError_t pool_of(cudaMemPool_t* out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  if (!g_pool[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool;
+    if ((e = cudaMemPoolCreate(&pool, &props)) != cudaSuccess) return e;
+    uint64_t keep = UINT64_MAX;
+    if ((e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess) {
+      cudaMemPoolDestroy(pool);
+      return e;
+    }
+    g_pool[dev] = pool;
+  }
+  *out = g_pool[dev];
+  return cudaSuccess;
+}
+
+// Stream-ordered allocation from the pool: usable on `st` at once, on other
+// streams after `st` is synchronised.
+cudaError_t pool_alloc(void** ptr, size_t bytes, cudaStream_t st) {
+  cudaMemPool_t pool;
+  cudaError_t e = pool_of(&pool);
+  if (e != cudaSuccess) return e;
+  return cudaMallocFromPoolAsync(ptr, bytes, pool, st);
+}
+
 template <typename T>
 tt_status dev_alloc(tt_plan* p, T** ptr, size_t count) {
   *ptr = nullptr;
   if (count == 0) count = 1;
-  CK(cudaMalloc((void**)ptr, count * sizeof(T)));
+  CK(pool_alloc((void**)ptr, count * sizeof(T), p->stream));
   p->allocs.push_back((void*)*ptr);
   p->device_bytes += (int64_t)(count * sizeof(T));
   return TT_OK;
 }
 
+// Like cudaFree, waits for the device before the memory goes back to the pool.
 void dev_free(tt_plan* p, void* ptr) {
   if (!ptr) return;
   auto it = std::find(p->allocs.begin(), p->allocs.end(), ptr);
   if (it != p->allocs.end()) p->allocs.erase(it);
-  cudaFree(ptr);
+  cudaDeviceSynchronize();
+  cudaFreeAsync(ptr, p->stream);
 }
 
-
-// 2^-floor(log2(m)) for m > 0 finite, else 1.
-float pow2_scale_for(float m) {
-  if (!(m > 0.f) || !std::isfinite(m)) return 1.f;
-  int e;
-  std::frexp(m, &e);  // m = f * 2^e, f in [0.5, 1)
-  return std::ldexp(1.f, -(e - 1));
-}
 
 int64_t pad16(int64_t n) { return ((n + 15) / 16) * 16 + 16; }
 
 tt_status alloc_walk_scratch(tt_plan* p, int P) {
   const int64_t nb = (p->nnz + P - 1) / P;
   if (nb > p->scratch_blocks) {
+    struct SyncAtEnd {  // pool memory becomes usable on every stream
+      cudaStream_t st;
+      ~SyncAtEnd() { cudaStreamSynchronize(st); }
+    } sync_at_end{p->stream};
     dev_free(p, p->d_part);
     dev_free(p, p->d_carry);
     p->d_part = nullptr;
@@ -248,6 +289,34 @@ tt_status prepare_partition(tt_plan* p) {
   if (e != cudaSuccess) return set_error(TT_ERR_CUDA, "partition: %s", cudaGetErrorString(e));
   p->part_ms = ms;
   p->part_ready = true;
+  return TT_OK;
+}
+
+// Structure check of every level on the plan's device copies (launch_csf_check),
+// before anything reads the arrays.
+tt_status device_csf_check(tt_plan* p, const CsfView& v, cudaStream_t st) {
+  const int L = v.order - 1;
+  int64_t maxn = 1;
+  for (int l = 1; l <= L; l++) maxn = std::max<int64_t>(maxn, v.count[l]);
+  uint32_t* starts = nullptr;
+  unsigned long long* err = nullptr;
+  CK(pool_alloc((void**)&starts, sizeof(uint32_t) * (size_t)((maxn + 31) / 32 + 1), st));
+  cudaError_t e = pool_alloc((void**)&err, sizeof(unsigned long long) * 2 * (size_t)L, st);
+  unsigned long long h[2 * TT_MAX_ORDER];
+  if (e == cudaSuccess) e = cudaMemsetAsync(err, 0xff, sizeof(unsigned long long) * 2 * (size_t)L, st);
+  for (int l = 1; l <= L && e == cudaSuccess; l++)
+    e = launch_csf_check(p->d_pos[l], v.count[l - 1], l >= 2 ? 1 : 0, p->d_crd[l], v.count[l], v.dims[l], starts,
+                         err + 2 * (l - 1), st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, err, sizeof(unsigned long long) * 2 * (size_t)L, cudaMemcpyDeviceToHost, st);
+  if (err) cudaFreeAsync(err, st);
+  cudaFreeAsync(starts, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return set_error(TT_ERR_CUDA, "structure check: %s", cudaGetErrorString(e));
+  for (int l = 1; l <= L; l++) {
+    tt_status s = csf_check_error(l, h[2 * (l - 1)]);  // pos first: the crd pass trusts its marks
+    if (s == TT_OK) s = csf_check_error(l, h[2 * (l - 1) + 1]);
+    if (s != TT_OK) return s;
+  }
   return TT_OK;
 }
 
@@ -503,7 +572,9 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
   CsfView v;
   tt_status s = csf_view(B, &v);
   if (s != TT_OK) return s;
-  if ((s = csf_check(v)) != TT_OK) return s;
+  // the root and pos[0] here; the levels on the host only for slab plans (built
+  // from the host arrays) and empty tensors, else on the device after upload
+  if ((s = csf_check_root(v)) != TT_OK) return s;
   if (op == TT_OP_MTTKRP) {
     if (v.order != 3 && v.order != 4) return set_error(TT_ERR_UNSUPPORTED, "MTTKRP needs order 3 or 4 (got %d)", v.order);
     if (rank < 1 || rank > TT_MAX_RANK) return set_error(TT_ERR_UNSUPPORTED, "rank %d (supported 1..%d)", rank, TT_MAX_RANK);
@@ -543,6 +614,7 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
     const int req = opts ? opts->slabs : 0;
     S = req > 0 ? req : auto_slabs(v.order, v.dims[v.order - 1], p->rp, (int)prec);
     if (S > kMaxSlabs) return fail(set_error(TT_ERR_INVALID_ARGUMENT, "slabs %d (at most %d)", S, kMaxSlabs));
+    if (S > 1 && (s = csf_check(v)) != TT_OK) return fail(s);
     if (S > 1 && (s = build_slabs(v, S, sc)) != TT_OK) return fail(s);
   } else if (opts && opts->slabs > 1) {
     return fail(set_error(TT_ERR_UNSUPPORTED, "slabs need an MTTKRP plan over a dense-root CSF"));
@@ -554,10 +626,11 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
     p->gpol = pol == 1 ? 0 : pol == 2 ? 1 : (S > 1 ? 1 : 0);
   }
   const int L = v.order - 1;
+  if (v.nnz == 0 && (s = csf_check(v)) != TT_OK) return fail(s);
   auto upload = [&](int32_t** d, const int32_t* h, int64_t n, size_t alloc, const char* what) -> tt_status {
     tt_status s2 = dev_alloc(p, d, alloc);
     if (s2 != TT_OK) return s2;
-    if (alloc > (size_t)n && cudaMemsetAsync(*d, 0, alloc * sizeof(int32_t), st) != cudaSuccess)
+    if (alloc > (size_t)n && cudaMemsetAsync(*d + n, 0, (alloc - (size_t)n) * sizeof(int32_t), st) != cudaSuccess)
       return set_error(TT_ERR_CUDA, "clear %s", what);
     if (n > 0 && cudaMemcpyAsync(*d, h, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, st) != cudaSuccess)
       return set_error(TT_ERR_CUDA, "upload %s", what);
@@ -577,6 +650,7 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
     for (int l = 0; l < TT_MAX_ORDER; l++) { p->slab[0].pos[l] = p->d_pos[l]; p->slab[0].crd[l] = p->d_crd[l]; }
     p->slab[0].nnz = v.nnz;
     p->slab[0].off = 0;
+    if (v.nnz > 0 && (s = device_csf_check(p, v, st)) != TT_OK) return fail(s);
   } else {
     for (int q = 0; q < S; q++) {
       const SlabCsf::Slab& h = sc.slab[q];
@@ -606,35 +680,39 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
     const size_t n = nvals_alloc;
     if (val_kind(p->prec) != kF32) {
       // values: one power-of-two scale (max in [1,2) for BF16, [2^14,2^15) for FP16),
-      // converted on the device with round-to-nearest-even
-      float vmax = 0.f;
-#pragma omp parallel for reduction(max : vmax)
-      for (int64_t i = 0; i < v.nnz; i++) vmax = std::max(vmax, std::fabs(v.vals[i]));
-      const float sc16 = pow2_scale_for(vmax) * (p->prec == kFP16 ? 16384.f : 1.f);
-      p->vinv = 1.f / sc16;
+      // found and applied on the device (absolute max, scale, round-to-nearest-even)
+      const bool h16 = p->prec == kFP16;
+      p->vinv = h16 ? 1.f / 16384.f : 1.f;  // (no values: never used)
       uint16_t* d = nullptr;
       if ((s = dev_alloc(p, &d, n)) != TT_OK) return fail(s);
       p->d_vals = d;
-      if (cudaMemsetAsync(d, 0, n * 2, st) != cudaSuccess) return fail(set_error(TT_ERR_CUDA, "clear vals"));
+      if (n > (size_t)nvals && cudaMemsetAsync(d + nvals, 0, (n - (size_t)nvals) * 2, st) != cudaSuccess)
+        return fail(set_error(TT_ERR_CUDA, "clear vals"));
       if (nvals > 0) {
         float* tmp = nullptr;
-        if (cudaMalloc((void**)&tmp, (size_t)nvals * 4 + 16) != cudaSuccess)
+        if (pool_alloc((void**)&tmp, (size_t)nvals * 4 + 64, st) != cudaSuccess)
           return fail(set_error(TT_ERR_OUT_OF_MEMORY, "value staging"));
-        float* dsc = reinterpret_cast<float*>(reinterpret_cast<char*>(tmp) + (size_t)nvals * 4);
-        dsc = reinterpret_cast<float*>(((uintptr_t)dsc + 3) & ~(uintptr_t)3);
-        cudaError_t e1 = cudaMemcpyAsync(tmp, hvals, (size_t)nvals * 4, cudaMemcpyHostToDevice, st);
-        cudaError_t e2 = e1 == cudaSuccess ? cudaMemcpyAsync(dsc, &sc16, 4, cudaMemcpyHostToDevice, st) : e1;
-        cudaError_t e3 = e2 == cudaSuccess ? launch_to_16(tmp, nvals, 1, 1, dsc, fac_kind(p->prec) == kH16 ? 2 : 1, d, st) : e2;
-        cudaError_t e4 = cudaStreamSynchronize(st);
-        cudaFree(tmp);
-        if (e3 != cudaSuccess || e4 != cudaSuccess)
-          return fail(set_error(TT_ERR_CUDA, "value conversion: %s", cudaGetErrorString(e3 != cudaSuccess ? e3 : e4)));
+        float* cmax = reinterpret_cast<float*>(((uintptr_t)(tmp + nvals) + 15) & ~(uintptr_t)15);
+        float* scl = cmax + 1;
+        float* inv = cmax + 2;
+        float vinv = 1.f;
+        cudaError_t e = cudaMemcpyAsync(tmp, hvals, (size_t)nvals * 4, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = launch_colmax(tmp, nvals, 1, cmax, st);
+        if (e == cudaSuccess) e = launch_pow2_scales(cmax, 1, h16 ? 14 : 0, scl, inv, st);
+        if (e == cudaSuccess) e = launch_to_16(tmp, nvals, 1, 1, scl, h16 ? 2 : 1, d, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&vinv, inv, 4, cudaMemcpyDeviceToHost, st);
+        cudaFreeAsync(tmp, st);
+        const cudaError_t e2 = cudaStreamSynchronize(st);
+        if (e != cudaSuccess || e2 != cudaSuccess)
+          return fail(set_error(TT_ERR_CUDA, "value conversion: %s", cudaGetErrorString(e != cudaSuccess ? e : e2)));
+        p->vinv = vinv;
       }
     } else {
       float* d = nullptr;
       if ((s = dev_alloc(p, &d, n)) != TT_OK) return fail(s);
       p->d_vals = d;
-      if (cudaMemsetAsync(d, 0, n * 4, st) != cudaSuccess) return fail(set_error(TT_ERR_CUDA, "clear vals"));
+      if (n > (size_t)nvals && cudaMemsetAsync(d + nvals, 0, (n - (size_t)nvals) * 4, st) != cudaSuccess)
+        return fail(set_error(TT_ERR_CUDA, "clear vals"));
       if (nvals > 0 && cudaMemcpyAsync(d, hvals, (size_t)nvals * 4, cudaMemcpyHostToDevice, st) != cudaSuccess)
         return fail(set_error(TT_ERR_CUDA, "upload vals"));
     }
@@ -713,7 +791,11 @@ TT_EXPORT tt_status tt_plan_destroy(tt_plan* p) {
   if (p->ev1) cudaEventDestroy(p->ev1);
   if (p->evk0) cudaEventDestroy(p->evk0);
   if (p->evk1) cudaEventDestroy(p->evk1);
-  for (void* a : p->allocs) cudaFree(a);
+  if (!p->allocs.empty()) {
+    cudaDeviceSynchronize();  // as cudaFree would
+    for (void* a : p->allocs) cudaFreeAsync(a, p->stream);
+    cudaStreamSynchronize(p->stream);
+  }
   delete p;
   return TT_OK;
 }
@@ -931,6 +1013,15 @@ tt_status time_variants(tt_plan* p, cudaStream_t st, const std::vector<int>& can
 }
 }  // namespace
 
+// Returns the memory the library's pool keeps for reuse (plans alive keep theirs).
+TT_EXPORT tt_status tt_release_cached_memory(void) {
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  for (int d = 0; d < kMaxDevices; d++)
+    if (g_pool[d] && cudaMemPoolTrimTo(g_pool[d], 0) != cudaSuccess)
+      return set_error(TT_ERR_CUDA, "trim device %d pool: %s", d, cudaGetErrorString(cudaGetLastError()));
+  return TT_OK;
+}
+
 // Per-variant mean ms measured at plan creation by TT_SELECT_SWEEP or by the
 // network's timed candidates (negative: not timed).
 TT_EXPORT tt_status tt_plan_sweep_times(const tt_plan* p, float* ms, int32_t n) {
@@ -962,17 +1053,18 @@ TT_EXPORT tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
   std::vector<float*> dfac(order - 1, nullptr);
   float* dA = nullptr;
   auto cleanup = [&]() {
-    for (float* d : dfac) cudaFree(d);
-    cudaFree(dA);
+    for (float* d : dfac)
+      if (d) cudaFreeAsync(d, 0);
+    if (dA) cudaFreeAsync(dA, 0);
     tt_plan_destroy(p);
   };
   for (int m = 0; m < order - 1; m++) {
     const size_t bytes = (size_t)factors[m]->dimensions[0] * rank * sizeof(float);
-    if (cudaMalloc((void**)&dfac[m], bytes) != cudaSuccess) { cleanup(); return set_error(TT_ERR_OUT_OF_MEMORY, "factor %d", m + 1); }
+    if (pool_alloc((void**)&dfac[m], bytes, 0) != cudaSuccess) { cleanup(); return set_error(TT_ERR_OUT_OF_MEMORY, "factor %d", m + 1); }
     if (cudaMemcpy(dfac[m], factors[m]->vals, bytes, cudaMemcpyHostToDevice) != cudaSuccess) { cleanup(); return set_error(TT_ERR_CUDA, "upload factor %d", m + 1); }
   }
   const size_t abytes = (size_t)A->dimensions[0] * rank * sizeof(float);
-  if (cudaMalloc((void**)&dA, abytes) != cudaSuccess) { cleanup(); return set_error(TT_ERR_OUT_OF_MEMORY, "output"); }
+  if (pool_alloc((void**)&dA, abytes, 0) != cudaSuccess) { cleanup(); return set_error(TT_ERR_OUT_OF_MEMORY, "output"); }
   tt_plan_set_timing(p, 1);
   if ((s = tt_plan_set_factors(p, (const float* const*)dfac.data(), nullptr)) != TT_OK) { cleanup(); return s; }
   if ((s = tt_plan_mttkrp(p, dA, nullptr)) != TT_OK) { cleanup(); return s; }
@@ -998,9 +1090,13 @@ TT_EXPORT tt_status tt_ttv_host(taco_tensor_t* y, const taco_tensor_t* B, const 
   const int64_t ny = p->nfib_last;
   if (y->dimensions && y->dimensions[0] < ny) { tt_plan_destroy(p); return set_error(TT_ERR_INVALID_ARGUMENT, "y has %d entries, need %lld", y->dimensions[0], (long long)ny); }
   float *dx = nullptr, *dy = nullptr;
-  auto cleanup = [&]() { cudaFree(dx); cudaFree(dy); tt_plan_destroy(p); };
-  if (cudaMalloc((void**)&dx, sizeof(float) * (size_t)std::max<int64_t>(1, nx)) != cudaSuccess ||
-      cudaMalloc((void**)&dy, sizeof(float) * (size_t)std::max<int64_t>(1, ny)) != cudaSuccess) {
+  auto cleanup = [&]() {
+    if (dx) cudaFreeAsync(dx, 0);
+    if (dy) cudaFreeAsync(dy, 0);
+    tt_plan_destroy(p);
+  };
+  if (pool_alloc((void**)&dx, sizeof(float) * (size_t)std::max<int64_t>(1, nx), 0) != cudaSuccess ||
+      pool_alloc((void**)&dy, sizeof(float) * (size_t)std::max<int64_t>(1, ny), 0) != cudaSuccess) {
     cleanup();
     return set_error(TT_ERR_OUT_OF_MEMORY, "ttv buffers");
   }

@@ -78,14 +78,18 @@ def test_variant_table():
     assert tt.variant_info(3)["staged"] == 0 and tt.variant_info(43)["name"].startswith("stage")
 
 
-def test_invalid_csf_rejected_before_device_use():
-    # pos not monotone: rejected by validation, whether or not a GPU exists
+def test_invalid_csf_rejected():
+    # pos not monotone: the host validator rejects it; a plan rejects it too (its
+    # structure check runs on the device copies, so without a GPU the plan stops
+    # at "no device" first; tests/test_gpu_mttkrp.py covers the device check)
     lv = [None, (np.array([0, 2, 1], np.int32), np.array([0, 1], np.int32)),
           (np.array([0, 1, 2], np.int32), np.array([0, 1], np.int32))]
     B = tt.HostTaco((2, 2, 2), vals=np.ones(2, np.float32), levels=lv)
+    assert tt.lib().tt_csf_validate(B.ptr) == tt.TT_ERR_INVALID_CSF
     with pytest.raises(tt.TTError) as e:
         tt.Plan(B, rank=8)
-    assert e.value.status == tt.TT_ERR_INVALID_CSF
+    expected = tt.TT_ERR_INVALID_CSF if tt.device_count() > 0 else tt.TT_ERR_NO_DEVICE
+    assert e.value.status == expected
 
 
 @pytest.mark.skipif(tt.device_count() > 0, reason="host has a GPU")

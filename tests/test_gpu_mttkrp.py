@@ -270,3 +270,33 @@ def test_slabs_over_large_leaf_factor():
     close(got, ref)
     got, plan = run_plan(B, facs, prec="fp16", slabs=8)
     close(got, ref, "fp16")
+
+
+def test_plan_rejects_malformed_csf_on_device():
+    """The plan's structure check runs on the device copies after upload: each
+    malformed level is reported as TT_ERR_INVALID_CSF, for MTTKRP and TTV plans
+    alike, and a well-formed tensor of the same shape passes."""
+    def taco(levels, dims=(2, 3, 3)):
+        lv = [None] + [(np.asarray(p, np.int32), np.asarray(c, np.int32)) for p, c in levels]
+        return tt.HostTaco(dims, vals=np.ones(8, np.float32), levels=lv)
+    ok = [([0, 1, 2], [0, 2]), ([0, 2, 3], [0, 1, 2])]
+    bad = {
+        "pos decreasing": [([0, 2, 1], [0, 2]), ([0, 2, 3], [0, 1, 2])],
+        "crd out of range": [([0, 1, 2], [0, 3]), ([0, 2, 3], [0, 1, 2])],
+        "empty inner fiber": [([0, 1, 2], [0, 2]), ([0, 0, 3], [0, 1, 2])],
+        "leaf crd unsorted": [([0, 1, 2], [0, 2]), ([0, 2, 3], [1, 0, 2])],
+        "leaf crd out of range": [([0, 1, 2], [0, 2]), ([0, 2, 3], [0, 1, 3])],
+        "inner crd unsorted": [([0, 2, 2], [2, 0]), ([0, 1, 2], [0, 1])],
+    }
+    for op in (tt.OP_MTTKRP, tt.OP_TTV):
+        tt.Plan(taco(ok), op=op, rank=8)
+        for name, lv in bad.items():
+            assert tt.lib().tt_csf_validate(taco(lv).ptr) == tt.TT_ERR_INVALID_CSF, name
+            with pytest.raises(tt.TTError) as e:
+                tt.Plan(taco(lv), op=op, rank=8)
+            assert e.value.status == tt.TT_ERR_INVALID_CSF, (name, e.value)
+    # a long valid tensor passes the device check and still computes the oracle's result
+    B = tt.gen_zipf((300, 200, 5000), (0.7, 0.7, 0.3), 200_000, 3)
+    C = tt.gen_dense(200, 8, 0, 1)
+    D = tt.gen_dense(5000, 8, 0, 2)
+    close(run_plan(B, [C, D])[0], O.mttkrp(to_oracle(B), [C, D]))
