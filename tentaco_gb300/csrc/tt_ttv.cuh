@@ -74,6 +74,14 @@ __global__ void __launch_bounds__(256, 4) ttv_stream_kernel(const __grid_constan
     }
   }
 
+  // the lane's x entries (x is small and stays in L1/L2); the coordinates are dead after this
+  float xv[NPT];
+  {
+    const float* xg = static_cast<const float*>(a.fac[0]);
+#pragma unroll
+    for (int k = 0; k < NPT; k++) xv[k] = __ldg(xg + lc[k]);
+  }
+
   // fiber window: fibers fs .. fs + W - 1; fiber fs + x ends at nonzero pos[fs + x + 1] - 1
   const int fs = a.part[u];
   const int fnext = a.part[u + 1];
@@ -104,12 +112,6 @@ __global__ void __launch_bounds__(256, 4) ttv_stream_kernel(const __grid_constan
   }
   const int f0 = fs + incl - __popc(m);  // fiber of the lane's first nonzero
 
-  float xv[NPT];
-  {
-    const float* xg = static_cast<const float*>(a.fac[0]);
-#pragma unroll
-    for (int k = 0; k < NPT; k++) xv[k] = __ldg(xg + lc[k]);
-  }
   float v[NPT];
   if constexpr (VK == kF32) {
 #pragma unroll
@@ -126,17 +128,22 @@ __global__ void __launch_bounds__(256, 4) ttv_stream_kernel(const __grid_constan
   float acc = 0.f, hacc = 0.f;
   bool hset = false;
   int f = f0;
+  auto step = [&](int k) {
+    acc = fmaf(v[k], xv[k], acc);
+    const bool e = (m >> k) & 1u;
+    if (e && hset) a.out[f] = acc;  // a fiber that started and ended in this lane
+    hacc = (e && !hset) ? acc : hacc;
+    hset = hset || e;
+    f += e ? 1 : 0;
+    acc = e ? 0.f : acc;
+  };
+  if (cnt == PU) {  // every lane full (all units but the tensor's last)
 #pragma unroll
-  for (int k = 0; k < NPT; k++) {
-    if (k < n) {
-      acc = fmaf(v[k], xv[k], acc);
-      const bool e = (m >> k) & 1u;
-      if (e && hset) a.out[f] = acc;  // a fiber that started and ended in this lane
-      hacc = (e && !hset) ? acc : hacc;
-      hset = hset || e;
-      f += e ? 1 : 0;
-      acc = e ? 0.f : acc;
-    }
+    for (int k = 0; k < NPT; k++) step(k);
+  } else {
+#pragma unroll
+    for (int k = 0; k < NPT; k++)
+      if (k < n) step(k);
   }
   Summ<1> X;
   X.t = kNone;
