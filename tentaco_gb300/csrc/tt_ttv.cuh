@@ -18,10 +18,10 @@
 //     fiber is fs + the set bits before it (a warp prefix sum of popcounts);
 //   * the per-nonzero loop has no branches: an FMA, a predicated store of a fiber
 //     that starts and ends in the lane, and selects;
-//   * the lanes' first and last partial fibers are merged by the warp's shuffle
-//     tree; fibers shared between warps go through the unit carry slots and the
-//     two-level merge of tt_mttkrp.cuh (FP32 Kahan inside a segment of units,
-//     FP64 across).
+//   * the lanes are merged by a segmented scan of their open tail sums (a lane
+//     where a fiber ends starts a segment); fibers shared between warps go
+//     through the unit carry slots and the two-level merge of tt_mttkrp.cuh
+//     (FP32 Kahan inside a segment of units, FP64 across).
 // Fibers are never empty (canonical CSF), so a nonzero ends at most one fiber.
 #pragma once
 #include "tt_mttkrp.cuh"
@@ -145,24 +145,52 @@ __global__ void __launch_bounds__(256, 4) ttv_stream_kernel(const __grid_constan
     for (int k = 0; k < NPT; k++)
       if (k < n) step(k);
   }
-  Summ<1> X;
-  X.t = kNone;
-  if (n <= 0) {
-    X.h = kEmpty;
-  } else if (!hset) {  // the lane lies inside one fiber
-    X.h = f0;
-    X.ha[0] = acc;
-  } else {
-    X.h = f0;
-    X.ha[0] = hacc;
-    if (!((m >> (n - 1)) & 1u)) {  // the lane's last fiber continues past it
-      X.t = f;
-      X.ta[0] = acc;
+  // Merge the lanes: a segmented inclusive scan of the lanes' open tail sums
+  // (a lane where a fiber ends starts a segment) gives the carry leaving each
+  // lane; the carry into lane L plus its sum up to its first fiber end is that
+  // fiber's total in the unit.  Fixed order, so deterministic.
+  const bool active = n > 0;
+  float val = active ? acc : 0.f;
+  bool head = active && hset;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const float vu = __shfl_up_sync(0xffffffffu, val, d);
+    const int hu = __shfl_up_sync(0xffffffffu, head ? 1 : 0, d);
+    if (lane >= d) {
+      if (!head) val = vu + val;
+      head = head || hu;
     }
   }
-  WK wk(a, 0);
-  warp_tree(wk, X);
-  if (lane == 0) settle_unit(a, wk, X, (int64_t)fs, (int64_t)fs, (int64_t)win0, ustart64, fnext, u, 0);
+  float cin = __shfl_up_sync(0xffffffffu, val, 1);
+  if (lane == 0) cin = 0.f;
+  const float total = cin + hacc;  // the lane's first fiber, when it ends in the lane
+  const unsigned ends = __ballot_sync(0xffffffffu, active && hset);
+  const int lstar = ends ? __ffs((int)ends) - 1 : -1;  // first lane where a fiber ends
+  // later lanes' first fibers started and ended inside the unit: final
+  if (active && hset && lane != lstar) a.out[f0] = total;
+  const int la = (cnt - 1) / NPT;  // last lane with nonzeros
+  const float tot_first = __shfl_sync(0xffffffffu, total, lstar < 0 ? 0 : lstar);
+  const float out_last = __shfl_sync(0xffffffffu, val, la);
+  const int f_last = __shfl_sync(0xffffffffu, f, la);
+  const uint32_t m_last = __shfl_sync(0xffffffffu, m, la);
+  const bool open = !((m_last >> (cnt - la * NPT - 1)) & 1u);  // the unit's last fiber continues
+  if (lane == 0) {
+    // the unit's summary: its first fiber fs and, if different, the fiber open at its end
+    Summ<1> X;
+    X.h = fs;
+    X.t = kNone;
+    if (lstar < 0) {
+      X.ha[0] = out_last;  // the whole unit lies in fiber fs
+    } else {
+      X.ha[0] = tot_first;
+      if (open) {
+        X.t = f_last;
+        X.ta[0] = out_last;
+      }
+    }
+    WK wk(a, 0);
+    settle_unit(a, wk, X, (int64_t)fs, (int64_t)fs, (int64_t)win0, ustart64, fnext, u, 0);
+  }
 }
 #endif  // TT_ARGS_ONLY
 }  // namespace tt
