@@ -13,9 +13,10 @@
 //     the kTtvNpt nonzeros from 16 L; the lane loads its coordinates and values
 //     straight into registers (16-byte loads, issued first: they depend on
 //     nothing), then its x entries;
-//   * the unit's fiber ends are a bit mask (bit e: nonzero e ends a fiber), set
-//     in shared memory from the fiber starts of the unit's window; a lane's first
-//     fiber is fs + the set bits before it (a warp prefix sum of popcounts);
+//   * the unit's fiber ends are byte flags in shared memory (flag e: nonzero e
+//     ends a fiber), set by plain byte stores from the fiber starts of the unit's
+//     window (no atomics), then packed into a 16-bit mask per lane; a lane's
+//     first fiber is fs + the ends before it (a warp prefix sum of popcounts);
 //   * the per-nonzero loop has no branches: an FMA, a predicated store of a fiber
 //     that starts and ends in the lane, and selects;
 //   * the lanes are merged by a segmented scan of their open tail sums (a lane
@@ -37,7 +38,7 @@ __global__ void __launch_bounds__(256, 4) ttv_stream_kernel(const __grid_constan
   static_assert(NPT == 16, "a lane's fiber-end bits are half a mask word");
   constexpr int NW = VK == kF32 ? NPT : NPT / 2;  // value words per lane
   using WK = Walk<3, kFP32, 1, 1>;                // the merge helpers for one output column
-  __shared__ uint32_t s_mask[8][NPT];             // per warp: 32 * NPT bits
+  __shared__ __align__(16) uint8_t s_end[8][32 * NPT];  // per warp: one flag per nonzero
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int u = blockIdx.x * (blockDim.x >> 5) + warp;
   if (u >= a.nblocks) return;  // whole warp
@@ -87,7 +88,7 @@ __global__ void __launch_bounds__(256, 4) ttv_stream_kernel(const __grid_constan
   const int fnext = a.part[u + 1];
   const int W = fnext - fs + 1;
   const int32_t* gpos = a.pos[1] + fs;
-  if (lane < NPT) s_mask[warp][lane] = 0u;
+  reinterpret_cast<uint4*>(s_end[warp])[lane] = make_uint4(0u, 0u, 0u, 0u);  // 32 x 16 bytes
   __syncwarp();
   const int ustart = (int)ustart64;
   for (int x0 = lane + 1; x0 <= W; x0 += 32 * 4) {
@@ -99,11 +100,19 @@ __global__ void __launch_bounds__(256, 4) ttv_stream_kernel(const __grid_constan
     }
 #pragma unroll
     for (int r = 0; r < 4; r++)
-      if (e[r] >= 0 && e[r] < cnt) atomicOr(&s_mask[warp][e[r] >> 5], 1u << (e[r] & 31));
+      if (e[r] >= 0 && e[r] < cnt) s_end[warp][e[r]] = 1;
   }
   const int win0 = lane == 0 ? gpos[0] : 0;  // start of the unit's first fiber
   __syncwarp();
-  const uint32_t m = (s_mask[warp][lane >> 1] >> ((lane & 1) * 16)) & 0xffffu;
+  uint32_t m = 0u;
+  {
+    // the lane's 16 flags (bytes 0 or 1) as bits 0..15
+    const uint4 b = reinterpret_cast<const uint4*>(s_end[warp])[lane];
+    const uint32_t w[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      m |= ((w[k] & 1u) | ((w[k] >> 7) & 2u) | ((w[k] >> 14) & 4u) | ((w[k] >> 21) & 8u)) << (4 * k);
+  }
   int incl = __popc(m);
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
