@@ -110,55 +110,109 @@ def compulsory_bytes(B, s_v, s_f):
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """SM clocks and throttle reasons sampled during the timed region only
+    (start() / stop() around it): in-process NVML queries every 2 ms through the
+    driver's libnvidia-ml (read-only), else nvidia-smi every 200 ms.  The samples
+    go to a CSV beside the run's output."""
 
-    def __init__(self, path):
+    # nvmlClocksEventReason* bits (nvml.h)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, path, period_s=0.002):
         self.path = path
+        self.period = period_s
+        self.rows = []  # (sm_mhz, max_mhz, reason bits)
         self.proc = None
+        self.thread = None
+        self.nvml = None
 
-    def __enter__(self):
+    def _nvml_open(self):
+        import ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            return None
+        h = ctypes.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(0, ctypes.byref(h)) != 0:
+            return None
+        mx = ctypes.c_uint()
+        lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))  # NVML_CLOCK_SM
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        return lib, h, mx.value, reasons
+
+    def start(self):
+        import threading
+        self.rows = []
+        try:
+            self.nvml = self._nvml_open()
+        except Exception:
+            self.nvml = None
+        if self.nvml:
+            import ctypes
+            lib, h, mx, reasons = self.nvml
+            self.stop_flag = threading.Event()
+
+            def loop():
+                c = ctypes.c_uint()
+                r = ctypes.c_ulonglong()
+                while not self.stop_flag.is_set():
+                    if lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(c)) == 0:
+                        bits = r.value if reasons(h, ctypes.byref(r)) == 0 else 0
+                        self.rows.append((float(c.value), float(mx), int(bits)))
+                    self.stop_flag.wait(self.period)
+
+            self.thread = threading.Thread(target=loop, daemon=True)
+            self.thread.start()
+            return
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
-            self.fh = open(self.path, "w")
+            self.fh = open(self.path + ".smi", "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
                                           "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
-        return self
 
-    def __exit__(self, *a):
+    def stop(self):
+        if self.thread:
+            self.stop_flag.set()
+            self.thread.join()
+            self.thread = None
         if self.proc:
             self.proc.terminate()
             self.proc.wait()
             self.fh.close()
+            self.proc = None
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            bitof = {v: k for k, v in self.REASONS.items()}
+            try:
+                for line in open(self.path + ".smi"):
+                    r = [x.strip() for x in line.split(",")]
+                    if len(r) < 9:
+                        continue
+                    bits = sum(bitof[nm] for nm, v in zip(names, r[5:9]) if v.lower().startswith("active"))
+                    self.rows.append((float(r[1]), float(r[2]), bits))
+            except (OSError, ValueError):
+                pass
+        try:
+            with open(self.path, "w") as fh:
+                fh.write("sm_mhz,max_sm_mhz,reason_bits\n")
+                for sm, mx, bits in self.rows:
+                    fh.write(f"{sm:.0f},{mx:.0f},{bits:#x}\n")
+        except OSError:
+            pass
 
     def summary(self):
-        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
-        try:
-            rows = [l.split(",") for l in open(self.path) if l.strip()]
-        except Exception:
-            return out
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in rows:
-            r = [x.strip() for x in r]
-            if len(r) < 9:
-                continue
-            try:
-                sm.append(float(r[1]))
-                mx.append(float(r[2]))
-            except ValueError:
-                continue
-            for nm, v in zip(names, r[5:9]):
-                if v.lower().startswith("active"):
-                    reasons.add(nm)
-        if sm:
-            out["sm_mhz"] = statistics.median(sm)
-            out["sm_max_mhz"] = max(mx)
-            out["samples"] = len(sm)
-        out["reasons"] = sorted(reasons)
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": len(self.rows),
+               "source": "nvml 2 ms" if self.nvml else "nvidia-smi 200 ms"}
+        if self.rows:
+            out["sm_mhz"] = statistics.median(r[0] for r in self.rows)
+            out["sm_max_mhz"] = max(r[1] for r in self.rows)
+            bits = 0
+            for r in self.rows:
+                bits |= r[2]
+            out["reasons"] = sorted(nm for b, nm in self.REASONS.items() if bits & b)
         return out
 
 
@@ -225,7 +279,7 @@ def run_gpu_arm(args, rank, world, d):
         sel = tt.SELECT_FIXED
     flops = 3.0 * B.nnz * RANK
 
-    def timed_plan(prec, select):
+    def timed_plan(prec, select, clk=None):
         plan = tt.Plan(B, rank=RANK, prec=prec, select=select, variant=max(args.variant, 0), slabs=args.slabs)
         if select == tt.SELECT_MODEL and plan.selected_by not in (1, 3):
             plan = tt.Plan(B, rank=RANK, prec=prec, select=tt.SELECT_SWEEP, slabs=args.slabs)
@@ -240,6 +294,8 @@ def run_gpu_arm(args, rank, world, d):
         step_ms, kern_ms = [], []
         barrier(d)
         tt.synchronize()
+        if clk:
+            clk.start()
         wall0 = time.perf_counter()
         for _ in range(args.steps):
             tt.l2_flush()
@@ -249,11 +305,13 @@ def run_gpu_arm(args, rank, world, d):
         tt.synchronize()
         barrier(d)
         wall = time.perf_counter() - wall0
+        if clk:
+            clk.stop()
         return plan, A, bufs, step_ms, kern_ms, wall
 
-    with Clocks(os.path.join(ROOT, "gpurun_out", "bench_clocks.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
-                else "/tmp/tt_bench_clocks.csv") as clk:
-        plan, A, bufs, step_ms, kern_ms, wall = timed_plan(args.prec, sel)
+    clk = Clocks(os.path.join(ROOT, "gpurun_out", "bench_clocks.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
+                 else "/tmp/tt_bench_clocks.csv")
+    plan, A, bufs, step_ms, kern_ms, wall = timed_plan(args.prec, sel, clk)
     clocks = clk.summary()
     ms = float(np.mean(step_ms))
     ms_max = allmax(d, ms)

@@ -119,22 +119,39 @@ cudaError_t launch_csf_check(const int32_t* pos, int64_t nf, int inner, const in
 // storage conversion (factors to BF16 with power-of-two column scales)
 // ---------------------------------------------------------------------------
 __global__ void colmax_kernel(const float* __restrict__ x, int64_t rows, int cols, float* colmax) {
-  // one thread per (row-slab, column); |x| >= 0 so unsigned compare of the bits orders it
+  // one thread per (row-slab, column); the block's slabs are reduced in shared
+  // memory first, so each block adds one atomic per column (|x| >= 0, so the
+  // unsigned compare of the bits orders it)
+  __shared__ float s_m[256];
   const int j = threadIdx.x % cols;
   const int lanes = blockDim.x / cols;
+  const int l = threadIdx.x / cols;
   float m = 0.f;
-  for (int64_t r = (int64_t)blockIdx.x * lanes + threadIdx.x / cols; r < rows; r += (int64_t)gridDim.x * lanes) {
-    const float v = fabsf(x[r * cols + j]);
-    m = v > m ? v : m;  // NaN ignored
+  if (l < lanes) {
+    for (int64_t r = (int64_t)blockIdx.x * lanes + l; r < rows; r += (int64_t)gridDim.x * lanes) {
+      const float v = fabsf(x[r * cols + j]);
+      m = v > m ? v : m;  // NaN ignored
+    }
   }
-  if (threadIdx.x < lanes * cols) atomicMax(reinterpret_cast<unsigned int*>(colmax) + j, __float_as_uint(m));
+  s_m[threadIdx.x] = m;
+  __syncthreads();
+  for (int h = lanes / 2; h > 0; h >>= 1) {  // lanes is a power of two
+    if (l < h) {
+      const float o = s_m[threadIdx.x + h * cols];
+      if (o > s_m[threadIdx.x]) s_m[threadIdx.x] = o;
+    }
+    __syncthreads();
+  }
+  if (l == 0) atomicMax(reinterpret_cast<unsigned int*>(colmax) + j, __float_as_uint(s_m[threadIdx.x]));
 }
 
 cudaError_t launch_colmax(const float* x, int64_t rows, int cols, float* colmax, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(colmax, 0, sizeof(float) * (size_t)cols, s);
   if (e != cudaSuccess) return e;
   if (rows == 0) return cudaSuccess;
-  const int lanes = 256 / cols > 0 ? 256 / cols : 1;
+  if (cols < 1 || cols > 256) return cudaErrorInvalidValue;  // one block holds every column
+  int lanes = 1;  // rows per block pass: the largest power of two with lanes * cols <= 256
+  while (2 * lanes * cols <= 256) lanes *= 2;
   const int tb = lanes * cols;
   int64_t grid = (rows + lanes * 32 - 1) / (lanes * 32);
   if (grid > 4096) grid = 4096;
