@@ -1,0 +1,50 @@
+"""The multi-process (N > 1) path on CPU: world_size-2 runs over gloo at
+127.0.0.1, launched the way the bench is launched for N GPUs.  Each GPU rank
+runs an independent replica (no data-path collective); what N > 1 adds is the
+barrier around the timed region, the max over ranks and rank 0 reporting,
+which these tests cover without a GPU."""
+import json
+import os
+import re
+import socket
+import subprocess
+import sys
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _torchrun(args, timeout=600):
+    pytest.importorskip("torch.distributed")
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port())] + args
+    env = dict(os.environ, OMP_NUM_THREADS="2")
+    return subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=timeout, env=env)
+
+
+def test_barrier_and_max_over_two_ranks():
+    r = _torchrun([os.path.join(HERE, "dist_worker.py")])
+    assert r.returncode == 0, r.stderr[-2000:]
+    # the two ranks write concurrently: read every flat JSON object in the stream
+    lines = [json.loads(m) for m in re.findall(r"\{[^{}]*\}", r.stdout)]
+    assert sorted(x["rank"] for x in lines) == [0, 1]
+    assert all(x["world"] == 2 and x["max"] == 2.5 for x in lines)
+
+
+def test_reference_arm_two_ranks_rank0_reports():
+    r = _torchrun([os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2", "--steps", "1",
+                   "--warmup", "0", "--nnz", "200000"])
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    out = lines[0]
+    assert out["impl"] == "reference" and out["n_gpus"] == 2 and out["value"] > 0
+    assert out["cpu_baseline"]["kind"] == "port" and out["e2e"]["h2d_bytes_per_step"] == 0
