@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--no-errors", action="store_true")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the TTV (50M nonzeros) and 4-mode MTTKRP (80M nonzeros) measurements")
-    ap.add_argument("--only", default=None, choices=["ttv", "mttkrp4"],
+    ap.add_argument("--only", default=None, choices=["ttv", "mttkrp4", "modes"],
                     help="run only this secondary measurement and print its JSON (for profiling)")
     return ap.parse_args()
 
@@ -392,7 +392,8 @@ def run_gpu_arm(args, rank, world, d):
         out["cpu_baseline"] = cpu_baseline(B, C, D, budget_s=15.0)
     if not args.no_secondary:
         del B, C, D, A, bufs, plan
-        out["secondary"] = {"ttv_config2": secondary_ttv(args), "mttkrp4_config5": secondary_mttkrp4(args)}
+        out["secondary"] = {"ttv_config2": secondary_ttv(args), "mttkrp4_config5": secondary_mttkrp4(args),
+                            "mttkrp3_other_modes": secondary_other_modes(args)}
     return out
 
 
@@ -466,6 +467,36 @@ def secondary_mttkrp4(args):
                                        "fro": float(np.linalg.norm(got - ref) / np.linalg.norm(ref))}}
         del plan
     res["speedup_fp16_vs_fp32"] = round(res["fp32"]["ms_per_step"] / res["fp16"]["ms_per_step"], 3)
+    return res
+
+
+def secondary_other_modes(args):
+    """MTTKRP of modes 1 and 2 of the headline tensor (FP16 storage, rank 32, the
+    learned selector): the plan re-roots the tensor at the mode once (timed as
+    plan setup), calls are timed like the headline's, sampled output rows are
+    checked against the FP64 oracle on the re-rooted tensor."""
+    import tentaco_gb300 as tt
+
+    B, C, D = make_workload(args.nnz)
+    facs = {0: tt.gen_dense(DIMS[0], RANK, 1, SEED * 10), 1: C, 2: D}
+    res = {"nnz": B.nnz}
+    for m in (1, 2):
+        others = [facs[n] for n in range(3) if n != m]
+        t0 = time.perf_counter()
+        plan = tt.Plan(B, rank=RANK, prec="fp16", select=tt.SELECT_MODEL, mode=m)
+        setup_s = time.perf_counter() - t0
+        bufs = [tt.DeviceBuffer.from_array(f) for f in others]
+        plan.set_factors(bufs)
+        A = tt.DeviceBuffer(DIMS[m] * RANK * 4)
+        ms = _timed(lambda: plan.mttkrp(A), plan, max(3, args.steps // 2), args.warmup)
+        Ah = A.to_array((DIMS[m], RANK))
+        Bm = tt.csf_reroot(B, m)
+        err = sample_errors(Bm, others[0], others[1], Ah, check_rows(Bm, n=1024))
+        res[f"mode{m}"] = {"rows": DIMS[m], "ms_per_step": round(ms, 4),
+                           "gflops": round(3.0 * B.nnz * RANK / (ms * 1e-3) / 1e9, 2),
+                           "variant": tt.variant_info(plan.variant)["name"], "plan_setup_s": round(setup_s, 2),
+                           "error_vs_fp64": {"normwise_max": err["normwise_max"], "fro": err["fro"]}}
+        del plan, bufs, A, Bm
     return res
 
 
@@ -563,7 +594,8 @@ def run_reference_arm(args, rank, world):
 def main():
     args = parse()
     if args.only:
-        print(json.dumps({"ttv": secondary_ttv, "mttkrp4": secondary_mttkrp4}[args.only](args)))
+        print(json.dumps({"ttv": secondary_ttv, "mttkrp4": secondary_mttkrp4,
+                          "modes": secondary_other_modes}[args.only](args)))
         return
     rank, world, d = dist_setup(args.gpus)
     if args.impl == "reference":

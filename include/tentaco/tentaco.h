@@ -116,7 +116,13 @@ typedef struct tt_plan_options {
    * choice, nothing timed) when every feature of the tensor lies inside the range
    * the network was trained on, else 6; 1 to 16 as given. */
   int32_t model_topk;
-  int32_t reserved[5];
+  /* MTTKRP output mode (0: the root mode, as in the reference).  For mode m > 0
+   * the plan re-roots the tensor once, on the host (level order m, then the other
+   * modes in increasing order), and computes A_m(j,:) = sum of B over the other
+   * coordinates times their factors' rows; tt_plan_set_factors then takes the
+   * factors of the other modes in increasing mode order, and A has dims[m] rows. */
+  int32_t mode;
+  int32_t reserved[4];
 } tt_plan_options;
 
 tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t rank, tt_precision prec,
@@ -249,6 +255,10 @@ tt_status tt_csf_from_coo(int32_t order, const int32_t* dims, int64_t nnz,
                           const int32_t* coords, const float* vals, taco_tensor_t** out);
 /* Check monotone pos, in-range crd, sorted distinct children, non-empty inner fibers. */
 tt_status tt_csf_validate(const taco_tensor_t* B);
+/* The same tensor as a canonical CSF rooted at `mode` (level order: mode, then
+ * the other modes in increasing order; dims permuted alike), e.g. for MTTKRP of
+ * another mode.  B is validated first.  *out is library-owned (tt_tensor_free). */
+tt_status tt_csf_reroot(const taco_tensor_t* B, int32_t mode, taco_tensor_t** out);
 void tt_tensor_free(taco_tensor_t* t);
 
 #ifdef __cplusplus

@@ -164,6 +164,39 @@ def mttkrp(csf: Csf, factors: list, rows: np.ndarray | None = None) -> np.ndarra
     return A
 
 
+def coords_of(csf: Csf) -> np.ndarray:
+    """Every nonzero's coordinates (nnz x order, int64), in CSF order."""
+    n = csf.nnz
+    out = np.empty((n, csf.order), dtype=np.int64)
+    # the leaf level: its own crd; upper levels: expand each fiber's coordinate
+    # over the nonzeros below it
+    out[:, csf.order - 1] = csf.crd[csf.order - 1]
+    span = np.arange(n + 1, dtype=np.int64)  # level-L position p covers nonzeros [p, p+1)
+    for l in range(csf.order - 1, 0, -1):
+        pos = np.asarray(csf.pos[l], dtype=np.int64)
+        starts = span[pos[:-1]]
+        ends = span[pos[1:]]
+        ids = np.asarray(csf.crd[l - 1], dtype=np.int64) if l >= 2 else np.arange(csf.dims[0], dtype=np.int64)
+        out[:, l - 1] = np.repeat(ids, ends - starts)
+        span = span[pos]
+    return out
+
+
+def mttkrp_coo(coords: np.ndarray, vals: np.ndarray, factors: list, mode: int, nrows: int) -> np.ndarray:
+    """MTTKRP of output mode `mode` in FP64 from coordinates (oracle_mttkrp_coo):
+    factors[n] is the mode-n factor (factors[mode] is ignored)."""
+    order = coords.shape[1]
+    co = np.ascontiguousarray(coords, dtype=np.int64)
+    v = _cf(vals)
+    R = next(f for n, f in enumerate(factors) if n != mode).shape[1]
+    fs = [_cf(f) if (n != mode and f is not None) else np.zeros((1, R)) for n, f in enumerate(factors)]
+    arr = (_P * order)(*[f.ctypes.data for f in fs])
+    A = np.zeros((nrows, R))
+    lib().oracle_mttkrp_coo(ctypes.c_int32(order), _I(co.shape[0]), _ptr(co), _ptr(v), ctypes.c_int32(mode),
+                            _I(R), arr, _I(nrows), _ptr(A))
+    return A
+
+
 def mttkrp3_workspace(csf: Csf, C, D) -> np.ndarray:
     C, D = _cf(C), _cf(D)
     R = C.shape[1]

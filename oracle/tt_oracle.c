@@ -326,3 +326,30 @@ ORACLE_API int oracle_max_threads(void) {
   return 1;
 #endif
 }
+
+/*
+ * MTTKRP of any output mode from coordinates:
+ *   A(c[mode], j) = sum over nonzeros p of vals[p] * prod_{n != mode} F_n(c[n], j),
+ * nonzeros in the given order, the product taken left to right over the other
+ * modes in increasing order ((v * F_a) * F_b) [* F_c]), serial, FP64.  The
+ * reference computes the root mode only; for mode 0, with nonzeros in CSF order,
+ * this is the same arithmetic as oracle_mttkrp3 / oracle_mttkrp4 (which follow
+ * tensor_kernels/mttkrp3_csf_cpu_taco.h:45 and mttkrp4_csf_cpu_taco.h:53).
+ *   coords: nnz x order (row-major); factors: order pointers (factors[mode]
+ *   unused), each dims[n] x R row-major; A: nrows x R, overwritten.
+ */
+ORACLE_API void oracle_mttkrp_coo(int32_t order, int64_t nnz, const int64_t* coords, const double* vals,
+                                  int32_t mode, int64_t R, const double* const* factors, int64_t nrows,
+                                  double* A) {
+  for (int64_t p = 0; p < nrows * R; p++) A[p] = 0.0;
+  for (int64_t p = 0; p < nnz; p++) {
+    const int64_t* c = coords + p * order;
+    double* a = A + c[mode] * R;
+    for (int64_t j = 0; j < R; j++) {
+      double t = vals[p];
+      for (int32_t n = 0; n < order; n++)
+        if (n != mode) t = t * factors[n][c[n] * R + j];
+      a[j] = a[j] + t;
+    }
+  }
+}

@@ -101,6 +101,7 @@ def lib():
         "tt_mttkrp_host": (S, [_TP, _TP, C.POINTER(_TP), S, S, C.c_int32]),
         "tt_ttv_host": (S, [_TP, _TP, _TP]),
         "tt_csf_from_coo": (S, [C.c_int32, C.POINTER(C.c_int32), C.c_int64, _P, _P, C.POINTER(_TP)]),
+        "tt_csf_reroot": (S, [_TP, C.c_int32, C.POINTER(_TP)]),
         "tt_csf_validate": (S, [_TP]),
         "tt_tensor_free": (None, [_TP]),
         "tt_gen_zipf": (S, [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_int64, C.c_float,
@@ -216,6 +217,13 @@ class Tensor:
         f = np.zeros(12, dtype=np.float32)
         check(lib().tt_csf_features(self.ptr, rank, f.ctypes.data_as(C.POINTER(C.c_float))))
         return f
+
+
+def csf_reroot(B, mode: int) -> "Tensor":
+    """B as the canonical CSF rooted at `mode` (other modes after it in increasing order)."""
+    out = _TP()
+    check(lib().tt_csf_reroot(_tensor_ptr(B), int(mode), C.byref(out)))
+    return Tensor(out)
 
 
 def csf_from_coo(dims, coords: np.ndarray, vals: np.ndarray) -> Tensor:
@@ -363,16 +371,18 @@ class DeviceBuffer:
 
 class PlanOptions(C.Structure):
     _fields_ = [("slabs", C.c_int32), ("l2_policy", C.c_int32), ("model_topk", C.c_int32),
-                ("reserved", C.c_int32 * 5)]
+                ("mode", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
 class Plan:
     """slabs: leaf-mode slabs for MTTKRP (None/0 automatic, 1 none, up to 16).
     model_topk: with SELECT_MODEL, how many of the network's best-ranked variants
-    to time at creation (0 automatic: 1 inside the training range, else 6)."""
+    to time at creation (0 automatic: 1 inside the training range, else 6).
+    mode: MTTKRP output mode; for mode m > 0 the plan re-roots the tensor at m and
+    set_factors takes the other modes' factors in increasing mode order."""
 
     def __init__(self, B, op=OP_MTTKRP, rank=32, prec="fp32", select=SELECT_DEFAULT, variant=0, stream=None,
-                 slabs=None, l2_policy=0, model_topk=0):
+                 slabs=None, l2_policy=0, model_topk=0, mode=0):
         self.ptr = _P()
         self.op = op
         self.rank = rank
@@ -381,6 +391,8 @@ class Plan:
         opts.slabs = int(slabs or 0)
         opts.l2_policy = int(l2_policy)
         opts.model_topk = int(model_topk)
+        opts.mode = int(mode)
+        self.mode = int(mode)
         check(lib().tt_plan_create_ex(_tensor_ptr(B), op, rank, PRECISIONS.get(prec, prec), select, variant,
                                       C.byref(opts), stream, C.byref(self.ptr)))
 

@@ -58,6 +58,9 @@ tt_status csf_check(const CsfView& v);
 tt_status csf_check_root(const CsfView& v);
 // Message for a device check result ((index << 3) | code, UINT64_MAX: none).
 tt_status csf_check_error(int level, uint64_t word);
+// The validated CSF v re-rooted at `mode` (level order: mode, then the other modes
+// in increasing order), as a library-owned tensor (free with tt_tensor_free).
+tt_status csf_reroot(const CsfView& v, int mode, taco_tensor_t** out);
 
 // A dense-root CSF split into leaf-mode slabs (leaf coordinate c is in slab
 // c / width).  Each slab is a CSF with every row; its leaf arrays are the run

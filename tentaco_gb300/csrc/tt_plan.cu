@@ -572,6 +572,23 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
   CsfView v;
   tt_status s = csf_view(B, &v);
   if (s != TT_OK) return s;
+  // MTTKRP of another mode: the plan holds the tensor re-rooted at that mode
+  // (levels: mode, then the other modes in increasing order) and runs the same
+  // mode-0 walk on it; the host arrays are read here, so they are checked first
+  const int mode = opts ? opts->mode : 0;
+  taco_tensor_t* rerooted = nullptr;
+  struct FreeRerooted {
+    taco_tensor_t*& t;
+    ~FreeRerooted() { if (t) tt_tensor_free(t); }
+  } free_rerooted{rerooted};
+  if (mode != 0) {
+    if (op != TT_OP_MTTKRP) return set_error(TT_ERR_UNSUPPORTED, "an output mode other than 0 needs an MTTKRP plan");
+    if (mode < 0 || mode >= v.order) return set_error(TT_ERR_INVALID_ARGUMENT, "mode %d of an order-%d tensor", mode, v.order);
+    if ((s = csf_check(v)) != TT_OK) return s;
+    if ((s = csf_reroot(v, mode, &rerooted)) != TT_OK) return s;
+    if ((s = csf_view(rerooted, &v)) != TT_OK) return s;
+    B = rerooted;
+  }
   // the root and pos[0] here; the levels on the host only for slab plans (built
   // from the host arrays) and empty tensors, else on the device after upload
   if ((s = csf_check_root(v)) != TT_OK) return s;
@@ -601,6 +618,7 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
   p->rank = op == TT_OP_MTTKRP ? rank : 1;
   p->rp = op == TT_OP_MTTKRP ? rank_pad(rank) : 1;
   p->prec = (int)prec;
+  p->mode = mode;
   p->stream = st;
   for (int l = 0; l < v.order; l++) p->count[l] = v.count[l];
   p->nfib_last = v.count[v.order - 2];

@@ -66,6 +66,7 @@ struct tt_plan {
     int64_t nnz = 0, off = 0;
   };
   int slabs = 1;
+  int mode = 0;  // output mode (the plan's tensor is re-rooted at it when not 0)
   int gpol = 0;  // WalkArgs::gpol
   SlabDev slab[tt::kMaxSlabs];
   // timing

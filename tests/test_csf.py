@@ -96,3 +96,22 @@ def test_dense_generator():
     assert np.array_equal(a, b) and a.std() > 0
     u = tt.gen_dense(1000, 4, 0, 1)
     assert u.min() >= 0 and u.max() < 1
+
+
+@pytest.mark.parametrize("order", [3, 4])
+def test_reroot_matches_builder_on_permuted_coordinates(order):
+    """tt_csf_reroot(B, m) is bit-identical to building the canonical CSF from B's
+    coordinates permuted to (m, then the other modes in increasing order)."""
+    dims = (40, 30, 50) if order == 3 else (20, 15, 12, 30)
+    B = tt.gen_zipf(dims, (0.8,) * order, 4000, 11 + order)
+    co = O.coords_of(to_oracle(B)).astype(np.int32)
+    for m in range(order):
+        perm = [m] + [n for n in range(order) if n != m]
+        rr = tt.csf_reroot(B, m)
+        ref = tt.csf_from_coo(tuple(dims[n] for n in perm), co[:, perm], B.vals)
+        assert rr.dims == ref.dims and rr.nnz == B.nnz
+        for l in range(1, order):
+            assert np.array_equal(rr.pos(l), ref.pos(l)) and np.array_equal(rr.crd(l), ref.crd(l)), (m, l)
+        assert np.array_equal(rr.vals, ref.vals)
+    with pytest.raises(tt.TTError):
+        tt.csf_reroot(B, order)

@@ -300,3 +300,30 @@ def test_plan_rejects_malformed_csf_on_device():
     C = tt.gen_dense(200, 8, 0, 1)
     D = tt.gen_dense(5000, 8, 0, 2)
     close(run_plan(B, [C, D])[0], O.mttkrp(to_oracle(B), [C, D]))
+
+
+@pytest.mark.parametrize("order,prec", [(3, "fp32"), (3, "fp16"), (4, "fp32"), (4, "bf16")])
+def test_other_output_modes(order, prec):
+    """MTTKRP of every non-root mode (plan option `mode`: the tensor re-rooted at
+    the mode, the other modes' factors in increasing mode order) against the
+    any-mode FP64 oracle."""
+    dims = (300, 200, 500) if order == 3 else (40, 30, 20, 500)
+    zipf = (0.9, 0.6, 0.3) if order == 3 else (0.9, 0.5, 0.5, 0.3)
+    B = tt.gen_zipf(dims, zipf, 200_000 if order == 3 else 150_000, 21 + order)
+    Oc = to_oracle(B)
+    co = O.coords_of(Oc)
+    R = 16
+    F = [tt.gen_dense(d, R, 0, 40 + n) for n, d in enumerate(dims)]
+    for m in range(1, order):
+        ref = O.mttkrp_coo(co, Oc.vals, F, m, dims[m])
+        plan = tt.Plan(B, rank=R, prec=prec, mode=m)
+        bufs = [tt.DeviceBuffer.from_array(F[n].astype(np.float32)) for n in range(order) if n != m]
+        plan.set_factors(bufs)
+        A = tt.DeviceBuffer(dims[m] * R * 4)
+        plan.mttkrp(A)
+        close(A.to_array((dims[m], R)), ref, prec)
+        assert plan.device_error() == 0
+    with pytest.raises(tt.TTError):
+        tt.Plan(B, rank=R, mode=order)
+    with pytest.raises(tt.TTError):
+        tt.Plan(B, op=tt.OP_TTV, mode=1)

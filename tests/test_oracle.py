@@ -96,3 +96,28 @@ def test_reference_matches_restatement_random():
     csf = O.build_csf(dims, co, rng.random(3000))
     x = rng.uniform(-1, 1, 50)
     assert np.array_equal(O.ttv(csf, x), O.ref_ttv(csf, x))
+
+
+@pytest.mark.parametrize("order", [3, 4])
+def test_any_mode_oracle(order):
+    """The any-mode oracle (oracle_mttkrp_coo) equals the reference-pinned CSF
+    oracle bit-for-bit for mode 0 (same nonzero order and product association)
+    and a dense einsum for every mode."""
+    rng = np.random.default_rng(5 + order)
+    dims = (12, 9, 11) if order == 3 else (7, 6, 5, 8)
+    co = np.array(sorted({tuple(int(rng.integers(0, d)) for d in dims) for _ in range(300)}), dtype=np.int64)
+    vals = rng.random(len(co))
+    csf = O.build_csf(dims, co, vals)
+    coords = O.coords_of(csf)
+    assert np.array_equal(coords, co)
+    F = [rng.random((d, 6)) for d in dims]
+    assert np.array_equal(O.mttkrp_coo(coords, csf.vals, F, 0, dims[0]), O.mttkrp(csf, F[1:]))
+    dense = np.zeros(dims)
+    dense[tuple(co.T)] = vals
+    letters = "abcd"[:order]
+    for m in range(order):
+        others = [n for n in range(order) if n != m]
+        eq = letters + "," + ",".join(letters[n] + "r" for n in others) + "->" + letters[m] + "r"
+        ref = np.einsum(eq, dense, *[F[n] for n in others])
+        got = O.mttkrp_coo(coords, csf.vals, F, m, dims[m])
+        assert np.allclose(got, ref, rtol=1e-12, atol=1e-12), m
