@@ -304,7 +304,6 @@ void csf_from_sorted_keys(const Packing& pk, const int32_t* dims, const std::vec
     o->crd[l].resize((size_t)total[l]);
     if (l >= 2) o->pos[l].resize((size_t)total[l - 1] + 1);
   }
-  std::vector<int64_t> rowcnt((size_t)dims[0] + 1, 0);
 #pragma omp parallel num_threads(nt)
   {
     const int t = omp_get_thread_num();
@@ -320,11 +319,18 @@ void csf_from_sorted_keys(const Packing& pk, const int32_t* dims, const std::vec
       }
     }
   }
-  // dense root: level-1 fibers per row
-  for (int64_t p = 0; p < n; p++)
-    if (nl[p] <= 1) rowcnt[(size_t)pk.get(keys[p], 0) + 1]++;
-  for (int64_t r = 0; r < dims[0]; r++) rowcnt[(size_t)r + 1] += rowcnt[(size_t)r];
-  for (int64_t r = 0; r <= dims[0]; r++) o->pos[1][(size_t)r] = (int32_t)rowcnt[(size_t)r];
+  // dense root: pos1[r] = level-1 fibers in rows below r (their rows are sorted)
+  std::vector<int32_t> frow((size_t)total[1]);
+#pragma omp parallel num_threads(nt)
+  {
+    const int t = omp_get_thread_num();
+    int64_t c1 = cnt[(size_t)t * TT_MAX_ORDER + 1];
+    for (int64_t p = n * t / nt; p < n * (t + 1) / nt; p++)
+      if (nl[p] <= 1) frow[(size_t)c1++] = pk.get(keys[p], 0);
+  }
+#pragma omp parallel for schedule(static)
+  for (int64_t r = 0; r <= dims[0]; r++)
+    o->pos[1][(size_t)r] = (int32_t)(std::lower_bound(frow.begin(), frow.end(), (int32_t)r) - frow.begin());
   for (int l = 2; l < order; l++) o->pos[l][(size_t)total[l - 1]] = (int32_t)total[l];
   // compressed-root arrays for reference callers (compress_top_level form)
   o->pos[0] = {0, dims[0]};
@@ -341,18 +347,39 @@ void sort_dedupe(const Packing& pk, std::vector<uint64_t>& keys, std::vector<flo
   std::vector<uint32_t> idx(n);
   std::iota(idx.begin(), idx.end(), 0u);
   radix_sort_pairs(keys, idx, pk.total);
-  size_t m = 0;
-  out_vals.clear();
-  out_vals.reserve(n);
-  for (size_t p = 0; p < n;) {
-    size_t q = p;
-    double s = 0.0;
-    while (q < n && keys[q] == keys[p]) { s += (double)vals[idx[q]]; q++; }
-    keys[m++] = keys[p];
-    out_vals.push_back((float)s);
-    p = q;
+  // runs of equal keys, in parallel: a run belongs to the thread whose chunk holds
+  // its first entry; its values are summed in FP64 in input order (the sort is stable)
+  std::vector<uint8_t> first(n);
+#pragma omp parallel for schedule(static)
+  for (size_t p = 0; p < n; p++) first[p] = p == 0 || keys[p] != keys[p - 1];
+  const int nt = std::max(1, std::min(omp_get_max_threads(), (int)(n / 65536) + 1));
+  std::vector<size_t> off((size_t)nt + 1, 0);
+#pragma omp parallel num_threads(nt)
+  {
+    const int t = omp_get_thread_num();
+    size_t c = 0;
+    for (size_t p = n * t / nt; p < n * (t + 1) / nt; p++) c += first[p];
+    off[(size_t)t + 1] = c;
   }
-  keys.resize(m);
+  for (int t = 0; t < nt; t++) off[(size_t)t + 1] += off[(size_t)t];
+  const size_t m = off[(size_t)nt];
+  std::vector<uint64_t> k2(m);
+  out_vals.assign(m, 0.f);
+#pragma omp parallel num_threads(nt)
+  {
+    const int t = omp_get_thread_num();
+    size_t r = off[(size_t)t];
+    for (size_t p = n * t / nt; p < n * (t + 1) / nt; p++) {
+      if (!first[p]) continue;
+      double s = 0.0;
+      size_t q = p;
+      do { s += (double)vals[idx[q]]; q++; } while (q < n && !first[q]);
+      k2[r] = keys[p];
+      out_vals[r] = (float)s;
+      r++;
+    }
+  }
+  keys.swap(k2);
 }
 
 }  // namespace
