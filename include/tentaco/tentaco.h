@@ -253,6 +253,12 @@ int32_t tt_abi_version(void);
  */
 tt_status tt_csf_from_coo(int32_t order, const int32_t* dims, int64_t nnz,
                           const int32_t* coords, const float* vals, taco_tensor_t** out);
+/* The same canonical CSF as tt_csf_from_coo, built on the GPU (stable radix
+ * sort of packed coordinates, duplicates summed in FP64 in input order, levels
+ * from prefix sums); bit-identical to the host builder.  nnz < 2^31; needs a
+ * CUDA device (TT_ERR_NO_DEVICE otherwise). */
+tt_status tt_csf_from_coo_gpu(int32_t order, const int32_t* dims, int64_t nnz,
+                              const int32_t* coords, const float* vals, taco_tensor_t** out);
 /* Check monotone pos, in-range crd, sorted distinct children, non-empty inner fibers. */
 tt_status tt_csf_validate(const taco_tensor_t* B);
 /* The same tensor as a canonical CSF rooted at `mode` (level order: mode, then

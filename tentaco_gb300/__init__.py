@@ -102,6 +102,7 @@ def lib():
         "tt_ttv_host": (S, [_TP, _TP, _TP]),
         "tt_csf_from_coo": (S, [C.c_int32, C.POINTER(C.c_int32), C.c_int64, _P, _P, C.POINTER(_TP)]),
         "tt_csf_reroot": (S, [_TP, C.c_int32, C.POINTER(_TP)]),
+        "tt_csf_from_coo_gpu": (S, [C.c_int32, C.POINTER(C.c_int32), C.c_int64, _P, _P, C.POINTER(_TP)]),
         "tt_csf_validate": (S, [_TP]),
         "tt_tensor_free": (None, [_TP]),
         "tt_gen_zipf": (S, [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_int64, C.c_float,
@@ -217,6 +218,17 @@ class Tensor:
         f = np.zeros(12, dtype=np.float32)
         check(lib().tt_csf_features(self.ptr, rank, f.ctypes.data_as(C.POINTER(C.c_float))))
         return f
+
+
+def csf_from_coo_gpu(dims, coords: np.ndarray, vals: np.ndarray) -> "Tensor":
+    """csf_from_coo built on the GPU (bit-identical result)."""
+    coords = np.ascontiguousarray(coords, dtype=np.int32)
+    vals = np.ascontiguousarray(vals, dtype=np.float32)
+    d = np.ascontiguousarray(dims, dtype=np.int32)
+    out = _TP()
+    check(lib().tt_csf_from_coo_gpu(len(d), _i32p(d), coords.shape[0], coords.ctypes.data, vals.ctypes.data,
+                                    C.byref(out)))
+    return Tensor(out)
 
 
 def csf_reroot(B, mode: int) -> "Tensor":

@@ -414,39 +414,34 @@ TT_EXPORT tt_status tt_csf_from_coo(int32_t order, const int32_t* dims, int64_t 
   return TT_OK;
 }
 
-// The same tensor as a CSF rooted at `mode`: level order (mode, then the other
-// modes in increasing order).  v must be a validated CSF; the new CSF is built
-// like tt_csf_from_coo (packed keys, radix sort, lexicographic, dense root) from
-// every nonzero's coordinates in the new order.
-tt_status tt::csf_reroot(const CsfView& v, int mode, taco_tensor_t** out) {
-  *out = nullptr;
+// Every nonzero's coordinates in the level order of the CSF rooted at `mode`
+// (mode, then the other modes in increasing order), at its leaf position:
+// co[p * order + k] = coordinate of old mode perm[k]; nd: the permuted dims.
+// v must be a validated CSF.
+tt_status tt::csf_rerooted_coords(const CsfView& v, int mode, std::vector<int32_t>& co, int32_t* nd) {
   const int order = v.order;
   if (mode < 0 || mode >= order) return set_error(TT_ERR_INVALID_ARGUMENT, "mode %d of an order-%d tensor", mode, order);
   int perm[TT_MAX_ORDER];  // new level k holds old mode perm[k]
   perm[0] = mode;
   for (int m = 0, k = 1; m < order; m++)
     if (m != mode) perm[k++] = m;
-  int32_t nd[TT_MAX_ORDER];
   for (int k = 0; k < order; k++) nd[k] = v.dims[perm[k]];
-  Packing pk(order, nd);
-  if (!pk.ok) return set_error(TT_ERR_UNSUPPORTED, "coordinates need %d bits (> 63)", pk.total);
-  std::vector<uint64_t> keys((size_t)v.nnz);
-  // walk every root position; a nonzero's key goes to its leaf position
+  co.resize((size_t)v.nnz * order);
+  // walk every root position depth first; a nonzero's coordinates go to its leaf position
 #pragma omp parallel for schedule(dynamic, 64)
   for (int64_t r = 0; r < v.nroot; r++) {
-    int32_t c[TT_MAX_ORDER], q[TT_MAX_ORDER];
+    int32_t c[TT_MAX_ORDER];
     c[0] = v.dense_root ? (int32_t)r : v.root_crd[r];
     int64_t lo[TT_MAX_ORDER], hi[TT_MAX_ORDER];
     lo[1] = v.pos[1][r];
     hi[1] = v.pos[1][r + 1];
-    // iterative depth-first walk over levels 1..order-1
     int l = 1;
     while (l >= 1) {
       if (lo[l] >= hi[l]) { l--; if (l >= 1) lo[l]++; continue; }
       c[l] = v.crd[l][lo[l]];
       if (l == order - 1) {
+        int32_t* q = co.data() + (size_t)lo[l] * order;
         for (int k = 0; k < order; k++) q[k] = c[perm[k]];
-        keys[(size_t)lo[l]] = pk.pack(q);
         lo[l]++;
       } else {
         lo[l + 1] = v.pos[l + 1][lo[l]];
@@ -455,12 +450,18 @@ tt_status tt::csf_reroot(const CsfView& v, int mode, taco_tensor_t** out) {
       }
     }
   }
-  std::vector<float> vals(v.vals, v.vals + v.nnz), uv;
-  sort_dedupe(pk, keys, vals, uv);  // distinct keys: only the sort does work
-  auto* o = new OwnedTensor();
-  csf_from_sorted_keys(pk, nd, keys, std::move(uv), o);
-  *out = &o->t;
   return TT_OK;
+}
+
+// The same tensor as a CSF rooted at `mode`, built on the host like
+// tt_csf_from_coo (packed keys, radix sort, lexicographic, dense root).
+tt_status tt::csf_reroot(const CsfView& v, int mode, taco_tensor_t** out) {
+  *out = nullptr;
+  std::vector<int32_t> co;
+  int32_t nd[TT_MAX_ORDER];
+  tt_status s = csf_rerooted_coords(v, mode, co, nd);
+  if (s != TT_OK) return s;
+  return tt_csf_from_coo(v.order, nd, v.nnz, co.data(), v.vals, out);
 }
 
 TT_EXPORT tt_status tt_csf_reroot(const taco_tensor_t* B, int32_t mode, taco_tensor_t** out) {

@@ -61,6 +61,9 @@ tt_status csf_check_error(int level, uint64_t word);
 // The validated CSF v re-rooted at `mode` (level order: mode, then the other modes
 // in increasing order), as a library-owned tensor (free with tt_tensor_free).
 tt_status csf_reroot(const CsfView& v, int mode, taco_tensor_t** out);
+// Every nonzero's coordinates (nnz x order) in the level order of the CSF rooted
+// at `mode`, and the permuted dims (nd), from the validated CSF v.
+tt_status csf_rerooted_coords(const CsfView& v, int mode, std::vector<int32_t>& co, int32_t* nd);
 
 // A dense-root CSF split into leaf-mode slabs (leaf coordinate c is in slab
 // c / width).  Each slab is a CSF with every row; its leaf arrays are the run

@@ -585,7 +585,13 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
     if (op != TT_OP_MTTKRP) return set_error(TT_ERR_UNSUPPORTED, "an output mode other than 0 needs an MTTKRP plan");
     if (mode < 0 || mode >= v.order) return set_error(TT_ERR_INVALID_ARGUMENT, "mode %d of an order-%d tensor", mode, v.order);
     if ((s = csf_check(v)) != TT_OK) return s;
-    if ((s = csf_reroot(v, mode, &rerooted)) != TT_OK) return s;
+    {
+      // coordinates in the new level order (host), sorted and built on the GPU
+      std::vector<int32_t> co;
+      int32_t nd[TT_MAX_ORDER];
+      if ((s = csf_rerooted_coords(v, mode, co, nd)) != TT_OK) return s;
+      if ((s = tt_csf_from_coo_gpu(v.order, nd, v.nnz, co.data(), v.vals, &rerooted)) != TT_OK) return s;
+    }
     if ((s = csf_view(rerooted, &v)) != TT_OK) return s;
     B = rerooted;
   }
