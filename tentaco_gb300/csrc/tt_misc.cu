@@ -63,6 +63,29 @@ cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+__global__ void flat_kexp_kernel(const int32_t* __restrict__ crd1, const int32_t* __restrict__ pos2, int64_t nf1,
+                                 int32_t* __restrict__ kexp) {
+  // one level-1 fiber per thread (grid-stride); its nonzeros get its coordinate
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nf1; f += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t k = crd1[f];
+    for (int32_t p = pos2[f]; p < pos2[f + 1]; p++) kexp[p] = k;
+  }
+}
+
+__global__ void flat_rnz_kernel(const int32_t* __restrict__ pos1, const int32_t* __restrict__ pos2, int64_t nroot,
+                                int32_t* __restrict__ rnz) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nroot; i += (int64_t)gridDim.x * blockDim.x)
+    rnz[i] = pos2[pos1[i]];
+}
+
+cudaError_t launch_flat_index(const int32_t* pos1, const int32_t* crd1, const int32_t* pos2, int64_t nroot,
+                              int64_t nf1, int32_t* kexp, int32_t* rnz, cudaStream_t s) {
+  auto grid = [](int64_t m) { return (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, 152 * 16)); };
+  if (nf1 > 0) flat_kexp_kernel<<<grid(nf1), 256, 0, s>>>(crd1, pos2, nf1, kexp);
+  flat_rnz_kernel<<<grid(nroot + 1), 256, 0, s>>>(pos1, pos2, nroot, rnz);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_ttv(const WalkArgs& a, int vals_kind, cudaStream_t s) {
   if (a.nblocks == 0) return cudaSuccess;
   const int grid = (a.nblocks + 7) / 8;  // one warp per unit, 8 warps per block

@@ -67,6 +67,8 @@ struct alignas(64) WalkArgs {
   int32_t* segmeta;       // 4 ints per segment
   int32_t wcap;           // staged kernels: window fibers per block the shared memory holds
   int32_t* err;           // staged kernels: set nonzero if a block's window exceeds wcap
+  const int32_t* kexp;    // flat walk: the middle coordinate of every nonzero (padded)
+  const int32_t* rnz;     // flat walk: first nonzero of every row (nrows + 1)
 };
 
 constexpr int kEmpty = -2;  // summary of a team that owns no nonzeros
@@ -100,6 +102,13 @@ __host__ __device__ inline size_t walk_smem_bytes(int P, int tb, int rp, int vby
 // Lean kernel, shared memory of one warp: coordinate runs TW x (G+4) int32,
 // value runs TW x (G*vbytes + 16) bytes, window starts and coordinates (a
 // warp's window has at most TW*G + 1 fibers).
+// Shared memory of one flat-walk warp: leaf and middle coordinate runs (tw runs of
+// G + 4 int32 each) and value runs (tw runs of G * vbytes + 16 bytes).
+__host__ __device__ inline size_t flat_warp_bytes(int G, int tw, int vbytes) {
+  size_t b = (size_t)2 * tw * (G + 4) * 4 + (size_t)tw * ((size_t)G * vbytes + 16);
+  return (b + 15) & ~(size_t)15;
+}
+
 __host__ __device__ inline size_t lean_warp_bytes(int G, int tw, int vbytes) {
   const size_t pu = (size_t)tw * G;
   size_t b = (size_t)tw * (G + 4) * 4 + (size_t)tw * ((size_t)G * vbytes + 16);
@@ -624,6 +633,126 @@ struct Walk {
 #pragma unroll
         for (int c = 0; c < CPT; c++) { f2[c] = fmaf(f3[c], cw[c], f2[c]); ra[c] = fmaf(f2[c], crow[c], ra[c]); }
       }
+    }
+    if (!flushed) {
+      X.h = ip; X.t = kNone;
+#pragma unroll
+      for (int c = 0; c < CPT; c++) X.ha[c] = ra[c];
+    } else {
+      X.t = ip;
+#pragma unroll
+      for (int c = 0; c < CPT; c++) X.ta[c] = ra[c];
+    }
+  }
+
+  // ---- flat walk (family 3, order 3) ------------------------------------------
+  // Every nonzero carries its middle coordinate k (a.kexp), so a team accumulates
+  // A(i,:) += (v * C(k,:)) * D(l,:) per nonzero with both factor rows gathered
+  // (C is small and stays in L2): the reference's own loop arithmetic
+  // (tensor_kernels/mttkrp3_csf_cpu_taco.h:45), with no fiber boundaries in the
+  // walk; only row ends (a.rnz) are checked, per batch.
+  //   lc, kc, vt: the team's leaf coordinates, middle coordinates and values
+  //   rlo, rhi: rows holding the unit's first nonzero and the next unit's
+  template <int U>
+  __device__ __forceinline__ void walk_flat(int s, int n, const int32_t* lc, const int32_t* kc, const unsigned char* vt,
+                                            int rlo, int rhi, Summ<CPT>& X) const {
+    static_assert(ORDER == 3, "the flat walk is built for three modes");
+    const uint64_t pol = a.gpol == 1 ? policy_evict_normal() : policy_evict_last();
+    const int32_t* rnz = a.rnz;
+    const unsigned char* fd = static_cast<const unsigned char*>(a.fac[1]) + q * LB;  // D: leaf factor
+    const unsigned char* fc = static_cast<const unsigned char*>(a.fac[0]) + q * LB;  // C: middle factor
+    int ip = (int)search_le(rnz, rlo, rhi, s);
+    int rend = rnz[ip + 1];
+    float ra[CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; c++) ra[c] = 0.f;
+    bool flushed = false;
+    // one nonzero: ra += (v * c) * d, value half HV of word vw (16-bit) or float v
+    auto acc16 = [&](const uint32_t (&gc)[NWD], const uint32_t (&gd)[NWD], uint32_t vw, auto hv) {
+      constexpr int HV = decltype(hv)::value;
+      float d[CPT];
+      piece_cvt(gd, d);
+      if constexpr (CPT == 1) {
+        float t = 0.f;
+        mfma1<FK, HV>(t, gc[0], vw);
+        ra[0] = fmaf(t, d[0], ra[0]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < CPT / 2; k++) {
+          float t0 = 0.f, t1 = 0.f;
+          mfma2<FK, HV>(t0, t1, gc[k], vw);
+          ra[2 * k] = fmaf(t0, d[2 * k], ra[2 * k]);
+          ra[2 * k + 1] = fmaf(t1, d[2 * k + 1], ra[2 * k + 1]);
+        }
+      }
+    };
+    auto acc32 = [&](const uint32_t (&gc)[NWD], const uint32_t (&gd)[NWD], float v) {
+      float c[CPT], d[CPT];
+      piece_cvt(gc, c);
+      piece_cvt(gd, d);
+#pragma unroll
+      for (int k = 0; k < CPT; k++) ra[k] = fmaf(v * c[k], d[k], ra[k]);
+    };
+    auto next_row = [&]() {
+      flush(ip, ra, flushed, X);
+      ip++;
+      rend = rnz[ip + 1];
+    };
+    auto load = [&](uint32_t (&gc)[U][NWD], uint32_t (&gd)[U][NWD], int j) {
+      int32_t l[U], k[U];
+#pragma unroll
+      for (int w = 0; w < U / 4; w++) {
+        const int4 l4 = reinterpret_cast<const int4*>(lc + j)[w];
+        const int4 k4 = reinterpret_cast<const int4*>(kc + j)[w];
+        l[4 * w] = l4.x; l[4 * w + 1] = l4.y; l[4 * w + 2] = l4.z; l[4 * w + 3] = l4.w;
+        k[4 * w] = k4.x; k[4 * w + 1] = k4.y; k[4 * w + 2] = k4.z; k[4 * w + 3] = k4.w;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        piece_load(fc + (size_t)(uint32_t)k[u] * FRB, pol, gc[u]);
+        piece_load(fd + (size_t)(uint32_t)l[u] * FRB, pol, gd[u]);
+      }
+    };
+    auto consume = [&](const uint32_t (&gc)[U][NWD], const uint32_t (&gd)[U][NWD], int j) {
+      const bool inside = s + j + U <= rend;  // the batch lies in one row
+      if constexpr (MIXED) {
+        uint32_t vw[U / 2];
+        vals_raw<U>(vt + (size_t)j * VB, vw);
+#pragma unroll
+        for (int u = 0; u < U; u += 2) {
+          if (!inside) while (s + j + u >= rend) next_row();
+          acc16(gc[u], gd[u], vw[u >> 1], std::integral_constant<int, 0>{});
+          if (!inside) while (s + j + u + 1 >= rend) next_row();
+          acc16(gc[u + 1], gd[u + 1], vw[u >> 1], std::integral_constant<int, 1>{});
+        }
+      } else {
+        float v[U];
+        vals_load<U>(vt + (size_t)j * VB, v);
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          if (!inside) while (s + j + u >= rend) next_row();
+          acc32(gc[u], gd[u], v[u]);
+        }
+      }
+    };
+    const int nb = n / U;
+    uint32_t cA[U][NWD], dA[U][NWD], cB[U][NWD], dB[U][NWD];
+    if (nb > 0) load(cA, dA, 0);
+    for (int b = 0; b < nb; b += 2) {
+      if (b + 1 < nb) load(cB, dB, (b + 1) * U);
+      consume(cA, dA, b * U);
+      if (b + 1 < nb) {
+        if (b + 2 < nb) load(cA, dA, (b + 2) * U);
+        consume(cB, dB, (b + 1) * U);
+      }
+    }
+    for (int j = nb * U; j < n; j++) {  // ragged end (the tensor's last tile only)
+      uint32_t gc[NWD], gd[NWD];
+      piece_load(fc + (size_t)(uint32_t)kc[j] * FRB, pol, gc);
+      piece_load(fd + (size_t)(uint32_t)lc[j] * FRB, pol, gd);
+      while (s + j >= rend) next_row();
+      if constexpr (MIXED) acc16(gc, gd, (uint32_t)reinterpret_cast<const uint16_t*>(vt)[j], std::integral_constant<int, 0>{});
+      else acc32(gc, gd, val_one(vt, j));
     }
     if (!flushed) {
       X.h = ip; X.t = kNone;
@@ -1368,6 +1497,26 @@ __device__ __forceinline__ void stage_runs(const int32_t* gl, const void* vals, 
   }
 }
 
+// A tile's int32 stream alone into per-run shared memory (the layout of
+// stage_runs' coordinate runs).
+__device__ __forceinline__ void stage_int_runs(const int32_t* g, int n4, int lg_cpr, int lane, int32_t* sdst,
+                                               uint64_t pol) {
+  constexpr int R = 4;
+  for (int c0 = lane; c0 < n4; c0 += 32 * R) {
+    int4 li[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int c = c0 + 32 * r;
+      if (c < n4) li[r] = ld_stream_i4(g + 4 * c, pol);
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int c = c0 + 32 * r;
+      if (c < n4) reinterpret_cast<int4*>(sdst)[c + (c >> lg_cpr)] = li[r];
+    }
+  }
+}
+
 // A tile's fiber window: W + 1 fiber starts and W fiber coordinates, all loads
 // of a round issued before its stores.
 __device__ __forceinline__ void stage_window(const int32_t* gpos, const int32_t* gcrd, int W, int lane,
@@ -1480,6 +1629,50 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_lean_kernel(const __grid_con
                              s_pos, s_fcrd, W, fs, pb, pn, X);
   warp_tree(wk, X);
   if (lane < LPR) settle_unit(a, wk, X, head_ff, fs, s_pos[0], ustart64, pn[0], u, q);
+}
+
+// Flat kernel (family 3, order 3): the lean kernel's warp tiles and merge, with
+// the middle coordinate of every nonzero staged beside its leaf coordinate and
+// value; teams run walk_flat (row ends only).
+template <int PREC, int CPT, int LPR, int MINB>
+__global__ void __launch_bounds__(256, MINB) mttkrp_flat_kernel(const __grid_constant__ WalkArgs a) {
+  using WK = Walk<3, PREC, CPT, LPR>;
+  constexpr int VB = WK::VB;
+  constexpr int TW = 32 / LPR;
+  constexpr int U = WK::LB >= 8 ? 4 : 8;  // nonzeros per gather batch (two batches of two rows each)
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int u = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (u >= a.nblocks) return;  // whole warp
+  const int G = a.G, PU = a.P;
+  unsigned char* ws = smem + (size_t)warp * flat_warp_bytes(G, TW, VB);
+  int32_t* s_lc = reinterpret_cast<int32_t*>(ws);
+  int32_t* s_kc = s_lc + TW * (G + 4);
+  unsigned char* s_val = reinterpret_cast<unsigned char*>(s_kc + TW * (G + 4));
+  const int32_t* pb = a.part + (size_t)u * 2;
+  const int32_t* pn = pb + 2;
+  const int64_t ustart64 = (int64_t)u * PU;
+  const int ustart = (int)ustart64;
+  const int cnt = (int)min((int64_t)PU, a.nnz - ustart64);
+  {
+    const uint64_t polF = policy_evict_first();
+    const int n4 = (cnt + 3) >> 2;
+    stage_runs<VB>(a.crd[2] + ustart64, a.vals, ustart64, n4, a.lgG - 2, lane, s_lc, s_val, polF);
+    stage_int_runs(a.kexp + ustart64, n4, a.lgG - 2, lane, s_kc, polF);
+  }
+  __syncwarp();
+  const int team = lane / LPR, q = lane % LPR;
+  WK wk(a, q);
+  Summ<CPT> X;
+  X.h = kEmpty;
+  X.t = kNone;
+  const int s = ustart + team * G;
+  if (s < ustart + cnt)
+    wk.template walk_flat<U>(s, min(G, ustart + cnt - s), s_lc + team * (G + 4), s_kc + team * (G + 4),
+                             s_val + (size_t)team * (G * VB + 16), pb[0], pn[0], X);
+  warp_tree(wk, X);
+  // the unit's first row started before it when its first nonzero lies earlier
+  if (lane < LPR) settle_unit(a, wk, X, 0, 0, a.rnz[pb[0]], ustart64, pn[0], u, q);
 }
 
 // TMA kernel (family 2): the lean kernel's warp tiles, with the nonzero-level

@@ -26,14 +26,15 @@ using namespace tt;
 namespace tt {
 
 // ---------------------------------------------------------------------------
-// variant table: family {lean warp tile, staged, ring} x threads {256,512} x
+// variant table: family {lean warp tile, staged, TMA gather, flat} x threads {256,512} x
 // nonzeros per team (5 values per family) x columns per lane {8,4,2,1}
 // ---------------------------------------------------------------------------
 static const int kTB[2] = {256, 512};
-static const int kGF[3][5] = {{16, 32, 64, 128, 256}, {4, 8, 16, 32, 64}, {16, 32, 64, 128, 256}};
+static const int kGF[4][5] = {{16, 32, 64, 128, 256}, {4, 8, 16, 32, 64}, {16, 32, 64, 128, 256},
+                              {16, 32, 64, 128, 256}};
 static const int kCPT[4] = {8, 4, 2, 1};
 constexpr int kPerFamily = 2 * 5 * 4;
-constexpr int kNumVariants = 3 * kPerFamily;  // lean, staged, TMA gather
+constexpr int kNumVariants = 4 * kPerFamily;  // lean, staged, TMA gather, flat
 constexpr size_t kSmemLimit = (size_t)227 * 1024;
 
 VariantSpec variant_spec(int id) {
@@ -59,14 +60,16 @@ int variant_id(int tb, int G, int cpt, int staged) {
 // Kernel family a variant launches: the lean family's second thread value selects
 // its tighter register budget (family 3); both launch 256-thread blocks.
 // The TMA family's second value selects 8 stages in flight per warp instead of 4 (family 5).
+// The flat family (order 3) launches family 6, or 7 with the tighter register budget.
 int launch_family(const VariantSpec& v) {
   if (v.staged == 0) return v.tb == 512 ? 3 : 0;
   if (v.staged == 2) return v.tb == 512 ? 5 : 2;
+  if (v.staged == 3) return v.tb == 512 ? 7 : 6;
   return v.staged;
 }
 int tma_stages(const VariantSpec& v) { return v.tb == 512 ? 8 : 4; }
 
-// Resident 256-thread blocks a lean variant's registers are budgeted for.
+// Resident 256-thread blocks a lean (or flat) variant's registers are budgeted for.
 int lean_blocks(const VariantSpec& v) { return v.cpt >= 4 ? (v.tb == 512 ? 3 : 2) : (v.tb == 512 ? 4 : 3); }
 
 // Nonzeros of one work unit: a warp's tile for the lean family, a block's tile otherwise.
@@ -81,6 +84,7 @@ size_t variant_smem(const VariantSpec& v, int rp, int prec, int wcap) {
   const int lpr = rp / v.cpt;
   const int P = (v.tb / lpr) * v.G;
   if (v.staged == 0) return (size_t)(256 / 32) * lean_warp_bytes(v.G, 32 / lpr, val_bytes(prec));
+  if (v.staged == 3) return (size_t)(256 / 32) * flat_warp_bytes(v.G, 32 / lpr, val_bytes(prec));
   if (v.staged == 2)  // TMA gather: 8 warps, each with its ring of row stages and its lean tile
     return (size_t)(256 / 32) * tma_warp_bytes(v.G, 32 / lpr, val_bytes(prec), rp * fac_bytes(prec), tma_stages(v));
   return v.staged ? stage_smem_bytes(P, wcap, v.tb, rp, val_bytes(prec), fac_bytes(prec))
@@ -110,6 +114,7 @@ bool variant_valid(int id, int order, int rank, int prec) {
   // TMA gather: four rows per copy land on 128-byte boundaries (rows of 32-byte
   // multiples), and a team's G nonzeros are whole stages of U = lanes-per-row rows
   if (v.staged == 2 && ((rp * fac_bytes(prec)) % 32 != 0 || v.G % lpr != 0)) return false;
+  if (v.staged == 3 && order != 3) return false;  // the flat walk is built for three modes
   return walk_launcher(order, prec, v.cpt, lpr, launch_family(v)) != nullptr;
 }
 
@@ -332,9 +337,19 @@ tt_status use_variant(tt_plan* p, int id) {
   p->nblocks = (int)((p->nnz + p->P - 1) / p->P);
   p->launcher = walk_launcher(p->order, p->prec, p->cpt, p->lpr, launch_family(v));
   if (!p->launcher) return set_error(TT_ERR_UNSUPPORTED, "variant %d not compiled for this shape", id);
+  if (v.staged == 3 && p->slabs != 1) return set_error(TT_ERR_UNSUPPORTED, "the flat walk runs without slabs");
   tt_status s = alloc_walk_scratch(p, p->P);
   if (s != TT_OK) return s;
   p->part_ready = false;
+  if (v.staged == 3 && !p->d_kexp && p->nnz > 0) {
+    // every nonzero's middle coordinate and every row's first nonzero (once per plan)
+    if ((s = dev_alloc(p, &p->d_kexp, (size_t)pad16(p->nnz))) != TT_OK) return s;
+    if ((s = dev_alloc(p, &p->d_rnz, (size_t)p->nroot + 1)) != TT_OK) return s;
+    CK(cudaMemsetAsync(p->d_kexp, 0, sizeof(int32_t) * (size_t)pad16(p->nnz), p->stream));
+    CK(launch_flat_index(p->d_pos[1], p->d_crd[1], p->d_pos[2], p->nroot, p->count[1], p->d_kexp, p->d_rnz,
+                         p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+  }
   p->wcap = 1;
   if (p->staged == 1 && p->nnz > 0) {
     // size the window-row region from this tensor's partition (computed once here)
@@ -386,6 +401,8 @@ WalkArgs walk_args(const tt_plan* p, float* A, int q) {
   a.nblocks = (int)((sl.nnz + p->P - 1) / p->P);
   a.wcap = p->wcap;
   a.err = p->d_err;
+  a.kexp = p->d_kexp;
+  a.rnz = p->d_rnz;
   for (int m = 0; m < 3; m++) a.fac_rows[m] = m + 1 < p->order ? (int32_t)p->dims[m + 1] : 0;
   return a;
 }
@@ -533,11 +550,11 @@ TT_EXPORT tt_status tt_variant_get(int32_t id, tt_variant_info* info) {
   info->lanes_per_row = 32 / v.cpt;
   info->nnz_per_block = v.tb / info->lanes_per_row * v.G;
   info->staged = v.staged;
-  static const char* fam[3] = {"lean", "stage", "tma"};
-  if (v.staged == 0) {  // lean: 256-thread blocks, register budget for b resident blocks per SM
+  static const char* fam[4] = {"lean", "stage", "tma", "flat"};
+  if (v.staged == 0 || v.staged == 3) {  // lean / flat: 256-thread blocks, budget for b resident blocks per SM
     info->threads = 256;
     info->nnz_per_block = 256 / info->lanes_per_row * v.G;
-    std::snprintf(info->name, sizeof(info->name), "lean_b%d_g%d_c%d", lean_blocks(v), v.G, v.cpt);
+    std::snprintf(info->name, sizeof(info->name), "%s_b%d_g%d_c%d", fam[v.staged], lean_blocks(v), v.G, v.cpt);
   } else if (v.staged == 2) {  // TMA gather: 256-thread blocks, s stages in flight per warp
     info->threads = 256;
     info->nnz_per_block = 256 / info->lanes_per_row * v.G;

@@ -48,6 +48,8 @@ struct tt_plan {
   int32_t* d_err = nullptr;  // [0]: kernel error word, [1]: scratch for the window size
   tt::WalkLauncher launcher = nullptr;
   int32_t* d_part = nullptr;
+  int32_t* d_kexp = nullptr;  // flat walk: middle coordinate of every nonzero (padded)
+  int32_t* d_rnz = nullptr;   // flat walk: first nonzero of every root position
   // the partition depends only on the CSF and the unit size: a single-slab plan
   // computes it once per variant (part_ready) and times it (part_ms)
   bool part_ready = false;
@@ -57,7 +59,7 @@ struct tt_plan {
   double* d_segcarry = nullptr;  // MTTKRP: 2 FP64 rows per segment of work units
   int32_t* d_segmeta = nullptr;  // MTTKRP: 4 ints per segment
   int64_t scratch_blocks = 0;
-  float sweep_ms[128] = {};
+  float sweep_ms[160] = {};
   // leaf-mode slabs: one walk pass per slab, adding into the output (slabs == 1:
   // slab[0] is the whole tensor)
   struct SlabDev {

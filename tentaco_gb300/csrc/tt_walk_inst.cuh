@@ -9,24 +9,21 @@
 namespace tt {
 namespace {
 // fam 0: lean warp-tile walk, 1: shared-memory staged, 2 / 5: TMA-gather walk with
-// 4 / 8 stages in flight per warp, 3: lean with the tighter register budget.
+// 4 / 8 stages in flight per warp, 3: lean with the tighter register budget,
+// 6 / 7: flat walk (order 3) with the looser / tighter budget.
 // units: work units of the partition (warp tiles except for fam 1, blocks there).
 // Resident blocks per SM the lean kernel's registers are budgeted for: the
 // variant's thread axis selects the looser (tb 256) or tighter (tb 512) budget;
 // both launch 256-thread blocks.
 constexpr int lean_minb(int cpt, bool tight) { return cpt >= 4 ? (tight ? 3 : 2) : (tight ? 4 : 3); }
 
-template <int CPT, int LPR, int FAM>
-cudaError_t launch_walk(const WalkArgs& a, int units, int tb, size_t smem, cudaStream_t s) {
-  constexpr bool kTight = FAM == 3;  // lean with the tighter register budget
-  auto k = FAM == 1   ? mttkrp_stage_kernel<TT_ORDER, TT_PREC, CPT, LPR>
-         : FAM == 2 ? mttkrp_tma_kernel<TT_ORDER, TT_PREC, CPT, LPR, 4>
-         : FAM == 5 ? mttkrp_tma_kernel<TT_ORDER, TT_PREC, CPT, LPR, 8>
-                    : mttkrp_lean_kernel<TT_ORDER, TT_PREC, CPT, LPR, lean_minb(CPT, kTight)>;
-  const bool warp_units = FAM != 1;  // lean and TMA: one work unit per warp, 256-thread blocks
-  if (warp_units) tb = 256;
+// One launch: warp-unit kernels run 256-thread blocks; `configured` is the calling
+// kernel's own record of the dynamic shared memory it was allowed.
+template <typename K>
+cudaError_t launch_k(K k, const WalkArgs& a, int units, int tb, size_t smem, cudaStream_t s, bool warp_units,
+                     size_t& configured) {
+  if (warp_units) tb = 256;  // lean, TMA and flat: one work unit per warp, 256-thread blocks
   const int grid = warp_units ? (units + tb / 32 - 1) / (tb / 32) : units;
-  static size_t configured = 48 * 1024;
   if (smem > configured) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -35,18 +32,45 @@ cudaError_t launch_walk(const WalkArgs& a, int units, int tb, size_t smem, cudaS
   k<<<grid, tb, smem, s>>>(a);
   return cudaGetLastError();
 }
+
+template <int CPT, int LPR, int FAM>
+cudaError_t launch_walk(const WalkArgs& a, int units, int tb, size_t smem, cudaStream_t s) {
+  constexpr bool kTight = FAM == 3;  // lean with the tighter register budget
+  auto k = FAM == 1   ? mttkrp_stage_kernel<TT_ORDER, TT_PREC, CPT, LPR>
+         : FAM == 2 ? mttkrp_tma_kernel<TT_ORDER, TT_PREC, CPT, LPR, 4>
+         : FAM == 5 ? mttkrp_tma_kernel<TT_ORDER, TT_PREC, CPT, LPR, 8>
+                    : mttkrp_lean_kernel<TT_ORDER, TT_PREC, CPT, LPR, lean_minb(CPT, kTight)>;
+  static size_t configured = 48 * 1024;
+  return launch_k(k, a, units, tb, smem, s, FAM != 1, configured);
+}
+
+#if TT_ORDER == 3
+// flat walk (families 6 / 7: looser / tighter register budget), three modes only
+template <int CPT, int LPR, int FAM>
+cudaError_t launch_flat(const WalkArgs& a, int units, int tb, size_t smem, cudaStream_t s) {
+  auto k = mttkrp_flat_kernel<TT_PREC, CPT, LPR, lean_minb(CPT, FAM == 7)>;
+  static size_t configured = 48 * 1024;
+  return launch_k(k, a, units, tb, smem, s, true, configured);
+}
+#endif
 }  // namespace
 
 WalkLauncher TT_LOOKUP(int cpt, int lpr, int fam) {
+#if TT_ORDER == 3
+#define TT_FLAT(C, L) fam == 6 ? &launch_flat<C, L, 6> : fam == 7 ? &launch_flat<C, L, 7> :
+#else
+#define TT_FLAT(C, L) fam >= 6 ? (WalkLauncher) nullptr :
+#endif
 #define TT_CASE(C, L)                                                        \
   if (cpt == C && lpr == L)                                                  \
-    return fam == 5 ? &launch_walk<C, L, 5> : fam == 3 ? &launch_walk<C, L, 3> : fam == 2 ? &launch_walk<C, L, 2> \
+    return TT_FLAT(C, L) fam == 5 ? &launch_walk<C, L, 5> : fam == 3 ? &launch_walk<C, L, 3> : fam == 2 ? &launch_walk<C, L, 2> \
          : fam == 1 ? &launch_walk<C, L, 1> : &launch_walk<C, L, 0>;
   TT_CASE(1, 8) TT_CASE(2, 4) TT_CASE(4, 2) TT_CASE(8, 1)     // rank 8
   TT_CASE(1, 16) TT_CASE(2, 8) TT_CASE(4, 4) TT_CASE(8, 2)    // rank 16
   TT_CASE(1, 32) TT_CASE(2, 16) TT_CASE(4, 8) TT_CASE(8, 4)   // rank 32
   TT_CASE(2, 32) TT_CASE(4, 16) TT_CASE(8, 8)                 // rank 64
 #undef TT_CASE
+#undef TT_FLAT
   return nullptr;
 }
 }  // namespace tt

@@ -64,7 +64,7 @@ def test_status_strings():
 
 
 def test_variant_table():
-    assert tt.num_variants() == 120
+    assert tt.num_variants() == 160
     for order in (3, 4):
         for rank in (1, 8, 10, 16, 20, 32, 40, 64):
             for prec in ("fp32", "bf16", "bf16f"):
@@ -76,6 +76,9 @@ def test_variant_table():
     assert info["name"] == "lean_b2_g64_c4"
     assert tt.variant_info(tt.default_variant(3, 32, "fp16"))["name"] == "lean_b2_g32_c8"
     assert tt.variant_info(3)["staged"] == 0 and tt.variant_info(43)["name"].startswith("stage")
+    # the flat family (ids 120..159) runs three-mode tensors only
+    assert tt.variant_info(134)["name"] == "flat_b3_g128_c2"
+    assert tt.variant_valid(134, 3, 32, "fp16") and not tt.variant_valid(134, 4, 32, "fp16")
 
 
 def test_invalid_csf_rejected():
