@@ -29,7 +29,7 @@ cudaError_t launch_partition(int order, const WalkArgs& a, cudaStream_t s);
 // Flat walk indexes of a 3-level CSF: kexp[p] = crd1 of the fiber holding nonzero p
 // (p < pos2[nf1]), rnz[i] = pos2[pos1[i]] for i = 0..nroot.
 cudaError_t launch_flat_index(const int32_t* pos1, const int32_t* crd1, const int32_t* pos2, int64_t nroot,
-                              int64_t nf1, int32_t* kexp, int32_t* rnz, cudaStream_t s);
+                              int64_t nf1, int64_t nnz, int32_t* kexp, int32_t* rnz, cudaStream_t s);
 // FP64 merge of the rows the walk left in the carry buffer (after the walk kernel).
 cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s);
 // TTV walk over units of 32 * kTtvNpt nonzeros (a: the 2-level view, see tt_ttv.cuh).

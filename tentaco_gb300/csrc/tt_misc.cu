@@ -63,12 +63,25 @@ cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// one thread per chunk of kChunk consecutive nonzeros: the fiber of the chunk's
+// first nonzero by binary search over pos2, then forward through the fiber ends
+// (a fiber of any length is spread over many threads)
+constexpr int kKexpChunk = 64;
 __global__ void flat_kexp_kernel(const int32_t* __restrict__ crd1, const int32_t* __restrict__ pos2, int64_t nf1,
                                  int32_t* __restrict__ kexp) {
-  // one level-1 fiber per thread (grid-stride); its nonzeros get its coordinate
-  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nf1; f += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t k = crd1[f];
-    for (int32_t p = pos2[f]; p < pos2[f + 1]; p++) kexp[p] = k;
+  const int64_t nnz = pos2[nf1];
+  const int64_t nchunks = (nnz + kKexpChunk - 1) / kKexpChunk;
+  for (int64_t ch = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; ch < nchunks; ch += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p0 = ch * kKexpChunk, p1 = min(nnz, p0 + kKexpChunk);
+    int64_t f = search_le(pos2, 0, nf1 - 1, p0);  // last fiber starting at or before p0
+    int64_t fend = pos2[f + 1];
+    for (int64_t p = p0; p < p1; p++) {
+      while (p >= fend) {  // empty fibers are skipped too
+        f++;
+        fend = pos2[f + 1];
+      }
+      kexp[p] = crd1[f];
+    }
   }
 }
 
@@ -79,9 +92,9 @@ __global__ void flat_rnz_kernel(const int32_t* __restrict__ pos1, const int32_t*
 }
 
 cudaError_t launch_flat_index(const int32_t* pos1, const int32_t* crd1, const int32_t* pos2, int64_t nroot,
-                              int64_t nf1, int32_t* kexp, int32_t* rnz, cudaStream_t s) {
+                              int64_t nf1, int64_t nnz, int32_t* kexp, int32_t* rnz, cudaStream_t s) {
   auto grid = [](int64_t m) { return (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, 152 * 16)); };
-  if (nf1 > 0) flat_kexp_kernel<<<grid(nf1), 256, 0, s>>>(crd1, pos2, nf1, kexp);
+  if (nf1 > 0 && nnz > 0) flat_kexp_kernel<<<grid((nnz + kKexpChunk - 1) / kKexpChunk), 256, 0, s>>>(crd1, pos2, nf1, kexp);
   flat_rnz_kernel<<<grid(nroot + 1), 256, 0, s>>>(pos1, pos2, nroot, rnz);
   return cudaGetLastError();
 }

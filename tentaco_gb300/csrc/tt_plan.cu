@@ -118,12 +118,30 @@ bool variant_valid(int id, int order, int rank, int prec) {
   return walk_launcher(order, prec, v.cpt, lpr, launch_family(v)) != nullptr;
 }
 
+int lean_default_variant(int order, int rank, int prec);
+
 int default_variant(int order, int rank, int prec, int64_t nnz) {
   (void)nnz;
+  if (order == 3) {
+    // flat family, 256 threads: the best single flat variant per (storage, rank)
+    // over the training split of the selector corpus (12-28% mean regret against
+    // the per-tensor sweep optimum): 4 columns per lane, or 8 for 16-bit factor
+    // rows of 32 columns and more
+    const int rp3 = rank_pad(rank);
+    const bool f32 = fac_kind(prec) == kF32;
+    const int cpt = (!f32 && rp3 >= 32) ? 8 : 4;
+    const int G = rp3 <= 8 ? 16 : rp3 <= 16 ? 32 : (f32 ? 64 : 32);
+    const int id = variant_id(256, G, cpt, 3);
+    if (variant_valid(id, order, rank, prec)) return id;
+  }
+  return lean_default_variant(order, rank, prec);
+}
+
+int lean_default_variant(int order, int rank, int prec) {
   // lean family, looser register budget, 16 bytes of a factor row per lane (4 FP32
-  // or 8 16-bit columns), G growing with the rank: the best single variant per
-  // (storage, rank) over the training split of the selector corpus (15-23% mean
-  // regret against the per-tensor sweep optimum)
+  // or 8 16-bit columns), G growing with the rank: before the flat family, the best
+  // single variant per (storage, rank) over the training split of the selector
+  // corpus; the rule for four modes and for slab plans
   const int rp = rank_pad(rank);
   int cpt = fac_kind(prec) == kF32 ? 4 : 8;
   while (cpt > 1 && rp / cpt < 1) cpt >>= 1;
@@ -325,6 +343,32 @@ tt_status device_csf_check(tt_plan* p, const CsfView& v, cudaStream_t st) {
   return TT_OK;
 }
 
+// Variants next to `id` in its family and thread value: one step in G, one step
+// in columns per lane.
+std::vector<int> variant_neighbours(int id) {
+  std::vector<int> out;
+  const VariantSpec v = variant_spec(id);
+  if (v.tb == 0) return out;
+  const int ti = v.tb == 512 ? 1 : 0;
+  int gi = 0, ci = 0;
+  for (int i = 0; i < 5; i++) if (kGF[v.staged][i] == v.G) gi = i;
+  for (int i = 0; i < 4; i++) if (kCPT[i] == v.cpt) ci = i;
+  const int d[4][2] = {{-1, 0}, {1, 0}, {0, -1}, {0, 1}};
+  for (const auto& dd : d) {
+    const int g = gi + dd[0], c = ci + dd[1];
+    if (g >= 0 && g < 5 && c >= 0 && c < 4) out.push_back(v.staged * kPerFamily + (ti * 5 + g) * 4 + c);
+  }
+  return out;
+}
+
+// The fixed heuristic for this plan: the flat family has no slab passes, so slab
+// plans take the lean rule.
+int plan_default_variant(const tt_plan* p) {
+  const int id = default_variant(p->order, p->rank, p->prec, p->nnz);
+  if (p->slabs > 1 && variant_spec(id).staged == 3) return lean_default_variant(p->order, p->rank, p->prec);
+  return id;
+}
+
 tt_status use_variant(tt_plan* p, int id) {
   VariantSpec v = variant_spec(id);
   p->variant = id;
@@ -346,7 +390,7 @@ tt_status use_variant(tt_plan* p, int id) {
     if ((s = dev_alloc(p, &p->d_kexp, (size_t)pad16(p->nnz))) != TT_OK) return s;
     if ((s = dev_alloc(p, &p->d_rnz, (size_t)p->nroot + 1)) != TT_OK) return s;
     CK(cudaMemsetAsync(p->d_kexp, 0, sizeof(int32_t) * (size_t)pad16(p->nnz), p->stream));
-    CK(launch_flat_index(p->d_pos[1], p->d_crd[1], p->d_pos[2], p->nroot, p->count[1], p->d_kexp, p->d_rnz,
+    CK(launch_flat_index(p->d_pos[1], p->d_crd[1], p->d_pos[2], p->nroot, p->count[1], p->nnz, p->d_kexp, p->d_rnz,
                          p->stream));
     CK(cudaStreamSynchronize(p->stream));
   }
@@ -781,8 +825,19 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
       if (selector_rank(p, B, ranked, &in_range) == TT_OK && !ranked.empty()) {
         const int k = req_k > 0 ? req_k : (in_range ? 1 : kTopkOutside);
         if (k > 1) {
-          const int dflt = default_variant(p->order, rank, p->prec, p->nnz);
+          const int dflt = plan_default_variant(p);
           s = time_variants(p, st, ranked, k, dflt);
+          // then a local search around the fastest: its neighbours in G and in
+          // columns per lane (same family and thread value), two rounds at most
+          for (int round = 0; s == TT_OK && round < 2; round++) {
+            const int before = p->variant;
+            std::vector<int> nb;
+            for (int cand : variant_neighbours(before))
+              if (p->sweep_ms[cand] < 0.f && variant_valid(cand, p->order, rank, p->prec)) nb.push_back(cand);
+            if (nb.empty()) break;
+            s = time_variants(p, st, nb, (int)nb.size(), -1);
+            if (p->variant == before) break;
+          }
           if (s == TT_OK) {
             id = p->variant;
             placed = true;
@@ -799,9 +854,9 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
         }
       }
       clear_error();
-      if (!placed) id = default_variant(p->order, rank, p->prec, p->nnz);
+      if (!placed) id = plan_default_variant(p);
     } else {
-      id = default_variant(p->order, rank, p->prec, p->nnz);
+      id = plan_default_variant(p);
     }
     if (id < 0) return fail(set_error(TT_ERR_UNSUPPORTED, "no variant for order %d rank %d", p->order, rank));
     if (!placed && (s = use_variant(p, id)) != TT_OK) return fail(s);
@@ -1006,8 +1061,9 @@ tt_status time_variants(tt_plan* p, cudaStream_t st, const std::vector<int>& can
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
+  // the plan's current variant, if already timed, stays the one to beat
   int best = p->variant;
-  float best_ms = 1e30f;
+  float best_ms = best >= 0 && best < kNumVariants && p->sweep_ms[best] > 0.f ? p->sweep_ms[best] : 1e30f;
   tt_status s = TT_OK;
   std::vector<int> order;
   order.reserve(cands.size() + 1);

@@ -178,7 +178,7 @@ def init_params(nout: int, seed: int) -> np.ndarray:
     return np.concatenate(parts).astype(np.float32)
 
 
-def train(recs: list, storage: int, nout: int, steps: int = 3000, lr: float = 1e-3, wd: float = 3e-3,
+def train(recs: list, storage: int, nout: int, steps: int = 6000, lr: float = 1e-3, wd: float = 3e-3,
           seed: int = 0, log=sys.stdout) -> dict:
     import tentaco_gb300 as tt
     _, X, T, M = dataset(recs, storage, "train")
@@ -251,7 +251,7 @@ def main(argv=None) -> int:
     t = sub.add_parser("train")
     t.add_argument("--corpus", required=True)
     t.add_argument("--out", required=True)
-    t.add_argument("--steps", type=int, default=3000)
+    t.add_argument("--steps", type=int, default=6000)
     t.add_argument("--lr", type=float, default=1e-3)
     t.add_argument("--report", default=None, help="write the held-out regret report (JSON) here")
     a = ap.parse_args(argv)

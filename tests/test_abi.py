@@ -70,11 +70,12 @@ def test_variant_table():
             for prec in ("fp32", "bf16", "bf16f"):
                 v = tt.default_variant(order, rank, prec)
                 assert v >= 0 and tt.variant_valid(v, order, rank, prec)
-    # the fixed heuristic: lean family, 16 bytes of a factor row per lane
+    # the fixed heuristic: flat family for three modes, lean for four
     info = tt.variant_info(tt.default_variant(3, 32, "fp32"))
-    assert info["threads"] == 256 and info["cols_per_lane"] == 4 and info["staged"] == 0
-    assert info["name"] == "lean_b2_g64_c4"
-    assert tt.variant_info(tt.default_variant(3, 32, "fp16"))["name"] == "lean_b2_g32_c8"
+    assert info["threads"] == 256 and info["cols_per_lane"] == 4 and info["staged"] == 3
+    assert info["name"] == "flat_b2_g64_c4"
+    assert tt.variant_info(tt.default_variant(3, 32, "fp16"))["name"] == "flat_b2_g32_c8"
+    assert tt.variant_info(tt.default_variant(4, 32, "fp16"))["name"] == "lean_b2_g32_c8"
     assert tt.variant_info(3)["staged"] == 0 and tt.variant_info(43)["name"].startswith("stage")
     # the flat family (ids 120..159) runs three-mode tensors only
     assert tt.variant_info(134)["name"] == "flat_b3_g128_c2"
