@@ -63,19 +63,23 @@ cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// one thread per chunk of kChunk consecutive nonzeros: the fiber of the chunk's
-// first nonzero by binary search over pos2, then forward through the fiber ends
-// (a fiber of any length is spread over many threads)
-constexpr int kKexpChunk = 64;
+// one warp per chunk of kKexpChunk consecutive nonzeros, lane i taking nonzeros
+// i, i+32, ... of it (stores of a warp instruction are consecutive): a lane finds
+// the fiber of its first nonzero by binary search over pos2, then moves forward
+// through the fiber ends (a fiber of any length is spread over many warps)
+constexpr int kKexpChunk = 2048;
 __global__ void flat_kexp_kernel(const int32_t* __restrict__ crd1, const int32_t* __restrict__ pos2, int64_t nf1,
                                  int32_t* __restrict__ kexp) {
   const int64_t nnz = pos2[nf1];
   const int64_t nchunks = (nnz + kKexpChunk - 1) / kKexpChunk;
-  for (int64_t ch = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; ch < nchunks; ch += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t p0 = ch * kKexpChunk, p1 = min(nnz, p0 + kKexpChunk);
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t ch = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ch < nchunks; ch += warps) {
+    const int64_t p0 = ch * kKexpChunk + lane, p1 = min(nnz, (ch + 1) * kKexpChunk);
+    if (p0 >= p1) continue;
     int64_t f = search_le(pos2, 0, nf1 - 1, p0);  // last fiber starting at or before p0
     int64_t fend = pos2[f + 1];
-    for (int64_t p = p0; p < p1; p++) {
+    for (int64_t p = p0; p < p1; p += 32) {
       while (p >= fend) {  // empty fibers are skipped too
         f++;
         fend = pos2[f + 1];
@@ -94,7 +98,8 @@ __global__ void flat_rnz_kernel(const int32_t* __restrict__ pos1, const int32_t*
 cudaError_t launch_flat_index(const int32_t* pos1, const int32_t* crd1, const int32_t* pos2, int64_t nroot,
                               int64_t nf1, int64_t nnz, int32_t* kexp, int32_t* rnz, cudaStream_t s) {
   auto grid = [](int64_t m) { return (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, 152 * 16)); };
-  if (nf1 > 0 && nnz > 0) flat_kexp_kernel<<<grid((nnz + kKexpChunk - 1) / kKexpChunk), 256, 0, s>>>(crd1, pos2, nf1, kexp);
+  if (nf1 > 0 && nnz > 0)  // one warp per chunk: 8 chunks per 256-thread block
+    flat_kexp_kernel<<<grid(((nnz + kKexpChunk - 1) / kKexpChunk) * 32), 256, 0, s>>>(crd1, pos2, nf1, kexp);
   flat_rnz_kernel<<<grid(nroot + 1), 256, 0, s>>>(pos1, pos2, nroot, rnz);
   return cudaGetLastError();
 }
