@@ -26,10 +26,13 @@ WalkLauncher walk_launcher_o3_fp16(int cpt, int lpr, int staged);
 WalkLauncher walk_launcher_o4_fp16(int cpt, int lpr, int staged);
 
 cudaError_t launch_partition(int order, const WalkArgs& a, cudaStream_t s);
-// Flat walk indexes of a 3-level CSF: kexp[p] = crd1 of the fiber holding nonzero p
-// (p < pos2[nf1]), rnz[i] = pos2[pos1[i]] for i = 0..nroot.
-cudaError_t launch_flat_index(const int32_t* pos1, const int32_t* crd1, const int32_t* pos2, int64_t nroot,
-                              int64_t nf1, int64_t nnz, int32_t* kexp, int32_t* rnz, cudaStream_t s);
+// Flat walk indexes.  launch_expand: out[p] = per_fiber[f] for every entry p of
+// fiber f of one level (p < pos[nf] = n).  launch_row_starts: rnz[i] = first
+// nonzero of root position i (pos2[pos1[i]], through pos3 for four modes).
+cudaError_t launch_expand(const int32_t* per_fiber, const int32_t* pos, int64_t nf, int64_t n, int32_t* out,
+                          cudaStream_t s);
+cudaError_t launch_row_starts(const int32_t* pos1, const int32_t* pos2, const int32_t* pos3, int64_t nroot,
+                              int32_t* rnz, cudaStream_t s);
 // FP64 merge of the rows the walk left in the carry buffer (after the walk kernel).
 cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s);
 // TTV walk over units of 32 * kTtvNpt nonzeros (a: the 2-level view, see tt_ttv.cuh).

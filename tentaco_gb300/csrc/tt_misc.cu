@@ -89,18 +89,28 @@ __global__ void flat_kexp_kernel(const int32_t* __restrict__ crd1, const int32_t
   }
 }
 
-__global__ void flat_rnz_kernel(const int32_t* __restrict__ pos1, const int32_t* __restrict__ pos2, int64_t nroot,
-                                int32_t* __restrict__ rnz) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nroot; i += (int64_t)gridDim.x * blockDim.x)
-    rnz[i] = pos2[pos1[i]];
+__global__ void flat_rnz_kernel(const int32_t* __restrict__ pos1, const int32_t* __restrict__ pos2,
+                                const int32_t* __restrict__ pos3, int64_t nroot, int32_t* __restrict__ rnz) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nroot; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t f2 = pos2[pos1[i]];
+    rnz[i] = pos3 ? pos3[f2] : f2;
+  }
 }
 
-cudaError_t launch_flat_index(const int32_t* pos1, const int32_t* crd1, const int32_t* pos2, int64_t nroot,
-                              int64_t nf1, int64_t nnz, int32_t* kexp, int32_t* rnz, cudaStream_t s) {
-  auto grid = [](int64_t m) { return (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, 152 * 16)); };
-  if (nf1 > 0 && nnz > 0)  // one warp per chunk: 8 chunks per 256-thread block
-    flat_kexp_kernel<<<grid(((nnz + kKexpChunk - 1) / kKexpChunk) * 32), 256, 0, s>>>(crd1, pos2, nf1, kexp);
-  flat_rnz_kernel<<<grid(nroot + 1), 256, 0, s>>>(pos1, pos2, nroot, rnz);
+namespace {
+int flat_grid(int64_t m) { return (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, 152 * 16)); }
+}  // namespace
+
+cudaError_t launch_expand(const int32_t* per_fiber, const int32_t* pos, int64_t nf, int64_t n, int32_t* out,
+                          cudaStream_t s) {
+  if (nf > 0 && n > 0)  // one warp per chunk: 8 chunks per 256-thread block
+    flat_kexp_kernel<<<flat_grid(((n + kKexpChunk - 1) / kKexpChunk) * 32), 256, 0, s>>>(per_fiber, pos, nf, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_row_starts(const int32_t* pos1, const int32_t* pos2, const int32_t* pos3, int64_t nroot,
+                              int32_t* rnz, cudaStream_t s) {
+  flat_rnz_kernel<<<flat_grid(nroot + 1), 256, 0, s>>>(pos1, pos2, pos3, nroot, rnz);
   return cudaGetLastError();
 }
 

@@ -67,7 +67,8 @@ struct alignas(64) WalkArgs {
   int32_t* segmeta;       // 4 ints per segment
   int32_t wcap;           // staged kernels: window fibers per block the shared memory holds
   int32_t* err;           // staged kernels: set nonzero if a block's window exceeds wcap
-  const int32_t* kexp;    // flat walk: the middle coordinate of every nonzero (padded)
+  const int32_t* kexp;    // flat walk: the level-1 coordinate of every nonzero (padded)
+  const int32_t* kexp2;   // flat walk, four modes: the level-2 coordinate of every nonzero (padded)
   const int32_t* rnz;     // flat walk: first nonzero of every row (nrows + 1)
 };
 
@@ -102,10 +103,11 @@ __host__ __device__ inline size_t walk_smem_bytes(int P, int tb, int rp, int vby
 // Lean kernel, shared memory of one warp: coordinate runs TW x (G+4) int32,
 // value runs TW x (G*vbytes + 16) bytes, window starts and coordinates (a
 // warp's window has at most TW*G + 1 fibers).
-// Shared memory of one flat-walk warp: leaf and middle coordinate runs (tw runs of
-// G + 4 int32 each) and value runs (tw runs of G * vbytes + 16 bytes).
-__host__ __device__ inline size_t flat_warp_bytes(int G, int tw, int vbytes) {
-  size_t b = (size_t)2 * tw * (G + 4) * 4 + (size_t)tw * ((size_t)G * vbytes + 16);
+// Shared memory of one flat-walk warp: leaf and upper coordinate runs (order - 1
+// sets of tw runs of G + 4 int32 each) and value runs (tw runs of G * vbytes + 16
+// bytes).
+__host__ __device__ inline size_t flat_warp_bytes(int G, int tw, int vbytes, int order = 3) {
+  size_t b = (size_t)(order - 1) * tw * (G + 4) * 4 + (size_t)tw * ((size_t)G * vbytes + 16);
   return (b + 15) & ~(size_t)15;
 }
 
@@ -382,6 +384,7 @@ struct Walk {
 
   // ---- lean walk (family 0) ------------------------------------------------
   static constexpr int NWD = LB >= 4 ? LB / 4 : 1;  // 32-bit words of a lane's row piece
+  static constexpr int MWD = ORDER == 4 ? NWD : 1;    // words of a level-2 piece (flat walk, four modes)
   static constexpr int FRB = RP * (FK == kF32 ? 4 : 2);  // bytes per factor row
 
   // The lane's piece (LB bytes) of a factor row, as raw words: the load is
@@ -645,75 +648,98 @@ struct Walk {
     }
   }
 
-  // ---- flat walk (family 3, order 3) ------------------------------------------
-  // Every nonzero carries its middle coordinate k (a.kexp), so a team accumulates
-  // A(i,:) += (v * C(k,:)) * D(l,:) per nonzero with both factor rows gathered
-  // (C is small and stays in L2): the reference's own loop arithmetic
-  // (tensor_kernels/mttkrp3_csf_cpu_taco.h:45), with no fiber boundaries in the
-  // walk; only row ends (a.rnz) are checked, per batch.
-  //   lc, kc, vt: the team's leaf coordinates, middle coordinates and values
+  // ---- flat walk (family 3) --------------------------------------------------
+  // Every nonzero carries its upper coordinates (a.kexp: level 1, a.kexp2: level 2
+  // for four modes), so a team accumulates A(i,:) += ((v * C(k,:)) [* D(l,:)]) *
+  // last(m,:) per nonzero with every factor row gathered (the upper factors are
+  // small and stay in L2): the reference's own loop arithmetic
+  // (tensor_kernels/mttkrp3_csf_cpu_taco.h:45, mttkrp4_csf_cpu_taco.h:53), with no
+  // fiber boundaries in the walk; only row ends (a.rnz) are checked, per batch.
+  //   lc, kc, k2c, vt: the team's leaf coordinates, level-1 coordinates, level-2
+  //   coordinates (four modes) and values
   //   rlo, rhi: rows holding the unit's first nonzero and the next unit's
   template <int U>
-  __device__ __forceinline__ void walk_flat(int s, int n, const int32_t* lc, const int32_t* kc, const unsigned char* vt,
-                                            int rlo, int rhi, Summ<CPT>& X) const {
-    static_assert(ORDER == 3, "the flat walk is built for three modes");
+  __device__ __forceinline__ void walk_flat(int s, int n, const int32_t* lc, const int32_t* kc, const int32_t* k2c,
+                                            const unsigned char* vt, int rlo, int rhi, Summ<CPT>& X) const {
     const uint64_t pol = a.gpol == 1 ? policy_evict_normal() : policy_evict_last();
     const int32_t* rnz = a.rnz;
-    const unsigned char* fd = static_cast<const unsigned char*>(a.fac[1]) + q * LB;  // D: leaf factor
-    const unsigned char* fc = static_cast<const unsigned char*>(a.fac[0]) + q * LB;  // C: middle factor
+    const unsigned char* fd = static_cast<const unsigned char*>(a.fac[ORDER - 2]) + q * LB;  // leaf factor
+    const unsigned char* fc = static_cast<const unsigned char*>(a.fac[0]) + q * LB;          // level-1 factor
+    const unsigned char* fm = static_cast<const unsigned char*>(a.fac[1]) + q * LB;          // level-2 factor (four modes)
     int ip = (int)search_le(rnz, rlo, rhi, s);
     int rend = rnz[ip + 1];
     float ra[CPT];
 #pragma unroll
     for (int c = 0; c < CPT; c++) ra[c] = 0.f;
     bool flushed = false;
-    // one nonzero: ra += (v * c) * d, value half HV of word vw (16-bit) or float v
-    auto acc16 = [&](const uint32_t (&gc)[NWD], const uint32_t (&gd)[NWD], uint32_t vw, auto hv) {
+    // one nonzero: ra += ((v * c) [* m]) * d, value half HV of word vw (16-bit) or
+    // float v; m: the level-2 piece (four modes; unused for three)
+    auto acc16 = [&](const uint32_t (&gc)[NWD], const uint32_t (&gm)[MWD], const uint32_t (&gd)[NWD], uint32_t vw,
+                     auto hv) {
       constexpr int HV = decltype(hv)::value;
-      float d[CPT];
+      float d[CPT], mm[CPT];
       piece_cvt(gd, d);
+      if constexpr (ORDER == 4) piece_cvt(gm, mm);
+      else (void)gm;
       if constexpr (CPT == 1) {
         float t = 0.f;
         mfma1<FK, HV>(t, gc[0], vw);
+        if constexpr (ORDER == 4) t = t * mm[0];
         ra[0] = fmaf(t, d[0], ra[0]);
       } else {
 #pragma unroll
         for (int k = 0; k < CPT / 2; k++) {
           float t0 = 0.f, t1 = 0.f;
           mfma2<FK, HV>(t0, t1, gc[k], vw);
+          if constexpr (ORDER == 4) { t0 = t0 * mm[2 * k]; t1 = t1 * mm[2 * k + 1]; }
           ra[2 * k] = fmaf(t0, d[2 * k], ra[2 * k]);
           ra[2 * k + 1] = fmaf(t1, d[2 * k + 1], ra[2 * k + 1]);
         }
       }
     };
-    auto acc32 = [&](const uint32_t (&gc)[NWD], const uint32_t (&gd)[NWD], float v) {
-      float c[CPT], d[CPT];
+    auto acc32 = [&](const uint32_t (&gc)[NWD], const uint32_t (&gm)[MWD], const uint32_t (&gd)[NWD], float v) {
+      float c[CPT], d[CPT], mm[CPT];
       piece_cvt(gc, c);
       piece_cvt(gd, d);
+      if constexpr (ORDER == 4) piece_cvt(gm, mm);
+      else (void)gm;
 #pragma unroll
-      for (int k = 0; k < CPT; k++) ra[k] = fmaf(v * c[k], d[k], ra[k]);
+      for (int k = 0; k < CPT; k++) {
+        float t = v * c[k];
+        if constexpr (ORDER == 4) t = t * mm[k];
+        ra[k] = fmaf(t, d[k], ra[k]);
+      }
     };
     auto next_row = [&]() {
       flush(ip, ra, flushed, X);
       ip++;
       rend = rnz[ip + 1];
     };
-    auto load = [&](uint32_t (&gc)[U][NWD], uint32_t (&gd)[U][NWD], int j) {
-      int32_t l[U], k[U];
+    auto load = [&](uint32_t (&gc)[U][NWD], uint32_t (&gm)[U][MWD], uint32_t (&gd)[U][NWD], int j) {
+      int32_t l[U], k[U], k2[U];
 #pragma unroll
       for (int w = 0; w < U / 4; w++) {
         const int4 l4 = reinterpret_cast<const int4*>(lc + j)[w];
         const int4 k4 = reinterpret_cast<const int4*>(kc + j)[w];
         l[4 * w] = l4.x; l[4 * w + 1] = l4.y; l[4 * w + 2] = l4.z; l[4 * w + 3] = l4.w;
         k[4 * w] = k4.x; k[4 * w + 1] = k4.y; k[4 * w + 2] = k4.z; k[4 * w + 3] = k4.w;
+        if constexpr (ORDER == 4) {
+          const int4 m4 = reinterpret_cast<const int4*>(k2c + j)[w];
+          k2[4 * w] = m4.x; k2[4 * w + 1] = m4.y; k2[4 * w + 2] = m4.z; k2[4 * w + 3] = m4.w;
+        }
       }
 #pragma unroll
       for (int u = 0; u < U; u++) {
         piece_load(fc + (size_t)(uint32_t)k[u] * FRB, pol, gc[u]);
+        if constexpr (ORDER == 4) piece_load(fm + (size_t)(uint32_t)k2[u] * FRB, pol, gm[u]);
         piece_load(fd + (size_t)(uint32_t)l[u] * FRB, pol, gd[u]);
       }
+      if constexpr (ORDER != 4) {
+#pragma unroll
+        for (int u = 0; u < U; u++) gm[u][0] = 0u;
+      }
     };
-    auto consume = [&](const uint32_t (&gc)[U][NWD], const uint32_t (&gd)[U][NWD], int j) {
+    auto consume = [&](const uint32_t (&gc)[U][NWD], const uint32_t (&gm)[U][MWD], const uint32_t (&gd)[U][NWD], int j) {
       const bool inside = s + j + U <= rend;  // the batch lies in one row
       if constexpr (MIXED) {
         uint32_t vw[U / 2];
@@ -721,9 +747,9 @@ struct Walk {
 #pragma unroll
         for (int u = 0; u < U; u += 2) {
           if (!inside) while (s + j + u >= rend) next_row();
-          acc16(gc[u], gd[u], vw[u >> 1], std::integral_constant<int, 0>{});
+          acc16(gc[u], gm[u], gd[u], vw[u >> 1], std::integral_constant<int, 0>{});
           if (!inside) while (s + j + u + 1 >= rend) next_row();
-          acc16(gc[u + 1], gd[u + 1], vw[u >> 1], std::integral_constant<int, 1>{});
+          acc16(gc[u + 1], gm[u + 1], gd[u + 1], vw[u >> 1], std::integral_constant<int, 1>{});
         }
       } else {
         float v[U];
@@ -731,28 +757,30 @@ struct Walk {
 #pragma unroll
         for (int u = 0; u < U; u++) {
           if (!inside) while (s + j + u >= rend) next_row();
-          acc32(gc[u], gd[u], v[u]);
+          acc32(gc[u], gm[u], gd[u], v[u]);
         }
       }
     };
     const int nb = n / U;
-    uint32_t cA[U][NWD], dA[U][NWD], cB[U][NWD], dB[U][NWD];
-    if (nb > 0) load(cA, dA, 0);
+    uint32_t cA[U][NWD], mA[U][MWD], dA[U][NWD], cB[U][NWD], mB[U][MWD], dB[U][NWD];
+    if (nb > 0) load(cA, mA, dA, 0);
     for (int b = 0; b < nb; b += 2) {
-      if (b + 1 < nb) load(cB, dB, (b + 1) * U);
-      consume(cA, dA, b * U);
+      if (b + 1 < nb) load(cB, mB, dB, (b + 1) * U);
+      consume(cA, mA, dA, b * U);
       if (b + 1 < nb) {
-        if (b + 2 < nb) load(cA, dA, (b + 2) * U);
-        consume(cB, dB, (b + 1) * U);
+        if (b + 2 < nb) load(cA, mA, dA, (b + 2) * U);
+        consume(cB, mB, dB, (b + 1) * U);
       }
     }
     for (int j = nb * U; j < n; j++) {  // ragged end (the tensor's last tile only)
-      uint32_t gc[NWD], gd[NWD];
+      uint32_t gc[NWD], gd[NWD], gm[MWD];
       piece_load(fc + (size_t)(uint32_t)kc[j] * FRB, pol, gc);
+      if constexpr (ORDER == 4) piece_load(fm + (size_t)(uint32_t)k2c[j] * FRB, pol, gm);
+      else gm[0] = 0u;
       piece_load(fd + (size_t)(uint32_t)lc[j] * FRB, pol, gd);
       while (s + j >= rend) next_row();
-      if constexpr (MIXED) acc16(gc, gd, (uint32_t)reinterpret_cast<const uint16_t*>(vt)[j], std::integral_constant<int, 0>{});
-      else acc32(gc, gd, val_one(vt, j));
+      if constexpr (MIXED) acc16(gc, gm, gd, (uint32_t)reinterpret_cast<const uint16_t*>(vt)[j], std::integral_constant<int, 0>{});
+      else acc32(gc, gm, gd, val_one(vt, j));
     }
     if (!flushed) {
       X.h = ip; X.t = kNone;
@@ -1631,12 +1659,12 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_lean_kernel(const __grid_con
   if (lane < LPR) settle_unit(a, wk, X, head_ff, fs, s_pos[0], ustart64, pn[0], u, q);
 }
 
-// Flat kernel (family 3, order 3): the lean kernel's warp tiles and merge, with
-// the middle coordinate of every nonzero staged beside its leaf coordinate and
-// value; teams run walk_flat (row ends only).
-template <int PREC, int CPT, int LPR, int MINB>
+// Flat kernel (family 3): the lean kernel's warp tiles and merge, with the upper
+// coordinates of every nonzero staged beside its leaf coordinate and value; teams
+// run walk_flat (row ends only).
+template <int ORDER, int PREC, int CPT, int LPR, int MINB>
 __global__ void __launch_bounds__(256, MINB) mttkrp_flat_kernel(const __grid_constant__ WalkArgs a) {
-  using WK = Walk<3, PREC, CPT, LPR>;
+  using WK = Walk<ORDER, PREC, CPT, LPR>;
   constexpr int VB = WK::VB;
   constexpr int TW = 32 / LPR;
   constexpr int U = WK::LB >= 8 ? 4 : 8;  // nonzeros per gather batch (two batches of two rows each)
@@ -1645,20 +1673,22 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_flat_kernel(const __grid_con
   const int u = blockIdx.x * (blockDim.x >> 5) + warp;
   if (u >= a.nblocks) return;  // whole warp
   const int G = a.G, PU = a.P;
-  unsigned char* ws = smem + (size_t)warp * flat_warp_bytes(G, TW, VB);
+  unsigned char* ws = smem + (size_t)warp * flat_warp_bytes(G, TW, VB, ORDER);
   int32_t* s_lc = reinterpret_cast<int32_t*>(ws);
   int32_t* s_kc = s_lc + TW * (G + 4);
-  unsigned char* s_val = reinterpret_cast<unsigned char*>(s_kc + TW * (G + 4));
-  const int32_t* pb = a.part + (size_t)u * 2;
-  const int32_t* pn = pb + 2;
+  int32_t* s_k2c = s_kc + TW * (G + 4);  // four modes only
+  unsigned char* s_val = reinterpret_cast<unsigned char*>(s_lc + (ORDER - 1) * TW * (G + 4));
+  const int32_t* pb = a.part + (size_t)u * (ORDER - 1);
+  const int32_t* pn = pb + (ORDER - 1);
   const int64_t ustart64 = (int64_t)u * PU;
   const int ustart = (int)ustart64;
   const int cnt = (int)min((int64_t)PU, a.nnz - ustart64);
   {
     const uint64_t polF = policy_evict_first();
     const int n4 = (cnt + 3) >> 2;
-    stage_runs<VB>(a.crd[2] + ustart64, a.vals, ustart64, n4, a.lgG - 2, lane, s_lc, s_val, polF);
+    stage_runs<VB>(a.crd[ORDER - 1] + ustart64, a.vals, ustart64, n4, a.lgG - 2, lane, s_lc, s_val, polF);
     stage_int_runs(a.kexp + ustart64, n4, a.lgG - 2, lane, s_kc, polF);
+    if constexpr (ORDER == 4) stage_int_runs(a.kexp2 + ustart64, n4, a.lgG - 2, lane, s_k2c, polF);
   }
   __syncwarp();
   const int team = lane / LPR, q = lane % LPR;
@@ -1669,7 +1699,7 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_flat_kernel(const __grid_con
   const int s = ustart + team * G;
   if (s < ustart + cnt)
     wk.template walk_flat<U>(s, min(G, ustart + cnt - s), s_lc + team * (G + 4), s_kc + team * (G + 4),
-                             s_val + (size_t)team * (G * VB + 16), pb[0], pn[0], X);
+                             s_k2c + team * (G + 4), s_val + (size_t)team * (G * VB + 16), pb[0], pn[0], X);
   warp_tree(wk, X);
   // the unit's first row started before it when its first nonzero lies earlier
   if (lane < LPR) settle_unit(a, wk, X, 0, 0, a.rnz[pb[0]], ustart64, pn[0], u, q);

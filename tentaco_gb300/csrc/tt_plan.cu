@@ -80,11 +80,11 @@ int variant_unit(const VariantSpec& v, int rp) {
 
 int fac_bytes(int prec) { return fac_kind(prec) == kF32 ? 4 : 2; }
 
-size_t variant_smem(const VariantSpec& v, int rp, int prec, int wcap) {
+size_t variant_smem(const VariantSpec& v, int rp, int prec, int wcap, int order) {
   const int lpr = rp / v.cpt;
   const int P = (v.tb / lpr) * v.G;
   if (v.staged == 0) return (size_t)(256 / 32) * lean_warp_bytes(v.G, 32 / lpr, val_bytes(prec));
-  if (v.staged == 3) return (size_t)(256 / 32) * flat_warp_bytes(v.G, 32 / lpr, val_bytes(prec));
+  if (v.staged == 3) return (size_t)(256 / 32) * flat_warp_bytes(v.G, 32 / lpr, val_bytes(prec), order);
   if (v.staged == 2)  // TMA gather: 8 warps, each with its ring of row stages and its lean tile
     return (size_t)(256 / 32) * tma_warp_bytes(v.G, 32 / lpr, val_bytes(prec), rp * fac_bytes(prec), tma_stages(v));
   return v.staged ? stage_smem_bytes(P, wcap, v.tb, rp, val_bytes(prec), fac_bytes(prec))
@@ -109,12 +109,11 @@ bool variant_valid(int id, int order, int rank, int prec) {
   if (lpr < 1 || lpr > 32) return false;
   // shared memory must fit the 227 KB opt-in limit (staged: with the smallest
   // window; a plan checks its own tensor's largest window)
-  if (variant_smem(v, rp, prec, 1) > kSmemLimit) return false;
+  if (variant_smem(v, rp, prec, 1, order) > kSmemLimit) return false;
   if (v.staged && (rp * fac_bytes(prec)) % 16) return false;
   // TMA gather: four rows per copy land on 128-byte boundaries (rows of 32-byte
   // multiples), and a team's G nonzeros are whole stages of U = lanes-per-row rows
   if (v.staged == 2 && ((rp * fac_bytes(prec)) % 32 != 0 || v.G % lpr != 0)) return false;
-  if (v.staged == 3 && order != 3) return false;  // the flat walk is built for three modes
   return walk_launcher(order, prec, v.cpt, lpr, launch_family(v)) != nullptr;
 }
 
@@ -386,12 +385,26 @@ tt_status use_variant(tt_plan* p, int id) {
   if (s != TT_OK) return s;
   p->part_ready = false;
   if (v.staged == 3 && !p->d_kexp && p->nnz > 0) {
-    // every nonzero's middle coordinate and every row's first nonzero (once per plan)
-    if ((s = dev_alloc(p, &p->d_kexp, (size_t)pad16(p->nnz))) != TT_OK) return s;
+    // every nonzero's upper coordinates and every row's first nonzero (once per plan)
+    const size_t np = (size_t)pad16(p->nnz);
+    if ((s = dev_alloc(p, &p->d_kexp, np)) != TT_OK) return s;
     if ((s = dev_alloc(p, &p->d_rnz, (size_t)p->nroot + 1)) != TT_OK) return s;
-    CK(cudaMemsetAsync(p->d_kexp, 0, sizeof(int32_t) * (size_t)pad16(p->nnz), p->stream));
-    CK(launch_flat_index(p->d_pos[1], p->d_crd[1], p->d_pos[2], p->nroot, p->count[1], p->nnz, p->d_kexp, p->d_rnz,
-                         p->stream));
+    CK(cudaMemsetAsync(p->d_kexp, 0, sizeof(int32_t) * np, p->stream));
+    if (p->order == 3) {
+      CK(launch_expand(p->d_crd[1], p->d_pos[2], p->count[1], p->nnz, p->d_kexp, p->stream));
+      CK(launch_row_starts(p->d_pos[1], p->d_pos[2], nullptr, p->nroot, p->d_rnz, p->stream));
+    } else {
+      if ((s = dev_alloc(p, &p->d_kexp2, np)) != TT_OK) return s;
+      int32_t* k1f2 = nullptr;  // level-1 coordinate of every level-2 fiber
+      if ((s = dev_alloc(p, &k1f2, (size_t)p->count[2] + 1)) != TT_OK) return s;
+      CK(cudaMemsetAsync(p->d_kexp2, 0, sizeof(int32_t) * np, p->stream));
+      CK(launch_expand(p->d_crd[1], p->d_pos[2], p->count[1], p->count[2], k1f2, p->stream));
+      CK(launch_expand(k1f2, p->d_pos[3], p->count[2], p->nnz, p->d_kexp, p->stream));
+      CK(launch_expand(p->d_crd[2], p->d_pos[3], p->count[2], p->nnz, p->d_kexp2, p->stream));
+      CK(launch_row_starts(p->d_pos[1], p->d_pos[2], p->d_pos[3], p->nroot, p->d_rnz, p->stream));
+      CK(cudaStreamSynchronize(p->stream));
+      dev_free(p, k1f2);
+    }
     CK(cudaStreamSynchronize(p->stream));
   }
   p->wcap = 1;
@@ -409,7 +422,7 @@ tt_status use_variant(tt_plan* p, int id) {
       wmax = std::max(wmax, w);
     }
     p->wcap = wmax;
-    const size_t need = variant_smem(v, p->rp, p->prec, p->wcap);
+    const size_t need = variant_smem(v, p->rp, p->prec, p->wcap, p->order);
     if (need > kSmemLimit)
       return set_error(TT_ERR_UNSUPPORTED, "variant %d needs %zu bytes of shared memory for this tensor", id, need);
   }
@@ -446,6 +459,7 @@ WalkArgs walk_args(const tt_plan* p, float* A, int q) {
   a.wcap = p->wcap;
   a.err = p->d_err;
   a.kexp = p->d_kexp;
+  a.kexp2 = p->d_kexp2;
   a.rnz = p->d_rnz;
   for (int m = 0; m < 3; m++) a.fac_rows[m] = m + 1 < p->order ? (int32_t)p->dims[m + 1] : 0;
   return a;
@@ -496,7 +510,7 @@ tt_status run_mttkrp(tt_plan* p, float* A, cudaStream_t st) {
   if (p->nnz == 0) return TT_OK;
   // one pass per slab, in slab order, each adding its rows into A; the kernel
   // timer spans the first pass's walk to the last one's
-  const size_t smem = variant_smem(variant_spec(p->variant), p->rp, p->prec, p->wcap);
+  const size_t smem = variant_smem(variant_spec(p->variant), p->rp, p->prec, p->wcap, p->order);
   int first = -1, last = -1;
   for (int q = 0; q < p->slabs; q++)
     if (p->slab[q].nnz > 0) { if (first < 0) first = q; last = q; }

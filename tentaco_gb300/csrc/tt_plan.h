@@ -48,7 +48,8 @@ struct tt_plan {
   int32_t* d_err = nullptr;  // [0]: kernel error word, [1]: scratch for the window size
   tt::WalkLauncher launcher = nullptr;
   int32_t* d_part = nullptr;
-  int32_t* d_kexp = nullptr;  // flat walk: middle coordinate of every nonzero (padded)
+  int32_t* d_kexp = nullptr;  // flat walk: level-1 coordinate of every nonzero (padded)
+  int32_t* d_kexp2 = nullptr; // flat walk, four modes: level-2 coordinate of every nonzero (padded)
   int32_t* d_rnz = nullptr;   // flat walk: first nonzero of every root position
   // the partition depends only on the CSF and the unit size: a single-slab plan
   // computes it once per variant (part_ready) and times it (part_ms)

@@ -10,7 +10,7 @@ namespace tt {
 namespace {
 // fam 0: lean warp-tile walk, 1: shared-memory staged, 2 / 5: TMA-gather walk with
 // 4 / 8 stages in flight per warp, 3: lean with the tighter register budget,
-// 6 / 7: flat walk (order 3) with the looser / tighter budget.
+// 6 / 7: flat walk with the looser / tighter budget.
 // units: work units of the partition (warp tiles except for fam 1, blocks there).
 // Resident blocks per SM the lean kernel's registers are budgeted for: the
 // variant's thread axis selects the looser (tb 256) or tighter (tb 512) budget;
@@ -44,23 +44,17 @@ cudaError_t launch_walk(const WalkArgs& a, int units, int tb, size_t smem, cudaS
   return launch_k(k, a, units, tb, smem, s, FAM != 1, configured);
 }
 
-#if TT_ORDER == 3
-// flat walk (families 6 / 7: looser / tighter register budget), three modes only
+// flat walk (families 6 / 7: looser / tighter register budget)
 template <int CPT, int LPR, int FAM>
 cudaError_t launch_flat(const WalkArgs& a, int units, int tb, size_t smem, cudaStream_t s) {
-  auto k = mttkrp_flat_kernel<TT_PREC, CPT, LPR, lean_minb(CPT, FAM == 7)>;
+  auto k = mttkrp_flat_kernel<TT_ORDER, TT_PREC, CPT, LPR, lean_minb(CPT, FAM == 7)>;
   static size_t configured = 48 * 1024;
   return launch_k(k, a, units, tb, smem, s, true, configured);
 }
-#endif
 }  // namespace
 
 WalkLauncher TT_LOOKUP(int cpt, int lpr, int fam) {
-#if TT_ORDER == 3
 #define TT_FLAT(C, L) fam == 6 ? &launch_flat<C, L, 6> : fam == 7 ? &launch_flat<C, L, 7> :
-#else
-#define TT_FLAT(C, L) fam >= 6 ? (WalkLauncher) nullptr :
-#endif
 #define TT_CASE(C, L)                                                        \
   if (cpt == C && lpr == L)                                                  \
     return TT_FLAT(C, L) fam == 5 ? &launch_walk<C, L, 5> : fam == 3 ? &launch_walk<C, L, 3> : fam == 2 ? &launch_walk<C, L, 2> \

@@ -77,9 +77,9 @@ def test_variant_table():
     assert tt.variant_info(tt.default_variant(3, 32, "fp16"))["name"] == "flat_b2_g32_c8"
     assert tt.variant_info(tt.default_variant(4, 32, "fp16"))["name"] == "lean_b2_g32_c8"
     assert tt.variant_info(3)["staged"] == 0 and tt.variant_info(43)["name"].startswith("stage")
-    # the flat family (ids 120..159) runs three-mode tensors only
+    # the flat family (ids 120..159)
     assert tt.variant_info(134)["name"] == "flat_b3_g128_c2"
-    assert tt.variant_valid(134, 3, 32, "fp16") and not tt.variant_valid(134, 4, 32, "fp16")
+    assert tt.variant_valid(134, 3, 32, "fp16") and tt.variant_valid(134, 4, 32, "fp16")
 
 
 def test_invalid_csf_rejected():
