@@ -460,12 +460,14 @@ struct Walk {
       for (int k = 0; k < CPT / 2; k++) mfma2<FK, HV>(f3[2 * k], f3[2 * k + 1], w[k], v);
     }
   }
-  // U consecutive stored 16-bit values as raw words, two per word (U % 4 == 0;
-  // runs of 4 or more start 16-byte aligned).
+  // U consecutive stored 16-bit values as raw words, two per word (U % 4 == 0 or
+  // U == 2; runs start 16-byte aligned and batches at multiples of U).
   template <int U>
   __device__ __forceinline__ static void vals_raw(const unsigned char* vt, uint32_t (&w)[U / 2]) {
-    static_assert(U % 4 == 0, "raw values come in 8-byte pieces");
-    if constexpr (U % 8 == 0) {
+    static_assert(U % 4 == 0 || U == 2, "raw values come in 4- or 8-byte pieces");
+    if constexpr (U == 2) {
+      w[0] = *reinterpret_cast<const uint32_t*>(vt);
+    } else if constexpr (U % 8 == 0) {
 #pragma unroll
       for (int k = 0; k < U / 8; k++) {
         const uint4 x = reinterpret_cast<const uint4*>(vt)[k];
@@ -717,6 +719,15 @@ struct Walk {
     };
     auto load = [&](uint32_t (&gc)[U][NWD], uint32_t (&gm)[U][MWD], uint32_t (&gd)[U][NWD], int j) {
       int32_t l[U], k[U], k2[U];
+      if constexpr (U == 2) {  // 8-byte coordinate pairs
+        const int2 l2 = *reinterpret_cast<const int2*>(lc + j);
+        const int2 kk = *reinterpret_cast<const int2*>(kc + j);
+        l[0] = l2.x; l[1] = l2.y; k[0] = kk.x; k[1] = kk.y;
+        if constexpr (ORDER == 4) {
+          const int2 m2 = *reinterpret_cast<const int2*>(k2c + j);
+          k2[0] = m2.x; k2[1] = m2.y;
+        }
+      }
 #pragma unroll
       for (int w = 0; w < U / 4; w++) {
         const int4 l4 = reinterpret_cast<const int4*>(lc + j)[w];
@@ -1667,7 +1678,9 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_flat_kernel(const __grid_con
   using WK = Walk<ORDER, PREC, CPT, LPR>;
   constexpr int VB = WK::VB;
   constexpr int TW = 32 / LPR;
-  constexpr int U = WK::LB >= 8 ? 4 : 8;  // nonzeros per gather batch (two batches of two rows each)
+  // nonzeros per gather batch (two batches of ORDER - 1 rows each in registers):
+  // 16-byte pieces under the tighter register budget take pairs
+  constexpr int U = WK::LB >= 16 && MINB >= 3 ? 2 : WK::LB >= 8 ? 4 : 8;
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int u = blockIdx.x * (blockDim.x >> 5) + warp;

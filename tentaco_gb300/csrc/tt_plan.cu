@@ -342,8 +342,8 @@ tt_status device_csf_check(tt_plan* p, const CsfView& v, cudaStream_t st) {
   return TT_OK;
 }
 
-// Variants next to `id` in its family and thread value: one step in G, one step
-// in columns per lane.
+// Variants next to `id` in its family: one step in G, one step in columns per
+// lane, or the other thread value (register budget).
 std::vector<int> variant_neighbours(int id) {
   std::vector<int> out;
   const VariantSpec v = variant_spec(id);
@@ -357,6 +357,7 @@ std::vector<int> variant_neighbours(int id) {
     const int g = gi + dd[0], c = ci + dd[1];
     if (g >= 0 && g < 5 && c >= 0 && c < 4) out.push_back(v.staged * kPerFamily + (ti * 5 + g) * 4 + c);
   }
+  out.push_back(v.staged * kPerFamily + ((1 - ti) * 5 + gi) * 4 + ci);
   return out;
 }
 
@@ -841,8 +842,8 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
         if (k > 1) {
           const int dflt = plan_default_variant(p);
           s = time_variants(p, st, ranked, k, dflt);
-          // then a local search around the fastest: its neighbours in G and in
-          // columns per lane (same family and thread value), two rounds at most
+          // then a local search around the fastest: its neighbours in G, in columns
+          // per lane and in register budget (same family), two rounds at most
           for (int round = 0; s == TT_OK && round < 2; round++) {
             const int before = p->variant;
             std::vector<int> nb;
