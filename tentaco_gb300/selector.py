@@ -178,7 +178,7 @@ def init_params(nout: int, seed: int) -> np.ndarray:
     return np.concatenate(parts).astype(np.float32)
 
 
-def train(recs: list, storage: int, nout: int, steps: int = 6000, lr: float = 1e-3, wd: float = 3e-3,
+def train(recs: list, storage: int, nout: int, steps: int = 3000, lr: float = 1e-3, wd: float = 3e-3,
           seed: int = 0, log=sys.stdout) -> dict:
     import tentaco_gb300 as tt
     _, X, T, M = dataset(recs, storage, "train")
@@ -251,8 +251,10 @@ def main(argv=None) -> int:
     t = sub.add_parser("train")
     t.add_argument("--corpus", required=True)
     t.add_argument("--out", required=True)
-    t.add_argument("--steps", type=int, default=6000)
+    t.add_argument("--steps", type=int, default=3000)
     t.add_argument("--lr", type=float, default=1e-3)
+    t.add_argument("--wd", type=float, default=3e-3, help="decoupled weight decay")
+    t.add_argument("--seed", type=int, default=0, help="seed of the initial weights")
     t.add_argument("--report", default=None, help="write the held-out regret report (JSON) here")
     a = ap.parse_args(argv)
     if a.cmd == "corpus":
@@ -262,7 +264,7 @@ def main(argv=None) -> int:
     with open(a.corpus) as f:
         recs = [json.loads(l) for l in f if l.strip()]
     nout = len(recs[0]["ms"])
-    models = [train(recs, s, nout, steps=a.steps, lr=a.lr) for s in (0, 1)]
+    models = [train(recs, s, nout, steps=a.steps, lr=a.lr, wd=a.wd, seed=a.seed) for s in (0, 1)]
     write_model(a.out, models)
     net = tt.Mlp(nout, 1024)
     rep = evaluate(recs, {m["storage"]: m for m in models},
