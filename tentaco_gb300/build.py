@@ -77,6 +77,8 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     os.makedirs(BUILD, exist_ok=True)
     hdr = _headers()
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
+    # the walk-kernel units take longest: start them first
+    srcs.sort(key=lambda f: 0 if os.path.basename(f).startswith("tt_walk_o") else 1)
     jobs = jobs or max(2, os.cpu_count() or 2)
     with cf.ThreadPoolExecutor(jobs) as ex:
         futs = [ex.submit(_compile, s, _obj(s, hdr, NVCC_FLAGS if s.endswith(".cu") else CXX_FLAGS), verbose)

@@ -1,7 +1,9 @@
 // tt_walk_inst.cuh -- explicit instantiations of the MTTKRP walk kernels for one
-// (order, precision) -- lean warp-tile walk, shared-memory staged walk and TMA
-// gather walk --, included by tt_walk_o{3,4}_{fp32,bf16,bf16f,fp16}.cu with TT_ORDER,
-// TT_PREC and TT_LOOKUP defined.  The (columns per lane, lanes per row)
+// (order, precision): the lean warp-tile walk, shared-memory staged walk and TMA
+// gather walk in tt_walk_o{3,4}_{fp32,bf16,bf16f,fp16}.cu (TT_ORDER, TT_PREC,
+// TT_LOOKUP, TT_LOOKUP_FLAT and TT_LOOKUP_TMA defined), the flat and TMA walks in
+// the matching _flat.cu / _tma.cu units (TT_FLAT_UNIT or TT_TMA_UNIT, and
+// TT_LOOKUP, defined), so the kernels compile in parallel.  The (columns per lane, lanes per row)
 // pairs cover factor ranks 8, 16, 32 and 64.
 #include "tt_mttkrp.cuh"
 #include "tt_kernels.h"
@@ -33,17 +35,29 @@ cudaError_t launch_k(K k, const WalkArgs& a, int units, int tb, size_t smem, cud
   return cudaGetLastError();
 }
 
+#if !defined(TT_FLAT_UNIT) && !defined(TT_TMA_UNIT)
+// lean (families 0 / 3) and staged (family 1) walks
 template <int CPT, int LPR, int FAM>
 cudaError_t launch_walk(const WalkArgs& a, int units, int tb, size_t smem, cudaStream_t s) {
   constexpr bool kTight = FAM == 3;  // lean with the tighter register budget
-  auto k = FAM == 1   ? mttkrp_stage_kernel<TT_ORDER, TT_PREC, CPT, LPR>
-         : FAM == 2 ? mttkrp_tma_kernel<TT_ORDER, TT_PREC, CPT, LPR, 4>
-         : FAM == 5 ? mttkrp_tma_kernel<TT_ORDER, TT_PREC, CPT, LPR, 8>
+  auto k = FAM == 1 ? mttkrp_stage_kernel<TT_ORDER, TT_PREC, CPT, LPR>
                     : mttkrp_lean_kernel<TT_ORDER, TT_PREC, CPT, LPR, lean_minb(CPT, kTight)>;
   static size_t configured = 48 * 1024;
   return launch_k(k, a, units, tb, smem, s, FAM != 1, configured);
 }
+#endif
 
+#ifdef TT_TMA_UNIT
+// TMA gather walk (families 2 / 5: 4 / 8 stages in flight per warp)
+template <int CPT, int LPR, int FAM>
+cudaError_t launch_tma(const WalkArgs& a, int units, int tb, size_t smem, cudaStream_t s) {
+  auto k = mttkrp_tma_kernel<TT_ORDER, TT_PREC, CPT, LPR, FAM == 5 ? 8 : 4>;
+  static size_t configured = 48 * 1024;
+  return launch_k(k, a, units, tb, smem, s, true, configured);
+}
+#endif
+
+#ifdef TT_FLAT_UNIT
 // flat walk (families 6 / 7: looser / tighter register budget)
 template <int CPT, int LPR, int FAM>
 cudaError_t launch_flat(const WalkArgs& a, int units, int tb, size_t smem, cudaStream_t s) {
@@ -51,20 +65,49 @@ cudaError_t launch_flat(const WalkArgs& a, int units, int tb, size_t smem, cudaS
   static size_t configured = 48 * 1024;
   return launch_k(k, a, units, tb, smem, s, true, configured);
 }
+#endif  // TT_FLAT_UNIT
 }  // namespace
 
+#if defined(TT_TMA_UNIT)
+// the TMA walk's launchers (families 2 and 5), in their own translation unit
 WalkLauncher TT_LOOKUP(int cpt, int lpr, int fam) {
-#define TT_FLAT(C, L) fam == 6 ? &launch_flat<C, L, 6> : fam == 7 ? &launch_flat<C, L, 7> :
-#define TT_CASE(C, L)                                                        \
-  if (cpt == C && lpr == L)                                                  \
-    return TT_FLAT(C, L) fam == 5 ? &launch_walk<C, L, 5> : fam == 3 ? &launch_walk<C, L, 3> : fam == 2 ? &launch_walk<C, L, 2> \
-         : fam == 1 ? &launch_walk<C, L, 1> : &launch_walk<C, L, 0>;
+#define TT_CASE(C, L) \
+  if (cpt == C && lpr == L) return fam == 2 ? &launch_tma<C, L, 2> : fam == 5 ? &launch_tma<C, L, 5> : nullptr;
   TT_CASE(1, 8) TT_CASE(2, 4) TT_CASE(4, 2) TT_CASE(8, 1)     // rank 8
   TT_CASE(1, 16) TT_CASE(2, 8) TT_CASE(4, 4) TT_CASE(8, 2)    // rank 16
   TT_CASE(1, 32) TT_CASE(2, 16) TT_CASE(4, 8) TT_CASE(8, 4)   // rank 32
   TT_CASE(2, 32) TT_CASE(4, 16) TT_CASE(8, 8)                 // rank 64
 #undef TT_CASE
-#undef TT_FLAT
   return nullptr;
 }
+#elif defined(TT_FLAT_UNIT)
+// the flat walk's launchers (families 6 and 7), in their own translation unit
+WalkLauncher TT_LOOKUP(int cpt, int lpr, int fam) {
+#define TT_CASE(C, L) \
+  if (cpt == C && lpr == L) return fam == 6 ? &launch_flat<C, L, 6> : fam == 7 ? &launch_flat<C, L, 7> : nullptr;
+  TT_CASE(1, 8) TT_CASE(2, 4) TT_CASE(4, 2) TT_CASE(8, 1)     // rank 8
+  TT_CASE(1, 16) TT_CASE(2, 8) TT_CASE(4, 4) TT_CASE(8, 2)    // rank 16
+  TT_CASE(1, 32) TT_CASE(2, 16) TT_CASE(4, 8) TT_CASE(8, 4)   // rank 32
+  TT_CASE(2, 32) TT_CASE(4, 16) TT_CASE(8, 8)                 // rank 64
+#undef TT_CASE
+  return nullptr;
+}
+#else
+WalkLauncher TT_LOOKUP_FLAT(int cpt, int lpr, int fam);  // the _flat translation unit
+WalkLauncher TT_LOOKUP_TMA(int cpt, int lpr, int fam);   // the _tma translation unit
+
+WalkLauncher TT_LOOKUP(int cpt, int lpr, int fam) {
+  if (fam == 6 || fam == 7) return TT_LOOKUP_FLAT(cpt, lpr, fam);
+  if (fam == 2 || fam == 5) return TT_LOOKUP_TMA(cpt, lpr, fam);
+#define TT_CASE(C, L)                                                                   \
+  if (cpt == C && lpr == L)                                                             \
+    return fam == 3 ? &launch_walk<C, L, 3> : fam == 1 ? &launch_walk<C, L, 1> : &launch_walk<C, L, 0>;
+  TT_CASE(1, 8) TT_CASE(2, 4) TT_CASE(4, 2) TT_CASE(8, 1)     // rank 8
+  TT_CASE(1, 16) TT_CASE(2, 8) TT_CASE(4, 4) TT_CASE(8, 2)    // rank 16
+  TT_CASE(1, 32) TT_CASE(2, 16) TT_CASE(4, 8) TT_CASE(8, 4)   // rank 32
+  TT_CASE(2, 32) TT_CASE(4, 16) TT_CASE(8, 8)                 // rank 64
+#undef TT_CASE
+  return nullptr;
+}
+#endif
 }  // namespace tt

@@ -1,0 +1,6 @@
+// MTTKRP flat walk kernels, order 3, storage bf16f.
+#define TT_ORDER 3
+#define TT_PREC kBF16F
+#define TT_FLAT_UNIT
+#define TT_LOOKUP walk_launcher_o3_bf16f_flat
+#include "tt_walk_inst.cuh"

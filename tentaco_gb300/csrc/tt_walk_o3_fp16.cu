@@ -1,5 +1,7 @@
-// MTTKRP walk kernels, order 3, storage fp16.
+// MTTKRP lean and staged walk kernels, order 3, storage fp16.
 #define TT_ORDER 3
 #define TT_PREC kFP16
 #define TT_LOOKUP walk_launcher_o3_fp16
+#define TT_LOOKUP_FLAT walk_launcher_o3_fp16_flat
+#define TT_LOOKUP_TMA walk_launcher_o3_fp16_tma
 #include "tt_walk_inst.cuh"

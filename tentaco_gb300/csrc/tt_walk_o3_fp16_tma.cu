@@ -1,0 +1,6 @@
+// MTTKRP TMA-gather walk kernels, order 3, storage fp16.
+#define TT_ORDER 3
+#define TT_PREC kFP16
+#define TT_TMA_UNIT
+#define TT_LOOKUP walk_launcher_o3_fp16_tma
+#include "tt_walk_inst.cuh"

@@ -1,0 +1,6 @@
+// MTTKRP TMA-gather walk kernels, order 3, storage fp32.
+#define TT_ORDER 3
+#define TT_PREC kFP32
+#define TT_TMA_UNIT
+#define TT_LOOKUP walk_launcher_o3_fp32_tma
+#include "tt_walk_inst.cuh"
