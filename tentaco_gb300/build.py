@@ -29,9 +29,6 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
                      "-Xcompiler", "-fPIC,-fopenmp,-fvisibility=hidden", "-I" + INCLUDE]
-# TT_CHECKED=1: device-side bounds checks on the ring kernels' copies (debug builds)
-if os.environ.get("TT_CHECKED") == "1":
-    NVCC_FLAGS = NVCC_FLAGS + ["-DTT_CHECKED"]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-fvisibility=hidden", "-Wall",
              "-Wno-unused-function", "-I" + INCLUDE, "-I" + os.path.join(CUDA_HOME, "include")]
 

@@ -89,11 +89,9 @@ __host__ __device__ inline int num_segments(int units) { return (units + kSeg - 
 __host__ __device__ inline size_t walk_tile_bytes(int P, int vbytes) {
   return (size_t)P * 4 + (((size_t)P * vbytes + 15) & ~(size_t)15);  // crd + vals tile
 }
-// tile_elems: entries of the coordinate/value tile (P, or P plus the per-team skew
-// of the ring kernels).
-__host__ __device__ inline size_t walk_smem_bytes(int P, int tb, int rp, int vbytes, int tile_elems = -1) {
+__host__ __device__ inline size_t walk_smem_bytes(int P, int tb, int rp, int vbytes) {
   size_t nw = (size_t)tb / 32;
-  size_t b = walk_tile_bytes(tile_elems < 0 ? P : tile_elems, vbytes);
+  size_t b = walk_tile_bytes(P, vbytes);
   b += (size_t)(2 * P + 4) * sizeof(int32_t);         // fiber window
   b += nw * 2 * sizeof(int32_t);                      // warp summary rows
   b += nw * 2 * (size_t)rp * sizeof(float);           // warp summary accs
