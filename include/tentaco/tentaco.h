@@ -78,11 +78,14 @@ typedef struct tt_variant_info {
   int32_t rank_pad;      /* rank this variant is compiled for (8,16,32,64)     */
   int32_t lanes_per_row; /* rank_pad / cols_per_lane                           */
   int32_t nnz_per_block; /* threads / lanes_per_row * nnz_per_team             */
-  int32_t staged;        /* 0: factor rows gathered into registers as the team
-                            walks; 1: every row of the block's tile gathered into
-                            shared memory (cp.async) before the walk; 2: each
-                            lane's factor-row pieces copied (cp.async) into its
-                            own shared-memory ring 8 nonzeros ahead of use     */
+  int32_t staged;        /* family. 0 lean: factor rows gathered into registers
+                            as the team walks a warp's tile; 1 staged: every row
+                            of the block's tile gathered into shared memory
+                            (cp.async) before the walk; 2 TMA: the nonzero-level
+                            rows fetched by TMA gather4 into a per-warp ring of
+                            stages; 3 flat: every nonzero gathers all its factor
+                            rows from plan-built per-nonzero coordinates, and the
+                            walk checks only row ends (no slab plans)          */
   char name[40];
 } tt_variant_info;
 
@@ -167,7 +170,10 @@ int64_t tt_plan_device_bytes(const tt_plan* plan);
 
 /* Walk work units of the plan's variant (blocks, or warp tiles for the lean family). */
 int32_t tt_plan_nblocks(const tt_plan* plan);
-/* Switch an MTTKRP plan to another valid variant (scratch grows as needed). */
+/* Switch an MTTKRP plan to another valid variant (scratch grows as needed).  A
+ * switch that fails (TT_ERR_UNSUPPORTED: the variant does not fit this tensor or
+ * plan, e.g. the flat family on a slab plan) leaves the plan without a usable
+ * variant: tt_plan_mttkrp returns TT_ERR_INVALID_ARGUMENT until a switch succeeds. */
 tt_status tt_plan_use_variant(tt_plan* plan, int32_t variant);
 /* Per-variant mean ms timed at plan creation by TT_SELECT_SWEEP, or by
  * TT_SELECT_MODEL's top-k candidates (negative: not timed); n entries. */

@@ -420,6 +420,8 @@ class Plan:
     def set_factors(self, bufs) -> None:
         arr = (_P * len(bufs))(*[b.ptr.value for b in bufs])
         check(lib().tt_plan_set_factors(self.ptr, arr, None))
+        # FP32 plans of rank 8/16/32/64 read the caller's buffers at every call
+        self._factors = list(bufs)
 
     def mttkrp(self, A: DeviceBuffer, stream=None) -> None:
         check(lib().tt_plan_mttkrp(self.ptr, A.ptr, stream))

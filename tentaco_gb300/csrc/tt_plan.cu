@@ -60,7 +60,7 @@ int variant_id(int tb, int G, int cpt, int staged) {
 // Kernel family a variant launches: the lean family's second thread value selects
 // its tighter register budget (family 3); both launch 256-thread blocks.
 // The TMA family's second value selects 8 stages in flight per warp instead of 4 (family 5).
-// The flat family (order 3) launches family 6, or 7 with the tighter register budget.
+// The flat family launches family 6, or 7 with the tighter register budget.
 int launch_family(const VariantSpec& v) {
   if (v.staged == 0) return v.tb == 512 ? 3 : 0;
   if (v.staged == 2) return v.tb == 512 ? 5 : 2;
@@ -369,7 +369,54 @@ int plan_default_variant(const tt_plan* p) {
   return id;
 }
 
-tt_status use_variant(tt_plan* p, int id) {
+// Builds the flat family's per-nonzero upper coordinates and per-row first nonzero
+// (once per plan).  All or nothing: on failure no array is kept.
+tt_status build_flat_arrays(tt_plan* p) {
+  const size_t np = (size_t)pad16(p->nnz);
+  int32_t *kexp = nullptr, *kexp2 = nullptr, *rnz = nullptr, *k1f2 = nullptr;
+  auto undo = [&](tt_status s) {
+    cudaStreamSynchronize(p->stream);
+    dev_free(p, k1f2);
+    dev_free(p, kexp2);
+    dev_free(p, rnz);
+    dev_free(p, kexp);
+    return s;
+  };
+  auto ck = [&](cudaError_t e, const char* what) {
+    return e == cudaSuccess ? TT_OK
+                            : set_error(e == cudaErrorMemoryAllocation ? TT_ERR_OUT_OF_MEMORY : TT_ERR_CUDA,
+                                        "%s: %s", what, cudaGetErrorString(e));
+  };
+  tt_status s;
+  if ((s = dev_alloc(p, &kexp, np)) != TT_OK) return undo(s);
+  if ((s = dev_alloc(p, &rnz, (size_t)p->nroot + 1)) != TT_OK) return undo(s);
+  if ((s = ck(cudaMemsetAsync(kexp, 0, sizeof(int32_t) * np, p->stream), "kexp clear")) != TT_OK) return undo(s);
+  if (p->order == 3) {
+    if ((s = ck(launch_expand(p->d_crd[1], p->d_pos[2], p->count[1], p->nnz, kexp, p->stream), "expand")) != TT_OK)
+      return undo(s);
+    if ((s = ck(launch_row_starts(p->d_pos[1], p->d_pos[2], nullptr, p->nroot, rnz, p->stream), "row starts")) != TT_OK)
+      return undo(s);
+  } else {
+    if ((s = dev_alloc(p, &kexp2, np)) != TT_OK) return undo(s);
+    // level-1 coordinate of every level-2 fiber
+    if ((s = dev_alloc(p, &k1f2, (size_t)p->count[2] + 1)) != TT_OK) return undo(s);
+    if ((s = ck(cudaMemsetAsync(kexp2, 0, sizeof(int32_t) * np, p->stream), "kexp2 clear")) != TT_OK) return undo(s);
+    if ((s = ck(launch_expand(p->d_crd[1], p->d_pos[2], p->count[1], p->count[2], k1f2, p->stream), "expand")) != TT_OK ||
+        (s = ck(launch_expand(k1f2, p->d_pos[3], p->count[2], p->nnz, kexp, p->stream), "expand")) != TT_OK ||
+        (s = ck(launch_expand(p->d_crd[2], p->d_pos[3], p->count[2], p->nnz, kexp2, p->stream), "expand")) != TT_OK ||
+        (s = ck(launch_row_starts(p->d_pos[1], p->d_pos[2], p->d_pos[3], p->nroot, rnz, p->stream), "row starts")) !=
+            TT_OK)
+      return undo(s);
+  }
+  if ((s = ck(cudaStreamSynchronize(p->stream), "flat arrays")) != TT_OK) return undo(s);
+  dev_free(p, k1f2);
+  p->d_kexp = kexp;
+  p->d_kexp2 = kexp2;
+  p->d_rnz = rnz;
+  return TT_OK;
+}
+
+tt_status set_variant(tt_plan* p, int id) {
   VariantSpec v = variant_spec(id);
   p->variant = id;
   p->staged = v.staged;
@@ -385,29 +432,7 @@ tt_status use_variant(tt_plan* p, int id) {
   tt_status s = alloc_walk_scratch(p, p->P);
   if (s != TT_OK) return s;
   p->part_ready = false;
-  if (v.staged == 3 && !p->d_kexp && p->nnz > 0) {
-    // every nonzero's upper coordinates and every row's first nonzero (once per plan)
-    const size_t np = (size_t)pad16(p->nnz);
-    if ((s = dev_alloc(p, &p->d_kexp, np)) != TT_OK) return s;
-    if ((s = dev_alloc(p, &p->d_rnz, (size_t)p->nroot + 1)) != TT_OK) return s;
-    CK(cudaMemsetAsync(p->d_kexp, 0, sizeof(int32_t) * np, p->stream));
-    if (p->order == 3) {
-      CK(launch_expand(p->d_crd[1], p->d_pos[2], p->count[1], p->nnz, p->d_kexp, p->stream));
-      CK(launch_row_starts(p->d_pos[1], p->d_pos[2], nullptr, p->nroot, p->d_rnz, p->stream));
-    } else {
-      if ((s = dev_alloc(p, &p->d_kexp2, np)) != TT_OK) return s;
-      int32_t* k1f2 = nullptr;  // level-1 coordinate of every level-2 fiber
-      if ((s = dev_alloc(p, &k1f2, (size_t)p->count[2] + 1)) != TT_OK) return s;
-      CK(cudaMemsetAsync(p->d_kexp2, 0, sizeof(int32_t) * np, p->stream));
-      CK(launch_expand(p->d_crd[1], p->d_pos[2], p->count[1], p->count[2], k1f2, p->stream));
-      CK(launch_expand(k1f2, p->d_pos[3], p->count[2], p->nnz, p->d_kexp, p->stream));
-      CK(launch_expand(p->d_crd[2], p->d_pos[3], p->count[2], p->nnz, p->d_kexp2, p->stream));
-      CK(launch_row_starts(p->d_pos[1], p->d_pos[2], p->d_pos[3], p->nroot, p->d_rnz, p->stream));
-      CK(cudaStreamSynchronize(p->stream));
-      dev_free(p, k1f2);
-    }
-    CK(cudaStreamSynchronize(p->stream));
-  }
+  if (v.staged == 3 && !p->d_kexp && p->nnz > 0 && (s = build_flat_arrays(p)) != TT_OK) return s;
   p->wcap = 1;
   if (p->staged == 1 && p->nnz > 0) {
     // size the window-row region from this tensor's partition (computed once here)
@@ -428,6 +453,16 @@ tt_status use_variant(tt_plan* p, int id) {
       return set_error(TT_ERR_UNSUPPORTED, "variant %d needs %zu bytes of shared memory for this tensor", id, need);
   }
   return prepare_partition(p);
+}
+
+// Switches the plan to variant `id`.  Until a switch succeeds the plan has no
+// usable variant, and calls on it report an error instead of launching a walk
+// whose scratch, tables or shared memory were not set up for it.
+tt_status use_variant(tt_plan* p, int id) {
+  p->variant_ready = false;
+  const tt_status s = set_variant(p, id);
+  p->variant_ready = s == TT_OK;
+  return s;
 }
 
 // Arguments of one walk pass over slab q (the whole tensor when slabs == 1).
@@ -507,6 +542,8 @@ tt_status encode_leaf_tmap(const tt_plan* p, CUtensorMap* m) {
 
 tt_status run_mttkrp(tt_plan* p, float* A, cudaStream_t st) {
   const size_t outbytes = (size_t)p->dims[0] * (size_t)p->rank * sizeof(float);
+  if (!p->variant_ready)
+    return set_error(TT_ERR_INVALID_ARGUMENT, "the plan's last variant switch failed: select a variant");
   CK(cudaMemsetAsync(A, 0, outbytes, st));
   if (p->nnz == 0) return TT_OK;
   // one pass per slab, in slab order, each adding its rows into A; the kernel

@@ -54,6 +54,7 @@ struct tt_plan {
   // the partition depends only on the CSF and the unit size: a single-slab plan
   // computes it once per variant (part_ready) and times it (part_ms)
   bool part_ready = false;
+  bool variant_ready = false;  // the last use_variant succeeded
   float part_ms = 0.f;
   float* d_carry = nullptr;
   int32_t* d_meta = nullptr;     // MTTKRP: 4 ints per work unit

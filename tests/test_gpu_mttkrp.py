@@ -237,6 +237,32 @@ def test_slabs_parity(skewed, slabs):
                 close(outs[0], ref, prec)
 
 
+def test_failed_variant_switch_blocks_calls(skewed):
+    """A failed switch (the flat family on a slab plan) leaves the plan without a
+    variant: a call reports an error instead of launching, until a switch succeeds."""
+    B, Oc = skewed
+    facs = [tt.gen_dense(2000, 32, 1, 71), tt.gen_dense(5000, 32, 1, 72)]
+    ref = O.mttkrp(Oc, facs)
+    plan = tt.Plan(B, rank=32, prec="fp32", slabs=2)
+    good = plan.variant
+    bufs = [tt.DeviceBuffer.from_array(f.astype(np.float32)) for f in facs]
+    plan.set_factors(bufs)
+    A = tt.DeviceBuffer(B.dims[0] * 32 * 4)
+    flat = [v for v in range(tt.num_variants())
+            if tt.variant_info(v)["staged"] == 3 and tt.variant_valid(v, 3, 32, "fp32")]
+    assert flat
+    with pytest.raises(tt.TTError) as e:
+        plan.use_variant(flat[0])
+    assert e.value.status == tt.TT_ERR_UNSUPPORTED
+    with pytest.raises(tt.TTError) as e:
+        plan.mttkrp(A)
+    assert e.value.status == tt.TT_ERR_INVALID_ARGUMENT
+    plan.use_variant(good)
+    plan.mttkrp(A)
+    close(A.to_array((B.dims[0], 32)), ref)
+    assert plan.device_error() == 0
+
+
 def test_slabs_long_fiber_and_order4(c5_small):
     # a fiber crossing every slab, rows spanning many warp tiles
     L = 200_000
