@@ -1094,68 +1094,78 @@ namespace {
 // skipped); extra (>= 0), if not timed yet, is timed as well.  The times go to
 // sweep_ms (untimed variants keep -1).
 tt_status time_variants(tt_plan* p, cudaStream_t st, const std::vector<int>& cands, int max_timed, int extra) {
-  const int nm = p->order - 1;
-  std::vector<void*> tmp;
-  const void* saved[3] = {p->fac[0], p->fac[1], p->fac[2]};
-  float* saved_scale = p->d_colscale;
-  const size_t esz = p->prec == kFP32 ? 4 : 2;
-  for (int m = 0; m < nm; m++) {
-    void* d = nullptr;
-    CK(cudaMalloc(&d, (size_t)p->dims[m + 1] * p->rp * esz));
-    CK(cudaMemsetAsync(d, 0, (size_t)p->dims[m + 1] * p->rp * esz, st));
-    tmp.push_back(d);
-    p->fac[m] = d;
-  }
-  p->d_colscale = nullptr;
-  float* A = nullptr;
-  CK(cudaMalloc(&A, (size_t)p->dims[0] * p->rank * sizeof(float)));
-  tmp.push_back(A);
-  cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
   // the plan's current variant, if already timed, stays the one to beat
   int best = p->variant;
   float best_ms = best >= 0 && best < kNumVariants && p->sweep_ms[best] > 0.f ? p->sweep_ms[best] : 1e30f;
   tt_status s = TT_OK;
-  std::vector<int> order;
-  order.reserve(cands.size() + 1);
-  for (int id : cands) order.push_back(id);
-  if (extra >= 0) order.push_back(extra);
-  int timed = 0;
-  for (size_t i = 0; i < order.size() && s == TT_OK; i++) {
-    const int id = order[i];
-    const bool is_extra = extra >= 0 && i + 1 == order.size();
-    if (is_extra ? p->sweep_ms[id] >= 0.f : timed >= max_timed) continue;
-    if (!variant_valid(id, p->order, p->rank, p->prec)) continue;
-    if ((s = use_variant(p, id)) != TT_OK) {
-      if (s == TT_ERR_UNSUPPORTED) { s = TT_OK; continue; }  // does not fit this tensor's windows
-      break;
+  {
+    // placeholder factors and output, and the events; on leaving this block, by
+    // any path, the temporaries are freed and the plan gets its own factors back
+    struct Scratch {
+      tt_plan* p;
+      cudaStream_t st;
+      const void* saved[3];
+      float* saved_scale;
+      std::vector<void*> tmp;
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      ~Scratch() {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        cudaStreamSynchronize(st);
+        for (void* d : tmp) cudaFree(d);
+        for (int m = 0; m < 3; m++) p->fac[m] = saved[m];
+        p->d_colscale = saved_scale;
+      }
+    } sc{p, st, {p->fac[0], p->fac[1], p->fac[2]}, p->d_colscale, {}};
+    const int nm = p->order - 1;
+    const size_t esz = p->prec == kFP32 ? 4 : 2;
+    for (int m = 0; m < nm; m++) {
+      void* d = nullptr;
+      CK(cudaMalloc(&d, (size_t)p->dims[m + 1] * p->rp * esz));
+      sc.tmp.push_back(d);
+      CK(cudaMemsetAsync(d, 0, (size_t)p->dims[m + 1] * p->rp * esz, st));
+      p->fac[m] = d;
     }
-    if ((s = run_mttkrp(p, A, st)) != TT_OK) {
-      if (s == TT_ERR_UNSUPPORTED) { s = TT_OK; clear_error(); continue; }  // e.g. no TMA descriptor
-      break;
+    p->d_colscale = nullptr;
+    float* A = nullptr;
+    CK(cudaMalloc(&A, (size_t)p->dims[0] * p->rank * sizeof(float)));
+    sc.tmp.push_back(A);
+    CK(cudaEventCreate(&sc.e0));
+    CK(cudaEventCreate(&sc.e1));
+    std::vector<int> order;
+    order.reserve(cands.size() + 1);
+    for (int id : cands) order.push_back(id);
+    if (extra >= 0) order.push_back(extra);
+    int timed = 0;
+    for (size_t i = 0; i < order.size() && s == TT_OK; i++) {
+      const int id = order[i];
+      const bool is_extra = extra >= 0 && i + 1 == order.size();
+      if (is_extra ? p->sweep_ms[id] >= 0.f : timed >= max_timed) continue;
+      if (!variant_valid(id, p->order, p->rank, p->prec)) continue;
+      if ((s = use_variant(p, id)) != TT_OK) {
+        if (s == TT_ERR_UNSUPPORTED) { s = TT_OK; continue; }  // does not fit this tensor's windows
+        break;
+      }
+      if ((s = run_mttkrp(p, A, st)) != TT_OK) {
+        if (s == TT_ERR_UNSUPPORTED) { s = TT_OK; clear_error(); continue; }  // e.g. no TMA descriptor
+        break;
+      }
+      float tot = 0.f;
+      for (int r = 0; r < 3; r++) {
+        cudaEventRecord(sc.e0, st);
+        if ((s = run_mttkrp(p, A, st)) != TT_OK) break;
+        cudaEventRecord(sc.e1, st);
+        cudaEventSynchronize(sc.e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, sc.e0, sc.e1);
+        tot += ms;
+      }
+      if (s != TT_OK) break;
+      p->sweep_ms[id] = tot / 3.f;
+      timed++;
+      if (tot / 3.f < best_ms) { best_ms = tot / 3.f; best = id; }
     }
-    float tot = 0.f;
-    for (int r = 0; r < 3; r++) {
-      cudaEventRecord(e0, st);
-      if ((s = run_mttkrp(p, A, st)) != TT_OK) break;
-      cudaEventRecord(e1, st);
-      cudaEventSynchronize(e1);
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, e0, e1);
-      tot += ms;
-    }
-    if (s != TT_OK) break;
-    p->sweep_ms[id] = tot / 3.f;
-    timed++;
-    if (tot / 3.f < best_ms) { best_ms = tot / 3.f; best = id; }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  cudaStreamSynchronize(st);
-  for (void* d : tmp) cudaFree(d);
-  for (int m = 0; m < 3; m++) p->fac[m] = saved[m];
-  p->d_colscale = saved_scale;
   if (s != TT_OK) return s;
   if (best < 0) return set_error(TT_ERR_UNSUPPORTED, "no candidate variant runs on this tensor");
   return use_variant(p, best);
