@@ -1196,8 +1196,10 @@ TT_EXPORT tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
                                    const taco_tensor_t* const* factors, tt_precision prec,
                                    tt_select select, int32_t variant) {
   clear_error();
-  if (!A || !B || !factors || !A->vals || !A->dimensions) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
+  if (!A || !B || !factors || !A->vals || !A->dimensions || !B->dimensions)
+    return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
   const int order = B->order;
+  if (order != 3 && order != 4) return set_error(TT_ERR_UNSUPPORTED, "MTTKRP needs order 3 or 4 (got %d)", order);
   const int rank = A->dimensions[1];
   if (A->dimensions[0] != B->dimensions[0]) return set_error(TT_ERR_INVALID_ARGUMENT, "A rows %d != B dims[0] %d", A->dimensions[0], B->dimensions[0]);
   for (int m = 0; m < order - 1; m++) {

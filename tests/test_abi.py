@@ -107,3 +107,15 @@ def test_no_device_is_an_error_not_a_fallback():
     A = np.zeros((2, 8), np.float32)
     with pytest.raises(tt.TTError):
         tt.mttkrp_host(B, [np.ones((2, 8), np.float32), np.ones((2, 8), np.float32)])
+
+
+def test_host_call_rejects_unsupported_orders_first():
+    """tt_mttkrp_host refuses an order it has no kernels for before it reads the
+    tensor's levels or the factor array (which has order - 1 entries)."""
+    lv = [None, (np.array([0, 1, 1], np.int32), np.array([0], np.int32)),
+          (np.array([0, 1], np.int32), np.array([1], np.int32))]
+    for order in (2, 5):
+        B = tt.HostTaco((2, 2, 2), vals=np.ones(1, np.float32), levels=lv, order=order)
+        with pytest.raises(tt.TTError) as e:
+            tt.mttkrp_host(B, [np.ones((2, 8), np.float32), np.ones((2, 8), np.float32)])
+        assert e.value.status == tt.TT_ERR_UNSUPPORTED
