@@ -1250,6 +1250,7 @@ TT_EXPORT tt_status tt_ttv_host(taco_tensor_t* y, const taco_tensor_t* B, const 
   const int64_t nx = B->dimensions[B->order - 1];
   const int64_t ny = p->nfib_last;
   if (y->dimensions && y->dimensions[0] < ny) { tt_plan_destroy(p); return set_error(TT_ERR_INVALID_ARGUMENT, "y has %d entries, need %lld", y->dimensions[0], (long long)ny); }
+  if (x->dimensions && x->dimensions[0] < nx) { tt_plan_destroy(p); return set_error(TT_ERR_INVALID_ARGUMENT, "x has %d entries, need %lld", x->dimensions[0], (long long)nx); }
   float *dx = nullptr, *dy = nullptr;
   auto cleanup = [&]() {
     if (dx) cudaFreeAsync(dx, 0);
