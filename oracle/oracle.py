@@ -142,6 +142,8 @@ def mttkrp(csf: Csf, factors: list, rows: np.ndarray | None = None) -> np.ndarra
     c = [None] + [_c64(x) for x in csf.crd[1:]]
     v = _cf(csf.vals)
     if rows is not None:
+        if csf.order not in (3, 4):
+            raise ValueError("row-sampled oracle MTTKRP supports orders 3 and 4")
         rows = _c64(rows)
         out = np.zeros((rows.shape[0], R))
         E = fs[2] if csf.order == 4 else None
@@ -159,8 +161,12 @@ def mttkrp(csf: Csf, factors: list, rows: np.ndarray | None = None) -> np.ndarra
         L.oracle_mttkrp4(_I(csf.dims[0]), _I(R), _ptr(p[1]), _ptr(c[1]), _ptr(p[2]), _ptr(c[2]),
                          _ptr(p[3]), _ptr(c[3]), _ptr(v), _ptr(fs[0]), _ptr(fs[1]), _ptr(fs[2]),
                          _ptr(A))
+    elif csf.order == 5:
+        L.oracle_mttkrp5(_I(csf.dims[0]), _I(R), _ptr(p[1]), _ptr(c[1]), _ptr(p[2]), _ptr(c[2]),
+                         _ptr(p[3]), _ptr(c[3]), _ptr(p[4]), _ptr(c[4]), _ptr(v),
+                         _ptr(fs[0]), _ptr(fs[1]), _ptr(fs[2]), _ptr(fs[3]), _ptr(A))
     else:
-        raise ValueError("oracle MTTKRP supports order 3 and 4")
+        raise ValueError("oracle MTTKRP supports orders 3, 4 and 5")
     return A
 
 
@@ -257,10 +263,16 @@ def ref_mttkrp(csf: Csf, factors: list, workspace: bool = False) -> np.ndarray:
         r.ref_mttkrp3(_I(csf.dims[0]), _I(csf.dims[1]), _I(csf.dims[2]), _I(R),
                       _ptr(p[1]), _ptr(c[1]), _ptr(p[2]), _ptr(c[2]), _ptr(v),
                       _ptr(fs[0]), _ptr(fs[1]), _ptr(A), ctypes.c_int(1 if workspace else 0))
-    else:
+    elif csf.order == 4:
         r.ref_mttkrp4(_I(csf.dims[0]), _I(csf.dims[1]), _I(csf.dims[2]), _I(csf.dims[3]), _I(R),
                       _ptr(p[1]), _ptr(c[1]), _ptr(p[2]), _ptr(c[2]), _ptr(p[3]), _ptr(c[3]),
                       _ptr(v), _ptr(fs[0]), _ptr(fs[1]), _ptr(fs[2]), _ptr(A))
+    else:
+        dims = _c64(csf.dims)
+        parr = (_P * 5)(None, *[x.ctypes.data for x in p[1:]])
+        carr = (_P * 5)(None, *[x.ctypes.data for x in c[1:]])
+        farr = (_P * 4)(*[f.ctypes.data for f in fs])
+        r.ref_mttkrp5(_ptr(dims), _I(R), parr, carr, _ptr(v), farr, _ptr(A))
     return A
 
 

@@ -3,8 +3,8 @@
  *
  * Compiles the reference's own CPU kernels, unmodified, from the reference
  * tree (tensor_kernels/mttkrp3_csf_cpu_taco.h, mttkrp3_csf_cpu_taco_workspace.h,
- * mttkrp4_csf_cpu_taco.h, ttv_csf_cpu_taco.h) and exposes them with plain-array
- * C signatures, so tests can pin the FP64 restatement in tt_oracle.c and
+ * mttkrp4_csf_cpu_taco.h, mttkrp5_csf_cpu_taco.h, ttv_csf_cpu_taco.h) and
+ * exposes them with plain-array C signatures, so tests can pin the FP64 restatement in tt_oracle.c and
  * generate golden vectors.  Built by oracle/Makefile into oracle/_ref/ only
  * where the reference sources are present.
  *
@@ -23,6 +23,7 @@ double ref_last_ms = 0.0;
 #include "mttkrp3_csf_cpu_taco.h"
 #include "mttkrp3_csf_cpu_taco_workspace.h"
 #include "mttkrp4_csf_cpu_taco.h"
+#include "mttkrp5_csf_cpu_taco.h"
 #include "ttv_csf_cpu_taco.h"
 
 namespace {
@@ -94,6 +95,16 @@ void ref_mttkrp4(int64_t nrows, int64_t n1, int64_t n2, int64_t n3, int64_t R,
   B.level(3, pos3, crd3);
   Dense Ad(nrows, R, A), Cd(n1, R, C), Dd(n2, R, D), Ed(n3, R, E);
   mttkrp4_cpu_taco(&Ad.t, &B.t, &Cd.t, &Dd.t, &Ed.t);
+}
+
+__attribute__((visibility("default")))
+void ref_mttkrp5(const int64_t* dims, int64_t R, const int64_t* const* pos, const int64_t* const* crd,
+                 const double* vals, const double* const* factors, double* A) {
+  Holder B(5, dims, (double*)vals);
+  for (int l = 1; l < 5; l++) B.level(l, pos[l], crd[l]);
+  Dense Ad(dims[0], R, A), Cd(dims[1], R, factors[0]), Dd(dims[2], R, factors[1]), Ed(dims[3], R, factors[2]),
+      Fd(dims[4], R, factors[3]);
+  mttkrp5_cpu_taco(&Ad.t, &B.t, &Cd.t, &Dd.t, &Ed.t, &Fd.t);
 }
 
 __attribute__((visibility("default")))

@@ -10,7 +10,7 @@
  *
  * Pinning: tests/golden/ holds outputs of the reference's own CPU kernels
  * (tensor_kernels/mttkrp3_csf_cpu_taco.h, mttkrp4_csf_cpu_taco.h,
- * ttv_csf_cpu_taco.h) compiled unmodified through oracle/shim by oracle/Makefile;
+ * mttkrp5_csf_cpu_taco.h, ttv_csf_cpu_taco.h) compiled unmodified through oracle/shim by oracle/Makefile;
  * tests/test_oracle.py checks every function here against them bit-for-bit.
  *
  * Index arrays are int64 (the reference CPU path reads splatt_idx_t / long),
@@ -93,6 +93,63 @@ ORACLE_API void oracle_mttkrp4(int64_t nrows, int64_t R,
         }
       }
     }
+  }
+}
+
+/*
+ * MTTKRP, 5 modes, mode 0:  A(i,j) = sum B(i,k,l,m,n) C(k,j) D(l,j) E(m,j) F(n,j).
+ * Follows tensor_kernels/mttkrp5_csf_cpu_taco.h:35-95, which, unlike the 3- and
+ * 4-mode kernels, factors the sum level by level (same schedule as above):
+ *   per level-3 fiber (i,k,l,m):  f(j) = sum_n B(..,n) * F(n,j)
+ *   per level-2 fiber (i,k,l):    e(j) = sum_m f(j) * E(m,j)
+ *   per level-1 fiber (i,k):      d(j) = sum_l e(j) * D(l,j)
+ *   then                          A(i,j) += d(j) * C(k,j)
+ * each sum taken in CSF order.  The three partial rows are per-thread buffers
+ * of R doubles, zeroed where the reference zeroes its per-fiber workspaces.
+ */
+ORACLE_API void oracle_mttkrp5(int64_t nrows, int64_t R,
+                               const int64_t* pos1, const int64_t* crd1,
+                               const int64_t* pos2, const int64_t* crd2,
+                               const int64_t* pos3, const int64_t* crd3,
+                               const int64_t* pos4, const int64_t* crd4,
+                               const double* vals, const double* C, const double* D,
+                               const double* E, const double* F, double* A) {
+  int64_t n = nrows * R;
+#pragma omp parallel for schedule(static)
+  for (int64_t p = 0; p < n; p++) A[p] = 0.0;
+#pragma omp parallel
+  {
+    double* part = (double*)malloc(sizeof(double) * (size_t)(3 * (R > 0 ? R : 1)));
+    double* d = part;          /* level-1 fiber partial */
+    double* e = part + R;      /* level-2 fiber partial */
+    double* f = part + 2 * R;  /* level-3 fiber partial */
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t i1 = 0; i1 < (nrows + 63) / 64; i1++) {
+      for (int64_t i2 = 0; i2 < 64; i2++) {
+        int64_t i = i1 * 64 + i2;
+        if (i >= nrows) continue;
+        for (int64_t kB = pos1[i]; kB < pos1[i + 1]; kB++) {
+          int64_t k = crd1[kB];
+          for (int64_t j = 0; j < R; j++) d[j] = 0.0;
+          for (int64_t lB = pos2[kB]; lB < pos2[kB + 1]; lB++) {
+            int64_t l = crd2[lB];
+            for (int64_t j = 0; j < R; j++) e[j] = 0.0;
+            for (int64_t mB = pos3[lB]; mB < pos3[lB + 1]; mB++) {
+              int64_t m = crd3[mB];
+              for (int64_t j = 0; j < R; j++) f[j] = 0.0;
+              for (int64_t nB = pos4[mB]; nB < pos4[mB + 1]; nB++) {
+                int64_t q = crd4[nB];
+                for (int64_t j = 0; j < R; j++) f[j] = f[j] + vals[nB] * F[q * R + j];
+              }
+              for (int64_t j = 0; j < R; j++) e[j] = e[j] + f[j] * E[m * R + j];
+            }
+            for (int64_t j = 0; j < R; j++) d[j] = d[j] + e[j] * D[l * R + j];
+          }
+          for (int64_t j = 0; j < R; j++) A[i * R + j] = A[i * R + j] + d[j] * C[k * R + j];
+        }
+      }
+    }
+    free(part);
   }
 }
 
@@ -244,7 +301,8 @@ ORACLE_API double oracle_compare_array_my(const float* x, const float* y, int64_
  * this is the canonical definition both the library's host and GPU builders
  * are checked against bit-for-bit.
  * ------------------------------------------------------------------------- */
-typedef struct { int64_t key[4]; double v; int64_t seq; } oracle_entry;
+#define ORACLE_MAX_ORDER 5
+typedef struct { int64_t key[ORACLE_MAX_ORDER]; double v; int64_t seq; } oracle_entry;
 static int oracle_order_g = 3;
 static int oracle_cmp(const void* a, const void* b) {
   const oracle_entry* x = (const oracle_entry*)a;
@@ -270,6 +328,7 @@ ORACLE_API int64_t oracle_build_csf(int32_t order, int64_t dims0, int64_t nnz,
                                     const int64_t* coords, const double* vals,
                                     int64_t** pos, int64_t** crd, double* out_vals,
                                     int64_t* counts) {
+  if (order < 2 || order > ORACLE_MAX_ORDER) return -1;
   oracle_entry* e = (oracle_entry*)malloc(sizeof(oracle_entry) * (size_t)(nnz > 0 ? nnz : 1));
   for (int64_t p = 0; p < nnz; p++) {
     for (int d = 0; d < order; d++) e[p].key[d] = coords[p * order + d];

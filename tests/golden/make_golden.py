@@ -2,7 +2,7 @@
 
 Runs where the reference sources exist: ``make -C oracle`` compiles
 tensor_kernels/mttkrp3_csf_cpu_taco.h, mttkrp3_csf_cpu_taco_workspace.h,
-mttkrp4_csf_cpu_taco.h and ttv_csf_cpu_taco.h unmodified into
+mttkrp4_csf_cpu_taco.h, mttkrp5_csf_cpu_taco.h and ttv_csf_cpu_taco.h unmodified into
 oracle/_ref/libtaco_ref.so, and this script feeds them small seeded inputs.
 Each fixture stores the inputs (canonical CSF as int64 arrays, float32-exact
 values and factors) and the reference's FP64 outputs, so the oracle
@@ -47,7 +47,10 @@ def save_mttkrp(name, dims, coords, vals, R, rng, dist="uniform", factors=None):
     else:
         facs = [f32exact(rng.random((d, R))) for d in dims[1:]]
     A = O.ref_mttkrp(csf, facs)
-    out = dict(kind="mttkrp", order=len(dims), dims=np.array(dims), R=R, vals=csf.vals, A=A)
+    # five modes have the oracle only (no library kernel yet): their own kind keeps
+    # them out of the library's golden tests
+    kind = "mttkrp5" if len(dims) == 5 else "mttkrp"
+    out = dict(kind=kind, order=len(dims), dims=np.array(dims), R=R, vals=csf.vals, A=A)
     for l in range(1, len(dims)):
         out[f"pos{l}"] = csf.pos[l]
         out[f"crd{l}"] = csf.crd[l]
@@ -95,6 +98,10 @@ def main():
     # TTV (config-2 shape family, scaled down)
     d = (200, 150, 120)
     save_ttv("ttv_zipf", d, coo(rng, d, 9000, zipf=(1.1, 1.1, 0)), rng.uniform(-1, 1, 9000), rng)
+    # 5-mode (the reference's mttkrp5_csf_cpu_taco.h; oracle only), Zipf on modes 0 and 4
+    d = (30, 12, 10, 8, 60)
+    save_mttkrp("mttkrp5_zipf_r16", d, coo(rng, d, 5000, zipf=(1.1, 0, 0, 0, 1.1)), rng.random(5000), 16, rng,
+                dist="normal")
     print("wrote", sorted(f for f in os.listdir(HERE) if f.endswith(".npz")))
 
 

@@ -86,7 +86,7 @@ def test_reference_comparators():
 @pytest.mark.skipif(O.ref_lib() is None, reason="reference sources absent on this host")
 def test_reference_matches_restatement_random():
     rng = np.random.default_rng(77)
-    for dims, R in (((40, 30, 50), 16), ((12, 9, 8, 20), 8)):
+    for dims, R in (((40, 30, 50), 16), ((12, 9, 8, 20), 8), ((8, 6, 5, 4, 20), 8)):
         co = np.stack([rng.integers(0, d, 2000) for d in dims], 1)
         csf = O.build_csf(dims, co, rng.random(2000))
         facs = [rng.standard_normal((d, R)) for d in dims[1:]]
@@ -98,23 +98,44 @@ def test_reference_matches_restatement_random():
     assert np.array_equal(O.ttv(csf, x), O.ref_ttv(csf, x))
 
 
-@pytest.mark.parametrize("order", [3, 4])
+@pytest.mark.parametrize("path", golden_files("mttkrp5"), ids=lambda p: p.split("/")[-1])
+def test_mttkrp5_golden_bitexact(path):
+    """Five modes (oracle only; the library's kernels cover three and four): the
+    restatement of the reference's level-by-level factored loop reproduces its
+    output bit-for-bit, and both agree with a dense einsum."""
+    z = np.load(path)
+    csf = golden_csf(z)
+    facs = [z[f"F{m}"] for m in range(1, 5)]
+    A = O.mttkrp(csf, facs)
+    assert np.array_equal(A, z["A"])
+    dense = np.zeros(csf.dims)
+    dense[tuple(O.coords_of(csf).T)] = csf.vals
+    ref = np.einsum("abcde,br,cr,dr,er->ar", dense, *facs, optimize=True)
+    assert np.allclose(A, ref, rtol=1e-10, atol=1e-10 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("order", [3, 4, 5])
 def test_any_mode_oracle(order):
     """The any-mode oracle (oracle_mttkrp_coo) equals the reference-pinned CSF
-    oracle bit-for-bit for mode 0 (same nonzero order and product association)
-    and a dense einsum for every mode."""
+    oracle bit-for-bit for mode 0 with three or four modes (same nonzero order and
+    product association; the five-mode kernel factors its sums level by level, so
+    there the two agree to rounding) and a dense einsum for every mode."""
     rng = np.random.default_rng(5 + order)
-    dims = (12, 9, 11) if order == 3 else (7, 6, 5, 8)
+    dims = {3: (12, 9, 11), 4: (7, 6, 5, 8), 5: (5, 4, 3, 4, 6)}[order]
     co = np.array(sorted({tuple(int(rng.integers(0, d)) for d in dims) for _ in range(300)}), dtype=np.int64)
     vals = rng.random(len(co))
     csf = O.build_csf(dims, co, vals)
     coords = O.coords_of(csf)
     assert np.array_equal(coords, co)
     F = [rng.random((d, 6)) for d in dims]
-    assert np.array_equal(O.mttkrp_coo(coords, csf.vals, F, 0, dims[0]), O.mttkrp(csf, F[1:]))
+    got0, csf0 = O.mttkrp_coo(coords, csf.vals, F, 0, dims[0]), O.mttkrp(csf, F[1:])
+    if order < 5:
+        assert np.array_equal(got0, csf0)
+    else:
+        assert np.allclose(got0, csf0, rtol=1e-12, atol=1e-12)
     dense = np.zeros(dims)
     dense[tuple(co.T)] = vals
-    letters = "abcd"[:order]
+    letters = "abcde"[:order]
     for m in range(order):
         others = [n for n in range(order) if n != m]
         eq = letters + "," + ",".join(letters[n] + "r" for n in others) + "->" + letters[m] + "r"
