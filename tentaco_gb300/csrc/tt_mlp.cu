@@ -5,8 +5,9 @@
 // The reference picks kernel variants by an offline codegen sweep
 // (generated_kernels/codegen.py:44-247 and the *_tune.sh scripts) and a person
 // reading the timings.  Here the sweep's timings train this network, which then
-// scores every variant from a tensor's features; the sweep stays available as
-// the fallback and as the judge of the network's picks.
+// scores every variant from a tensor's features; the sweep stays available as a
+// selection mode and as the yardstick of the network's picks (regret against the
+// sweep's best), and the fixed heuristic is the fallback where no model applies.
 //
 // Parameters are one flat FP32 array, layer by layer: W_l (K_l x N_l, row-major,
 // W[k * N + n]) then b_l (N_l).  Every reduction is a serial loop in a fixed
