@@ -203,6 +203,34 @@ def mttkrp_coo(coords: np.ndarray, vals: np.ndarray, factors: list, mode: int, n
     return A
 
 
+def coo_ttv(coords: np.ndarray, vals: np.ndarray, c: np.ndarray):
+    """COO TTV of the reference's MATLAB interface (oracle_coo_ttv): fibers are runs
+    of equal (i, j); returns (fibers x 2 coordinates, y)."""
+    co = np.ascontiguousarray(coords, dtype=np.int64)
+    n = co.shape[0]
+    fib = np.zeros((max(n, 1), 2), dtype=np.int64)
+    y = np.zeros(max(n, 1))
+    L = lib()
+    L.oracle_coo_ttv.restype = ctypes.c_int64
+    nf = L.oracle_coo_ttv(_I(n), _ptr(co), _ptr(_cf(vals)), _ptr(_cf(c)), _ptr(fib), _ptr(y))
+    return fib[:nf].copy(), y[:nf].copy()
+
+
+def coo_ttm(coords: np.ndarray, vals: np.ndarray, U: np.ndarray):
+    """COO TTM of the reference's MATLAB interface (oracle_coo_ttm): Y(f, r) =
+    sum v * U(r, k) over fiber f's nonzeros; U is R x K.  Returns (fibers x 2, Y)."""
+    co = np.ascontiguousarray(coords, dtype=np.int64)
+    U = _cf(U)
+    n = co.shape[0]
+    R, K = U.shape
+    fib = np.zeros((max(n, 1), 2), dtype=np.int64)
+    Y = np.zeros((max(n, 1), R))
+    L = lib()
+    L.oracle_coo_ttm.restype = ctypes.c_int64
+    nf = L.oracle_coo_ttm(_I(n), _ptr(co), _ptr(_cf(vals)), _I(R), _I(K), _ptr(U), _ptr(fib), _ptr(Y))
+    return fib[:nf].copy(), Y[:nf].copy()
+
+
 def mttkrp3_workspace(csf: Csf, C, D) -> np.ndarray:
     C, D = _cf(C), _cf(D)
     R = C.shape[1]

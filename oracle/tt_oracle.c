@@ -412,3 +412,56 @@ ORACLE_API void oracle_mttkrp_coo(int32_t order, int64_t nnz, const int64_t* coo
     }
   }
 }
+
+/* ---------------------------------------------------------------------------
+ * COO kernels of the reference's MATLAB interface (tensor_kernels/fmtaco.cpp),
+ * restated without MATLAB.  Parity unpinned against fmtaco.cpp itself, which
+ * needs MATLAB's mex.h and matrix.h to compile: its MTTKRP (fmtaco.cpp:741-780)
+ * is oracle_mttkrp_coo for mode 0 (same order, same association ((v * C) * D));
+ * its TTV (fmtaco.cpp:32-115) sums each fiber from 0 in nonzero order, the
+ * arithmetic of the pinned CSF TTV (ttv_csf_cpu_taco.h:61-63); its TTM
+ * (fmtaco.cpp:117-223) is checked against a dense evaluation.
+ *
+ * Fibers are runs of consecutive nonzeros with equal (i, j), as in fmtaco.cpp:
+ * sorted input gives one run per fiber.  coords: nnz x 3 (row-major).  Outputs
+ * are sized by the caller for nnz fibers; the functions return the fiber count.
+ * ------------------------------------------------------------------------- */
+
+/* y(f) = sum over the run's nonzeros of v * c[k]; fib[2f], fib[2f+1] = (i, j). */
+ORACLE_API int64_t oracle_coo_ttv(int64_t nnz, const int64_t* coords, const double* vals,
+                                  const double* c, int64_t* fib, double* y) {
+  int64_t nf = 0;
+  for (int64_t p = 0; p < nnz;) {
+    const int64_t i = coords[3 * p], j = coords[3 * p + 1];
+    double t = 0.0;
+    int64_t q = p;
+    for (; q < nnz && coords[3 * q] == i && coords[3 * q + 1] == j; q++) t = t + vals[q] * c[coords[3 * q + 2]];
+    fib[2 * nf] = i;
+    fib[2 * nf + 1] = j;
+    y[nf++] = t;
+    p = q;
+  }
+  return nf;
+}
+
+/* Y(f, r) = sum over the run's nonzeros of v * U(r, k), r = 0..R-1; U is R x K
+ * row-major (the reference's C: C0_size x C1_size, C1_size the last mode). */
+ORACLE_API int64_t oracle_coo_ttm(int64_t nnz, const int64_t* coords, const double* vals, int64_t R,
+                                  int64_t K, const double* U, int64_t* fib, double* Y) {
+  int64_t nf = 0;
+  for (int64_t p = 0; p < nnz;) {
+    const int64_t i = coords[3 * p], j = coords[3 * p + 1];
+    int64_t e = p;
+    while (e < nnz && coords[3 * e] == i && coords[3 * e + 1] == j) e++;
+    for (int64_t r = 0; r < R; r++) {
+      double t = 0.0;
+      for (int64_t q = p; q < e; q++) t = t + vals[q] * U[r * K + coords[3 * q + 2]];
+      Y[nf * R + r] = t;
+    }
+    fib[2 * nf] = i;
+    fib[2 * nf + 1] = j;
+    nf++;
+    p = e;
+  }
+  return nf;
+}

@@ -142,3 +142,32 @@ def test_any_mode_oracle(order):
         ref = np.einsum(eq, dense, *[F[n] for n in others])
         got = O.mttkrp_coo(coords, csf.vals, F, m, dims[m])
         assert np.allclose(got, ref, rtol=1e-12, atol=1e-12), m
+
+
+def test_coo_kernels_of_the_matlab_interface():
+    """COO TTV / TTM / MTTKRP as in the reference's MATLAB interface (fmtaco.cpp,
+    which needs MATLAB to compile, so parity is anchored here): over the canonical
+    nonzero order, COO TTV reproduces the reference's CSF TTV output bit-for-bit and
+    COO MTTKRP the CSF MTTKRP; TTM agrees with a dense evaluation."""
+    z = np.load(golden_files("ttv")[0])
+    csf = golden_csf(z)
+    co = O.coords_of(csf)
+    fib, y = O.coo_ttv(co, csf.vals, z["x"])
+    assert np.array_equal(y, z["y"])
+    assert fib.shape[0] == csf.nfibers(1)
+    assert np.array_equal(fib[:, 1], csf.crd[1])
+    zm = np.load([p for p in golden_files("mttkrp") if "zipf_r20" in p][0])
+    cm = golden_csf(zm)
+    F = [None, zm["F1"], zm["F2"]]
+    assert np.array_equal(O.mttkrp_coo(O.coords_of(cm), cm.vals, F, 0, cm.dims[0]), zm["A"])
+    rng = np.random.default_rng(31)
+    U = rng.standard_normal((7, csf.dims[2]))
+    fib2, Y = O.coo_ttm(co, csf.vals, U)
+    assert np.array_equal(fib2, fib)
+    dense = np.zeros(csf.dims)
+    dense[tuple(co.T)] = csf.vals
+    ref = np.einsum("ijk,rk->ijr", dense, U)[fib[:, 0], fib[:, 1]]
+    assert np.allclose(Y, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+    # runs, not sorting: an unsorted stream splits a fiber wherever (i, j) changes
+    fib3, y3 = O.coo_ttv(co[::-1], csf.vals[::-1], z["x"])
+    assert fib3.shape[0] == fib.shape[0] and np.allclose(y3[::-1], y, rtol=1e-12, atol=1e-12)
