@@ -356,9 +356,10 @@ def run_gpu_arm(args, rank, world, d):
                      "peak_source": f"{peak_kind} hbm_gbs", "kernel_ms": round(kern, 4),
                      "compulsory_bytes": int(cbytes), "U1": U1, "U2": U2},
         "clocks": clocks,
-        # our kernels per step and slab: partition, walk, segment fold, segment chain (the
-        # output clear is a cudaMemsetAsync)
-        "gpu_launches": args.steps * 4 * plan.slabs,
+        # our kernels per step and slab: walk, segment fold, segment chain, plus the
+        # partition where a slab plan runs it per pass (a single-slab plan computes it
+        # once at creation); the output clear is a cudaMemsetAsync
+        "gpu_launches": args.steps * plan.slabs * (3 if plan.slabs == 1 else 4),
     }
     if "fp32" in others:
         out["speedup_vs_fp32"] = round(others["fp32"]["ms_per_step"] / ms, 3)
