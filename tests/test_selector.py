@@ -212,3 +212,29 @@ def test_model_topk_times_candidates():
     assert np.count_nonzero(far.sweep_times() > 0) >= 6
     with pytest.raises(tt.TTError):
         tt.Plan(small, rank=32, prec="fp16", select=tt.SELECT_MODEL, model_topk=17)
+
+
+@pytest.mark.parametrize("order", [3, 4])
+def test_features_match_a_numpy_restatement(order):
+    """The 12 selector features (tt_csf_features) from the CSF arrays, restated in
+    numpy: mode sizes, nnz, nnz per row and per last-level fiber, the spread and
+    skew of fiber lengths, and the spread of row nnz."""
+    dims = (300, 200, 500) if order == 3 else (60, 40, 30, 200)
+    B = tt.gen_zipf(dims, (1.2, 1.0) + (0,) * (order - 2), 40_000, seed=12)
+    L = order - 1
+    lens = np.diff(B.pos(L).astype(np.int64)).astype(np.float64)
+    rows = B.pos(1).astype(np.int64)
+    for l in range(2, L + 1):
+        rows = B.pos(l).astype(np.int64)[rows]
+    rnz = np.diff(rows).astype(np.float64)
+    nnz = float(B.nnz)
+    lg = lambda x: np.log2(max(1.0, x))  # noqa: E731
+    mean, rm = nnz / lens.size, nnz / rnz.size
+    ll = np.log2(np.maximum(1.0, lens))
+    lvar = max(0.0, (ll * ll).mean() - ll.mean() ** 2)
+    skew = ((ll - ll.mean()) ** 3).mean() / lvar ** 1.5 if lvar > 1e-12 else 0.0
+    want = np.array([lg(dims[0]), lg(dims[1]), lg(dims[2]), lg(nnz), lg(rm), lg(mean),
+                     np.sqrt(((lens - mean) ** 2).mean()) / mean, skew, lg(lens.max() / mean),
+                     np.sqrt(((rnz - rm) ** 2).mean()) / rm, order, lg(32)])
+    got = B.features(32).astype(np.float64)
+    assert np.allclose(got, want, rtol=1e-5, atol=1e-5), (got, want)
