@@ -395,7 +395,7 @@ def run_gpu_arm(args, rank, world, d):
         out["cpu_baseline"] = cpu_baseline(B, C, D, budget_s=15.0)
     if not args.no_secondary:
         del B, C, D, A, bufs, plan
-        out["secondary"] = {"ttv_config2": secondary_ttv(args), "mttkrp4_config5": secondary_mttkrp4(args),
+        out["secondary"] = {"ttv_50M": secondary_ttv(args), "mttkrp4_80M": secondary_mttkrp4(args),
                             "mttkrp3_other_modes": secondary_other_modes(args)}
     return out
 
@@ -417,7 +417,7 @@ def _timed(call, plan, steps, warmup):
 
 
 def secondary_ttv(args):
-    """TTV on config 2: 50,000 x 40,000 x 30,000, 50M nonzeros, Zipf(1.1) on modes 0 and 1,
+    """TTV on the 50M-nonzero tensor: 50,000 x 40,000 x 30,000, 50M nonzeros, Zipf(1.1) on modes 0 and 1,
     uniform mode 2, values and vector U(-1,1); checked against the FP64 oracle."""
     import tentaco_gb300 as tt
     from oracle import oracle as O
@@ -443,7 +443,7 @@ def secondary_ttv(args):
 
 
 def secondary_mttkrp4(args):
-    """MTTKRP on config 5: 4-mode 5,000 x 3,000 x 2,000 x 100,000, 80M nonzeros, Zipf(1.2) on
+    """MTTKRP on the 80M-nonzero 4-mode tensor: 5,000 x 3,000 x 2,000 x 100,000, 80M nonzeros, Zipf(1.2) on
     modes 0 and 3, rank 32 N(0,1) factors; FP16 storage (sweep-selected: the learned model
     covers 3-mode tensors) against plain FP32, sampled rows checked against the FP64 oracle."""
     import tentaco_gb300 as tt

@@ -8,7 +8,7 @@ Each fixture stores the inputs (canonical CSF as int64 arrays, float32-exact
 values and factors) and the reference's FP64 outputs, so the oracle
 restatement and the GPU kernels can be checked on hosts without the reference.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py [--out DIR]   (default: this directory)
 """
 from __future__ import annotations
 
@@ -19,6 +19,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+OUT = HERE
 
 from oracle import oracle as O  # noqa: E402
 
@@ -58,7 +59,7 @@ def save_mttkrp(name, dims, coords, vals, R, rng, dist="uniform", factors=None):
         out[f"F{m + 1}"] = f
     if len(dims) == 3:
         out["A_workspace"] = O.ref_mttkrp(csf, facs, workspace=True)
-    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
     return csf
 
 
@@ -66,12 +67,14 @@ def save_ttv(name, dims, coords, vals, rng):
     csf = O.build_csf(dims, coords, f32exact(vals))
     x = f32exact(rng.uniform(-1, 1, dims[2]))
     y = O.ref_ttv(csf, x)
-    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), kind="ttv", order=3, dims=np.array(dims),
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), kind="ttv", order=3, dims=np.array(dims),
                         pos1=csf.pos[1], crd1=csf.crd[1], pos2=csf.pos[2], crd2=csf.crd[2], vals=csf.vals,
                         x=x, y=y)
 
 
-def main():
+def main(out: str = HERE):
+    global OUT
+    OUT = out
     if O.ref_lib() is None:
         raise SystemExit("reference kernels could not be built (sources absent)")
     rng = np.random.default_rng(20261203)
@@ -79,7 +82,7 @@ def main():
     save_mttkrp("mttkrp3_hand", (2, 2, 2), np.array([[0, 0, 1], [0, 1, 0], [1, 1, 1]]),
                 np.array([2.0, 3.0, 4.0]), 2, rng,
                 factors=[np.array([[1.0, 2.0], [3.0, 4.0]]), np.array([[5.0, 6.0], [7.0, 8.0]])])
-    # uniform 3-mode (config-1 shape family, scaled down), ranks 8 and 32
+    # uniform 3-mode (the 1024^3 uniform family, scaled down), ranks 8 and 32
     d = (96, 64, 80)
     save_mttkrp("mttkrp3_uniform_r32", d, coo(rng, d, 6000), rng.random(6000), 32, rng)
     save_mttkrp("mttkrp3_uniform_r8", d, coo(rng, d, 3000), rng.random(3000), 8, rng)
@@ -91,19 +94,19 @@ def main():
     L = 5000
     coords = [(3, 7, l) for l in range(L)] + [(0, 1, 5), (0, 2, 9), (5, 0, 1), (9, 9, 9)]
     save_mttkrp("mttkrp3_longfiber_r16", (10, 10, L), np.array(coords), rng.random(len(coords)), 16, rng)
-    # 4-mode (config-5 shape family, scaled down)
+    # 4-mode (the 80M-nonzero 4-mode family, scaled down)
     d = (40, 30, 20, 100)
     save_mttkrp("mttkrp4_zipf_r32", d, coo(rng, d, 7000, zipf=(1.2, 0, 0, 1.2)), rng.random(7000), 32, rng,
                 dist="normal")
-    # TTV (config-2 shape family, scaled down)
+    # TTV (the 50M-nonzero TTV family, scaled down)
     d = (200, 150, 120)
     save_ttv("ttv_zipf", d, coo(rng, d, 9000, zipf=(1.1, 1.1, 0)), rng.uniform(-1, 1, 9000), rng)
     # 5-mode (the reference's mttkrp5_csf_cpu_taco.h; oracle only), Zipf on modes 0 and 4
     d = (30, 12, 10, 8, 60)
     save_mttkrp("mttkrp5_zipf_r16", d, coo(rng, d, 5000, zipf=(1.1, 0, 0, 0, 1.1)), rng.random(5000), 16, rng,
                 dist="normal")
-    print("wrote", sorted(f for f in os.listdir(HERE) if f.endswith(".npz")))
+    print("wrote", sorted(f for f in os.listdir(OUT) if f.endswith(".npz")))
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[sys.argv.index("--out") + 1] if "--out" in sys.argv else HERE)

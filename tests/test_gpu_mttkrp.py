@@ -63,7 +63,7 @@ def test_golden_vectors(path):
 
 @pytest.fixture(scope="module")
 def c1():
-    """Config-1 shape: 1024^3, 1,000,000 distinct uniform coordinates, U(0,1), R=32 U(0,1)."""
+    """Uniform 1024^3 tensor: 1,000,000 distinct uniform coordinates, U(0,1), R=32 U(0,1)."""
     B = tt.gen_zipf((1024, 1024, 1024), (0, 0, 0), 1_000_000, seed=1)
     C = tt.gen_dense(1024, 32, 0, 11)
     D = tt.gen_dense(1024, 32, 0, 12)
@@ -183,7 +183,7 @@ def test_compressed_root_with_gaps():
 
 @pytest.fixture(scope="module")
 def c5_small():
-    """Config-5 shape family scaled to 2M nonzeros: 4-mode, Zipf(1.2) on modes 0 and 3."""
+    """The 80M-nonzero 4-mode family scaled to 2M nonzeros: 4-mode, Zipf(1.2) on modes 0 and 3."""
     B = tt.gen_zipf((5000, 3000, 2000, 100000), (1.2, 0, 0, 1.2), 2_000_000, seed=5)
     facs = [tt.gen_dense(d, 32, 1, 50 + m) for m, d in enumerate((3000, 2000, 100000))]
     return B, facs, O.mttkrp(to_oracle(B), facs)

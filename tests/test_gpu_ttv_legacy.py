@@ -43,7 +43,7 @@ def test_ttv_golden(path):
 
 @pytest.fixture(scope="module")
 def c2_small():
-    """Config-2 shape family scaled to 3M nonzeros: Zipf(1.1) on modes 0 and 1, U(-1,1)."""
+    """The 50M-nonzero TTV tensor's shape family scaled to 3M nonzeros: Zipf(1.1) on modes 0 and 1, U(-1,1)."""
     B = tt.gen_zipf((50000, 40000, 30000), (1.1, 1.1, 0), 3_000_000, seed=2, vlo=-1, vhi=1)
     x = tt.gen_dense(30000, 1, 2, 22).ravel()
     return B, x, O.ttv(to_oracle(B), x)

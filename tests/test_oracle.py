@@ -171,3 +171,23 @@ def test_coo_kernels_of_the_matlab_interface():
     # runs, not sorting: an unsorted stream splits a fiber wherever (i, j) changes
     fib3, y3 = O.coo_ttv(co[::-1], csf.vals[::-1], z["x"])
     assert fib3.shape[0] == fib.shape[0] and np.allclose(y3[::-1], y, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.skipif(O.ref_lib() is None, reason="reference sources absent on this host")
+def test_golden_fixtures_regenerate_identically(tmp_path):
+    """The committed fixtures are exactly what tests/golden/make_golden.py makes from
+    the compiled reference kernels."""
+    import importlib.util
+    import os
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(here, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    mg.main(str(tmp_path))
+    made = sorted(p.name for p in tmp_path.glob("*.npz"))
+    assert made == sorted(f for f in os.listdir(here) if f.endswith(".npz"))
+    for name in made:
+        a, b = np.load(tmp_path / name), np.load(os.path.join(here, name))
+        assert sorted(a.files) == sorted(b.files), name
+        for k in a.files:
+            assert np.array_equal(a[k], b[k]), (name, k)
