@@ -3,7 +3,7 @@
 // The reference loads tensors with SPLATT's splatt_csf_load (ds.h:351-366) from
 // FROSTT .tns files: one nonzero per line, `order` 1-based integer coordinates
 // followed by the value, whitespace separated; lines starting with '#' are
-// comments.  SPLATT is not part of this build, so this reader produces the
+// comments.  SPLATT is not a dependency of this library, so this reader produces the
 // same coordinates and values and hands them to the canonical CSF builder
 // (tt_csf_from_coo: modes in file order, lexicographic, duplicates summed).
 //

@@ -1,6 +1,6 @@
 """Shared test helpers: fixture loading, conversions to the oracle, error norms.
 
-The oracle (oracle/oracle.py) is the checker here; the library under test is
+The oracle (oracle/oracle.py) gives the expected results; the library under test is
 always called through its C ABI (tentaco_gb300 wraps it with ctypes).
 """
 from __future__ import annotations
