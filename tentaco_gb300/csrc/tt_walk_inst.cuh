@@ -5,6 +5,8 @@
 // the matching _flat.cu / _tma.cu units (TT_FLAT_UNIT or TT_TMA_UNIT, and
 // TT_LOOKUP, defined), so the kernels compile in parallel.  The (columns per lane, lanes per row)
 // pairs cover factor ranks 8, 16, 32 and 64.
+#include <atomic>
+#include <mutex>
 #include "tt_mttkrp.cuh"
 #include "tt_kernels.h"
 
@@ -19,17 +21,41 @@ namespace {
 // both launch 256-thread blocks.
 constexpr int lean_minb(int cpt, bool tight) { return cpt >= 4 ? (tight ? 3 : 2) : (tight ? 4 : 3); }
 
-// One launch: warp-unit kernels run 256-thread blocks; `configured` is the calling
+// Dynamic shared memory one kernel is allowed, per device (the attribute is set per
+// device).  Raises are serialised and never lower it, so a launch on another host
+// thread keeps what it was allowed.
+struct SmemLimit {
+  static constexpr int kDevices = 64;
+  std::atomic<size_t> bytes[kDevices];
+  SmemLimit() {
+    for (auto& b : bytes) b.store(48 * 1024);
+  }
+};
+inline std::mutex& smem_limit_mutex() {
+  static std::mutex m;
+  return m;
+}
+
+// One launch: warp-unit kernels run 256-thread blocks; `lim` is the calling
 // kernel's own record of the dynamic shared memory it was allowed.
 template <typename K>
 cudaError_t launch_k(K k, const WalkArgs& a, int units, int tb, size_t smem, cudaStream_t s, bool warp_units,
-                     size_t& configured) {
+                     SmemLimit& lim) {
   if (warp_units) tb = 256;  // lean, TMA and flat: one work unit per warp, 256-thread blocks
   const int grid = warp_units ? (units + tb / 32 - 1) / (tb / 32) : units;
-  if (smem > configured) {
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem > 48 * 1024) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    configured = smem;
+    if (dev < 0 || dev >= SmemLimit::kDevices) return cudaErrorInvalidDevice;
+    if (smem > lim.bytes[dev].load(std::memory_order_acquire)) {
+      std::lock_guard<std::mutex> lk(smem_limit_mutex());
+      if (smem > lim.bytes[dev].load(std::memory_order_relaxed)) {
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        lim.bytes[dev].store(smem, std::memory_order_release);
+      }
+    }
   }
   k<<<grid, tb, smem, s>>>(a);
   return cudaGetLastError();
@@ -42,7 +68,7 @@ cudaError_t launch_walk(const WalkArgs& a, int units, int tb, size_t smem, cudaS
   constexpr bool kTight = FAM == 3;  // lean with the tighter register budget
   auto k = FAM == 1 ? mttkrp_stage_kernel<TT_ORDER, TT_PREC, CPT, LPR>
                     : mttkrp_lean_kernel<TT_ORDER, TT_PREC, CPT, LPR, lean_minb(CPT, kTight)>;
-  static size_t configured = 48 * 1024;
+  static SmemLimit configured;
   return launch_k(k, a, units, tb, smem, s, FAM != 1, configured);
 }
 #endif
@@ -52,7 +78,7 @@ cudaError_t launch_walk(const WalkArgs& a, int units, int tb, size_t smem, cudaS
 template <int CPT, int LPR, int FAM>
 cudaError_t launch_tma(const WalkArgs& a, int units, int tb, size_t smem, cudaStream_t s) {
   auto k = mttkrp_tma_kernel<TT_ORDER, TT_PREC, CPT, LPR, FAM == 5 ? 8 : 4>;
-  static size_t configured = 48 * 1024;
+  static SmemLimit configured;
   return launch_k(k, a, units, tb, smem, s, true, configured);
 }
 #endif
@@ -62,7 +88,7 @@ cudaError_t launch_tma(const WalkArgs& a, int units, int tb, size_t smem, cudaSt
 template <int CPT, int LPR, int FAM>
 cudaError_t launch_flat(const WalkArgs& a, int units, int tb, size_t smem, cudaStream_t s) {
   auto k = mttkrp_flat_kernel<TT_ORDER, TT_PREC, CPT, LPR, lean_minb(CPT, FAM == 7)>;
-  static size_t configured = 48 * 1024;
+  static SmemLimit configured;
   return launch_k(k, a, units, tb, smem, s, true, configured);
 }
 #endif  // TT_FLAT_UNIT
