@@ -119,3 +119,37 @@ def test_host_call_rejects_unsupported_orders_first():
         with pytest.raises(tt.TTError) as e:
             tt.mttkrp_host(B, [np.ones((2, 8), np.float32), np.ones((2, 8), np.float32)])
         assert e.value.status == tt.TT_ERR_UNSUPPORTED
+
+
+def test_last_error_is_per_thread():
+    """tt_last_error_string() reports the calling thread's last failure: threads
+    validating different malformed tensors at once each read their own message."""
+    import threading
+
+    def bad(t):
+        # t + 1 fibers of one nonzero each; fiber t's coordinate is outside the last mode
+        n = t + 1
+        lv = [None, (np.array([0, n], np.int32), np.arange(n, dtype=np.int32)),
+              (np.arange(n + 1, dtype=np.int32), np.array([0] * t + [4], np.int32))]
+        return tt.HostTaco((1, n, 4), vals=np.ones(n, np.float32), levels=lv)
+
+    tensors = [bad(t) for t in range(8)]
+    errors = []
+
+    def work(t):
+        L = tt.lib()
+        for _ in range(300):
+            if L.tt_csf_validate(tensors[t].ptr) != tt.TT_ERR_INVALID_CSF:
+                errors.append((t, "status"))
+                return
+            msg = L.tt_last_error_string().decode()
+            if f"fiber {t}:" not in msg:
+                errors.append((t, msg))
+                return
+
+    threads = [threading.Thread(target=work, args=(t,)) for t in range(8)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
