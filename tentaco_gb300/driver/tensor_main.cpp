@@ -4,6 +4,10 @@
 // with tensor_experiments/mttkrp_csf_gpu.h:51-218 and timers.h:93-137):
 //
 //   tensor-eval-gpu [tensor_dir] [tensor_name] [experiment] [results_dir] [hardware] [feature_dim]
+//                   [precision]
+//
+// precision (an addition; the plan experiments only): fp32 (default), bf16, bf16f
+// (FP32 values, BF16 factors) or fp16 storage, FP32 accumulation.
 //
 // reads <tensor_dir>/<tensor_name>.tns (FROSTT), runs the experiment and appends
 // one line per trial to <results_dir>/<experiment>_<feature_dim>_<hardware>.csv:
@@ -133,9 +137,18 @@ int main(int argc, char* argv[]) {
   const std::string results_dir = argc > 4 ? argv[4] : ".";
   const std::string hardware = argc > 5 ? argv[5] : "gb300";
   const std::string feature_dim = argc > 6 ? argv[6] : "32";
+  const std::string precision = argc > 7 ? argv[7] : "fp32";
   const int R = std::atoi(feature_dim.c_str());
   if (R < 1 || R > TT_MAX_RANK) {
     std::cerr << "feature_dim must be 1.." << TT_MAX_RANK << std::endl;
+    return 2;
+  }
+  tt_precision prec = TT_PREC_FP32;
+  if (precision == "bf16") prec = TT_PREC_BF16;
+  else if (precision == "bf16f") prec = TT_PREC_BF16_FACTORS;
+  else if (precision == "fp16") prec = TT_PREC_FP16;
+  else if (precision != "fp32") {
+    std::cerr << "precision must be fp32, bf16, bf16f or fp16" << std::endl;
     return 2;
   }
 
@@ -201,7 +214,7 @@ int main(int argc, char* argv[]) {
     if (tt_device_malloc((int64_t)B->dimensions[0] * R * 4, (void**)&dA) != TT_OK) return fail("A alloc");
     const tt_select sel = experiment == "mttkrp_csf_gpu_sweep" ? TT_SELECT_SWEEP : TT_SELECT_MODEL;
     tt_plan* p = nullptr;
-    if (tt_plan_create(B, TT_OP_MTTKRP, R, TT_PREC_FP32, sel, 0, nullptr, &p) != TT_OK) return fail("plan");
+    if (tt_plan_create(B, TT_OP_MTTKRP, R, prec, sel, 0, nullptr, &p) != TT_OK) return fail("plan");
     std::vector<const float*> fp(dF.begin(), dF.end());
     if (tt_plan_set_factors(p, fp.data(), nullptr) != TT_OK) return fail("factors");
     tt_plan_set_timing(p, 1);

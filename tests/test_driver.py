@@ -29,6 +29,8 @@ def test_bad_arguments(tmp_path):
     assert r.returncode == 2 and "no tensor file" in r.stderr
     r = run([tmp_path, "synthetic-10x10x10-50", "no_such_experiment", tmp_path, "gb300", 32], tmp_path)
     assert r.returncode == 2 and "unknown experiment" in r.stderr
+    r = run([tmp_path, "synthetic-10x10x10-50", "mttkrp_csf_gpu_plan", tmp_path, "gb300", 32, "fp8"], tmp_path)
+    assert r.returncode == 2 and "precision" in r.stderr
 
 
 def test_malformed_tns_is_reported(tmp_path):
