@@ -198,7 +198,9 @@ tt_status tt_l2_flush(void* stream);
 
 /* ---- one-shot host calls (H2D, run, D2H inside) ------------------------ */
 
-/* A->vals (host, dims[0] x rank) = MTTKRP(B, factors[0..order-2]) (host dense). */
+/* A->vals (host, dims[0] x rank) = MTTKRP(B, factors[0..order-2]) (host dense).
+ * Returns TT_ERR_DEVICE_WAIT if a walk's bounded wait ran out (A is then
+ * incomplete), like any nonzero device error word of the call. */
 tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
                          const taco_tensor_t* const* factors, tt_precision prec,
                          tt_select select, int32_t variant);

@@ -1237,6 +1237,13 @@ TT_EXPORT tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
     cleanup();
     return e;
   }
+  // a walk that gave up (a bounded wait that ran out: 301) left A incomplete
+  const int32_t derr = tt_plan_device_error(p);
+  if (derr != 0) {
+    tt_status e = set_error(derr == 301 ? TT_ERR_DEVICE_WAIT : TT_ERR_CUDA, "device error word %d", (int)derr);
+    cleanup();
+    return e;
+  }
   cleanup();
   return TT_OK;
 }
