@@ -48,3 +48,10 @@ def test_reference_arm_two_ranks_rank0_reports():
     out = lines[0]
     assert out["impl"] == "reference" and out["n_gpus"] == 2 and out["value"] > 0
     assert out["cpu_baseline"]["kind"] == "port" and out["e2e"]["h2d_bytes_per_step"] == 0
+    # the same metric and workload as the GPU arm's line, so the two arms compare
+    sys.path.insert(0, ROOT)
+    import bench
+    assert out["metric"] == bench.METRIC and out["config"]["workload"] == bench.WORKLOAD
+    assert out["unit"] == "GFLOP/s" and out["higher_is_better"] is True
+    for k in ("steps", "warmup", "ms_per_step", "scaling", "vs_baseline", "dtype", "data"):
+        assert k in out, k
