@@ -57,9 +57,17 @@ typedef enum tt_precision {
   TT_PREC_BF16 = 1,        /* values and factors stored BF16 with power-of-two
                               per-column scales; FP32 accumulation, FP64 cross-block merge */
   TT_PREC_BF16_FACTORS = 2, /* values FP32, factors BF16 (per-column scales)           */
-  TT_PREC_FP16 = 3          /* values and factors stored FP16 with power-of-two per-column
+  TT_PREC_FP16 = 3,         /* values and factors stored FP16 with power-of-two per-column
                                scales (column max in [2^14, 2^15)); FP32 accumulation.
                                Same bytes as BF16 with an 11-bit significand.            */
+  TT_PREC_FX16 = 4          /* the last mode's factor stored as 16-bit fixed point (each
+                               column's max maps to 32767, then each row is scaled by a
+                               power of two so its largest entry lies in [16384, 32767]);
+                               values FP32 (each multiplied by its leaf row's power of
+                               two, exactly) and the other factors FP32; FP32
+                               accumulation.  The leaf rows cost the bytes of FP16 with
+                               all 16 bits spent on the significand.  MTTKRP with the
+                               strip family only (TT_ERR_UNSUPPORTED for TTV).           */
 } tt_precision;
 
 typedef enum tt_select {
@@ -85,7 +93,11 @@ typedef struct tt_variant_info {
                             rows fetched by TMA gather4 into a per-warp ring of
                             stages; 3 flat: every nonzero gathers all its factor
                             rows from plan-built per-nonzero coordinates, and the
-                            walk checks only row ends (no slab plans)          */
+                            walk checks only row ends (no slab plans); 4 strip:
+                            the flat family's per-nonzero rows walked warp-
+                            synchronously in steps of nonzeros, row ends decided
+                            once per step (tensors with long rows); on a slab
+                            plan one launch walks all slabs in slab-major order */
   char name[40];
 } tt_variant_info;
 
@@ -105,10 +117,13 @@ tt_status tt_plan_destroy(tt_plan* plan);
 /* Plan options (zero-initialise; NULL means all defaults). */
 typedef struct tt_plan_options {
   /* MTTKRP over a dense-root CSF: split the last mode's index range into this
-   * many slabs and run one walk pass per slab, each adding into A, so that one
-   * slab's rows of the last factor stay resident in L2.  0: automatic (no
-   * slabs: the walk is issue-bound, and slabs trade DRAM traffic for extra
-   * fiber work); 1: no slabs; at most 16. */
+   * many slabs, so that one slab's rows of the last factor stay resident in L2
+   * while they are gathered.  The strip family walks all slabs in one launch in
+   * slab-major order (one output row per slab and row, summed into A in FP64 in
+   * slab order); the lean, staged and TMA families run one pass per slab, each
+   * adding into A; the flat family runs without slabs.  0: automatic (slabs of at
+   * most 32 MB of the last factor as stored, when it exceeds 48 MB); 1: no slabs;
+   * at most 16.  One-shot calls (tt_mttkrp_host) use no slabs. */
   int32_t slabs;
   /* L2 policy of factor-row gathers in the lean walk: 0 automatic (evict_last
    * without slabs, evict_normal with them), 1 evict_last, 2 evict_normal. */

@@ -26,9 +26,9 @@ TT_ERR_NO_DEVICE = 6
 TT_ERR_DEVICE_WAIT = 7
 
 OP_MTTKRP, OP_TTV = 0, 1
-PREC_FP32, PREC_BF16, PREC_BF16_FACTORS, PREC_FP16 = 0, 1, 2, 3
+PREC_FP32, PREC_BF16, PREC_BF16_FACTORS, PREC_FP16, PREC_FX16 = 0, 1, 2, 3, 4
 SELECT_DEFAULT, SELECT_MODEL, SELECT_SWEEP, SELECT_FIXED = 0, 1, 2, 3
-PRECISIONS = {"fp32": PREC_FP32, "bf16": PREC_BF16, "bf16f": PREC_BF16_FACTORS, "fp16": PREC_FP16}
+PRECISIONS = {"fp32": PREC_FP32, "bf16": PREC_BF16, "bf16f": PREC_BF16_FACTORS, "fp16": PREC_FP16, "fx16": PREC_FX16}
 
 
 class TacoTensor(C.Structure):

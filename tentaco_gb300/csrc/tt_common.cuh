@@ -22,11 +22,20 @@ namespace tt {
 //   kFP16  values FP16, factors FP16 (power-of-two per-column scales that put
 //          each column's max in [2^14, 2^15), so the 11-bit significand is used
 //          over the whole column and nothing overflows)
-enum Prec : int { kFP32 = 0, kBF16 = 1, kBF16F = 2, kFP16 = 3 };
-// Element kinds of one stored array.
-enum Kind : int { kF32 = 0, kB16 = 1, kH16 = 2 };
-__host__ __device__ constexpr int fac_kind(int prec) { return prec == kFP32 ? kF32 : (prec == kFP16 ? kH16 : kB16); }
-__host__ __device__ constexpr int val_kind(int prec) { return prec == kBF16 ? kB16 : (prec == kFP16 ? kH16 : kF32); }
+//   kFX16  the leaf-level factor as 16-bit fixed point (kI16: each column scaled so
+//          its max maps to 32767, then each row by a power of two so its largest
+//          entry lies in [16384, 32767]); the values FP32, each multiplied by its
+//          leaf row's power of two (exact); the other factors FP32 (small, they stay
+//          in L2).  Strip walk only.
+enum Prec : int { kFP32 = 0, kBF16 = 1, kBF16F = 2, kFP16 = 3, kFX16 = 4 };
+// Element kinds of one stored array.  kI16: a 16-bit integer q in [-32767, 32767]
+// stored offset-binary (q + 32768), value = q / scale.
+enum Kind : int { kF32 = 0, kB16 = 1, kH16 = 2, kI16 = 3 };
+// Kind of the (leaf-level) factors and of the values.
+__host__ __device__ constexpr int fac_kind(int prec) {
+  return prec == kFP32 ? kF32 : prec == kFP16 ? kH16 : prec == kFX16 ? kI16 : kB16;
+}
+__host__ __device__ constexpr int val_kind(int prec) { return prec == kBF16 ? kB16 : prec == kFP16 ? kH16 : kF32; }
 
 // ---------------------------------------------------------------------------
 // L2 cache policies (createpolicy, sm_80+).
@@ -272,10 +281,72 @@ __device__ __forceinline__ void mfma1(float& a0, uint32_t d, uint32_t v) {
   }
 }
 
+// Exact products of the 16-bit halves of two packed words: (lo(c) * lo(d),
+// hi(c) * hi(d)) in FP32 by the mixed-precision FMA with a zero addend (two
+// 11-bit or 8-bit significands multiply exactly into FP32's 24 bits).
 template <int KIND>
-__device__ __forceinline__ float lo16(uint32_t w) { return KIND == kB16 ? bf16lo(w) : h16lo(w); }
+__device__ __forceinline__ float2 hprod2(uint32_t c, uint32_t d) {
+  float p0, p1;
+  if constexpr (KIND == kB16)
+    asm("{\n\t.reg .b16 cl, ch, dl, dh;\n\tmov.b32 {cl, ch}, %2;\n\tmov.b32 {dl, dh}, %3;\n\t"
+        "fma.rn.f32.bf16 %0, cl, dl, 0f00000000;\n\tfma.rn.f32.bf16 %1, ch, dh, 0f00000000;\n\t}"
+        : "=f"(p0), "=f"(p1) : "r"(c), "r"(d));
+  else
+    asm("{\n\t.reg .b16 cl, ch, dl, dh;\n\tmov.b32 {cl, ch}, %2;\n\tmov.b32 {dl, dh}, %3;\n\t"
+        "fma.rn.f32.f16 %0, cl, dl, 0f00000000;\n\tfma.rn.f32.f16 %1, ch, dh, 0f00000000;\n\t}"
+        : "=f"(p0), "=f"(p1) : "r"(c), "r"(d));
+  return make_float2(p0, p1);
+}
+// Exact product of one 16-bit half of each of two words (HC of c, HD of d).
+template <int KIND, int HC, int HD>
+__device__ __forceinline__ float hprod1(uint32_t c, uint32_t d) {
+  const unsigned short a = (unsigned short)(HC ? c >> 16 : c), b = (unsigned short)(HD ? d >> 16 : d);
+  float p;
+  if constexpr (KIND == kB16)
+    asm("fma.rn.f32.bf16 %0, %1, %2, 0f00000000;" : "=f"(p) : "h"(a), "h"(b));
+  else
+    asm("fma.rn.f32.f16 %0, %1, %2, 0f00000000;" : "=f"(p) : "h"(a), "h"(b));
+  return p;
+}
+
+// Packed FP32 arithmetic (sm_100 and later): two lanes of FP32 per instruction,
+// each rounded like its scalar form.  The FMA pipe's throughput is the same;
+// the issue slots are halved.
+//   ffma2: (a0, a1) += (b0, b1) * (c0, c1)
+__device__ __forceinline__ void ffma2(float& a0, float& a1, float b0, float b1, float c0, float c1) {
+  asm("{\n\t.reg .b64 ra, rb, rc;\n\tmov.b64 ra, {%0, %1};\n\tmov.b64 rb, {%2, %3};\n\tmov.b64 rc, {%4, %5};\n\t"
+      "fma.rn.f32x2 ra, rb, rc, ra;\n\tmov.b64 {%0, %1}, ra;\n\t}"
+      : "+f"(a0), "+f"(a1) : "f"(b0), "f"(b1), "f"(c0), "f"(c1));
+}
+//   fmul2: (b0, b1) * (c0, c1)
+__device__ __forceinline__ float2 fmul2(float b0, float b1, float c0, float c1) {
+  float r0, r1;
+  asm("{\n\t.reg .b64 rr, rb, rc;\n\tmov.b64 rb, {%2, %3};\n\tmov.b64 rc, {%4, %5};\n\t"
+      "mul.rn.f32x2 rr, rb, rc;\n\tmov.b64 {%0, %1}, rr;\n\t}"
+      : "=f"(r0), "=f"(r1) : "f"(b0), "f"(b1), "f"(c0), "f"(c1));
+  return make_float2(r0, r1);
+}
+
+// 16-bit fixed point (offset-binary halves) to FP32: the half placed in the
+// mantissa of 2^23 gives the float 2^23 + u exactly; subtracting 2^23 + 2^15
+// leaves q exactly.  One integer op per half, one packed subtraction per pair.
+__device__ __forceinline__ float2 i16pair(uint32_t w) {
+  uint32_t lo, hi;
+  asm("prmt.b32 %0, %1, 0x4B000000, 0x7510;" : "=r"(lo) : "r"(w));
+  asm("prmt.b32 %0, %1, 0x4B000000, 0x7532;" : "=r"(hi) : "r"(w));
+  float r0, r1;
+  asm("{\n\t.reg .b64 ra, rk;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rk, {%4, %4};\n\t"
+      "sub.rn.f32x2 ra, ra, rk;\n\tmov.b64 {%0, %1}, ra;\n\t}"
+      : "=f"(r0), "=f"(r1) : "f"(__uint_as_float(lo)), "f"(__uint_as_float(hi)), "f"(8421376.0f));
+  return make_float2(r0, r1);
+}
+__device__ __forceinline__ float i16lo(uint32_t w) { return __uint_as_float(0x4B000000u | (w & 0xffffu)) - 8421376.0f; }
+__device__ __forceinline__ float i16hi(uint32_t w) { return __uint_as_float(0x4B000000u | (w >> 16)) - 8421376.0f; }
+
 template <int KIND>
-__device__ __forceinline__ float hi16(uint32_t w) { return KIND == kB16 ? bf16hi(w) : h16hi(w); }
+__device__ __forceinline__ float lo16(uint32_t w) { return KIND == kB16 ? bf16lo(w) : KIND == kI16 ? i16lo(w) : h16lo(w); }
+template <int KIND>
+__device__ __forceinline__ float hi16(uint32_t w) { return KIND == kB16 ? bf16hi(w) : KIND == kI16 ? i16hi(w) : h16hi(w); }
 
 // Load CPT consecutive entries starting at element offset `off` of a row-major
 // array stored as KIND, as floats (gather path: L2 evict_last).

@@ -24,15 +24,42 @@ WalkLauncher walk_launcher_o4_bf16(int cpt, int lpr, int staged);
 WalkLauncher walk_launcher_o4_bf16f(int cpt, int lpr, int staged);
 WalkLauncher walk_launcher_o3_fp16(int cpt, int lpr, int staged);
 WalkLauncher walk_launcher_o4_fp16(int cpt, int lpr, int staged);
+// strip walk units (family 4; launch families 8 and 9)
+WalkLauncher walk_launcher_o3_fp32_strip(int cpt, int lpr, int fam);
+WalkLauncher walk_launcher_o3_bf16_strip(int cpt, int lpr, int fam);
+WalkLauncher walk_launcher_o3_bf16f_strip(int cpt, int lpr, int fam);
+WalkLauncher walk_launcher_o3_fp16_strip(int cpt, int lpr, int fam);
+WalkLauncher walk_launcher_o3_fx16_strip(int cpt, int lpr, int fam);
+WalkLauncher walk_launcher_o4_fp32_strip(int cpt, int lpr, int fam);
+WalkLauncher walk_launcher_o4_bf16_strip(int cpt, int lpr, int fam);
+WalkLauncher walk_launcher_o4_bf16f_strip(int cpt, int lpr, int fam);
+WalkLauncher walk_launcher_o4_fp16_strip(int cpt, int lpr, int fam);
+WalkLauncher walk_launcher_o4_fx16_strip(int cpt, int lpr, int fam);
+// Strip-walk partition: the row (through a.rnz) of every unit boundary, at stride order - 1.
+cudaError_t launch_partition_rows(int order, const WalkArgs& a, cudaStream_t s);
+// A(i, j) = FP64 sum over slabs k in order of V(k * vstride + i, j) for i < nrows, rounded
+// once; virtual rows r with rnz[r + 1] == rnz[r] are skipped (slab-major strip plans).
+cudaError_t launch_virtual_rows(const float* V, const int32_t* rnz, int S, int64_t nrows, int64_t vstride, int ld,
+                                int R, float* A, cudaStream_t s);
+// scale[j] = 32767 / colmax[j], inv[j] = colmax[j] / 32767 (1 for an empty or non-finite column).
+cudaError_t launch_fullrange_scales(const float* colmax, int cols, float* scale, float* inv, cudaStream_t s);
+// 16-bit fixed point of a leaf factor (rows x cols FP32 -> rows x rp offset-binary
+// int16): column scale `scale`, then a power of two 2^rowexp[r] per row that puts
+// the row's largest entry in [16384, 32767].  cols and rp at most 64.
+cudaError_t launch_fx16_rows(const float* src, int64_t rows, int cols, int rp, const float* scale, uint16_t* dst,
+                             int8_t* rowexp, cudaStream_t s);
+// out[p] = vals[p] * 2^-rowexp[leaf[p]] for p < n (exact).
+cudaError_t launch_fx16_values(const float* vals, const int32_t* leaf, const int8_t* rowexp, int64_t n, float* out,
+                               cudaStream_t s);
 
 cudaError_t launch_partition(int order, const WalkArgs& a, cudaStream_t s);
 // Flat walk indexes.  launch_expand: out[p] = per_fiber[f] for every entry p of
-// fiber f of one level (p < pos[nf] = n).  launch_row_starts: rnz[i] = first
+// fiber f of one level (p < pos[nf] = n).  launch_row_starts: rnz[i] = off + first
 // nonzero of root position i (pos2[pos1[i]], through pos3 for four modes).
 cudaError_t launch_expand(const int32_t* per_fiber, const int32_t* pos, int64_t nf, int64_t n, int32_t* out,
                           cudaStream_t s);
 cudaError_t launch_row_starts(const int32_t* pos1, const int32_t* pos2, const int32_t* pos3, int64_t nroot,
-                              int32_t* rnz, cudaStream_t s);
+                              int32_t* rnz, cudaStream_t s, int64_t off = 0);
 // FP64 merge of the rows the walk left in the carry buffer (after the walk kernel).
 cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s);
 // TTV walk over units of 32 * kTtvNpt nonzeros (a: the 2-level view, see tt_ttv.cuh).

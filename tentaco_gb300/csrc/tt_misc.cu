@@ -5,10 +5,28 @@
 #include "tt_kernels.h"
 #include "tt_mttkrp.cuh"
 #include "tt_ttv.cuh"
+#include "tt_strip.cuh"
 
 namespace tt {
 
 WalkLauncher walk_launcher(int order, int prec, int cpt, int lpr, int staged) {
+  if (staged == 8 || staged == 9) {  // strip walk (U = 4 / 2 nonzeros per team and step)
+    if (order == 3) {
+      if (prec == kFP32) return walk_launcher_o3_fp32_strip(cpt, lpr, staged);
+      if (prec == kBF16) return walk_launcher_o3_bf16_strip(cpt, lpr, staged);
+      if (prec == kBF16F) return walk_launcher_o3_bf16f_strip(cpt, lpr, staged);
+      if (prec == kFP16) return walk_launcher_o3_fp16_strip(cpt, lpr, staged);
+      if (prec == kFX16) return walk_launcher_o3_fx16_strip(cpt, lpr, staged);
+    } else if (order == 4) {
+      if (prec == kFP32) return walk_launcher_o4_fp32_strip(cpt, lpr, staged);
+      if (prec == kBF16) return walk_launcher_o4_bf16_strip(cpt, lpr, staged);
+      if (prec == kBF16F) return walk_launcher_o4_bf16f_strip(cpt, lpr, staged);
+      if (prec == kFP16) return walk_launcher_o4_fp16_strip(cpt, lpr, staged);
+      if (prec == kFX16) return walk_launcher_o4_fx16_strip(cpt, lpr, staged);
+    }
+    return nullptr;
+  }
+  if (prec == kFX16) return nullptr;  // 16-bit fixed point: strip walk only
   if (order == 3) {
     if (prec == kFP32) return walk_launcher_o3_fp32(cpt, lpr, staged);
     if (prec == kBF16) return walk_launcher_o3_bf16(cpt, lpr, staged);
@@ -29,6 +47,50 @@ cudaError_t launch_partition(int order, const WalkArgs& a, cudaStream_t s) {
   if (order == 2) partition_kernel<2><<<grid, tb, 0, s>>>(a);
   else if (order == 3) partition_kernel<3><<<grid, tb, 0, s>>>(a);
   else partition_kernel<4><<<grid, tb, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// Partition for the strip walk: for each unit boundary b in [0, nblocks], the row
+// (through rnz) holding nonzero min(b * P, nnz - 1), at stride `stride` in part.
+__global__ void partition_rows_kernel(const __grid_constant__ WalkArgs a, int stride) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b > a.nblocks) return;
+  const int64_t s = (b < a.nblocks) ? (int64_t)b * a.P : a.nnz - 1;
+  const_cast<int32_t*>(a.part)[(size_t)b * stride] = (int32_t)search_le(a.rnz, 0, a.nrows - 1, s);
+}
+
+cudaError_t launch_partition_rows(int order, const WalkArgs& a, cudaStream_t s) {
+  const int n = a.nblocks + 1;
+  partition_rows_kernel<<<(n + 255) / 256, 256, 0, s>>>(a, order - 1);
+  return cudaGetLastError();
+}
+
+// A(i, j) = sum over slabs k, in slab order and in FP64, of V(k * vstride + i, j):
+// the virtual rows of a slab-major plan summed into the output, rounded once.  A
+// virtual row without nonzeros (rnz[r] == rnz[r + 1]) was never written and
+// counts as zero.  ld: row stride of V and A.
+__global__ void virtual_rows_kernel(const float* __restrict__ V, const int32_t* __restrict__ rnz, int S,
+                                    int64_t nrows, int64_t vstride, int ld, int R, float* __restrict__ A) {
+  const int64_t n = nrows * (int64_t)R;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / R;
+    const int j = (int)(e - i * R);
+    double acc = 0.0;
+    for (int k = 0; k < S; k++) {
+      const int64_t r = (int64_t)k * vstride + i;
+      if (rnz[r + 1] > rnz[r]) acc += (double)V[r * ld + j];
+    }
+    A[i * ld + j] = (float)acc;
+  }
+}
+
+cudaError_t launch_virtual_rows(const float* V, const int32_t* rnz, int S, int64_t nrows, int64_t vstride, int ld,
+                                int R, float* A, cudaStream_t s) {
+  const int64_t n = nrows * (int64_t)R;
+  if (n == 0) return cudaSuccess;
+  int64_t grid = (n + 255) / 256;
+  if (grid > 152 * 16) grid = 152 * 16;
+  virtual_rows_kernel<<<(int)grid, 256, 0, s>>>(V, rnz, S, nrows, vstride, ld, R, A);
   return cudaGetLastError();
 }
 
@@ -90,10 +152,11 @@ __global__ void flat_kexp_kernel(const int32_t* __restrict__ crd1, const int32_t
 }
 
 __global__ void flat_rnz_kernel(const int32_t* __restrict__ pos1, const int32_t* __restrict__ pos2,
-                                const int32_t* __restrict__ pos3, int64_t nroot, int32_t* __restrict__ rnz) {
+                                const int32_t* __restrict__ pos3, int64_t nroot, int32_t* __restrict__ rnz,
+                                int64_t off) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nroot; i += (int64_t)gridDim.x * blockDim.x) {
     const int32_t f2 = pos2[pos1[i]];
-    rnz[i] = pos3 ? pos3[f2] : f2;
+    rnz[i] = (int32_t)(off + (pos3 ? pos3[f2] : f2));
   }
 }
 
@@ -109,8 +172,8 @@ cudaError_t launch_expand(const int32_t* per_fiber, const int32_t* pos, int64_t 
 }
 
 cudaError_t launch_row_starts(const int32_t* pos1, const int32_t* pos2, const int32_t* pos3, int64_t nroot,
-                              int32_t* rnz, cudaStream_t s) {
-  flat_rnz_kernel<<<flat_grid(nroot + 1), 256, 0, s>>>(pos1, pos2, pos3, nroot, rnz);
+                              int32_t* rnz, cudaStream_t s, int64_t off) {
+  flat_rnz_kernel<<<flat_grid(nroot + 1), 256, 0, s>>>(pos1, pos2, pos3, nroot, rnz, off);
   return cudaGetLastError();
 }
 
@@ -245,6 +308,85 @@ __global__ void to_16_kernel(const float* __restrict__ src, int64_t rows, int co
     const float v = j < cols ? src[r * cols + j] * (scale ? scale[j] : 1.f) : 0.f;
     dst[i] = kind == 2 ? __half_as_ushort(__float2half_rn(v)) : __bfloat16_as_ushort(__float2bfloat16_rn(v));
   }
+}
+
+// Full-range fixed-point scales: scale[j] = 32767 / colmax[j], inv[j] = colmax[j] / 32767
+// (1 where colmax is 0 or not finite), so each column's max maps to 32767.
+__global__ void fullrange_scales_kernel(const float* colmax, int cols, float* scale, float* inv) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= cols) return;
+  const float m = colmax[j];
+  const bool ok = m > 0.f && m <= 3.4e38f;
+  scale[j] = ok ? (float)(32767.0 / (double)m) : 1.f;
+  inv[j] = ok ? (float)((double)m / 32767.0) : 1.f;
+}
+
+cudaError_t launch_fullrange_scales(const float* colmax, int cols, float* scale, float* inv, cudaStream_t s) {
+  fullrange_scales_kernel<<<(cols + 63) / 64, 64, 0, s>>>(colmax, cols, scale, inv);
+  return cudaGetLastError();
+}
+
+// 16-bit fixed point of the leaf factor, one warp per row: x = src * scale[col]
+// (column max -> 32767), then the row's power of two e (0..40) that puts its
+// largest |x| in [16384, 32767]; q = rint(x * 2^e) stored offset-binary (q + 32768),
+// zero for cols <= j < rp; rowexp[r] = e.
+__global__ void fx16_rows_kernel(const float* __restrict__ src, int64_t rows, int cols, int rp,
+                                 const float* __restrict__ scale, uint16_t* __restrict__ dst,
+                                 int8_t* __restrict__ rowexp) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += warps) {
+    float x[2];
+    float m = 0.f;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int j = lane + 32 * h;
+      x[h] = j < cols ? src[r * cols + j] * scale[j] : 0.f;
+      if (!(fabsf(x[h]) <= 3.4e38f)) x[h] = 0.f;  // non-finite entries are stored as 0
+      m = fmaxf(m, fabsf(x[h]));
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, d));
+    int e = 0;
+    while (e < 40 && m > 0.f && m * 2.f <= 32767.f) {
+      m *= 2.f;
+      e++;
+    }
+    const float f = __uint_as_float((uint32_t)(127 + e) << 23);  // 2^e
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int j = lane + 32 * h;
+      if (j < rp) {
+        const float q = fminf(fmaxf(rintf(x[h] * f), -32767.f), 32767.f);
+        dst[r * rp + j] = (uint16_t)((int)q + 32768);
+      }
+    }
+    if (lane == 0) rowexp[r] = (int8_t)e;
+  }
+}
+
+cudaError_t launch_fx16_rows(const float* src, int64_t rows, int cols, int rp, const float* scale, uint16_t* dst,
+                             int8_t* rowexp, cudaStream_t s) {
+  if (rows == 0) return cudaSuccess;
+  if (cols < 1 || cols > 64 || rp > 64) return cudaErrorInvalidValue;
+  fx16_rows_kernel<<<(int)std::min<int64_t>((rows + 7) / 8, 152 * 64), 256, 0, s>>>(src, rows, cols, rp, scale, dst,
+                                                                                    rowexp);
+  return cudaGetLastError();
+}
+
+// out[p] = vals[p] * 2^-rowexp[leaf[p]]: an exact power-of-two scaling (padding
+// entries have value 0 and leaf coordinate 0).
+__global__ void fx16_values_kernel(const float* __restrict__ vals, const int32_t* __restrict__ leaf,
+                                   const int8_t* __restrict__ rowexp, int64_t n, float* __restrict__ out) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
+    out[p] = ldexpf(vals[p], -(int)rowexp[leaf[p]]);
+}
+
+cudaError_t launch_fx16_values(const float* vals, const int32_t* leaf, const int8_t* rowexp, int64_t n, float* out,
+                               cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  fx16_values_kernel<<<(int)std::min<int64_t>((n + 255) / 256, 152 * 32), 256, 0, s>>>(vals, leaf, rowexp, n, out);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_to_16(const float* src, int64_t rows, int cols, int rp, const float* scale, int kind,

@@ -387,20 +387,24 @@ struct Walk {
 
   // The lane's piece (LB bytes) of a factor row, as raw words: the load is
   // issued now, the conversion happens when the words are used.
+  // L1: allocate the piece in L1 (rows that the next nonzeros of the same fiber
+  // read again: the flat walk's upper-level rows); otherwise L1 is bypassed.
+  template <bool L1 = false>
   __device__ __forceinline__ static void piece_load(const unsigned char* p, uint64_t pol, uint32_t (&w)[NWD]) {
     if constexpr (LB == 32) {
-      const uint4 x = ld_gather_16_na(p, pol), y = ld_gather_16_na(p + 16, pol);
+      const uint4 x = L1 ? ld_gather_16(p, pol) : ld_gather_16_na(p, pol);
+      const uint4 y = L1 ? ld_gather_16(p + 16, pol) : ld_gather_16_na(p + 16, pol);
       w[0] = x.x; w[1] = x.y; w[2] = x.z; w[3] = x.w; w[4] = y.x; w[5] = y.y; w[6] = y.z; w[7] = y.w;
     } else if constexpr (LB == 16) {
-      const uint4 x = ld_gather_16_na(p, pol);
+      const uint4 x = L1 ? ld_gather_16(p, pol) : ld_gather_16_na(p, pol);
       w[0] = x.x; w[1] = x.y; w[2] = x.z; w[3] = x.w;
     } else if constexpr (LB == 8) {
-      const uint2 x = ld_gather_8_na(p, pol);
+      const uint2 x = L1 ? ld_gather_8(p, pol) : ld_gather_8_na(p, pol);
       w[0] = x.x; w[1] = x.y;
     } else if constexpr (LB == 4) {
-      w[0] = ld_gather_4_na(p, pol);
+      w[0] = L1 ? ld_gather_4(p, pol) : ld_gather_4_na(p, pol);
     } else {
-      w[0] = ld_gather_2_na(p, pol);
+      w[0] = L1 ? ld_gather_2(p, pol) : ld_gather_2_na(p, pol);
     }
   }
   __device__ __forceinline__ static void piece_cvt(const uint32_t (&w)[NWD], float (&g)[CPT]) {
@@ -672,28 +676,31 @@ struct Walk {
 #pragma unroll
     for (int c = 0; c < CPT; c++) ra[c] = 0.f;
     bool flushed = false;
-    // one nonzero: ra += ((v * c) [* m]) * d, value half HV of word vw (16-bit) or
-    // float v; m: the level-2 piece (four modes; unused for three)
+    // one nonzero: ra += v * (c * d) (three modes) or (c * d) * (v * m) (four),
+    // value half HV of word vw.  The 16-bit products c * d and v * m are exact in
+    // FP32 (mixed-precision FMA with a zero addend), so each column takes one
+    // rounding per nonzero, as (v * c) * d does; the FP32 FMAs go two columns per
+    // instruction.
     auto acc16 = [&](const uint32_t (&gc)[NWD], const uint32_t (&gm)[MWD], const uint32_t (&gd)[NWD], uint32_t vw,
                      auto hv) {
       constexpr int HV = decltype(hv)::value;
-      float d[CPT], mm[CPT];
-      piece_cvt(gd, d);
-      if constexpr (ORDER == 4) piece_cvt(gm, mm);
-      else (void)gm;
       if constexpr (CPT == 1) {
-        float t = 0.f;
-        mfma1<FK, HV>(t, gc[0], vw);
-        if constexpr (ORDER == 4) t = t * mm[0];
-        ra[0] = fmaf(t, d[0], ra[0]);
+        const float p = hprod1<FK, 0, 0>(gc[0], gd[0]);
+        if constexpr (ORDER == 4) ra[0] = fmaf(p, hprod1<FK, HV, 0>(vw, gm[0]), ra[0]);
+        else ra[0] = fmaf(HV ? hi16<VK>(vw) : lo16<VK>(vw), p, ra[0]);
       } else {
+        const float v = HV ? hi16<VK>(vw) : lo16<VK>(vw);
+        const uint32_t vv = HV ? (vw >> 16) | (vw & 0xffff0000u) : (vw << 16) | (vw & 0xffffu);  // v in both halves
 #pragma unroll
         for (int k = 0; k < CPT / 2; k++) {
-          float t0 = 0.f, t1 = 0.f;
-          mfma2<FK, HV>(t0, t1, gc[k], vw);
-          if constexpr (ORDER == 4) { t0 = t0 * mm[2 * k]; t1 = t1 * mm[2 * k + 1]; }
-          ra[2 * k] = fmaf(t0, d[2 * k], ra[2 * k]);
-          ra[2 * k + 1] = fmaf(t1, d[2 * k + 1], ra[2 * k + 1]);
+          const float2 p = hprod2<FK>(gc[k], gd[k]);
+          if constexpr (ORDER == 4) {
+            const float2 t = hprod2<FK>(vv, gm[k]);
+            ffma2(ra[2 * k], ra[2 * k + 1], p.x, p.y, t.x, t.y);
+          } else {
+            (void)vv;
+            ffma2(ra[2 * k], ra[2 * k + 1], v, v, p.x, p.y);
+          }
         }
       }
     };
@@ -703,11 +710,17 @@ struct Walk {
       piece_cvt(gd, d);
       if constexpr (ORDER == 4) piece_cvt(gm, mm);
       else (void)gm;
+      if constexpr (CPT == 1) {
+        float t = v * c[0];
+        if constexpr (ORDER == 4) t = t * mm[0];
+        ra[0] = fmaf(t, d[0], ra[0]);
+      } else {
 #pragma unroll
-      for (int k = 0; k < CPT; k++) {
-        float t = v * c[k];
-        if constexpr (ORDER == 4) t = t * mm[k];
-        ra[k] = fmaf(t, d[k], ra[k]);
+        for (int k = 0; k < CPT; k += 2) {
+          float2 t = fmul2(v, v, c[k], c[k + 1]);
+          if constexpr (ORDER == 4) t = fmul2(t.x, t.y, mm[k], mm[k + 1]);
+          ffma2(ra[k], ra[k + 1], t.x, t.y, d[k], d[k + 1]);
+        }
       }
     };
     auto next_row = [&]() {
@@ -739,8 +752,8 @@ struct Walk {
       }
 #pragma unroll
       for (int u = 0; u < U; u++) {
-        piece_load(fc + (size_t)(uint32_t)k[u] * FRB, pol, gc[u]);
-        if constexpr (ORDER == 4) piece_load(fm + (size_t)(uint32_t)k2[u] * FRB, pol, gm[u]);
+        piece_load<true>(fc + (size_t)(uint32_t)k[u] * FRB, pol, gc[u]);
+        if constexpr (ORDER == 4) piece_load<true>(fm + (size_t)(uint32_t)k2[u] * FRB, pol, gm[u]);
         piece_load(fd + (size_t)(uint32_t)l[u] * FRB, pol, gd[u]);
       }
       if constexpr (ORDER != 4) {
@@ -783,8 +796,8 @@ struct Walk {
     }
     for (int j = nb * U; j < n; j++) {  // ragged end (the tensor's last tile only)
       uint32_t gc[NWD], gd[NWD], gm[MWD];
-      piece_load(fc + (size_t)(uint32_t)kc[j] * FRB, pol, gc);
-      if constexpr (ORDER == 4) piece_load(fm + (size_t)(uint32_t)k2c[j] * FRB, pol, gm);
+      piece_load<true>(fc + (size_t)(uint32_t)kc[j] * FRB, pol, gc);
+      if constexpr (ORDER == 4) piece_load<true>(fm + (size_t)(uint32_t)k2c[j] * FRB, pol, gm);
       else gm[0] = 0u;
       piece_load(fd + (size_t)(uint32_t)lc[j] * FRB, pol, gd);
       while (s + j >= rend) next_row();

@@ -19,6 +19,7 @@
 #define TT_ARGS_ONLY
 #include "tt_mttkrp.cuh"
 #include "tt_ttv.cuh"
+#include "tt_strip.cuh"
 #include "tt_plan.h"
 
 using namespace tt;
@@ -26,15 +27,14 @@ using namespace tt;
 namespace tt {
 
 // ---------------------------------------------------------------------------
-// variant table: family {lean warp tile, staged, TMA gather, flat} x threads {256,512} x
-// nonzeros per team (5 values per family) x columns per lane {8,4,2,1}
+// variant table: family {lean warp tile, staged, TMA gather, flat, strip} x threads
+// {256,512} x nonzeros per team (5 values per family) x columns per lane {8,4,2,1}
 // ---------------------------------------------------------------------------
 static const int kTB[2] = {256, 512};
-static const int kGF[4][5] = {{16, 32, 64, 128, 256}, {4, 8, 16, 32, 64}, {16, 32, 64, 128, 256},
-                              {16, 32, 64, 128, 256}};
+static const int kGF[kFamilies][5] = {{16, 32, 64, 128, 256}, {4, 8, 16, 32, 64}, {16, 32, 64, 128, 256},
+                                      {16, 32, 64, 128, 256}, {16, 32, 64, 128, 256}};
 static const int kCPT[4] = {8, 4, 2, 1};
 constexpr int kPerFamily = 2 * 5 * 4;
-constexpr int kNumVariants = 4 * kPerFamily;  // lean, staged, TMA gather, flat
 constexpr size_t kSmemLimit = (size_t)227 * 1024;
 
 VariantSpec variant_spec(int id) {
@@ -65,12 +65,17 @@ int launch_family(const VariantSpec& v) {
   if (v.staged == 0) return v.tb == 512 ? 3 : 0;
   if (v.staged == 2) return v.tb == 512 ? 5 : 2;
   if (v.staged == 3) return v.tb == 512 ? 7 : 6;
+  if (v.staged == 4) return v.tb == 512 ? 9 : 8;
   return v.staged;
 }
 int tma_stages(const VariantSpec& v) { return v.tb == 512 ? 8 : 4; }
 
-// Resident 256-thread blocks a lean (or flat) variant's registers are budgeted for.
-int lean_blocks(const VariantSpec& v) { return v.cpt >= 4 ? (v.tb == 512 ? 3 : 2) : (v.tb == 512 ? 4 : 3); }
+// Resident 256-thread blocks a lean (or flat) variant's registers are budgeted for;
+// a strip variant's: 2 (four nonzeros per team and step) or 3 (two).
+int lean_blocks(const VariantSpec& v) {
+  if (v.staged == 4) return v.tb == 512 ? 3 : 2;
+  return v.cpt >= 4 ? (v.tb == 512 ? 3 : 2) : (v.tb == 512 ? 4 : 3);
+}
 
 // Nonzeros of one work unit: a warp's tile for the lean family, a block's tile otherwise.
 int variant_unit(const VariantSpec& v, int rp) {
@@ -85,6 +90,7 @@ size_t variant_smem(const VariantSpec& v, int rp, int prec, int wcap, int order)
   const int P = (v.tb / lpr) * v.G;
   if (v.staged == 0) return (size_t)(256 / 32) * lean_warp_bytes(v.G, 32 / lpr, val_bytes(prec));
   if (v.staged == 3) return (size_t)(256 / 32) * flat_warp_bytes(v.G, 32 / lpr, val_bytes(prec), order);
+  if (v.staged == 4) return (size_t)(256 / 32) * strip_warp_bytes((32 / lpr) * v.G, val_bytes(prec), order);
   if (v.staged == 2)  // TMA gather: 8 warps, each with its ring of row stages and its lean tile
     return (size_t)(256 / 32) * tma_warp_bytes(v.G, 32 / lpr, val_bytes(prec), rp * fac_bytes(prec), tma_stages(v));
   return v.staged ? stage_smem_bytes(P, wcap, v.tb, rp, val_bytes(prec), fac_bytes(prec))
@@ -107,10 +113,13 @@ bool variant_valid(int id, int order, int rank, int prec) {
   if (rp % v.cpt) return false;
   const int lpr = rp / v.cpt;
   if (lpr < 1 || lpr > 32) return false;
+  // the strip walk works on column pairs; 16-bit fixed point is strip-only
+  if (v.staged == 4 && v.cpt < 2) return false;
+  if (prec == kFX16 && v.staged != 4) return false;
   // shared memory must fit the 227 KB opt-in limit (staged: with the smallest
   // window; a plan checks its own tensor's largest window)
   if (variant_smem(v, rp, prec, 1, order) > kSmemLimit) return false;
-  if (v.staged && (rp * fac_bytes(prec)) % 16) return false;
+  if (v.staged && v.staged != 4 && (rp * fac_bytes(prec)) % 16) return false;
   // TMA gather: four rows per copy land on 128-byte boundaries (rows of 32-byte
   // multiples), and a team's G nonzeros are whole stages of U = lanes-per-row rows
   if (v.staged == 2 && ((rp * fac_bytes(prec)) % 32 != 0 || v.G % lpr != 0)) return false;
@@ -153,18 +162,17 @@ int lean_default_variant(int order, int rank, int prec) {
   return -1;
 }
 
-// Leaf-mode slabs chosen automatically: none.  Slabs of about 32 MB keep the leaf
-// factor's rows L2-resident (on a 20M-nonzero slice of the 100M-nonzero rank-32
-// tensor, 4 slabs cut the walk's DRAM reads 3x and raise its L2 hit rate from
-// 31% to 72%), but the walk is bound by instruction issue rather than by DRAM,
-// and the extra fiber pieces of every slab add more issue than the saved DRAM
-// traffic returns.  Callers can still ask for slabs (tt_plan_options::slabs).
+// Leaf-mode slabs chosen automatically: when the leaf factor (as stored) exceeds
+// 48 MB, slices of at most 32 MB, so that the slab being walked stays L2-resident
+// beside the streams (129 MB of L2).  The strip walk runs all slabs in one launch
+// in slab-major order (virtual rows, summed afterwards); the lean, staged and TMA
+// walks run one pass per slab; the flat walk does not run on slab plans.
 int auto_slabs(int order, int64_t leaf_dim, int rp, int prec) {
   (void)order;
-  (void)leaf_dim;
-  (void)rp;
-  (void)prec;
-  return 1;
+  const int64_t bytes = leaf_dim * (int64_t)rp * fac_bytes(prec);
+  constexpr int64_t kMB = 1 << 20;
+  if (bytes <= 48 * kMB) return 1;
+  return (int)std::min<int64_t>(kMaxSlabs, (bytes + 32 * kMB - 1) / (32 * kMB));
 }
 
 }  // namespace tt
@@ -250,8 +258,15 @@ void dev_free(tt_plan* p, void* ptr) {
 
 int64_t pad16(int64_t n) { return ((n + 15) / 16) * 16 + 16; }
 
+// Work units of the plan's walk: the nonzeros (slab passes: the largest slab is
+// no larger), or for the strip walk on a slab plan the slab-major arrays.
+int64_t walk_units(const tt_plan* p, int P) {
+  const int64_t n = p->staged == 4 && p->slabs > 1 ? p->leaf_len : p->nnz;
+  return (n + P - 1) / P;
+}
+
 tt_status alloc_walk_scratch(tt_plan* p, int P) {
-  const int64_t nb = (p->nnz + P - 1) / P;
+  const int64_t nb = walk_units(p, P);
   if (nb > p->scratch_blocks) {
     struct SyncAtEnd {  // pool memory becomes usable on every stream
       cudaStream_t st;
@@ -292,7 +307,7 @@ WalkArgs ttv_args(const tt_plan* p, const float* x, float* y);
 tt_status prepare_partition(tt_plan* p) {
   p->part_ready = false;
   p->part_ms = 0.f;
-  if (p->slabs != 1 || p->nnz == 0) return TT_OK;
+  if ((p->slabs != 1 && !(p->op == TT_OP_MTTKRP && p->staged == 4)) || p->nnz == 0) return TT_OK;
   const WalkArgs a = p->op == TT_OP_TTV ? ttv_args(p, nullptr, nullptr) : walk_args(p, nullptr, 0);
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
@@ -301,7 +316,8 @@ tt_status prepare_partition(tt_plan* p) {
     return set_error(TT_ERR_CUDA, "partition timer");
   }
   cudaError_t e = cudaEventRecord(e0, p->stream);
-  if (e == cudaSuccess) e = launch_partition(p->op == TT_OP_TTV ? 2 : p->order, a, p->stream);
+  if (e == cudaSuccess) e = p->op == TT_OP_MTTKRP && p->staged == 4 ? launch_partition_rows(p->order, a, p->stream)
+                                                                     : launch_partition(p->op == TT_OP_TTV ? 2 : p->order, a, p->stream);
   if (e == cudaSuccess) e = cudaEventRecord(e1, p->stream);
   if (e == cudaSuccess) e = cudaEventSynchronize(e1);
   float ms = 0.f;
@@ -361,17 +377,39 @@ std::vector<int> variant_neighbours(int id) {
   return out;
 }
 
-// The fixed heuristic for this plan: the flat family has no slab passes, so slab
-// plans take the lean rule.
-int plan_default_variant(const tt_plan* p) {
-  const int id = default_variant(p->order, p->rank, p->prec, p->nnz);
-  if (p->slabs > 1 && variant_spec(id).staged == 3) return lean_default_variant(p->order, p->rank, p->prec);
-  return id;
+// The strip rule: G 128 with four nonzeros per team and step, 8 columns per lane
+// for 16-bit factors (16 bytes of a factor row), else 4.
+int strip_default_variant(int order, int rank, int prec) {
+  const int rp = rank_pad(rank);
+  int cpt = fac_kind(prec) == kF32 || prec == kFX16 ? 4 : 8;
+  while (cpt > 2 && rp / cpt < 1) cpt >>= 1;
+  const int id = variant_id(256, 128, cpt, 4);
+  if (variant_valid(id, order, rank, prec)) return id;
+  for (int i = 4 * kPerFamily; i < kNumVariants; i++)
+    if (variant_valid(i, order, rank, prec)) return i;
+  return -1;
 }
 
-// Builds the flat family's per-nonzero upper coordinates and per-row first nonzero
-// (once per plan).  All or nothing: on failure no array is kept.
+// The fixed heuristic for this plan: slab plans and 16-bit fixed point take the
+// strip rule (one launch over the slab-major layout; the flat family has no slab
+// passes), other plans the shape rule.
+int plan_default_variant(const tt_plan* p) {
+  if (p->slabs > 1 || p->prec == kFX16) {
+    const int id = strip_default_variant(p->order, p->rank, p->prec);
+    if (id >= 0) return id;
+    return lean_default_variant(p->order, p->rank, p->prec);
+  }
+  return default_variant(p->order, p->rank, p->prec, p->nnz);
+}
+
+// Builds the flat and strip families' per-nonzero upper coordinates and per-row
+// first nonzero (once per plan).  On a slab plan (strip walk only) the arrays follow
+// the slab-major layout: slab q's nonzeros at slab[q].off, and rnz over
+// slabs * (nroot + 1) virtual rows, row nroot of each slab covering its padding.
+// All or nothing: on failure no array is kept.
+tt_status build_slab_flat_arrays(tt_plan* p);
 tt_status build_flat_arrays(tt_plan* p) {
+  if (p->slabs > 1) return build_slab_flat_arrays(p);
   const size_t np = (size_t)pad16(p->nnz);
   int32_t *kexp = nullptr, *kexp2 = nullptr, *rnz = nullptr, *k1f2 = nullptr;
   auto undo = [&](tt_status s) {
@@ -416,6 +454,64 @@ tt_status build_flat_arrays(tt_plan* p) {
   return TT_OK;
 }
 
+tt_status build_slab_flat_arrays(tt_plan* p) {
+  const int S = p->slabs;
+  const int64_t I = p->nroot;
+  const size_t np = (size_t)pad16(p->leaf_len);
+  int32_t *kexp = nullptr, *kexp2 = nullptr, *rnz = nullptr, *k1f2 = nullptr;
+  auto undo = [&](tt_status s) {
+    cudaStreamSynchronize(p->stream);
+    dev_free(p, k1f2);
+    dev_free(p, kexp2);
+    dev_free(p, rnz);
+    dev_free(p, kexp);
+    return s;
+  };
+  auto ck = [&](cudaError_t e, const char* what) {
+    return e == cudaSuccess ? TT_OK
+                            : set_error(e == cudaErrorMemoryAllocation ? TT_ERR_OUT_OF_MEMORY : TT_ERR_CUDA,
+                                        "%s: %s", what, cudaGetErrorString(e));
+  };
+  tt_status s;
+  const int64_t nv = (int64_t)S * (I + 1);
+  if (nv + 1 > INT32_MAX || p->leaf_len > INT32_MAX)
+    return set_error(TT_ERR_UNSUPPORTED, "slab-major strip layout: %lld virtual rows", (long long)nv);
+  if ((s = dev_alloc(p, &kexp, np)) != TT_OK) return undo(s);
+  if ((s = dev_alloc(p, &rnz, (size_t)nv + 1)) != TT_OK) return undo(s);
+  if ((s = ck(cudaMemsetAsync(kexp, 0, sizeof(int32_t) * np, p->stream), "kexp clear")) != TT_OK) return undo(s);
+  if (p->order == 4) {
+    if ((s = dev_alloc(p, &kexp2, np)) != TT_OK) return undo(s);
+    if ((s = ck(cudaMemsetAsync(kexp2, 0, sizeof(int32_t) * np, p->stream), "kexp2 clear")) != TT_OK) return undo(s);
+    int64_t m2 = 1;
+    for (int q = 0; q < S; q++) m2 = std::max<int64_t>(m2, p->slab[q].count[2] + 1);
+    if ((s = dev_alloc(p, &k1f2, (size_t)m2)) != TT_OK) return undo(s);
+  }
+  for (int q = 0; q < S; q++) {
+    const tt_plan::SlabDev& sl = p->slab[q];
+    int32_t* rq = rnz + (size_t)q * (size_t)(I + 1);
+    if (p->order == 3) {
+      if ((s = ck(launch_expand(sl.crd[1], sl.pos[2], sl.count[1], sl.nnz, kexp + sl.off, p->stream), "expand")) != TT_OK ||
+          (s = ck(launch_row_starts(sl.pos[1], sl.pos[2], nullptr, I, rq, p->stream, sl.off), "row starts")) != TT_OK)
+        return undo(s);
+    } else {
+      if ((s = ck(launch_expand(sl.crd[1], sl.pos[2], sl.count[1], sl.count[2], k1f2, p->stream), "expand")) != TT_OK ||
+          (s = ck(launch_expand(k1f2, sl.pos[3], sl.count[2], sl.nnz, kexp + sl.off, p->stream), "expand")) != TT_OK ||
+          (s = ck(launch_expand(sl.crd[2], sl.pos[3], sl.count[2], sl.nnz, kexp2 + sl.off, p->stream), "expand")) != TT_OK ||
+          (s = ck(launch_row_starts(sl.pos[1], sl.pos[2], sl.pos[3], I, rq, p->stream, sl.off), "row starts")) != TT_OK)
+        return undo(s);
+    }
+  }
+  const int32_t end = (int32_t)p->leaf_len;
+  if ((s = ck(cudaMemcpyAsync(rnz + nv, &end, sizeof(int32_t), cudaMemcpyHostToDevice, p->stream), "rnz end")) != TT_OK)
+    return undo(s);
+  if ((s = ck(cudaStreamSynchronize(p->stream), "slab flat arrays")) != TT_OK) return undo(s);
+  dev_free(p, k1f2);
+  p->d_kexp = kexp;
+  p->d_kexp2 = kexp2;
+  p->d_rnz = rnz;
+  return TT_OK;
+}
+
 tt_status set_variant(tt_plan* p, int id) {
   VariantSpec v = variant_spec(id);
   p->variant = id;
@@ -425,14 +521,17 @@ tt_status set_variant(tt_plan* p, int id) {
   p->lpr = p->rp / v.cpt;
   p->G = v.G;
   p->P = variant_unit(v, p->rp);
-  p->nblocks = (int)((p->nnz + p->P - 1) / p->P);
+  p->nblocks = (int)walk_units(p, p->P);
   p->launcher = walk_launcher(p->order, p->prec, p->cpt, p->lpr, launch_family(v));
   if (!p->launcher) return set_error(TT_ERR_UNSUPPORTED, "variant %d not compiled for this shape", id);
   if (v.staged == 3 && p->slabs != 1) return set_error(TT_ERR_UNSUPPORTED, "the flat walk runs without slabs");
   tt_status s = alloc_walk_scratch(p, p->P);
   if (s != TT_OK) return s;
   p->part_ready = false;
-  if (v.staged == 3 && !p->d_kexp && p->nnz > 0 && (s = build_flat_arrays(p)) != TT_OK) return s;
+  if ((v.staged == 3 || v.staged == 4) && !p->d_kexp && p->nnz > 0 && (s = build_flat_arrays(p)) != TT_OK) return s;
+  if (v.staged == 4 && p->slabs > 1 && !p->d_vrows && p->nnz > 0 &&
+      (s = dev_alloc(p, &p->d_vrows, (size_t)p->slabs * (size_t)(p->nroot + 1) * (size_t)p->rank)) != TT_OK)
+    return s;
   p->wcap = 1;
   if (p->staged == 1 && p->nnz > 0) {
     // size the window-row region from this tensor's partition (computed once here)
@@ -465,13 +564,19 @@ tt_status use_variant(tt_plan* p, int id) {
   return s;
 }
 
+WalkArgs strip_slab_args(const tt_plan* p);
+
 // Arguments of one walk pass over slab q (the whole tensor when slabs == 1).
 WalkArgs walk_args(const tt_plan* p, float* A, int q) {
+  if (p->staged == 4 && p->slabs > 1) return strip_slab_args(p);
   WalkArgs a{};
   const tt_plan::SlabDev& sl = p->slab[q];
   for (int l = 0; l < TT_MAX_ORDER; l++) { a.pos[l] = sl.pos[l]; a.crd[l] = sl.crd[l]; }
   a.crd[0] = p->dense_root ? nullptr : p->d_crd[0];
-  a.vals = static_cast<const unsigned char*>(p->d_vals) + (size_t)sl.off * (size_t)val_bytes(p->prec);
+  // 16-bit fixed point reads the values scaled by their leaf rows' powers of two,
+  // which exist once factors are set (the unscaled values before: placeholder runs)
+  a.vals = static_cast<const unsigned char*>(p->prec == kFX16 && p->d_vals_fx ? (const void*)p->d_vals_fx : p->d_vals) +
+           (size_t)sl.off * (size_t)val_bytes(p->prec);
   a.accum = p->slabs > 1 ? 1 : 0;
   a.gpol = p->gpol;
   for (int m = 0; m < 3; m++) a.fac[m] = p->fac[m];
@@ -493,6 +598,41 @@ WalkArgs walk_args(const tt_plan* p, float* A, int q) {
   while ((1 << a.lgG) < p->G) a.lgG++;
   a.nblocks = (int)((sl.nnz + p->P - 1) / p->P);
   a.wcap = p->wcap;
+  a.err = p->d_err;
+  a.kexp = p->d_kexp;
+  a.kexp2 = p->d_kexp2;
+  a.rnz = p->d_rnz;
+  for (int m = 0; m < 3; m++) a.fac_rows[m] = m + 1 < p->order ? (int32_t)p->dims[m + 1] : 0;
+  return a;
+}
+
+// The strip walk's single pass over a slab plan's slab-major arrays: virtual rows
+// q * (nroot + 1) + i, written once each into d_vrows.
+WalkArgs strip_slab_args(const tt_plan* p) {
+  WalkArgs a{};
+  const int L = p->order - 1;
+  a.crd[L] = p->d_crd[L];
+  a.vals = p->prec == kFX16 && p->d_vals_fx ? (const void*)p->d_vals_fx : p->d_vals;
+  a.accum = 0;
+  a.gpol = p->gpol;
+  for (int m = 0; m < 3; m++) a.fac[m] = p->fac[m];
+  a.colscale = p->d_colscale;
+  a.out = p->d_vrows;
+  a.part = p->d_part;
+  a.carry = p->d_carry;
+  a.meta = p->d_meta;
+  a.segcarry = p->d_segcarry;
+  a.segmeta = p->d_segmeta;
+  a.nnz = p->leaf_len;
+  a.nrows = (int32_t)((int64_t)p->slabs * (p->nroot + 1));
+  a.rp = p->rp;
+  a.R = p->rank;
+  a.ldo = p->rank;
+  a.P = p->P;
+  a.G = p->G;
+  a.lgG = 0;
+  while ((1 << a.lgG) < p->G) a.lgG++;
+  a.nblocks = p->nblocks;
   a.err = p->d_err;
   a.kexp = p->d_kexp;
   a.kexp2 = p->d_kexp2;
@@ -544,6 +684,23 @@ tt_status run_mttkrp(tt_plan* p, float* A, cudaStream_t st) {
   const size_t outbytes = (size_t)p->dims[0] * (size_t)p->rank * sizeof(float);
   if (!p->variant_ready)
     return set_error(TT_ERR_INVALID_ARGUMENT, "the plan's last variant switch failed: select a variant");
+  // the device error word reports this call only: a bounded wait that ran out in an
+  // earlier call (or in a variant timed at plan creation) does not stop this one
+  if (p->d_err) CK(cudaMemsetAsync(p->d_err, 0, sizeof(int32_t), st));
+  if (p->nnz > 0 && p->staged == 4 && p->slabs > 1) {
+    // strip walk over the slab-major layout: one launch, the virtual rows' merge,
+    // then the slabs' rows summed into A (every row of A written, no clear)
+    WalkArgs a = walk_args(p, A, 0);
+    const size_t smem = variant_smem(variant_spec(p->variant), p->rp, p->prec, p->wcap, p->order);
+    a.smem_bytes = (int32_t)smem;
+    if (!p->part_ready) CK(launch_partition_rows(p->order, a, st));
+    if (p->timing) CK(cudaEventRecord(p->evk0, st));
+    CK(p->launcher(a, a.nblocks, p->tb, smem, st));
+    if (p->timing) CK(cudaEventRecord(p->evk1, st));
+    CK(launch_chain_fixup(p->order, a, st));
+    CK(launch_virtual_rows(p->d_vrows, p->d_rnz, p->slabs, p->nroot, p->nroot + 1, p->rank, p->rank, A, st));
+    return TT_OK;
+  }
   CK(cudaMemsetAsync(A, 0, outbytes, st));
   if (p->nnz == 0) return TT_OK;
   // one pass per slab, in slab order, each adding its rows into A; the kernel
@@ -560,7 +717,7 @@ tt_status run_mttkrp(tt_plan* p, float* A, cudaStream_t st) {
       const tt_status s2 = encode_leaf_tmap(p, &a.tmap);
       if (s2 != TT_OK) return s2;
     }
-    if (!p->part_ready) CK(launch_partition(p->order, a, st));
+    if (!p->part_ready) CK(p->staged == 4 ? launch_partition_rows(p->order, a, st) : launch_partition(p->order, a, st));
     if (p->timing && q == first) CK(cudaEventRecord(p->evk0, st));
     CK(p->launcher(a, a.nblocks, p->tb, smem, st));
     if (p->timing && q == last) CK(cudaEventRecord(p->evk1, st));
@@ -646,8 +803,8 @@ TT_EXPORT tt_status tt_variant_get(int32_t id, tt_variant_info* info) {
   info->lanes_per_row = 32 / v.cpt;
   info->nnz_per_block = v.tb / info->lanes_per_row * v.G;
   info->staged = v.staged;
-  static const char* fam[4] = {"lean", "stage", "tma", "flat"};
-  if (v.staged == 0 || v.staged == 3) {  // lean / flat: 256-thread blocks, budget for b resident blocks per SM
+  static const char* fam[kFamilies] = {"lean", "stage", "tma", "flat", "strip"};
+  if (v.staged == 0 || v.staged == 3 || v.staged == 4) {  // lean / flat / strip: 256-thread blocks, budget for b resident blocks per SM
     info->threads = 256;
     info->nnz_per_block = 256 / info->lanes_per_row * v.G;
     std::snprintf(info->name, sizeof(info->name), "%s_b%d_g%d_c%d", fam[v.staged], lean_blocks(v), v.G, v.cpt);
@@ -716,8 +873,11 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
     if (rank < 1 || rank > TT_MAX_RANK) return set_error(TT_ERR_UNSUPPORTED, "rank %d (supported 1..%d)", rank, TT_MAX_RANK);
   } else if (op != TT_OP_TTV) {
     return set_error(TT_ERR_INVALID_ARGUMENT, "op %d", (int)op);
+  } else if (prec == TT_PREC_FX16) {
+    return set_error(TT_ERR_UNSUPPORTED, "TTV does not take 16-bit fixed-point storage");
   }
-  if (prec != TT_PREC_FP32 && prec != TT_PREC_BF16 && prec != TT_PREC_BF16_FACTORS && prec != TT_PREC_FP16)
+  if (prec != TT_PREC_FP32 && prec != TT_PREC_BF16 && prec != TT_PREC_BF16_FACTORS && prec != TT_PREC_FP16 &&
+      prec != TT_PREC_FX16)
     return set_error(TT_ERR_INVALID_ARGUMENT, "precision %d", (int)prec);
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -785,8 +945,10 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
         return fail(s);
     }
     for (int l = 0; l < TT_MAX_ORDER; l++) { p->slab[0].pos[l] = p->d_pos[l]; p->slab[0].crd[l] = p->d_crd[l]; }
+    for (int l = 0; l < v.order; l++) p->slab[0].count[l] = v.count[l];
     p->slab[0].nnz = v.nnz;
     p->slab[0].off = 0;
+    p->leaf_len = v.nnz;
     if (v.nnz > 0 && (s = device_csf_check(p, v, st)) != TT_OK) return fail(s);
   } else {
     for (int q = 0; q < S; q++) {
@@ -798,6 +960,7 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
         if ((s = upload(&d.crd[l], h.crd[l].data(), h.count[l], (size_t)h.count[l], "slab crd")) != TT_OK) return fail(s);
       d.nnz = h.nnz;
       d.off = h.leaf_off;
+      for (int l = 0; l < TT_MAX_ORDER; l++) d.count[l] = h.count[l];
     }
     if ((s = upload(&p->d_crd[L], sc.leaf_crd.data(), (int64_t)sc.leaf_crd.size(), sc.leaf_crd.size(), "slab leaf crd")) != TT_OK)
       return fail(s);
@@ -805,6 +968,7 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
     hvals = sc.leaf_vals.data();
     nvals = (int64_t)sc.leaf_vals.size();
     nvals_alloc = sc.leaf_vals.size();
+    p->leaf_len = (int64_t)sc.leaf_vals.size();
   }
   if (!v.dense_root) {
     if ((s = dev_alloc(p, &p->d_crd[0], (size_t)v.nroot)) != TT_OK) return fail(s);
@@ -813,6 +977,7 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
       return fail(set_error(TT_ERR_CUDA, "upload root crd"));
     p->slab[0].crd[0] = p->d_crd[0];
   }
+  p->nvals_alloc = nvals_alloc;
   {
     const size_t n = nvals_alloc;
     if (val_kind(p->prec) != kF32) {
@@ -875,7 +1040,8 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
       if (req_k < 0 || req_k > kMaxTopk)
         return fail(set_error(TT_ERR_INVALID_ARGUMENT, "model_topk %d (0..%d)", req_k, kMaxTopk));
       if (selector_rank(p, B, ranked, &in_range) == TT_OK && !ranked.empty()) {
-        const int k = req_k > 0 ? req_k : (in_range ? 1 : kTopkOutside);
+        // slab plans time the candidates too: the network was trained without slabs
+        const int k = req_k > 0 ? req_k : (in_range && p->slabs == 1 ? 1 : kTopkOutside);
         if (k > 1) {
           const int dflt = plan_default_variant(p);
           s = time_variants(p, st, ranked, k, dflt);
@@ -980,19 +1146,45 @@ TT_EXPORT tt_status tt_plan_set_factors(tt_plan* p, const float* const* factors,
     const float* inv[3] = {nullptr, nullptr, nullptr};
     for (int m = 0; m < nm; m++) {
       const int64_t rows = p->dims[m + 1];
+      if (p->prec == kFX16 && m < nm - 1) {
+        // 16-bit fixed point keeps the upper-level factors in FP32 (small, L2-resident)
+        if (p->rank == p->rp) {
+          p->fac[m] = factors[m];
+        } else {
+          if (!p->fac_own[m]) {
+            float* d = nullptr;
+            if ((s = dev_alloc(p, &d, (size_t)rows * p->rp)) != TT_OK) return s;
+            p->fac_own[m] = d;
+          }
+          CK(launch_pad_fp32(factors[m], rows, p->rank, p->rp, (float*)p->fac_own[m], st));
+          p->fac[m] = p->fac_own[m];
+        }
+        continue;
+      }
       float* cmax = p->d_scales + (size_t)(3 * m) * p->rp;
       float* scl = cmax + p->rp;
       float* iv = scl + p->rp;
       CK(cudaMemsetAsync(cmax, 0, sizeof(float) * p->rp, st));
       CK(launch_colmax(factors[m], rows, p->rank, cmax, st));
-      const bool h16 = fac_kind(p->prec) == kH16;
-      CK(launch_pow2_scales(cmax, p->rp, h16 ? 14 : 0, scl, iv, st));
       if (!p->fac_own[m]) {
         uint16_t* d = nullptr;
         if ((s = dev_alloc(p, &d, (size_t)rows * p->rp)) != TT_OK) return s;
         p->fac_own[m] = d;
       }
-      CK(launch_to_16(factors[m], rows, p->rank, p->rp, scl, h16 ? 2 : 1, (uint16_t*)p->fac_own[m], st));
+      if (p->prec == kFX16) {
+        // leaf factor: column scales, then a power of two per row (kept for the
+        // values: each nonzero's value is multiplied by its row's inverse power)
+        if (!p->d_rowexp && (s = dev_alloc(p, &p->d_rowexp, (size_t)rows)) != TT_OK) return s;
+        if (!p->d_vals_fx && (s = dev_alloc(p, &p->d_vals_fx, p->nvals_alloc)) != TT_OK) return s;
+        CK(launch_fullrange_scales(cmax, p->rp, scl, iv, st));
+        CK(launch_fx16_rows(factors[m], rows, p->rank, p->rp, scl, (uint16_t*)p->fac_own[m], p->d_rowexp, st));
+        CK(launch_fx16_values(static_cast<const float*>(p->d_vals), p->d_crd[p->order - 1], p->d_rowexp,
+                              (int64_t)p->nvals_alloc, p->d_vals_fx, st));
+      } else {
+        const bool h16 = fac_kind(p->prec) == kH16;
+        CK(launch_pow2_scales(cmax, p->rp, h16 ? 14 : 0, scl, iv, st));
+        CK(launch_to_16(factors[m], rows, p->rank, p->rp, scl, h16 ? 2 : 1, (uint16_t*)p->fac_own[m], st));
+      }
       p->fac[m] = p->fac_own[m];
       inv[m] = iv;
     }
@@ -1118,8 +1310,10 @@ tt_status time_variants(tt_plan* p, cudaStream_t st, const std::vector<int>& can
       }
     } sc{p, st, {p->fac[0], p->fac[1], p->fac[2]}, p->d_colscale, {}};
     const int nm = p->order - 1;
-    const size_t esz = p->prec == kFP32 ? 4 : 2;
     for (int m = 0; m < nm; m++) {
+      // bytes per entry of factor m in this plan's storage (16-bit fixed point keeps
+      // the upper-level factors in FP32)
+      const size_t esz = p->prec == kFP32 || (p->prec == kFX16 && m < nm - 1) ? 4 : 2;
       void* d = nullptr;
       CK(cudaMalloc(&d, (size_t)p->dims[m + 1] * p->rp * esz));
       sc.tmp.push_back(d);
@@ -1208,8 +1402,11 @@ TT_EXPORT tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
     if (F->dimensions[1] != rank || F->dimensions[0] != B->dimensions[m + 1])
       return set_error(TT_ERR_INVALID_ARGUMENT, "factor %d is %dx%d, expected %dx%d", m + 1, F->dimensions[0], F->dimensions[1], B->dimensions[m + 1], rank);
   }
+  // one call cannot repay the slab-major layout's one-time host build: no slabs
+  tt_plan_options opts{};
+  opts.slabs = 1;
   tt_plan* p = nullptr;
-  tt_status s = tt_plan_create(B, TT_OP_MTTKRP, rank, prec, select, variant, nullptr, &p);
+  tt_status s = tt_plan_create_ex(B, TT_OP_MTTKRP, rank, prec, select, variant, &opts, nullptr, &p);
   if (s != TT_OK) return s;
   std::vector<float*> dfac(order - 1, nullptr);
   float* dA = nullptr;

@@ -8,6 +8,10 @@
 
 namespace tt {
 
+// Kernel families of the variant table (lean, staged, TMA gather, flat, strip), 40 ids each.
+constexpr int kFamilies = 5;
+constexpr int kNumVariants = kFamilies * 40;
+
 struct VariantSpec {
   int id, tb, cpt, G, staged;
 };
@@ -36,6 +40,9 @@ struct tt_plan {
   int32_t* d_crd[TT_MAX_ORDER] = {nullptr, nullptr, nullptr, nullptr};
   void* d_vals = nullptr;
   float vinv = 1.f;  // 16-bit values: stored = value * (1/vinv)
+  size_t nvals_alloc = 0;        // entries of d_vals (padded)
+  float* d_vals_fx = nullptr;    // 16-bit fixed point: values times their leaf row's power of two
+  int8_t* d_rowexp = nullptr;    // 16-bit fixed point: power of two of every leaf-factor row
   // factors in storage precision
   const void* fac[3] = {nullptr, nullptr, nullptr};
   void* fac_own[3] = {nullptr, nullptr, nullptr};
@@ -61,14 +68,22 @@ struct tt_plan {
   double* d_segcarry = nullptr;  // MTTKRP: 2 FP64 rows per segment of work units
   int32_t* d_segmeta = nullptr;  // MTTKRP: 4 ints per segment
   int64_t scratch_blocks = 0;
-  float sweep_ms[160] = {};
+  float sweep_ms[tt::kNumVariants] = {};
   // leaf-mode slabs: one walk pass per slab, adding into the output (slabs == 1:
   // slab[0] is the whole tensor)
   struct SlabDev {
     int32_t* pos[TT_MAX_ORDER] = {nullptr, nullptr, nullptr, nullptr};
     int32_t* crd[TT_MAX_ORDER] = {nullptr, nullptr, nullptr, nullptr};
+    int64_t count[TT_MAX_ORDER] = {0, 0, 0, 0};  // entries per level (count[0]: root positions)
     int64_t nnz = 0, off = 0;
   };
+  // entries of the nonzero-level arrays: nnz, or with slabs the slab-major
+  // concatenation (each slab's run padded)
+  int64_t leaf_len = 0;
+  // strip walk on a slab plan: one pass over the slab-major arrays with
+  // slabs * (nroot + 1) virtual rows (row nroot of each slab holds its padding),
+  // written here and summed into the output by launch_virtual_rows
+  float* d_vrows = nullptr;
   int slabs = 1;
   int mode = 0;  // output mode (the plan's tensor is re-rooted at it when not 0)
   int gpol = 0;  // WalkArgs::gpol

@@ -1,14 +1,18 @@
 // tt_walk_inst.cuh -- explicit instantiations of the MTTKRP walk kernels for one
 // (order, precision): the lean warp-tile walk, shared-memory staged walk and TMA
 // gather walk in tt_walk_o{3,4}_{fp32,bf16,bf16f,fp16}.cu (TT_ORDER, TT_PREC,
-// TT_LOOKUP, TT_LOOKUP_FLAT and TT_LOOKUP_TMA defined), the flat and TMA walks in
-// the matching _flat.cu / _tma.cu units (TT_FLAT_UNIT or TT_TMA_UNIT, and
-// TT_LOOKUP, defined), so the kernels compile in parallel.  The (columns per lane, lanes per row)
+// TT_LOOKUP, TT_LOOKUP_FLAT and TT_LOOKUP_TMA defined), the flat, TMA and strip
+// walks in the matching _flat.cu / _tma.cu / _strip.cu units (TT_FLAT_UNIT,
+// TT_TMA_UNIT or TT_STRIP_UNIT, and TT_LOOKUP, defined), so the kernels compile in
+// parallel.  The strip walk also has fx16 units (16-bit fixed point).  The (columns per lane, lanes per row)
 // pairs cover factor ranks 8, 16, 32 and 64.
 #include <atomic>
 #include <mutex>
 #include "tt_mttkrp.cuh"
 #include "tt_kernels.h"
+#ifdef TT_STRIP_UNIT
+#include "tt_strip.cuh"
+#endif
 
 namespace tt {
 namespace {
@@ -92,9 +96,32 @@ cudaError_t launch_flat(const WalkArgs& a, int units, int tb, size_t smem, cudaS
   return launch_k(k, a, units, tb, smem, s, true, configured);
 }
 #endif  // TT_FLAT_UNIT
+
+#ifdef TT_STRIP_UNIT
+// strip walk (families 8 / 9: four nonzeros per team and step with registers for
+// two resident blocks, or two with registers for three)
+template <int CPT, int LPR, int FAM>
+cudaError_t launch_strip(const WalkArgs& a, int units, int tb, size_t smem, cudaStream_t s) {
+  auto k = mttkrp_strip_kernel<TT_ORDER, TT_PREC, CPT, LPR, FAM == 9 ? 2 : 4, FAM == 9 ? 3 : 2>;
+  static SmemLimit configured;
+  return launch_k(k, a, units, tb, smem, s, true, configured);
+}
+#endif  // TT_STRIP_UNIT
 }  // namespace
 
-#if defined(TT_TMA_UNIT)
+#if defined(TT_STRIP_UNIT)
+// the strip walk's launchers (families 8 and 9); two or more columns per lane
+WalkLauncher TT_LOOKUP(int cpt, int lpr, int fam) {
+#define TT_CASE(C, L) \
+  if (cpt == C && lpr == L) return fam == 8 ? &launch_strip<C, L, 8> : fam == 9 ? &launch_strip<C, L, 9> : nullptr;
+  TT_CASE(2, 4) TT_CASE(4, 2) TT_CASE(8, 1)      // rank 8
+  TT_CASE(2, 8) TT_CASE(4, 4) TT_CASE(8, 2)      // rank 16
+  TT_CASE(2, 16) TT_CASE(4, 8) TT_CASE(8, 4)     // rank 32
+  TT_CASE(2, 32) TT_CASE(4, 16) TT_CASE(8, 8)    // rank 64
+#undef TT_CASE
+  return nullptr;
+}
+#elif defined(TT_TMA_UNIT)
 // the TMA walk's launchers (families 2 and 5), in their own translation unit
 WalkLauncher TT_LOOKUP(int cpt, int lpr, int fam) {
 #define TT_CASE(C, L) \

@@ -1,0 +1,6 @@
+// MTTKRP strip walk kernels, order 3, storage bf16f.
+#define TT_ORDER 3
+#define TT_PREC kBF16F
+#define TT_STRIP_UNIT
+#define TT_LOOKUP walk_launcher_o3_bf16f_strip
+#include "tt_walk_inst.cuh"

@@ -147,8 +147,9 @@ int main(int argc, char* argv[]) {
   if (precision == "bf16") prec = TT_PREC_BF16;
   else if (precision == "bf16f") prec = TT_PREC_BF16_FACTORS;
   else if (precision == "fp16") prec = TT_PREC_FP16;
+  else if (precision == "fx16") prec = TT_PREC_FX16;
   else if (precision != "fp32") {
-    std::cerr << "precision must be fp32, bf16, bf16f or fp16" << std::endl;
+    std::cerr << "precision must be fp32, bf16, bf16f, fp16 or fx16" << std::endl;
     return 2;
   }
 

