@@ -69,7 +69,7 @@ struct alignas(64) WalkArgs {
   int32_t* err;           // staged kernels: set nonzero if a block's window exceeds wcap
   const int32_t* kexp;    // flat walk: the level-1 coordinate of every nonzero (padded)
   const int32_t* kexp2;   // flat walk, four modes: the level-2 coordinate of every nonzero (padded)
-  const int32_t* rnz;     // flat walk: first nonzero of every row (nrows + 1)
+  const int32_t* rnz;     // flat and strip walks: first nonzero of every row (nrows + 1); null otherwise
 };
 
 constexpr int kEmpty = -2;  // summary of a team that owns no nonzeros
@@ -1371,10 +1371,17 @@ __global__ void __launch_bounds__(256) seg_chain_kernel(const __grid_constant__ 
   const bool before = m.z & 1, after = m.z & 2, single = m.z & 4;
   if (!after || (single && before)) return;  // warp-uniform: no crossing row starts here
   const int r = m.y;
+  // end of row r: through rnz for the flat and strip walks (whose rows may be a
+  // slab plan's virtual rows, with no pos arrays), else through the pos levels;
   // ORDER 2: the "rows" are TTV fibers (pos[1] = fiber starts)
-  int64_t f1 = ORDER == 2 ? (int64_t)r + 1 : (int64_t)a.pos[1][r + 1];
-  if constexpr (ORDER == 4) f1 = a.pos[2][f1];
-  const int64_t n1 = a.pos[ORDER - 1][f1];
+  int64_t n1;
+  if (a.rnz) {
+    n1 = a.rnz[r + 1];
+  } else {
+    int64_t f1 = ORDER == 2 ? (int64_t)r + 1 : (int64_t)a.pos[1][r + 1];
+    if constexpr (ORDER == 4) f1 = a.pos[2][f1];
+    n1 = a.pos[ORDER - 1][f1];
+  }
   const int s1 = (int)((n1 - 1) / a.P) / kSeg;  // segment holding the row's last nonzero
   const int rp = a.rp;
   const int slot0 = single ? 0 : 1;  // this segment's slot; later segments hold the row in slot 0

@@ -601,7 +601,8 @@ WalkArgs walk_args(const tt_plan* p, float* A, int q) {
   a.err = p->d_err;
   a.kexp = p->d_kexp;
   a.kexp2 = p->d_kexp2;
-  a.rnz = p->d_rnz;
+  // rows through rnz only for the families that walk by it (the row merge uses it too)
+  a.rnz = p->staged == 3 || p->staged == 4 ? p->d_rnz : nullptr;
   for (int m = 0; m < 3; m++) a.fac_rows[m] = m + 1 < p->order ? (int32_t)p->dims[m + 1] : 0;
   return a;
 }
