@@ -289,7 +289,10 @@ def test_slabs_over_large_leaf_factor():
     facs = [tt.gen_dense(800, 32, 1, 3), tt.gen_dense(2_000_000, 32, 1, 4)]
     ref = O.mttkrp(to_oracle(B), facs)
     got, plan = run_plan(B, facs)
-    assert plan.slabs == 1  # automatic: no slabs
+    assert plan.slabs == 8  # automatic: slabs of at most 32 MB of the leaf factor
+    close(got, ref)
+    got, plan = run_plan(B, facs, slabs=1)
+    assert plan.slabs == 1
     close(got, ref)
     got, plan = run_plan(B, facs, slabs=8)
     assert plan.slabs == 8
