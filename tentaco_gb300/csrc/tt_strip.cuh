@@ -19,9 +19,12 @@
 //   * a step inside one output row (all of them on tensors with long rows) is only
 //     loads and FMAs: each team adds its nonzeros' products into its partial row;
 //   * a step holding a row end adds each nonzero to the row it belongs to (masked
-//     passes over the step, one per row piece); at the end the teams' partials are
-//     summed by a fixed butterfly of shuffles and the row is stored, or kept for
-//     the unit's merge if it is the unit's first row.
+//     passes over the step, one per row piece); the teams' partials of a finished
+//     row are summed by a fixed reduce-scatter of shuffles that leaves each lane a
+//     few of the row's columns to store (one coalesced store per row), or, for the
+//     unit's first row, by a full butterfly that keeps the row for the unit's merge;
+//     the end of the next row is loaded ahead, so a row end waits on no search
+//     unless empty rows follow.
 //
 // The gathered rows of the next step are in flight while the current step is
 // consumed (two register buffers).  Upper-level rows are gathered through L1 (the
@@ -224,6 +227,57 @@ __device__ __forceinline__ void strip_team_sum(const float (&acc)[CPT], float (&
     for (int c = 0; c < CPT; c++) r[c] += __shfl_xor_sync(0xffffffffu, r[c], d);
 }
 
+// Reduce-scatter of the teams' partial rows: split butterfly levels halve the
+// columns a lane keeps (lanes exchange the half they give away), then plain
+// levels sum what is left across the remaining teams.  Lane (team, q) ends with W
+// columns' totals, columns q*CPT + off(lane) + [0, W); among lanes that differ only
+// in the plain levels' bits, the one with those bits clear stores them.  Fixed
+// order: bitwise reproducible.
+template <int CPT, int LPR>
+struct TeamScatter {
+  static constexpr int lg(int x) { return x <= 1 ? 0 : 1 + lg(x / 2); }
+  static constexpr int TW = 32 / LPR;
+  static constexpr int NS = lg(CPT) < lg(TW) ? lg(CPT) : lg(TW);  // split levels
+  static constexpr int NP = lg(TW) - NS;                           // plain levels
+  static constexpr int W = CPT >> NS;                              // columns kept per lane
+  __device__ __forceinline__ static int offset(int lane) {
+    int off = 0;
+#pragma unroll
+    for (int k = 0; k < NS; k++)
+      if (lane & (LPR << k)) off += CPT >> (k + 1);
+    return off;
+  }
+  __device__ __forceinline__ static bool stores(int lane) {
+    bool st = true;
+#pragma unroll
+    for (int k = NS; k < NS + NP; k++)
+      if (lane & (LPR << k)) st = false;
+    return st;
+  }
+  __device__ __forceinline__ static void run(const float (&acc)[CPT], float (&r)[CPT], int lane) {
+#pragma unroll
+    for (int c = 0; c < CPT; c++) r[c] = acc[c];
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+      const int d = LPR << k;
+      const bool hi = (lane & d) != 0;
+      const int half = (CPT >> k) / 2;
+#pragma unroll
+      for (int c = 0; c < CPT / 2; c++) {
+        if (c < half) {
+          const float send = hi ? r[c] : r[c + half];
+          const float keep = hi ? r[c + half] : r[c];
+          r[c] = keep + __shfl_xor_sync(0xffffffffu, send, d);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = NS; k < NS + NP; k++)
+#pragma unroll
+      for (int c = 0; c < W; c++) r[c] += __shfl_xor_sync(0xffffffffu, r[c], LPR << k);
+  }
+};
+
 // Strip kernel: one work unit (P = TW * G nonzeros) per warp, 256-thread blocks.
 // part[u * (ORDER - 1)]: the row holding unit u's first nonzero (launch_partition_rows).
 template <int ORDER, int PREC, int CPT, int LPR, int U, int MINB>
@@ -278,7 +332,16 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_strip_kernel(const __grid_co
   const int first_row = (int)search_le(rnz, pb[0], rhi, ustart);
   int ip = first_row;
   int64_t rend = rnz[ip + 1];
+  int64_t rnext = rnz[min(ip + 2, a.nrows)];  // end of the next row (loaded ahead)
   bool first_done = false;
+  // interior rows leave through the reduce-scatter: this lane's columns, and their
+  // output scales, are fixed for the whole walk
+  using TS = TeamScatter<CPT, LPR>;
+  const int scol = q * CPT + TS::offset(lane);
+  const bool sstore = TS::stores(lane);
+  float sscale[TS::W];
+#pragma unroll
+  for (int c = 0; c < TS::W; c++) sscale[c] = a.colscale && scol + c < a.R ? a.colscale[scol + c] : 1.f;
   Summ<CPT> X;
   X.h = kEmpty;
   X.t = kNone;
@@ -290,19 +353,34 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_strip_kernel(const __grid_co
   // or straight to the output, then the walk moves to the row holding `at`
   auto row_end = [&](int64_t at) {
     float r[CPT];
-    strip_team_sum<CPT, LPR>(acc, r);
     if (!first_done) {
+      strip_team_sum<CPT, LPR>(acc, r);
       X.h = ip;
 #pragma unroll
       for (int c = 0; c < CPT; c++) X.ha[c] = r[c];
       first_done = true;
-    } else if (team == 0) {
-      wk.store_row(ip, r);
+    } else {
+      // a row that starts and ends inside the unit: complete, stored once
+      TS::run(acc, r, lane);
+      if (sstore) {
+        float* o = a.out + (int64_t)wk.row_id(ip) * a.ldo + scol;
+#pragma unroll
+        for (int c = 0; c < TS::W; c++)
+          if (scol + c < a.R) o[c] = r[c] * sscale[c];
+      }
     }
 #pragma unroll
     for (int c = 0; c < CPT; c++) acc[c] = 0.f;
-    ip = (int)search_le(rnz, ip + 1, rhi, at);
-    rend = rnz[ip + 1];
+    // the next row holds `at` unless it is empty (then search past the empty rows)
+    int nip = ip + 1;
+    int64_t nend = rnext;
+    if (nend <= at) {
+      nip = (int)search_le(rnz, ip + 1, rhi, at);
+      nend = rnz[nip + 1];
+    }
+    ip = nip;
+    rend = nend;
+    rnext = rnz[min(ip + 2, a.nrows)];
   };
   auto consume = [&](const typename ST::Batch& b, int s) {
     const int64_t sb = ustart + (int64_t)s * STEP;
