@@ -6,17 +6,20 @@ clipped to [1, 2M] with 3 fibers forced above 1M nonzeros, values U(0,1), factor
 N(0,1) with per-column scales, rank 32.  Seeded synthetic data (seed 3); the
 reference's FROSTT tensors are not available.
 
-One step = one MTTKRP call on device-resident inputs: partition + output clear
-+ walk kernel.  L2 is flushed (512 MB write) between timed steps, outside the
-per-step CUDA events.  ``value`` is GFLOP/s with the reference's flop count
-(3 * nnz * R); ``e2e`` is the same metric through the one-shot host API
-(tt_mttkrp_host: host buffers in, host result out, every copy inside the timed
-region).  ``roofline`` relates the walk kernel's compulsory HBM bytes to its
-CUDA-event duration and the measured copy bandwidth.
+One step = one MTTKRP call on device-resident inputs: the walk kernel, the row
+merge and (slab plans) the sum of the slabs' rows; the plan's partition was
+computed once at plan creation and is reported as ``partition_ms``.  L2 is flushed
+(512 MB write) between timed steps, outside the per-step CUDA events.  ``value`` is
+GFLOP/s with the reference's flop count (3 * nnz * R); ``e2e`` is the same metric
+through the one-shot host API (tt_mttkrp_host: host buffers in, host result out,
+every copy inside the timed region).  ``roofline`` relates the walk kernel's
+compulsory HBM bytes to its CUDA-event duration and the measured copy bandwidth.
+Every result carries its error against the FP64 oracle over all output rows.
 
 ``--impl reference`` times the reference's CPU TACO MTTKRP3 algorithm
-(tensor_kernels/mttkrp3_csf_cpu_taco.h, as restated in oracle/tt_oracle.c)
-on the host cores, on a bounded row sample of the same tensor.
+(tensor_kernels/mttkrp3_csf_cpu_taco.h, as restated in oracle/tt_oracle.c) on the
+host cores, on a bounded row sample of the same tensor, built by the oracle's own
+restatement of the generators (no product code runs in that arm).
 """
 from __future__ import annotations
 
@@ -38,8 +41,9 @@ NNZ = 100_000_000
 RANK = 32
 SEED = 3
 WORKLOAD = "mttkrp3_skewed_100M_r32"
-# the same metric for both arms; the arithmetic of each arm is in its "dtype" and config
+# the same metric for both arms; the arithmetic of each arm is in its "dtype" and "plan"
 METRIC = f"MTTKRP3 GFLOP/s (3*nnz*R), {WORKLOAD}"
+L2_NOTE = "flushed between steps (GPU arm: 512 MB device write; CPU arm: 80 MB host stream)"
 
 
 def parse():
@@ -48,20 +52,21 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--prec", default="fp16", choices=["fp32", "bf16", "bf16f", "fp16"],
-                    help="storage precision of the headline run (fp16: the 16-bit mode within 1e-3 of FP64)")
-    ap.add_argument("--compare", default="fp32,bf16",
+    ap.add_argument("--prec", default="fp16", choices=["fp32", "bf16", "bf16f", "fp16", "fx16"],
+                    help="storage precision of the headline run")
+    ap.add_argument("--compare", default="fp32,fx16",
                     help="other storage precisions timed on the same tensor (comma list, '' for none)")
     ap.add_argument("--select", default="model", choices=["default", "model", "sweep"])
     ap.add_argument("--variant", type=int, default=-1, help="run this variant id (overrides --select)")
     ap.add_argument("--nnz", type=int, default=NNZ, help="smaller nonzero count for quick checks")
     ap.add_argument("--slabs", type=int, default=0, help="leaf-mode slabs (0: the plan's automatic choice)")
+    ap.add_argument("--clocks-csv", default=None, help="write the sampled SM clocks to this CSV")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-errors", action="store_true")
     ap.add_argument("--no-secondary", action="store_true",
-                    help="skip the TTV (50M nonzeros) and 4-mode MTTKRP (80M nonzeros) measurements")
-    ap.add_argument("--only", default=None, choices=["ttv", "mttkrp4", "modes"],
+                    help="skip TTV, MTTKRP4, other modes and other ranks")
+    ap.add_argument("--only", default=None, choices=["ttv", "mttkrp4", "modes", "ranks"],
                     help="run only this secondary measurement and print its JSON (for profiling)")
     return ap.parse_args()
 
@@ -92,41 +97,57 @@ def allmax(d, v: float) -> float:
     return float(t.item())
 
 
-def make_workload(nnz):
+def make_workload(nnz, rank=RANK):
     import tentaco_gb300 as tt
 
     B = tt.gen_lognormal_fibers(DIMS, nnz, 1.5, 1.8, 3, 1_000_000, SEED)
-    C = tt.gen_dense(DIMS[1], RANK, 1, SEED * 10 + 1)
-    D = tt.gen_dense(DIMS[2], RANK, 1, SEED * 10 + 2)
+    C = tt.gen_dense(DIMS[1], rank, 1, SEED * 10 + 1)
+    D = tt.gen_dense(DIMS[2], rank, 1, SEED * 10 + 2)
     return B, C, D
 
 
-def compulsory_bytes(B, s_v, s_f):
-    """Compulsory HBM bytes of one MTTKRP3 call (index int32, values s_v, factors s_f bytes)."""
+def workload_config(nnz, fibers, world):
+    """Identical in both arms: the workload, not how an arm runs it."""
+    return {"workload": WORKLOAD, "dims": list(DIMS), "nnz": int(nnz), "fibers": int(fibers), "rank": RANK,
+            "seed": SEED, "l2": L2_NOTE, "parallelism": f"replicas{world}"}
+
+
+def prec_bytes(prec):
+    """(value bytes, upper-factor bytes, leaf-factor bytes) of a storage precision."""
+    return {"fp32": (4, 4, 4), "bf16": (2, 2, 2), "bf16f": (4, 2, 2), "fp16": (2, 2, 2), "fx16": (4, 4, 2)}[prec]
+
+
+def compulsory_bytes(B, prec, rank=RANK):
+    """Compulsory HBM bytes of one MTTKRP3 call in the stored format: int32 indices,
+    values, each distinct factor row once (16-bit fixed point adds one exponent byte
+    per leaf row), the output written once."""
+    s_v, s_u, s_l = prec_bytes(prec)
     nnz = B.nnz
     F = B.count(1)
     I = B.dims[0]
     U1 = int(np.count_nonzero(np.bincount(B.crd(1), minlength=B.dims[1])))
     U2 = int(np.count_nonzero(np.bincount(B.crd(2), minlength=B.dims[2])))
-    return nnz * (4 + s_v) + F * 8 + (I + 1) * 4 + (U1 + U2) * RANK * s_f + I * RANK * 4, U1, U2
+    leaf_row = rank * s_l + (1 if prec == "fx16" else 0)
+    return nnz * (4 + s_v) + F * 8 + (I + 1) * 4 + U1 * rank * s_u + U2 * leaf_row + I * rank * 4, U1, U2
 
 
 class Clocks:
     """SM clocks and throttle reasons sampled during the timed region only
     (start() / stop() around it): in-process NVML queries every 2 ms through the
     driver's libnvidia-ml (read-only), else nvidia-smi every 200 ms.  The samples
-    go to a CSV beside the run's output."""
+    are kept in memory (and written to a CSV only when a path is given)."""
 
     # nvmlClocksEventReason* bits (nvml.h)
     REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
 
-    def __init__(self, path, period_s=0.002):
+    def __init__(self, path=None, period_s=0.002):
         self.path = path
         self.period = period_s
         self.rows = []  # (sm_mhz, max_mhz, reason bits)
         self.proc = None
         self.thread = None
         self.nvml = None
+        self.smi_lines = []
 
     def _nvml_open(self):
         import ctypes
@@ -170,9 +191,8 @@ class Clocks:
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
-            self.fh = open(self.path + ".smi", "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                          "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
 
@@ -183,27 +203,27 @@ class Clocks:
             self.thread = None
         if self.proc:
             self.proc.terminate()
-            self.proc.wait()
-            self.fh.close()
+            out, _ = self.proc.communicate()
             self.proc = None
             names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
             bitof = {v: k for k, v in self.REASONS.items()}
-            try:
-                for line in open(self.path + ".smi"):
-                    r = [x.strip() for x in line.split(",")]
-                    if len(r) < 9:
-                        continue
+            for line in (out or "").splitlines():
+                r = [x.strip() for x in line.split(",")]
+                if len(r) < 9:
+                    continue
+                try:
                     bits = sum(bitof[nm] for nm, v in zip(names, r[5:9]) if v.lower().startswith("active"))
                     self.rows.append((float(r[1]), float(r[2]), bits))
-            except (OSError, ValueError):
+                except ValueError:
+                    pass
+        if self.path:
+            try:
+                with open(self.path, "w") as fh:
+                    fh.write("sm_mhz,max_sm_mhz,reason_bits\n")
+                    for sm, mx, bits in self.rows:
+                        fh.write(f"{sm:.0f},{mx:.0f},{bits:#x}\n")
+            except OSError:
                 pass
-        try:
-            with open(self.path, "w") as fh:
-                fh.write("sm_mhz,max_sm_mhz,reason_bits\n")
-                for sm, mx, bits in self.rows:
-                    fh.write(f"{sm:.0f},{mx:.0f},{bits:#x}\n")
-        except OSError:
-            pass
 
     def summary(self):
         out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": len(self.rows),
@@ -228,50 +248,98 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(prec, variant):
-    """Per-launch DRAM bytes of the walk kernel from the committed ncu capture of the
-    same workload, precision and variant (None when there is none)."""
+def ncu_profile(prec, variant, slabs):
+    """The committed ncu summary of the walk kernel for this workload, precision,
+    variant and slab count (None when there is none): DRAM bytes per launch and the
+    L2 hit rate."""
     path = os.path.join(ROOT, "profiles", f"walk_kernel_{WORKLOAD}_{prec}.json")
     try:
         with open(path) as fh:
             p = json.load(fh)
-        return p.get("dram_bytes_per_launch") if p.get("variant") == variant else None
+        if p.get("variant") == variant and p.get("slabs", 1) == slabs:
+            return p
     except Exception:
-        return None
+        pass
+    return None
 
 
-def sample_errors(B, C, D, A, rows):
+def errors(got, ref):
+    """Error of got against the FP64 oracle over every output row, in every norm:
+    normwise max|x-y|/max|y|; row-normwise ||x_i-y_i||/||y_i|| (max and mean over
+    rows with ||y_i|| > tau); Frobenius; elementwise |x-y|/max(|y|, tau) (max and
+    mean), tau = 1e-6 max|y|; and the reference's comparators (ds.h:551-580)."""
     from oracle import oracle as O
 
-    Oc = O.Csf(3, B.dims, [None, B.pos(1).astype(np.int64), B.pos(2).astype(np.int64)],
-               [None, B.crd(1).astype(np.int64), B.crd(2).astype(np.int64)], B.vals.astype(np.float64))
-    ref = O.mttkrp(Oc, [C, D], rows=rows)
-    got = A[rows].astype(np.float64)
-    amax = float(np.abs(ref).max())
-    rn = np.linalg.norm(ref, axis=1)
-    m = rn > 0
-    tau = 1e-6 * amax
-    e = np.abs(got - ref) / np.maximum(np.abs(ref), tau)
-    return {"rows_checked": int(len(rows)), "normwise_max": float(np.abs(got - ref).max() / amax),
-            "row_max": float((np.linalg.norm(got - ref, axis=1)[m] / rn[m]).max()),
-            "fro": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
-            "elem_max": float(e.max()), "elem_mean": float(e.mean())}
+    got64 = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    d = got64 - ref
+    amax = float(np.abs(ref).max()) if ref.size else 0.0
+    tau = max(1e-6 * amax, 1e-300)
+    e = np.abs(d) / np.maximum(np.abs(ref), tau)
+    out = {"rows_checked": int(ref.shape[0]) if ref.ndim else int(ref.size),
+           "normwise_max": float(np.abs(d).max() / amax) if amax > 0 else 0.0,
+           "fro": float(np.linalg.norm(d) / max(np.linalg.norm(ref), 1e-300)),
+           "elem_max": float(e.max()) if e.size else 0.0, "elem_mean": float(e.mean()) if e.size else 0.0}
+    if ref.ndim == 2:
+        rn = np.linalg.norm(ref, axis=1)
+        m = rn > tau
+        rw = np.linalg.norm(d, axis=1)[m] / rn[m]
+        out["row_max"] = float(rw.max()) if rw.size else 0.0
+        out["row_mean"] = float(rw.mean()) if rw.size else 0.0
+    out["ref_compare_array"] = float(O.compare_array(np.asarray(got, np.float32), ref.astype(np.float32)))
+    out["ref_compare_array_my"] = float(O.compare_array_my(np.asarray(got, np.float32), ref.astype(np.float32)))
+    return out
 
 
-def check_rows(B, n=4096):
-    rng = np.random.default_rng(0)
-    pos1 = B.pos(1)
-    nz_rows = np.flatnonzero(np.diff(pos1))
-    sel = rng.choice(nz_rows, size=min(n, nz_rows.size), replace=False)
-    # include the rows holding the longest fibers (cross-block merges)
-    lens = np.diff(B.pos(2))
-    top = np.argsort(lens)[-8:]
-    rows_of_top = np.searchsorted(pos1, top, side="right") - 1
-    return np.unique(np.concatenate([sel, rows_of_top]))
+def oracle_csf(B):
+    from oracle import oracle as O
+
+    return O.Csf(B.order, B.dims, [None] + [B.pos(l).astype(np.int64) for l in range(1, B.order)],
+                 [None] + [B.crd(l).astype(np.int64) for l in range(1, B.order)], B.vals.astype(np.float64))
+
+
+def timed_plan(tt, B, facs, prec, select, args, clk=None, variant=0, rank=RANK, steps=None, mode=0):
+    """A plan on device-resident inputs: setup timed on the host; W warm-up calls,
+    then K timed calls with the L2 flushed before each (CUDA events)."""
+    steps = args.steps if steps is None else steps
+    t0 = time.perf_counter()
+    plan = tt.Plan(B, rank=rank, prec=prec, select=select, variant=variant, slabs=args.slabs, mode=mode)
+    setup_s = time.perf_counter() - t0
+    bufs = [tt.DeviceBuffer.from_array(f) for f in facs]
+    plan.set_factors(bufs)
+    rows = B.dims[mode]
+    A = tt.DeviceBuffer(rows * rank * 4)
+    plan.set_timing(True)
+    for _ in range(args.warmup):
+        tt.l2_flush()
+        plan.mttkrp(A)
+    tt.synchronize()
+    step_ms, kern_ms = [], []
+    if clk:
+        clk.start()
+    for _ in range(steps):
+        tt.l2_flush()
+        plan.mttkrp(A)
+        step_ms.append(plan.last_ms())
+        kern_ms.append(plan.last_kernel_ms())
+    tt.synchronize()
+    if clk:
+        clk.stop()
+    assert plan.device_error() == 0
+    info = {"ms_per_step": float(np.mean(step_ms)), "kernel_ms": float(np.mean(kern_ms)),
+            "variant": plan.variant, "variant_name": tt.variant_info(plan.variant)["name"], "slabs": plan.slabs,
+            "selected_by": "fixed" if select == tt.SELECT_FIXED else
+            ["heuristic", "model", "sweep", "model top-k timed"][plan.selected_by],
+            "plan_setup_s": round(setup_s, 2), "partition_ms": round(plan.partition_ms(), 4)}
+    if plan.selected_by == 3:
+        info["candidates_ms"] = {tt.variant_info(v)["name"]: round(float(t), 4)
+                                 for v, t in enumerate(plan.sweep_times()) if t > 0}
+    return plan, A.to_array((rows, rank)), info
 
 
 def run_gpu_arm(args, rank, world, d):
     import tentaco_gb300 as tt
+    from oracle import oracle as O
 
     t0 = time.time()
     B, C, D = make_workload(args.nnz)
@@ -281,122 +349,107 @@ def run_gpu_arm(args, rank, world, d):
         sel = tt.SELECT_FIXED
     flops = 3.0 * B.nnz * RANK
 
-    def timed_plan(prec, select, clk=None):
-        plan = tt.Plan(B, rank=RANK, prec=prec, select=select, variant=max(args.variant, 0), slabs=args.slabs)
-        if select == tt.SELECT_MODEL and plan.selected_by not in (1, 3):
-            plan = tt.Plan(B, rank=RANK, prec=prec, select=tt.SELECT_SWEEP, slabs=args.slabs)
-        bufs = [tt.DeviceBuffer.from_array(C), tt.DeviceBuffer.from_array(D)]
-        plan.set_factors(bufs)
-        A = tt.DeviceBuffer(B.dims[0] * RANK * 4)
-        plan.set_timing(True)
-        for _ in range(args.warmup):
-            tt.l2_flush()
-            plan.mttkrp(A)
-        tt.synchronize()
-        step_ms, kern_ms = [], []
-        barrier(d)
-        tt.synchronize()
-        if clk:
-            clk.start()
-        wall0 = time.perf_counter()
-        for _ in range(args.steps):
-            tt.l2_flush()
-            plan.mttkrp(A)
-            step_ms.append(plan.last_ms())
-            kern_ms.append(plan.last_kernel_ms())
-        tt.synchronize()
-        barrier(d)
-        wall = time.perf_counter() - wall0
-        if clk:
-            clk.stop()
-        return plan, A, bufs, step_ms, kern_ms, wall
-
-    clk = Clocks(os.path.join(ROOT, "gpurun_out", "bench_clocks.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
-                 else "/tmp/tt_bench_clocks.csv")
-    plan, A, bufs, step_ms, kern_ms, wall = timed_plan(args.prec, sel, clk)
+    clk = Clocks(args.clocks_csv)
+    barrier(d)
+    plan, Ah, info = timed_plan(tt, B, [C, D], args.prec, sel, args, clk=clk, variant=max(args.variant, 0))
+    barrier(d)
     clocks = clk.summary()
-    ms = float(np.mean(step_ms))
+    ms = info["ms_per_step"]
     ms_max = allmax(d, ms)
-    kern = float(np.mean(kern_ms))
+    kern = info["kernel_ms"]
     value = world * flops / (ms_max * 1e-3) / 1e9
+    variant, slabs = plan.variant, plan.slabs
+    del plan
 
-    # other storage precisions on the same tensor (plain FP32 gives the 16-bit speed-up)
+    # other storage precisions on the same tensor (plain FP32 gives the 16-bit speed-ups)
     others = {}
     for prec in [x for x in args.compare.split(",") if x and x != args.prec]:
-        po, Ao, bo, so, ko, _ = timed_plan(prec, tt.SELECT_SWEEP if args.select != "default" else tt.SELECT_DEFAULT)
-        others[prec] = {"ms_per_step": float(np.mean(so)), "kernel_ms": float(np.mean(ko)),
-                        "gflops": flops / (np.mean(so) * 1e-3) / 1e9, "variant": po.variant,
-                        "_A": Ao.to_array((B.dims[0], RANK))}
-        del po, Ao, bo
+        po, Ao, oi = timed_plan(tt, B, [C, D], prec, tt.SELECT_SWEEP if args.select != "default" else
+                                tt.SELECT_DEFAULT, args)
+        oi["gflops"] = flops / (oi["ms_per_step"] * 1e-3) / 1e9
+        cb, _, _ = compulsory_bytes(B, prec)
+        oi["gbs_compulsory"] = round(cb / (oi["ms_per_step"] * 1e-3) / 1e9, 1)
+        oi["_A"] = Ao
+        others[prec] = oi
+        del po
 
-    s_v = 2 if args.prec in ("bf16", "fp16") else 4
-    s_f = 2 if args.prec in ("bf16", "bf16f", "fp16") else 4
-    cbytes, U1, U2 = compulsory_bytes(B, s_v, s_f)
+    cbytes, U1, U2 = compulsory_bytes(B, args.prec)
     peak, peak_kind = peaks()
     achieved = cbytes / (kern * 1e-3) / 1e9
-    traffic = ncu_traffic(args.prec, plan.variant) if args.nnz == NNZ else None
+    prof = ncu_profile(args.prec, variant, slabs) if args.nnz == NNZ else None
 
     out = {
         "metric": METRIC,
         "value": round(value, 2), "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_max, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": args.prec if args.prec != "bf16f" else "bf16+fp32",
+        "scaling": "weak", "vs_baseline": None, "dtype": args.prec,
         "data": "synthetic (seeded lognormal-fiber tensor; FROSTT data absent)",
-        "config": {"workload": WORKLOAD, "dims": list(DIMS), "nnz": B.nnz, "fibers": B.count(1), "rank": RANK,
-                   "precision": args.prec, "select": args.select, "variant": plan.variant, "slabs": plan.slabs,
-                   "selected_by": "fixed" if args.variant >= 0 else
-                   ["heuristic", "model", "sweep", "model top-k timed"][plan.selected_by],
-                   "candidates_ms": {str(v): round(float(t), 4) for v, t in enumerate(plan.sweep_times()) if t > 0}
-                   if plan.selected_by == 3 else None,
-                   "l2": "flushed between steps (512 MB write)", "parallelism": f"replicas{world}",
-                   "gen_s": round(gen_s, 1)},
+        "config": workload_config(B.nnz, B.count(1), world),
+        "plan": dict(info, precision=args.prec, select=args.select, gen_s=round(gen_s, 1)),
         "gbs_compulsory": round(cbytes / (ms * 1e-3) / 1e9, 1),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "frac": round(achieved / peak, 4), "traffic": prof.get("dram_bytes_per_launch") if prof else None,
+                     "l2_hit_rate_pct": prof.get("l2_hit_rate_pct") if prof else None,
                      "peak_source": f"{peak_kind} hbm_gbs", "kernel_ms": round(kern, 4),
                      "compulsory_bytes": int(cbytes), "U1": U1, "U2": U2},
         "clocks": clocks,
-        # our kernels per step and slab: walk, segment fold, segment chain, plus the
-        # partition where a slab plan runs it per pass (a single-slab plan computes it
-        # once at creation); the output clear is a cudaMemsetAsync
-        "gpu_launches": args.steps * plan.slabs * (3 if plan.slabs == 1 else 4),
+        # our kernels per step: walk, segment fold, segment chain, and for a slab plan
+        # of the strip walk the slabs' row sum (one pass); slab passes of the other
+        # families run walk, fold, chain and the partition per slab
+        "gpu_launches": args.steps * (4 if (slabs > 1 and tt.variant_info(variant)["staged"] == 4)
+                                      else slabs * (3 if slabs == 1 else 4)),
     }
+    for prec, o in others.items():
+        o["speedup_vs_fp32"] = None
     if "fp32" in others:
         out["speedup_vs_fp32"] = round(others["fp32"]["ms_per_step"] / ms, 3)
+        for prec, o in others.items():
+            if prec != "fp32":
+                o["speedup_vs_fp32"] = round(others["fp32"]["ms_per_step"] / o["ms_per_step"], 3)
     if not args.no_errors:
-        Ah = A.to_array((B.dims[0], RANK))
-        rows = check_rows(B)
-        out["error_vs_fp64"] = sample_errors(B, C, D, Ah, rows)
-        for k, o in others.items():
-            o["error_vs_fp64"] = sample_errors(B, C, D, o["_A"], rows)
+        ref = O.mttkrp(oracle_csf(B), [C.astype(np.float64), D.astype(np.float64)])
+        out["error_vs_fp64"] = errors(Ah, ref)
+        for o in others.values():
+            o["error_vs_fp64"] = errors(o["_A"], ref)
+        del ref
     for o in others.values():
         o.pop("_A", None)
     out["compare"] = others
+    if not args.no_errors and others:
+        # the fastest mode whose row-normwise error over all rows meets 1e-3
+        cands = [(out["ms_per_step"], args.prec, out["error_vs_fp64"]["row_max"])] + \
+                [(o["ms_per_step"], p, o["error_vs_fp64"]["row_max"]) for p, o in others.items()]
+        ok = sorted(c for c in cands if c[2] <= 1e-3)
+        out["tradeoff"] = {"fastest": min(cands)[1],
+                           "fastest_row_normwise_le_1e-3": ok[0][1] if ok else None,
+                           "row_max_by_precision": {c[1]: c[2] for c in cands},
+                           "ms_by_precision": {c[1]: round(c[0], 4) for c in cands}}
 
     if not args.no_e2e:
-        prec_map = {"fp32": 0, "bf16": 1, "bf16f": 2, "fp16": 3}
+        prec_map = {"fp32": 0, "bf16": 1, "bf16f": 2, "fp16": 3, "fx16": 4}
         e2e_ms = []
         # warm-up calls like the device leg's (the first one also grows the
         # library's device memory pool), then min(steps, 5) timed calls
         n_e2e = max(1, min(args.steps, 5))
         for i in range(args.warmup + n_e2e):
             t = time.perf_counter()
-            Ahost = tt.mttkrp_host(B, [C, D], prec=prec_map[args.prec], select=tt.SELECT_FIXED,
-                                   variant=plan.variant)
+            Ahost = tt.mttkrp_host(B, [C, D], prec=prec_map[args.prec], select=tt.SELECT_FIXED, variant=variant)
             if i >= args.warmup:
                 e2e_ms.append((time.perf_counter() - t) * 1e3)
         h2d = B.nnz * 8 + (B.dims[0] + 1 + 2 * B.count(1) + 1) * 4 + (C.size + D.size) * 4
         out["e2e"] = {"value": round(flops / (np.mean(e2e_ms) * 1e-3) / 1e9, 2), "unit": "GFLOP/s",
                       "ms_per_step": round(float(np.mean(e2e_ms)), 2), "h2d_bytes_per_step": int(h2d),
                       "d2h_bytes_per_step": int(Ahost.nbytes),
-                      "api": "tt_mttkrp_host (plan create + upload + factor conversion + run + download)"}
+                      "api": "tt_mttkrp_host (plan create + upload + factor conversion + run + download; "
+                             "no slabs: one call cannot repay the slab layout's host build)"}
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(B, C, D, budget_s=15.0)
+        out["cpu_baseline"] = cpu_baseline(oracle_csf(B), C, D, budget_s=12.0)
     if not args.no_secondary:
-        del B, C, D, A, bufs, plan
+        del B, C, D, Ah
         out["secondary"] = {"ttv_50M": secondary_ttv(args), "mttkrp4_80M": secondary_mttkrp4(args),
-                            "mttkrp3_other_modes": secondary_other_modes(args)}
+                            "mttkrp3_other_modes": secondary_other_modes(args),
+                            "mttkrp3_ranks": secondary_ranks(args)}
     return out
 
 
@@ -418,7 +471,7 @@ def _timed(call, plan, steps, warmup):
 
 def secondary_ttv(args):
     """TTV on the 50M-nonzero tensor: 50,000 x 40,000 x 30,000, 50M nonzeros, Zipf(1.1) on modes 0 and 1,
-    uniform mode 2, values and vector U(-1,1); checked against the FP64 oracle."""
+    uniform mode 2, values and vector U(-1,1); every output checked against the FP64 oracle."""
     import tentaco_gb300 as tt
     from oracle import oracle as O
 
@@ -429,169 +482,207 @@ def secondary_ttv(args):
     dx = tt.DeviceBuffer.from_array(x)
     dy = tt.DeviceBuffer(nfib * 4)
     ms = _timed(lambda: plan.ttv(dx, dy), plan, max(3, args.steps), args.warmup)
+    kern = plan.last_kernel_ms()
     y = dy.to_array((nfib,))
-    Oc = O.Csf(3, B.dims, [None, B.pos(1).astype(np.int64), B.pos(2).astype(np.int64)],
-               [None, B.crd(1).astype(np.int64), B.crd(2).astype(np.int64)], B.vals.astype(np.float64))
-    ref = O.ttv(Oc, x.astype(np.float64))
+    ref = O.ttv(oracle_csf(B), x.astype(np.float64))
     U = int(np.count_nonzero(np.bincount(B.crd(2), minlength=B.dims[2])))
     cbytes = B.nnz * 8 + nfib * 12 + (B.dims[0] + 1) * 4 + U * 4
-    return {"nnz": B.nnz, "fibers": nfib, "ms_per_step": round(ms, 4),
+    peak, _ = peaks()
+    return {"nnz": B.nnz, "fibers": nfib, "ms_per_step": round(ms, 4), "kernel_ms": round(kern, 4),
+            "partition_ms": round(plan.partition_ms(), 4),
             "gflops": round(2.0 * B.nnz / (ms * 1e-3) / 1e9, 2),
             "gbs_compulsory": round(cbytes / (ms * 1e-3) / 1e9, 1),
-            "error_vs_fp64": {"normwise_max": float(np.abs(y - ref).max() / max(np.abs(ref).max(), 1e-300)),
-                              "fro": float(np.linalg.norm(y - ref) / max(np.linalg.norm(ref), 1e-300))}}
+            "roofline_frac": round(cbytes / (ms * 1e-3) / 1e9 / peak, 4),
+            "error_vs_fp64": errors(y, ref)}
 
 
 def secondary_mttkrp4(args):
     """MTTKRP on the 80M-nonzero 4-mode tensor: 5,000 x 3,000 x 2,000 x 100,000, 80M nonzeros, Zipf(1.2) on
-    modes 0 and 3, rank 32 N(0,1) factors; FP16 storage (sweep-selected: the learned model
-    covers 3-mode tensors) against plain FP32, sampled rows checked against the FP64 oracle."""
+    modes 0 and 3, rank 32 N(0,1) factors; 16-bit storage against plain FP32 (selected by the learned
+    selector's timed candidates and the fixed heuristic); every output row checked against the FP64 oracle."""
     import tentaco_gb300 as tt
     from oracle import oracle as O
 
     dims = (5_000, 3_000, 2_000, 100_000)
     B = tt.gen_zipf(dims, (1.2, 0.0, 0.0, 1.2), 80_000_000, seed=5)
     facs = [tt.gen_dense(d, RANK, 1, 50 + m) for m, d in enumerate(dims[1:])]
-    bufs = [tt.DeviceBuffer.from_array(f) for f in facs]
-    A = tt.DeviceBuffer(dims[0] * RANK * 4)
-    Oc = O.Csf(4, B.dims, [None] + [B.pos(l).astype(np.int64) for l in (1, 2, 3)],
-               [None] + [B.crd(l).astype(np.int64) for l in (1, 2, 3)], B.vals.astype(np.float64))
-    rows = np.random.default_rng(0).choice(np.flatnonzero(np.diff(B.pos(1))), 512, replace=False)
-    ref = O.mttkrp(Oc, facs, rows=rows)
+    ref = O.mttkrp(oracle_csf(B), [f.astype(np.float64) for f in facs])
+    peak, _ = peaks()
     res = {"nnz": B.nnz}
-    for prec in ("fp16", "fp32"):
-        plan = tt.Plan(B, rank=RANK, prec=prec, select=tt.SELECT_SWEEP)
-        plan.set_factors(bufs)
-        ms = _timed(lambda: plan.mttkrp(A), plan, max(3, args.steps // 2), args.warmup)
-        got = A.to_array((dims[0], RANK))[rows].astype(np.float64)
-        res[prec] = {"ms_per_step": round(ms, 4), "gflops": round(4.0 * B.nnz * RANK / (ms * 1e-3) / 1e9, 2),
-                     "variant": tt.variant_info(plan.variant)["name"],
-                     "error_vs_fp64": {"normwise_max": float(np.abs(got - ref).max() / np.abs(ref).max()),
-                                       "fro": float(np.linalg.norm(got - ref) / np.linalg.norm(ref))}}
+    sub = argparse.Namespace(**vars(args))
+    sub.steps = max(3, args.steps // 2)
+    for prec in ("fp16", "fx16", "fp32"):
+        plan, A, info = timed_plan(tt, B, facs, prec, tt.SELECT_MODEL, sub)
+        info["gflops"] = round(4.0 * B.nnz * RANK / (info["ms_per_step"] * 1e-3) / 1e9, 2)
+        s_v, s_u, s_l = prec_bytes(prec)
+        U = [int(np.count_nonzero(np.bincount(B.crd(l), minlength=dims[l]))) for l in (1, 2, 3)]
+        cb = B.nnz * (4 + s_v) + (B.count(2) + B.count(1)) * 8 + (dims[0] + 1) * 4 + \
+            (U[0] + U[1]) * RANK * s_u + U[2] * RANK * s_l + dims[0] * RANK * 4
+        info["roofline_frac"] = round(cb / (info["kernel_ms"] * 1e-3) / 1e9 / peak, 4)
+        info["error_vs_fp64"] = errors(A, ref)
+        res[prec] = info
         del plan
-    res["speedup_fp16_vs_fp32"] = round(res["fp32"]["ms_per_step"] / res["fp16"]["ms_per_step"], 3)
+    for prec in ("fp16", "fx16"):
+        res[f"speedup_{prec}_vs_fp32"] = round(res["fp32"]["ms_per_step"] / res[prec]["ms_per_step"], 3)
     return res
 
 
 def secondary_other_modes(args):
     """MTTKRP of modes 1 and 2 of the headline tensor (FP16 storage, rank 32, the
-    learned selector): the plan re-roots the tensor at the mode once (timed as
-    plan setup), calls are timed like the headline's, sampled output rows are
-    checked against the FP64 oracle on the re-rooted tensor."""
+    learned selector): the plan re-roots the tensor at the mode once (timed as plan
+    setup), calls are timed like the headline's, every output row is checked
+    against the FP64 oracle on the re-rooted tensor."""
     import tentaco_gb300 as tt
+    from oracle import oracle as O
 
     B, C, D = make_workload(args.nnz)
     facs = {0: tt.gen_dense(DIMS[0], RANK, 1, SEED * 10), 1: C, 2: D}
     res = {"nnz": B.nnz}
+    sub = argparse.Namespace(**vars(args))
+    sub.steps = max(3, args.steps // 2)
     for m in (1, 2):
         others = [facs[n] for n in range(3) if n != m]
-        t0 = time.perf_counter()
-        plan = tt.Plan(B, rank=RANK, prec="fp16", select=tt.SELECT_MODEL, mode=m)
-        setup_s = time.perf_counter() - t0
-        bufs = [tt.DeviceBuffer.from_array(f) for f in others]
-        plan.set_factors(bufs)
-        A = tt.DeviceBuffer(DIMS[m] * RANK * 4)
-        ms = _timed(lambda: plan.mttkrp(A), plan, max(3, args.steps // 2), args.warmup)
-        Ah = A.to_array((DIMS[m], RANK))
+        plan, A, info = timed_plan(tt, B, others, "fp16", tt.SELECT_MODEL, sub, mode=m)
+        info["gflops"] = round(3.0 * B.nnz * RANK / (info["ms_per_step"] * 1e-3) / 1e9, 2)
         Bm = tt.csf_reroot(B, m)
-        err = sample_errors(Bm, others[0], others[1], Ah, check_rows(Bm, n=1024))
-        res[f"mode{m}"] = {"rows": DIMS[m], "ms_per_step": round(ms, 4),
-                           "gflops": round(3.0 * B.nnz * RANK / (ms * 1e-3) / 1e9, 2),
-                           "variant": tt.variant_info(plan.variant)["name"], "plan_setup_s": round(setup_s, 2),
-                           "error_vs_fp64": {"normwise_max": err["normwise_max"], "fro": err["fro"]}}
-        del plan, bufs, A, Bm
+        ref = O.mttkrp(oracle_csf(Bm), [f.astype(np.float64) for f in others])
+        info["rows"] = DIMS[m]
+        info["error_vs_fp64"] = errors(A, ref)
+        res[f"mode{m}"] = info
+        del plan, Bm, ref
     return res
 
 
-def cpu_rows_sample(B, budget_nnz):
+def secondary_ranks(args):
+    """The headline tensor at ranks 16 and 64 (the other ranks of the configuration):
+    FP16 and FX16 storage against plain FP32, each selected like the headline, every
+    output row checked against the FP64 oracle."""
+    import tentaco_gb300 as tt
+    from oracle import oracle as O
+
+    res = {}
+    peak, _ = peaks()
+    sub = argparse.Namespace(**vars(args))
+    sub.steps = max(3, args.steps // 2)
+    for R in (16, 64):
+        B, C, D = make_workload(args.nnz, rank=R)
+        ref = O.mttkrp(oracle_csf(B), [C.astype(np.float64), D.astype(np.float64)])
+        r = {}
+        for prec in ("fp16", "fx16", "fp32"):
+            plan, A, info = timed_plan(tt, B, [C, D], prec, tt.SELECT_MODEL, sub, rank=R)
+            info["gflops"] = round(3.0 * B.nnz * R / (info["ms_per_step"] * 1e-3) / 1e9, 2)
+            cb, _, _ = compulsory_bytes(B, prec, rank=R)
+            info["roofline_frac"] = round(cb / (info["kernel_ms"] * 1e-3) / 1e9 / peak, 4)
+            info["error_vs_fp64"] = errors(A, ref)
+            r[prec] = info
+            del plan
+        for prec in ("fp16", "fx16"):
+            r[f"speedup_{prec}_vs_fp32"] = round(r["fp32"]["ms_per_step"] / r[prec]["ms_per_step"], 3)
+        res[f"r{R}"] = r
+        del B, C, D, ref
+    return res
+
+
+def cpu_rows_sample(pos1, pos2, nnz, budget_nnz):
     """A contiguous row range holding about budget_nnz nonzeros (all rows if that covers the tensor)."""
-    pos1 = B.pos(1)
-    pos2 = B.pos(2)
     row_nnz_end = pos2[pos1]
-    if budget_nnz >= B.nnz:
-        return 0, B.dims[0], B.nnz
-    start = int(np.searchsorted(row_nnz_end, B.nnz // 3))
+    nrows = len(pos1) - 1
+    if budget_nnz >= nnz:
+        return 0, nrows, int(nnz)
+    start = int(np.searchsorted(row_nnz_end, nnz // 3))
     end = int(np.searchsorted(row_nnz_end, row_nnz_end[start] + budget_nnz))
-    end = max(min(end, B.dims[0]), start + 1)
+    end = max(min(end, nrows), start + 1)
     return start, end, int(row_nnz_end[end] - row_nnz_end[start])
 
 
-def cpu_baseline(B, C, D, budget_s=15.0, steps=1):
-    """The reference CPU algorithm (oracle port of mttkrp3_csf_cpu_taco) on a bounded row range."""
+def _subtensor(Oc, s, e):
     from oracle import oracle as O
 
-    threads = O.max_threads()
-    pos1 = B.pos(1).astype(np.int64)
-    Cd, Dd = C.astype(np.float64), D.astype(np.float64)
-    # calibrate on a small range, then size the sample to the budget
-    s, e, nz = cpu_rows_sample(B, 2_000_000)
-    sub = _subtensor(B, pos1, s, e)
-    t = O.now_ms()
-    O.mttkrp(sub, [Cd, Dd])
-    per_nnz = (O.now_ms() - t) * 1e-3 / max(nz, 1)
-    target = int(min(B.nnz, max(nz, budget_s / max(per_nnz, 1e-12) / max(steps, 1))))
-    if target >= 0.8 * B.nnz:
-        target = B.nnz
-    s, e, nz = cpu_rows_sample(B, target)
-    sub = _subtensor(B, pos1, s, e)
-    times = []
-    for _ in range(steps):
-        t = O.now_ms()
-        O.mttkrp(sub, [Cd, Dd])
-        times.append((O.now_ms() - t) * 1e-3)
-    sec = float(np.mean(times))
-    return {"value": round(3.0 * nz * RANK / sec / 1e9, 3), "unit": "GFLOP/s", "cores": threads,
-            "kind": "port", "seconds": round(sec, 2),
-            "sample": f"rows {s}..{e} ({nz} nonzeros, {100.0 * nz / B.nnz:.1f}% of the tensor), FP64, "
-                      f"reference loop order and OpenMP schedule"}
-
-
-def _subtensor(B, pos1, s, e):
-    from oracle import oracle as O
-
-    pos2 = B.pos(2).astype(np.int64)
+    pos1, pos2 = Oc.pos[1], Oc.pos[2]
     f0, f1 = int(pos1[s]), int(pos1[e])
     n0, n1 = int(pos2[f0]), int(pos2[f1])
-    p1 = pos1[s:e + 1] - f0
-    p2 = pos2[f0:f1 + 1] - n0
-    return O.Csf(3, (e - s, B.dims[1], B.dims[2]), [None, p1, p2],
-                 [None, B.crd(1)[f0:f1].astype(np.int64), B.crd(2)[n0:n1].astype(np.int64)],
-                 B.vals[n0:n1].astype(np.float64))
+    return O.Csf(3, (e - s, Oc.dims[1], Oc.dims[2]), [None, pos1[s:e + 1] - f0, pos2[f0:f1 + 1] - n0],
+                 [None, Oc.crd[1][f0:f1], Oc.crd[2][n0:n1]], Oc.vals[n0:n1])
+
+
+def _flush_host_cache(buf):
+    """Stream 80 MB through the host caches (the reference's TIME_COLD, timers.h:62-75)."""
+    buf += 1.0
+    return float(buf[::4096].sum())
+
+
+def cpu_baseline(Oc, C, D, budget_s=12.0, steps=1, threads=None):
+    """The reference CPU algorithm (oracle port of mttkrp3_csf_cpu_taco) on a bounded
+    row range, with all host cores and with 4 threads (the reference's
+    run_gpu.sh:9)."""
+    from oracle import oracle as O
+
+    Cd, Dd = C.astype(np.float64), D.astype(np.float64)
+    all_cores = O.max_threads()
+    flush = np.zeros(80 * 1024 * 1024 // 8)
+    legs = {}
+    for nthreads in (all_cores, 4):
+        O.set_threads(nthreads)
+        s, e, nz = cpu_rows_sample(Oc.pos[1], Oc.pos[2], Oc.nnz, 2_000_000)
+        sub = _subtensor(Oc, s, e)
+        t = O.now_ms()
+        O.mttkrp(sub, [Cd, Dd])
+        per_nnz = (O.now_ms() - t) * 1e-3 / max(nz, 1)
+        target = int(min(Oc.nnz, max(nz, budget_s / 2 / max(per_nnz, 1e-12) / max(steps, 1))))
+        if target >= 0.8 * Oc.nnz:
+            target = Oc.nnz
+        s, e, nz = cpu_rows_sample(Oc.pos[1], Oc.pos[2], Oc.nnz, target)
+        sub = _subtensor(Oc, s, e)
+        times = []
+        for _ in range(steps):
+            _flush_host_cache(flush)
+            t = O.now_ms()
+            O.mttkrp(sub, [Cd, Dd])
+            times.append((O.now_ms() - t) * 1e-3)
+        sec = float(np.mean(times))
+        legs[nthreads] = {"value": round(3.0 * nz * RANK / sec / 1e9, 3), "unit": "GFLOP/s", "cores": nthreads,
+                          "seconds": round(sec, 3), "rows": [s, e], "nnz": nz,
+                          "sample": f"rows {s}..{e} ({nz} nonzeros, {100.0 * nz / Oc.nnz:.1f}% of the tensor), "
+                                    f"FP64, reference loop order and OpenMP schedule, {nthreads} threads"}
+    O.set_threads(all_cores)
+    main = legs[all_cores]
+    return dict(main, kind="port", threads_4=legs[4])
 
 
 def run_reference_arm(args, rank, world):
     if rank != 0:
         return None
-    import tentaco_gb300 as tt  # generator only; the timed work is the CPU oracle port
-
+    # the tensor from the oracle's restatement of the generators: no product code here
     from oracle import oracle as O
 
-    B, C, D = make_workload(args.nnz)
-    base = cpu_baseline(B, C, D, budget_s=8.0, steps=1)
-    # steps: repeat the same bounded sample
-    pos1 = B.pos(1).astype(np.int64)
-    s, e = [int(x) for x in base["sample"].split()[1].split("..")]
-    sub = _subtensor(B, pos1, s, e)
+    Oc = O.gen_lognormal(DIMS, args.nnz, 1.5, 1.8, 3, 1_000_000, SEED)
+    C = O.gen_dense(DIMS[1], RANK, 1, SEED * 10 + 1)
+    D = O.gen_dense(DIMS[2], RANK, 1, SEED * 10 + 2)
+    base = cpu_baseline(Oc, C, D, budget_s=8.0, steps=1)
+    s, e = base["rows"]
+    sub = _subtensor(Oc, s, e)
     Cd, Dd = C.astype(np.float64), D.astype(np.float64)
-    nz = sub.nnz
+    flush = np.zeros(80 * 1024 * 1024 // 8)
     for _ in range(args.warmup):
-        pass  # the reference CPU kernel has no warm-up state beyond the page cache
+        O.mttkrp(sub, [Cd, Dd])
     times = []
     for _ in range(args.steps):
+        _flush_host_cache(flush)
         t = O.now_ms()
         O.mttkrp(sub, [Cd, Dd])
         times.append((O.now_ms() - t) * 1e-3)
     sec = float(np.mean(times))
-    val = 3.0 * nz * RANK / sec / 1e9
+    val = 3.0 * sub.nnz * RANK / sec / 1e9
     return {"metric": METRIC,
             "impl": "reference", "value": round(val, 3), "unit": "GFLOP/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 2),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded lognormal-fiber tensor; FROSTT data absent)",
-            "config": {"workload": WORKLOAD, "dims": list(DIMS), "nnz": B.nnz, "rank": RANK,
-                       "precision": "fp64 (the reference's CPU kernel on FP32-exact inputs)"},
+            "config": workload_config(Oc.nnz, len(Oc.crd[1]), world),
+            "plan": {"precision": "fp64 (the reference's CPU kernel on FP32-exact inputs)",
+                     "rows": [s, e], "sample_nnz": int(sub.nnz)},
             "cpu_baseline": {"value": round(val, 3), "unit": "GFLOP/s", "cores": base["cores"], "kind": "port",
-                             "sample": base["sample"]},
+                             "sample": base["sample"], "threads_4": base["threads_4"]},
             "e2e": {"value": round(val, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -599,7 +690,7 @@ def main():
     args = parse()
     if args.only:
         print(json.dumps({"ttv": secondary_ttv, "mttkrp4": secondary_mttkrp4,
-                          "modes": secondary_other_modes}[args.only](args)))
+                          "modes": secondary_other_modes, "ranks": secondary_ranks}[args.only](args)))
         return
     rank, world, d = dist_setup(args.gpus)
     if args.impl == "reference":

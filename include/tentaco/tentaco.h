@@ -177,6 +177,11 @@ tt_status tt_plan_set_timing(tt_plan* plan, int32_t enabled);
  * once, when the plan (or its variant) is set up; slab plans run it per pass. */
 float tt_plan_last_ms(tt_plan* plan);
 
+/* Milliseconds of the work-unit partition, computed once when the plan's variant
+ * was set and reused by every call (0 when calls run it themselves: slab passes).
+ * The reference runs its partition inside every timed call
+ * (tensor_kernels/mttkrp3_csf_ebpr.h:74-79); this is that time. */
+float tt_plan_partition_ms(const tt_plan* plan);
 int32_t tt_plan_variant(const tt_plan* plan);
 int64_t tt_plan_nnz(const tt_plan* plan);
 int64_t tt_plan_num_fibers(const tt_plan* plan, int32_t level);
@@ -235,14 +240,14 @@ tt_status tt_ttv_host(taco_tensor_t* y, const taco_tensor_t* B, const taco_tenso
  * padding needed), FP32 factors C (dims[1] x rank) and D (dims[2] x rank), and
  * the FP32 output A (nrows x rank, overwritten).  crd2, vals, C, D and A must
  * be 16-byte aligned; the CSF must be valid (tt_csf_validate on the host copy).
- * rank must be 8, 16, 32 or 64.  Limits: nrows <= 524,288 and
- * nnz <= 16,777,216; larger inputs return TT_ERR_INVALID_ARGUMENT (use the
- * plan API).  The call allocates nothing: its scratch is a fixed 4.7 MB device
- * array that every GPU loading this library holds until the process exits.
- * The first call on each device looks that array's address up (make it before
- * any stream capture).  All calls share the array, so calls whose work
- * overlaps on the GPU (different streams, or several host threads) race and
- * must be serialised by the caller.
+ * rank must be 8, 16, 32 or 64.  Limit: nnz <= 16,777,216 (the scratch holds
+ * per-block state for 8192 blocks of 2048 nonzeros); a larger tensor returns
+ * TT_ERR_INVALID_ARGUMENT (use the plan API).  The call allocates nothing: its
+ * scratch is a fixed 4.7 MB device array that every GPU loading this library
+ * holds until the process exits.  Each call looks that array's address up on the
+ * current device (make calls outside stream capture).  All calls share the array,
+ * so calls whose work overlaps on the GPU (different streams, or several host
+ * threads) race and must be serialised by the caller.
  */
 tt_status tt_mttkrp3_noalloc(int32_t nrows, int64_t nnz, int32_t rank,
                              const int32_t* pos1, const int32_t* crd1,

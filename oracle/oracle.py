@@ -265,8 +265,40 @@ def compare_array_my(x: np.ndarray, y: np.ndarray) -> float:
     return lib().oracle_compare_array_my(_ptr(x), _ptr(y), _I(x.size))
 
 
+def gen_dense(rows: int, cols: int, dist: int, seed: int) -> np.ndarray:
+    """The library's seeded dense generator (tt_gen_dense), restated in tt_gen.c."""
+    out = np.empty((rows, cols), dtype=np.float32)
+    lib().oracle_gen_dense(_I(rows), _I(cols), ctypes.c_int(dist), ctypes.c_uint64(seed), _ptr(out))
+    return out
+
+
+def gen_lognormal(dims, nnz: int, mu: float, sigma: float, n_long: int, long_min: int, seed: int) -> Csf:
+    """The library's lognormal-fiber 3-mode tensor (tt_gen_lognormal_fibers), restated
+    in tt_gen.c, as an oracle CSF with int64 indices and FP64 values."""
+    L = lib()
+    d = np.ascontiguousarray(dims, dtype=np.int32)
+    args = (_I(nnz), ctypes.c_double(mu), ctypes.c_double(sigma), _I(n_long), _I(long_min), ctypes.c_uint64(seed))
+    L.oracle_lognormal_nfibers.restype = ctypes.c_int64
+    nf = int(L.oracle_lognormal_nfibers(_ptr(d), *args))
+    pos1 = np.empty(int(d[0]) + 1, np.int32)
+    crd1 = np.empty(nf, np.int32)
+    pos2 = np.empty(nf + 1, np.int32)
+    crd2 = np.empty(nnz, np.int32)
+    vals = np.empty(nnz, np.float32)
+    rc = L.oracle_gen_lognormal(_ptr(d), *args, _ptr(pos1), _ptr(crd1), _ptr(pos2), _ptr(crd2), _ptr(vals))
+    if rc != 0:
+        raise ValueError("could not draw distinct fibers")
+    return Csf(3, tuple(int(x) for x in d), [None, pos1.astype(np.int64), pos2.astype(np.int64)],
+               [None, crd1.astype(np.int64), crd2.astype(np.int64)], vals.astype(np.float64))
+
+
 def now_ms() -> float:
     return lib().oracle_now_ms()
+
+
+def set_threads(n: int) -> None:
+    """Threads the oracle's OpenMP loops use from now on."""
+    lib().oracle_set_threads(ctypes.c_int(int(n)))
 
 
 def max_threads() -> int:

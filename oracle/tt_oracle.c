@@ -378,6 +378,15 @@ ORACLE_API double oracle_now_ms(void) {
   return ts.tv_sec * 1e3 + ts.tv_nsec * 1e-6;
 }
 
+/* Threads of the oracle's parallel loops from now on (the CPU baseline's legs). */
+ORACLE_API void oracle_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
 ORACLE_API int oracle_max_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -89,6 +89,7 @@ def lib():
         "tt_plan_set_timing": (S, [_P, C.c_int32]),
         "tt_plan_last_ms": (C.c_float, [_P]),
         "tt_plan_last_kernel_ms": (C.c_float, [_P]),
+        "tt_plan_partition_ms": (C.c_float, [_P]),
         "tt_plan_variant": (C.c_int32, [_P]),
         "tt_plan_selected_by": (C.c_int32, [_P]),
         "tt_plan_nnz": (C.c_int64, [_P]),
@@ -437,6 +438,9 @@ class Plan:
 
     def last_kernel_ms(self) -> float:
         return float(lib().tt_plan_last_kernel_ms(self.ptr))
+
+    def partition_ms(self) -> float:
+        return float(lib().tt_plan_partition_ms(self.ptr))
 
     @property
     def variant(self) -> int:

@@ -18,8 +18,9 @@
 //     warp by a shuffle tree keyed by row (the EBPR idea, segmented by output
 //     row, so it crosses fiber boundaries), then across warps in shared memory.
 //   * the block's first and last rows, if they extend into other blocks, go to
-//     a carry buffer; the last block to arrive at a row (a per-row ticket,
-//     reset by that block) sums all of the row's block partials in FP64, in
+//     the block's two carry slots; after the walk, seg_fold_kernel sums each
+//     row's carries inside a segment of 32 blocks (FP32, Kahan-compensated) and
+//     seg_chain_kernel sums the FP64 partials of rows crossing segments, both in
 //     block order.  No float atomics on A: every output is written once and the
 //     result is bitwise reproducible run to run.
 //

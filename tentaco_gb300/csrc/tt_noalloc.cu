@@ -14,7 +14,6 @@
 // the per-block partition, the per-block row metadata, the cross-block carry
 // rows and the FP64 partials of the two-level cross-block merge.
 #include <cuda_runtime.h>
-#include <mutex>
 #include "tt_internal.h"
 #include "tt_kernels.h"
 #include "tt_mttkrp.cuh"
@@ -28,8 +27,9 @@ constexpr int kLPR = 8;
 constexpr int kG = 64;
 constexpr int kP = (kTB / kLPR) * kG;
 
-// Limits of the scratch array (about 4.7 MB).
-constexpr int64_t kMaxRows = 1 << 19;    // root positions
+// Limit of the scratch array (about 4.7 MB): its parts are sized per block of the
+// walk, so the nonzero count is what it bounds; the output rows live in the
+// caller's A and need no scratch.
 constexpr int64_t kMaxBlocks = 8192;     // so nnz <= 8192 * 2048 = 16,777,216
 constexpr int kMaxRankPad = 64;
 constexpr size_t kMetaBytes = (size_t)kMaxBlocks * 16;
@@ -43,25 +43,16 @@ constexpr size_t kScratchBytes = kMetaBytes + kPartBytes + kCarryBytes + kSegMet
 // Every call writes the parts of it that it reads (partition, metadata, carries).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-std::mutex g_mu;
-void* g_scratch_addr[64] = {nullptr};
-
-// Device address of the scratch array on the current device (looked up once per
-// device: in host code the array's name is only a host-side stand-in).
+// Device address of the scratch array on the current device.  In host code the
+// array's name is only a host-side stand-in, so the address is looked up with the
+// device current; it is looked up on every call (no allocation, and no address
+// kept that a device reset would leave stale).
 tt_status scratch_address(void** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return tt::set_error(TT_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
-  if (dev < 0 || dev >= 64) return tt::set_error(TT_ERR_UNSUPPORTED, "device ordinal %d", dev);
-  std::lock_guard<std::mutex> g(g_mu);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return tt::set_error(TT_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
-    g_scratch_addr[dev] = p;
-  }
-  *out = g_scratch_addr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return tt::set_error(TT_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+  *out = p;
   return TT_OK;
 }
 
@@ -86,10 +77,6 @@ TT_EXPORT tt_status tt_mttkrp3_noalloc(int32_t nrows, int64_t nnz, int32_t rank,
     return tt::set_error(TT_ERR_UNSUPPORTED, "tt_mttkrp3_noalloc: rank must be 8, 16, 32 or 64 (got %d)", rank);
   if (nrows < 1 || nnz < 0 || !pos1 || !pos2 || !A || (nnz > 0 && (!crd1 || !crd2 || !vals || !C || !D)))
     return tt::set_error(TT_ERR_INVALID_ARGUMENT, "tt_mttkrp3_noalloc: null pointer or negative size");
-  if (nrows > kMaxRows)
-    return tt::set_error(TT_ERR_INVALID_ARGUMENT,
-                         "tt_mttkrp3_noalloc: %d rows exceed the scratch limit of %lld rows; use tt_plan_create",
-                         nrows, (long long)kMaxRows);
   const int64_t nblocks = (nnz + kP - 1) / kP;
   if (nblocks > kMaxBlocks)
     return tt::set_error(TT_ERR_INVALID_ARGUMENT,

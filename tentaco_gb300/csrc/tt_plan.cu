@@ -1367,6 +1367,10 @@ tt_status time_variants(tt_plan* p, cudaStream_t st, const std::vector<int>& can
 }
 }  // namespace
 
+// Milliseconds of the work-unit partition computed once when the plan's variant was
+// set (0 when the plan runs it in every call: slab passes).
+TT_EXPORT float tt_plan_partition_ms(const tt_plan* p) { return p && p->part_ready ? p->part_ms : 0.f; }
+
 // Returns the memory the library's pool keeps for reuse (plans alive keep theirs).
 TT_EXPORT tt_status tt_release_cached_memory(void) {
   std::lock_guard<std::mutex> lk(g_pool_mu);

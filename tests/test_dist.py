@@ -55,3 +55,19 @@ def test_reference_arm_two_ranks_rank0_reports():
     assert out["unit"] == "GFLOP/s" and out["higher_is_better"] is True
     for k in ("steps", "warmup", "ms_per_step", "scaling", "vs_baseline", "dtype", "data"):
         assert k in out, k
+
+
+def test_reference_arm_loads_no_product_code():
+    """The reference arm builds its tensor with the oracle's generators: after a run,
+    no module of the product package is loaded in the process, and its config has
+    exactly the GPU arm's keys (the workload, not how an arm runs it)."""
+    code = ("import sys, json, argparse; sys.path.insert(0, %r); import bench;"
+            "a = argparse.Namespace(nnz=200000, steps=1, warmup=0);"
+            "out = bench.run_reference_arm(a, 0, 1);"
+            "print(json.dumps({'mods': sorted(m for m in sys.modules if m.startswith('tentaco_gb300')),"
+            " 'keys': sorted(out['config']), 'want': sorted(bench.workload_config(1, 1, 1))}))" % ROOT)
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    assert res["mods"] == []
+    assert res["keys"] == res["want"]

@@ -90,7 +90,7 @@ def test_c1_every_variant(c1):
     assert nvalid >= 50
 
 
-def test_c1_deterministic_and_tickets_reset(c1):
+def test_c1_deterministic_repeated_calls(c1):
     B, facs, ref = c1
     outs, _ = run_plan(B, facs, reps=4)
     for o in outs[1:]:

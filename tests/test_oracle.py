@@ -191,3 +191,21 @@ def test_golden_fixtures_regenerate_identically(tmp_path):
         assert sorted(a.files) == sorted(b.files), name
         for k in a.files:
             assert np.array_equal(a[k], b[k]), (name, k)
+
+
+@pytest.mark.parametrize("seed", [3, 11])
+def test_generator_restatement_matches_library(seed):
+    """The oracle's C restatement of the seeded generators (used by the bench's
+    reference arm, which must not load the product library) yields the library's
+    tensors and factors bit for bit."""
+    import tentaco_gb300 as tt
+
+    dims = (300, 200, 5000)
+    B = tt.gen_lognormal_fibers(dims, 200_000, 1.5, 1.8, 2, 2000, seed)
+    G = O.gen_lognormal(dims, 200_000, 1.5, 1.8, 2, 2000, seed)
+    for lvl in (1, 2):
+        assert np.array_equal(B.pos(lvl).astype(np.int64), G.pos[lvl])
+        assert np.array_equal(B.crd(lvl).astype(np.int64), G.crd[lvl])
+    assert np.array_equal(B.vals.astype(np.float64), G.vals)
+    for dist in (0, 1, 2):
+        assert np.array_equal(tt.gen_dense(5000, 32, dist, seed), O.gen_dense(5000, 32, dist, seed))
