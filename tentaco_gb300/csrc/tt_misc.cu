@@ -68,28 +68,32 @@ cudaError_t launch_partition_rows(int order, const WalkArgs& a, cudaStream_t s) 
 // A(i, j) = sum over slabs k, in slab order and in FP64, of V(k * vstride + i, j):
 // the virtual rows of a slab-major plan summed into the output, rounded once.  A
 // virtual row without nonzeros (rnz[r] == rnz[r + 1]) was never written and
-// counts as zero.  ld: row stride of V and A.
+// counts as zero.  One warp per output row, lanes over columns (coalesced rows);
+// ld: row stride of V and A.
 __global__ void virtual_rows_kernel(const float* __restrict__ V, const int32_t* __restrict__ rnz, int S,
                                     int64_t nrows, int64_t vstride, int ld, int R, float* __restrict__ A) {
-  const int64_t n = nrows * (int64_t)R;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = e / R;
-    const int j = (int)(e - i * R);
-    double acc = 0.0;
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < nrows; i += warps) {
+    double acc0 = 0.0, acc1 = 0.0;  // columns lane and lane + 32
     for (int k = 0; k < S; k++) {
       const int64_t r = (int64_t)k * vstride + i;
-      if (rnz[r + 1] > rnz[r]) acc += (double)V[r * ld + j];
+      if (rnz[r + 1] > rnz[r]) {
+        const float* v = V + r * ld;
+        if (lane < R) acc0 += (double)v[lane];
+        if (lane + 32 < R) acc1 += (double)v[lane + 32];
+      }
     }
-    A[i * ld + j] = (float)acc;
+    if (lane < R) A[i * ld + lane] = (float)acc0;
+    if (lane + 32 < R) A[i * ld + lane + 32] = (float)acc1;
   }
 }
 
 cudaError_t launch_virtual_rows(const float* V, const int32_t* rnz, int S, int64_t nrows, int64_t vstride, int ld,
                                 int R, float* A, cudaStream_t s) {
-  const int64_t n = nrows * (int64_t)R;
-  if (n == 0) return cudaSuccess;
-  int64_t grid = (n + 255) / 256;
-  if (grid > 152 * 16) grid = 152 * 16;
+  if (nrows == 0 || R == 0) return cudaSuccess;
+  if (R > 64) return cudaErrorInvalidValue;
+  const int64_t grid = std::min<int64_t>((nrows + 7) / 8, 152 * 32);
   virtual_rows_kernel<<<(int)grid, 256, 0, s>>>(V, rnz, S, nrows, vstride, ld, R, A);
   return cudaGetLastError();
 }
