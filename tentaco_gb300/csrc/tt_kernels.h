@@ -39,8 +39,9 @@ WalkLauncher walk_launcher_o4_fx16_strip(int cpt, int lpr, int fam);
 cudaError_t launch_partition_rows(int order, const WalkArgs& a, cudaStream_t s);
 // A(i, j) = FP64 sum over slabs k in order of V(k * vstride + i, j) for i < nrows, rounded
 // once; virtual rows r with rnz[r + 1] == rnz[r] are skipped (slab-major strip plans).
-cudaError_t launch_virtual_rows(const float* V, const int32_t* rnz, int S, int64_t nrows, int64_t vstride, int ld,
-                                int R, float* A, cudaStream_t s);
+// ldv: V's row stride (a multiple of 4, at least R rounded up to 4); lda: A's; S <= 16.
+cudaError_t launch_virtual_rows(const float* V, const int32_t* rnz, int S, int64_t nrows, int64_t vstride, int ldv,
+                                int lda, int R, float* A, cudaStream_t s);
 // scale[j] = 32767 / colmax[j], inv[j] = colmax[j] / 32767 (1 for an empty or non-finite column).
 cudaError_t launch_fullrange_scales(const float* colmax, int cols, float* scale, float* inv, cudaStream_t s);
 // 16-bit fixed point of a leaf factor (rows x cols FP32 -> rows x rp offset-binary

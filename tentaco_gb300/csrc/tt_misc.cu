@@ -68,33 +68,52 @@ cudaError_t launch_partition_rows(int order, const WalkArgs& a, cudaStream_t s) 
 // A(i, j) = sum over slabs k, in slab order and in FP64, of V(k * vstride + i, j):
 // the virtual rows of a slab-major plan summed into the output, rounded once.  A
 // virtual row without nonzeros (rnz[r] == rnz[r + 1]) was never written and
-// counts as zero.  One warp per output row, lanes over columns (coalesced rows);
-// ld: row stride of V and A.
+// counts as zero.  One thread per 4 columns of a row: every load of a row is
+// issued before any is used (the emptiness test selects, it does not branch, and
+// V is allocated for every virtual row).  ldv: row stride of V, a multiple of 4;
+// lda: row stride of A.
+constexpr int kVirtMaxSlabs = 16;
 __global__ void virtual_rows_kernel(const float* __restrict__ V, const int32_t* __restrict__ rnz, int S,
-                                    int64_t nrows, int64_t vstride, int ld, int R, float* __restrict__ A) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < nrows; i += warps) {
-    double acc0 = 0.0, acc1 = 0.0;  // columns lane and lane + 32
-    for (int k = 0; k < S; k++) {
-      const int64_t r = (int64_t)k * vstride + i;
-      if (rnz[r + 1] > rnz[r]) {
-        const float* v = V + r * ld;
-        if (lane < R) acc0 += (double)v[lane];
-        if (lane + 32 < R) acc1 += (double)v[lane + 32];
+                                    int64_t nrows, int64_t vstride, int ldv, int lda, int R, float* __restrict__ A) {
+  const int q4 = (R + 3) >> 2;  // 4-column groups per row
+  const int64_t n = nrows * q4;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / q4;
+    const int j = (int)(e - i * q4) * 4;
+    float4 v[kVirtMaxSlabs];
+    bool live[kVirtMaxSlabs];
+#pragma unroll
+    for (int k = 0; k < kVirtMaxSlabs; k++) {
+      if (k < S) {
+        const int64_t r = (int64_t)k * vstride + i;
+        live[k] = rnz[r + 1] > rnz[r];
+        v[k] = *reinterpret_cast<const float4*>(V + r * ldv + j);
       }
     }
-    if (lane < R) A[i * ld + lane] = (float)acc0;
-    if (lane + 32 < R) A[i * ld + lane + 32] = (float)acc1;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+#pragma unroll
+    for (int k = 0; k < kVirtMaxSlabs; k++) {
+      if (k < S && live[k]) {
+        a0 += (double)v[k].x; a1 += (double)v[k].y; a2 += (double)v[k].z; a3 += (double)v[k].w;
+      }
+    }
+    float* o = A + i * lda + j;
+    if (j + 3 < R && (lda & 3) == 0) {
+      *reinterpret_cast<float4*>(o) = make_float4((float)a0, (float)a1, (float)a2, (float)a3);
+    } else {
+      const double t[4] = {a0, a1, a2, a3};
+      for (int c = 0; c < 4 && j + c < R; c++) o[c] = (float)t[c];
+    }
   }
 }
 
-cudaError_t launch_virtual_rows(const float* V, const int32_t* rnz, int S, int64_t nrows, int64_t vstride, int ld,
-                                int R, float* A, cudaStream_t s) {
+cudaError_t launch_virtual_rows(const float* V, const int32_t* rnz, int S, int64_t nrows, int64_t vstride, int ldv,
+                                int lda, int R, float* A, cudaStream_t s) {
   if (nrows == 0 || R == 0) return cudaSuccess;
-  if (R > 64) return cudaErrorInvalidValue;
-  const int64_t grid = std::min<int64_t>((nrows + 7) / 8, 152 * 32);
-  virtual_rows_kernel<<<(int)grid, 256, 0, s>>>(V, rnz, S, nrows, vstride, ld, R, A);
+  if (S < 1 || S > kVirtMaxSlabs || (ldv & 3) != 0 || ldv < ((R + 3) & ~3) || lda < R) return cudaErrorInvalidValue;
+  const int64_t n = nrows * ((R + 3) / 4);
+  const int64_t grid = std::min<int64_t>((n + 255) / 256, 152 * 16);
+  virtual_rows_kernel<<<(int)grid, 256, 0, s>>>(V, rnz, S, nrows, vstride, ldv, lda, R, A);
   return cudaGetLastError();
 }
 

@@ -127,9 +127,16 @@ bool variant_valid(int id, int order, int rank, int prec) {
 }
 
 int lean_default_variant(int order, int rank, int prec);
+int strip_default_variant(int order, int rank, int prec);
 
 int default_variant(int order, int rank, int prec, int64_t nnz) {
   (void)nnz;
+  // four modes and 16-bit fixed point: the strip rule (the fastest family on the
+  // 80M-nonzero 4-mode tensor in every storage precision)
+  if (order == 4 || prec == kFX16) {
+    const int id = strip_default_variant(order, rank, prec);
+    if (id >= 0) return id;
+  }
   if (order == 3) {
     // flat family, 256 threads: the best single flat variant per (storage, rank)
     // over the training split of the selector corpus (12-28% mean regret against
@@ -158,6 +165,19 @@ int lean_default_variant(int order, int rank, int prec) {
   const int id = variant_id(256, G, cpt, 0);
   if (variant_valid(id, order, rank, prec)) return id;
   for (int i = 0; i < kNumVariants; i++)
+    if (variant_valid(i, order, rank, prec)) return i;
+  return -1;
+}
+
+// The strip rule: G 128 with four nonzeros per team and step, 8 columns per lane
+// for 16-bit factors (16 bytes of a factor row), else 4.
+int strip_default_variant(int order, int rank, int prec) {
+  const int rp = rank_pad(rank);
+  int cpt = fac_kind(prec) == kF32 || prec == kFX16 ? 4 : 8;
+  while (cpt > 2 && rp / cpt < 1) cpt >>= 1;
+  const int id = variant_id(256, 128, cpt, 4);
+  if (variant_valid(id, order, rank, prec)) return id;
+  for (int i = 4 * kPerFamily; i < kNumVariants; i++)
     if (variant_valid(i, order, rank, prec)) return i;
   return -1;
 }
@@ -377,19 +397,6 @@ std::vector<int> variant_neighbours(int id) {
   return out;
 }
 
-// The strip rule: G 128 with four nonzeros per team and step, 8 columns per lane
-// for 16-bit factors (16 bytes of a factor row), else 4.
-int strip_default_variant(int order, int rank, int prec) {
-  const int rp = rank_pad(rank);
-  int cpt = fac_kind(prec) == kF32 || prec == kFX16 ? 4 : 8;
-  while (cpt > 2 && rp / cpt < 1) cpt >>= 1;
-  const int id = variant_id(256, 128, cpt, 4);
-  if (variant_valid(id, order, rank, prec)) return id;
-  for (int i = 4 * kPerFamily; i < kNumVariants; i++)
-    if (variant_valid(i, order, rank, prec)) return i;
-  return -1;
-}
-
 // The fixed heuristic for this plan: slab plans and 16-bit fixed point take the
 // strip rule (one launch over the slab-major layout; the flat family has no slab
 // passes), other plans the shape rule.
@@ -530,7 +537,7 @@ tt_status set_variant(tt_plan* p, int id) {
   p->part_ready = false;
   if ((v.staged == 3 || v.staged == 4) && !p->d_kexp && p->nnz > 0 && (s = build_flat_arrays(p)) != TT_OK) return s;
   if (v.staged == 4 && p->slabs > 1 && !p->d_vrows && p->nnz > 0 &&
-      (s = dev_alloc(p, &p->d_vrows, (size_t)p->slabs * (size_t)(p->nroot + 1) * (size_t)p->rank)) != TT_OK)
+      (s = dev_alloc(p, &p->d_vrows, (size_t)p->slabs * (size_t)(p->nroot + 1) * (size_t)p->rp)) != TT_OK)
     return s;
   p->wcap = 1;
   if (p->staged == 1 && p->nnz > 0) {
@@ -628,7 +635,7 @@ WalkArgs strip_slab_args(const tt_plan* p) {
   a.nrows = (int32_t)((int64_t)p->slabs * (p->nroot + 1));
   a.rp = p->rp;
   a.R = p->rank;
-  a.ldo = p->rank;
+  a.ldo = p->rp;  // virtual rows RP floats apart (16-byte rows for the slab sum)
   a.P = p->P;
   a.G = p->G;
   a.lgG = 0;
@@ -699,7 +706,7 @@ tt_status run_mttkrp(tt_plan* p, float* A, cudaStream_t st) {
     CK(p->launcher(a, a.nblocks, p->tb, smem, st));
     if (p->timing) CK(cudaEventRecord(p->evk1, st));
     CK(launch_chain_fixup(p->order, a, st));
-    CK(launch_virtual_rows(p->d_vrows, p->d_rnz, p->slabs, p->nroot, p->nroot + 1, p->rank, p->rank, A, st));
+    CK(launch_virtual_rows(p->d_vrows, p->d_rnz, p->slabs, p->nroot, p->nroot + 1, p->rp, p->rank, p->rank, A, st));
     return TT_OK;
   }
   CK(cudaMemsetAsync(A, 0, outbytes, st));

@@ -40,29 +40,7 @@
 #pragma once
 #include "tt_mttkrp.cuh"
 
-// 1: the walk's FP32 multiplies and FMAs go two columns per instruction; 0: scalar.
-#ifndef TT_STRIP_PACKED
-#define TT_STRIP_PACKED 1
-#endif
-
 namespace tt {
-
-// (a0, a1) += (b0, b1) * (c0, c1) and (b0, b1) * (c0, c1), packed or scalar.
-__device__ __forceinline__ void strip_fma2(float& a0, float& a1, float b0, float b1, float c0, float c1) {
-#if TT_STRIP_PACKED
-  ffma2(a0, a1, b0, b1, c0, c1);
-#else
-  a0 = fmaf(b0, c0, a0);
-  a1 = fmaf(b1, c1, a1);
-#endif
-}
-__device__ __forceinline__ float2 strip_mul2(float b0, float b1, float c0, float c1) {
-#if TT_STRIP_PACKED
-  return fmul2(b0, b1, c0, c1);
-#else
-  return make_float2(b0 * c0, b1 * c1);
-#endif
-}
 
 // Element kinds of the strip walk's arrays per storage precision:
 // V values, U upper-level factors, L leaf-level factor.
@@ -215,23 +193,23 @@ struct Strip {
             t = hprod2<FK>(vv, b.m[u][j]);
           } else {
             const float2 mm = pair16<FK>(b.m[u][j]);
-            t = strip_mul2(v, v, mm.x, mm.y);
+            t = fmul2(v, v, mm.x, mm.y);
           }
-          strip_fma2(acc[2 * j], acc[2 * j + 1], p.x, p.y, t.x, t.y);
+          ffma2(acc[2 * j], acc[2 * j + 1], p.x, p.y, t.x, t.y);
         } else {
-          strip_fma2(acc[2 * j], acc[2 * j + 1], v, v, p.x, p.y);
+          ffma2(acc[2 * j], acc[2 * j + 1], v, v, p.x, p.y);
         }
       }
     } else {
       // FP32 upper rows: t = v * c [* m], then acc += t * d with d FP32 or 16-bit fixed point
 #pragma unroll
       for (int j = 0; j < CPT / 2; j++) {
-        float2 t = strip_mul2(v, v, __uint_as_float(b.c[u][2 * j]), __uint_as_float(b.c[u][2 * j + 1]));
-        if constexpr (ORDER == 4) t = strip_mul2(t.x, t.y, __uint_as_float(b.m[u][2 * j]), __uint_as_float(b.m[u][2 * j + 1]));
+        float2 t = fmul2(v, v, __uint_as_float(b.c[u][2 * j]), __uint_as_float(b.c[u][2 * j + 1]));
+        if constexpr (ORDER == 4) t = fmul2(t.x, t.y, __uint_as_float(b.m[u][2 * j]), __uint_as_float(b.m[u][2 * j + 1]));
         float2 dd;
         if constexpr (K::L == kF32) dd = make_float2(__uint_as_float(b.d[u][2 * j]), __uint_as_float(b.d[u][2 * j + 1]));
         else dd = i16pair(b.d[u][j]);
-        strip_fma2(acc[2 * j], acc[2 * j + 1], t.x, t.y, dd.x, dd.y);
+        ffma2(acc[2 * j], acc[2 * j + 1], t.x, t.y, dd.x, dd.y);
       }
     }
   }

@@ -78,7 +78,9 @@ def test_variant_table():
     assert info["threads"] == 256 and info["cols_per_lane"] == 4 and info["staged"] == 3
     assert info["name"] == "flat_b2_g64_c4"
     assert tt.variant_info(tt.default_variant(3, 32, "fp16"))["name"] == "flat_b2_g32_c8"
-    assert tt.variant_info(tt.default_variant(4, 32, "fp16"))["name"] == "lean_b2_g32_c8"
+    assert tt.variant_info(tt.default_variant(4, 32, "fp16"))["name"] == "strip_b2_g128_c8"
+    assert tt.variant_info(tt.default_variant(4, 32, "fp32"))["name"] == "strip_b2_g128_c4"
+    assert tt.variant_info(tt.default_variant(3, 32, "fx16"))["name"] == "strip_b2_g128_c4"
     assert tt.variant_info(3)["staged"] == 0 and tt.variant_info(43)["name"].startswith("stage")
     # the flat family (ids 120..159)
     assert tt.variant_info(134)["name"] == "flat_b3_g128_c2"

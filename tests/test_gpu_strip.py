@@ -203,3 +203,15 @@ def test_slab_major_selection(zipf_rows):
         A = tt.DeviceBuffer(B.dims[0] * 32 * 4)
         plan.mttkrp(A)
         close(A.to_array((B.dims[0], 32)), ref, "fp32")
+
+
+@pytest.mark.parametrize("R", [10, 20, 40, 64])
+def test_slab_major_padded_ranks(zipf_rows, R):
+    """Slab plans at ranks whose rows are padded: the virtual rows are RP floats
+    apart, the output R."""
+    B, Oc = zipf_rows
+    facs = [tt.gen_dense(2000, R, 1, 31 + R), tt.gen_dense(5000, R, 1, 32 + R)]
+    ref = O.mttkrp(Oc, facs)
+    for prec in ("fp32", "fp16", "fx16"):
+        v = strip_variants(3, R, prec)[0]
+        close(run(B, facs, prec, v, slabs=3)[0], ref, prec)
