@@ -119,7 +119,7 @@ typedef struct tt_plan_options {
   /* MTTKRP over a dense-root CSF: split the last mode's index range into this
    * many slabs, so that one slab's rows of the last factor stay resident in L2
    * while they are gathered.  The strip family walks all slabs in one launch in
-   * slab-major order (one output row per slab and row, summed into A in FP64 in
+   * slab-major order (one output row per slab and row, summed into A in FP32 with Kahan compensation in
    * slab order); the lean, staged and TMA families run one pass per slab, each
    * adding into A; the flat family runs without slabs.  0: automatic (slabs of at
    * most 32 MB of the last factor as stored, when it exceeds 48 MB); 1: no slabs;

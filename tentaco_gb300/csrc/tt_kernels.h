@@ -37,8 +37,9 @@ WalkLauncher walk_launcher_o4_fp16_strip(int cpt, int lpr, int fam);
 WalkLauncher walk_launcher_o4_fx16_strip(int cpt, int lpr, int fam);
 // Strip-walk partition: the row (through a.rnz) of every unit boundary, at stride order - 1.
 cudaError_t launch_partition_rows(int order, const WalkArgs& a, cudaStream_t s);
-// A(i, j) = FP64 sum over slabs k in order of V(k * vstride + i, j) for i < nrows, rounded
-// once; virtual rows r with rnz[r + 1] == rnz[r] are skipped (slab-major strip plans).
+// A(i, j) = sum over slabs k in order of V(k * vstride + i, j) for i < nrows, FP32 with
+// Kahan compensation; virtual rows r with rnz[r + 1] == rnz[r] are skipped (slab-major
+// strip plans).
 // ldv: V's row stride (a multiple of 4, at least R rounded up to 4); lda: A's; S <= 16.
 cudaError_t launch_virtual_rows(const float* V, const int32_t* rnz, int S, int64_t nrows, int64_t vstride, int ldv,
                                 int lda, int R, float* A, cudaStream_t s);

@@ -65,8 +65,10 @@ cudaError_t launch_partition_rows(int order, const WalkArgs& a, cudaStream_t s) 
   return cudaGetLastError();
 }
 
-// A(i, j) = sum over slabs k, in slab order and in FP64, of V(k * vstride + i, j):
-// the virtual rows of a slab-major plan summed into the output, rounded once.  A
+// A(i, j) = sum over slabs k, in slab order, of V(k * vstride + i, j): the virtual
+// rows of a slab-major plan summed into the output in FP32 with Kahan compensation
+// (at most 16 terms: within an ulp or two of the exact sum; GB300's FP64 pipe runs at
+// 1/64 of the FP32 rate and would bound this kernel).  A
 // virtual row without nonzeros (rnz[r] == rnz[r + 1]) was never written and
 // counts as zero.  One thread per 4 columns of a row: every load of a row is
 // issued before any is used (the emptiness test selects, it does not branch, and
@@ -90,19 +92,25 @@ __global__ void virtual_rows_kernel(const float* __restrict__ V, const int32_t* 
         v[k] = *reinterpret_cast<const float4*>(V + r * ldv + j);
       }
     }
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    float sum[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int k = 0; k < kVirtMaxSlabs; k++) {
       if (k < S && live[k]) {
-        a0 += (double)v[k].x; a1 += (double)v[k].y; a2 += (double)v[k].z; a3 += (double)v[k].w;
+        const float x[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
+#pragma unroll
+        for (int c = 0; c < 4; c++) {  // Kahan: cmp holds the low part lost so far
+          const float y = __fsub_rn(x[c], cmp[c]);
+          const float t = __fadd_rn(sum[c], y);
+          cmp[c] = __fsub_rn(__fsub_rn(t, sum[c]), y);
+          sum[c] = t;
+        }
       }
     }
     float* o = A + i * lda + j;
     if (j + 3 < R && (lda & 3) == 0) {
-      *reinterpret_cast<float4*>(o) = make_float4((float)a0, (float)a1, (float)a2, (float)a3);
+      *reinterpret_cast<float4*>(o) = make_float4(sum[0], sum[1], sum[2], sum[3]);
     } else {
-      const double t[4] = {a0, a1, a2, a3};
-      for (int c = 0; c < 4 && j + c < R; c++) o[c] = (float)t[c];
+      for (int c = 0; c < 4 && j + c < R; c++) o[c] = sum[c];
     }
   }
 }
