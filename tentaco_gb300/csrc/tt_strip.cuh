@@ -110,6 +110,8 @@ struct Strip {
   static constexpr int LB = CPT * (K::L == kF32 ? 4 : 2);  // bytes of a lane's leaf-row piece
   static constexpr int UW = UB / 4, LW = LB / 4;
   static constexpr int MW = ORDER == 4 ? UW : 1;
+  // bytes per factor row (the kernel is compiled for rows of RP = CPT * LPR entries)
+  static constexpr uint32_t URB = (uint32_t)LPR * UB, LRB = (uint32_t)LPR * LB;
   static_assert(CPT >= 2 && CPT % 2 == 0, "the strip walk works on column pairs");
 
   // gathered pieces of one step's U nonzeros of a team, and their values
@@ -121,7 +123,6 @@ struct Strip {
   };
 
   const unsigned char *fc, *fm, *fd;  // this lane's piece of row 0 of each factor
-  int URB, LRB;                       // bytes per factor row (upper, leaf)
   uint64_t pol_u, pol_l;
 
   __device__ __forceinline__ void load(Batch& b, const int32_t* s_l, const int32_t* s_k, const int32_t* s_k2,
@@ -160,9 +161,9 @@ struct Strip {
     }
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      strip_piece<UB, true>(fc + (size_t)(uint32_t)k[u] * URB, pol_u, b.c[u]);
-      if constexpr (ORDER == 4) strip_piece<UB, true>(fm + (size_t)(uint32_t)k2[u] * URB, pol_u, b.m[u]);
-      strip_piece<LB, false>(fd + (size_t)(uint32_t)l[u] * LRB, pol_l, b.d[u]);
+      strip_piece<UB, true>(fc + (uint64_t)(uint32_t)k[u] * URB, pol_u, b.c[u]);
+      if constexpr (ORDER == 4) strip_piece<UB, true>(fm + (uint64_t)(uint32_t)k2[u] * URB, pol_u, b.m[u]);
+      strip_piece<LB, false>(fd + (uint64_t)(uint32_t)l[u] * LRB, pol_l, b.d[u]);
     }
   }
 
@@ -297,7 +298,6 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_strip_kernel(const __grid_co
   unsigned char* s_v = reinterpret_cast<unsigned char*>(s_l + (size_t)(ORDER - 1) * P);
   const int64_t ustart = (int64_t)unit * P;
   const int cnt = (int)min((int64_t)P, a.nnz - ustart);
-  const int64_t uend = ustart + cnt;
   {
     const uint64_t polF = policy_evict_first();
     const int n4 = (cnt + 3) >> 2;
@@ -318,8 +318,6 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_strip_kernel(const __grid_co
   const int team = lane / LPR, q = lane % LPR;
   WK wk(a, q);
   ST st;
-  st.URB = a.rp * (ST::UB / CPT);
-  st.LRB = a.rp * (ST::LB / CPT);
   st.fc = static_cast<const unsigned char*>(a.fac[0]) + q * ST::UB;
   st.fm = static_cast<const unsigned char*>(a.fac[1]) + q * ST::UB;
   st.fd = static_cast<const unsigned char*>(a.fac[ORDER - 2]) + q * ST::LB;
@@ -330,8 +328,11 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_strip_kernel(const __grid_co
   const int32_t* pb = a.part + (size_t)unit * (ORDER - 1);
   const int rhi = pb[ORDER - 1];  // row of the next unit's first nonzero
   const int first_row = (int)search_le(rnz, pb[0], rhi, ustart);
+  // positions below are relative to the unit's start (32-bit); a row end past the
+  // unit is clamped to it (only "inside the unit or not" matters)
+  auto rel = [&](int64_t abs_pos) { return (int)min(abs_pos - ustart, (int64_t)cnt + STEP); };
   int ip = first_row;
-  int64_t rend = rnz[ip + 1];
+  int rend = rel(rnz[ip + 1]);
   int64_t rnext = rnz[min(ip + 2, a.nrows)];  // end of the next row (loaded ahead)
   bool first_done = false;
   // interior rows leave through the reduce-scatter: this lane's columns, and their
@@ -351,7 +352,8 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_strip_kernel(const __grid_co
 
   // row ip ends inside the step: its total goes to the unit's summary (first row)
   // or straight to the output, then the walk moves to the row holding `at`
-  auto row_end = [&](int64_t at) {
+  auto row_end = [&](int at_rel) {
+    const int64_t at = ustart + at_rel;
     float r[CPT];
     if (!first_done) {
       strip_team_sum<CPT, LPR>(acc, r);
@@ -379,21 +381,21 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_strip_kernel(const __grid_co
       nend = rnz[nip + 1];
     }
     ip = nip;
-    rend = nend;
+    rend = rel(nend);
     rnext = rnz[min(ip + 2, a.nrows)];
   };
   auto consume = [&](const typename ST::Batch& b, int s) {
-    const int64_t sb = ustart + (int64_t)s * STEP;
-    const int64_t se = min(sb + STEP, uend);
+    const int sb = s * STEP;
+    const int se = min(sb + STEP, cnt);
     if (se <= rend && se == sb + STEP) {
 #pragma unroll
       for (int u = 0; u < U; u++) ST::add(acc, b, u);
       return;
     }
-    const int64_t mine = sb + team * U;  // this team's first nonzero of the step
-    int64_t lo = sb;
+    const int mine = sb + team * U;  // this team's first nonzero of the step
+    int lo = sb;
     while (true) {
-      const int64_t hi = min(rend, se);
+      const int hi = min(rend, se);
 #pragma unroll
       for (int u = 0; u < U; u++)
         if (mine + u >= lo && mine + u < hi) ST::add(acc, b, u);
