@@ -33,7 +33,7 @@ extern "C" {
 #endif
 
 #define TT_ABI_VERSION 1
-#define TT_MAX_ORDER 4
+#define TT_MAX_ORDER 5
 #define TT_MAX_RANK 64
 
 typedef enum tt_status {

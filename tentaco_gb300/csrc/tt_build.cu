@@ -224,9 +224,9 @@ __global__ void level_flags_kernel(const uint64_t* __restrict__ ukeys, int64_t m
 // (root coordinate of every level-1 fiber)
 __global__ void levels_kernel(const uint64_t* __restrict__ ukeys, int64_t m, PackDev pk, const uint32_t* __restrict__ flags,
                               const uint32_t* __restrict__ fidx, int32_t* crd1, int32_t* crd2, int32_t* crd3,
-                              int32_t* pos2, int32_t* pos3, int32_t* __restrict__ frow) {
-  int32_t* crd[TT_MAX_ORDER] = {nullptr, crd1, crd2, crd3};
-  int32_t* pos[TT_MAX_ORDER] = {nullptr, nullptr, pos2, pos3};
+                              int32_t* crd4, int32_t* pos2, int32_t* pos3, int32_t* pos4, int32_t* __restrict__ frow) {
+  int32_t* crd[TT_MAX_ORDER] = {nullptr, crd1, crd2, crd3, crd4};
+  int32_t* pos[TT_MAX_ORDER] = {nullptr, nullptr, pos2, pos3, pos4};
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x) {
     for (int l = 1; l < pk.order; l++) {
       if (!flags[(size_t)(l - 1) * m + r]) continue;
@@ -396,8 +396,8 @@ TT_EXPORT tt_status tt_csf_from_coo_gpu(int32_t order, const int32_t* dims, int6
   }
   CKB(db.get(&frow, (size_t)cnt[1]));
   if (m > 0) {
-    levels_kernel<<<grid_for(m), kThreads, 0, st>>>(uk, m, pk, flags, fidx, dcrd[1], dcrd[2], dcrd[3], dpos[2],
-                                                     dpos[3], frow);
+    levels_kernel<<<grid_for(m), kThreads, 0, st>>>(uk, m, pk, flags, fidx, dcrd[1], dcrd[2], dcrd[3], dcrd[4],
+                                                     dpos[2], dpos[3], dpos[4], frow);
     CKB(cudaGetLastError());
   }
   root_pos_kernel<<<grid_for((int64_t)dims[0] + 1), kThreads, 0, st>>>(frow, cnt[1], dims[0], dpos[1]);

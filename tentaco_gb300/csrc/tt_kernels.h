@@ -35,6 +35,9 @@ WalkLauncher walk_launcher_o4_bf16_strip(int cpt, int lpr, int fam);
 WalkLauncher walk_launcher_o4_bf16f_strip(int cpt, int lpr, int fam);
 WalkLauncher walk_launcher_o4_fp16_strip(int cpt, int lpr, int fam);
 WalkLauncher walk_launcher_o4_fx16_strip(int cpt, int lpr, int fam);
+WalkLauncher walk_launcher_o5_fp32_strip(int cpt, int lpr, int fam);
+WalkLauncher walk_launcher_o5_fp16_strip(int cpt, int lpr, int fam);
+WalkLauncher walk_launcher_o5_fx16_strip(int cpt, int lpr, int fam);
 // Strip-walk partition: the row (through a.rnz) of every unit boundary, at stride order - 1.
 cudaError_t launch_partition_rows(int order, const WalkArgs& a, cudaStream_t s);
 // A(i, j) = sum over slabs k in order of V(k * vstride + i, j) for i < nrows, FP32 with
@@ -57,11 +60,11 @@ cudaError_t launch_fx16_values(const float* vals, const int32_t* leaf, const int
 cudaError_t launch_partition(int order, const WalkArgs& a, cudaStream_t s);
 // Flat walk indexes.  launch_expand: out[p] = per_fiber[f] for every entry p of
 // fiber f of one level (p < pos[nf] = n).  launch_row_starts: rnz[i] = off + first
-// nonzero of root position i (pos2[pos1[i]], through pos3 for four modes).
+// nonzero of root position i (pos2[pos1[i]], through pos3 for four modes and pos4 for five).
 cudaError_t launch_expand(const int32_t* per_fiber, const int32_t* pos, int64_t nf, int64_t n, int32_t* out,
                           cudaStream_t s);
 cudaError_t launch_row_starts(const int32_t* pos1, const int32_t* pos2, const int32_t* pos3, int64_t nroot,
-                              int32_t* rnz, cudaStream_t s, int64_t off = 0);
+                              int32_t* rnz, cudaStream_t s, int64_t off = 0, const int32_t* pos4 = nullptr);
 // FP64 merge of the rows the walk left in the carry buffer (after the walk kernel).
 cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s);
 // TTV walk over units of 32 * kTtvNpt nonzeros (a: the 2-level view, see tt_ttv.cuh).

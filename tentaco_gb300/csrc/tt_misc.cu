@@ -23,9 +23,14 @@ WalkLauncher walk_launcher(int order, int prec, int cpt, int lpr, int staged) {
       if (prec == kBF16F) return walk_launcher_o4_bf16f_strip(cpt, lpr, staged);
       if (prec == kFP16) return walk_launcher_o4_fp16_strip(cpt, lpr, staged);
       if (prec == kFX16) return walk_launcher_o4_fx16_strip(cpt, lpr, staged);
+    } else if (order == 5) {  // five modes: FP32, FP16 and 16-bit fixed point
+      if (prec == kFP32) return walk_launcher_o5_fp32_strip(cpt, lpr, staged);
+      if (prec == kFP16) return walk_launcher_o5_fp16_strip(cpt, lpr, staged);
+      if (prec == kFX16) return walk_launcher_o5_fx16_strip(cpt, lpr, staged);
     }
     return nullptr;
   }
+  if (order > 4) return nullptr;  // five modes: strip walk only
   if (prec == kFX16) return nullptr;  // 16-bit fixed point: strip walk only
   if (order == 3) {
     if (prec == kFP32) return walk_launcher_o3_fp32(cpt, lpr, staged);
@@ -46,7 +51,8 @@ cudaError_t launch_partition(int order, const WalkArgs& a, cudaStream_t s) {
   const int tb = 256, grid = (n + tb - 1) / tb;
   if (order == 2) partition_kernel<2><<<grid, tb, 0, s>>>(a);
   else if (order == 3) partition_kernel<3><<<grid, tb, 0, s>>>(a);
-  else partition_kernel<4><<<grid, tb, 0, s>>>(a);
+  else if (order == 4) partition_kernel<4><<<grid, tb, 0, s>>>(a);
+  else return cudaErrorInvalidValue;  // five modes: launch_partition_rows (strip walk)
   return cudaGetLastError();
 }
 
@@ -149,9 +155,12 @@ cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s) {
   } else if (order == 3) {
     seg_fold_kernel<3><<<grid, 256, 0, s>>>(a);
     seg_chain_kernel<3><<<grid, 256, 0, s>>>(a);
-  } else {
+  } else if (order == 4) {
     seg_fold_kernel<4><<<grid, 256, 0, s>>>(a);
     seg_chain_kernel<4><<<grid, 256, 0, s>>>(a);
+  } else {
+    seg_fold_kernel<5><<<grid, 256, 0, s>>>(a);
+    seg_chain_kernel<5><<<grid, 256, 0, s>>>(a);
   }
   return cudaGetLastError();
 }
@@ -183,11 +192,13 @@ __global__ void flat_kexp_kernel(const int32_t* __restrict__ crd1, const int32_t
 }
 
 __global__ void flat_rnz_kernel(const int32_t* __restrict__ pos1, const int32_t* __restrict__ pos2,
-                                const int32_t* __restrict__ pos3, int64_t nroot, int32_t* __restrict__ rnz,
-                                int64_t off) {
+                                const int32_t* __restrict__ pos3, const int32_t* __restrict__ pos4, int64_t nroot,
+                                int32_t* __restrict__ rnz, int64_t off) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nroot; i += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t f2 = pos2[pos1[i]];
-    rnz[i] = (int32_t)(off + (pos3 ? pos3[f2] : f2));
+    int32_t f = pos2[pos1[i]];
+    if (pos3) f = pos3[f];
+    if (pos4) f = pos4[f];
+    rnz[i] = (int32_t)(off + f);
   }
 }
 
@@ -203,8 +214,8 @@ cudaError_t launch_expand(const int32_t* per_fiber, const int32_t* pos, int64_t 
 }
 
 cudaError_t launch_row_starts(const int32_t* pos1, const int32_t* pos2, const int32_t* pos3, int64_t nroot,
-                              int32_t* rnz, cudaStream_t s, int64_t off) {
-  flat_rnz_kernel<<<flat_grid(nroot + 1), 256, 0, s>>>(pos1, pos2, pos3, nroot, rnz, off);
+                              int32_t* rnz, cudaStream_t s, int64_t off, const int32_t* pos4) {
+  flat_rnz_kernel<<<flat_grid(nroot + 1), 256, 0, s>>>(pos1, pos2, pos3, pos4, nroot, rnz, off);
   return cudaGetLastError();
 }
 

@@ -41,10 +41,10 @@ namespace tt {
 
 struct alignas(64) WalkArgs {
   CUtensorMap tmap;       // TMA walk: 2-D map of the leaf factor (RP columns x rows, box RP x 1)
-  const int32_t* pos[4];  // pos[l], l = 1..order-1 (pos[1] indexed by root position)
-  const int32_t* crd[4];  // crd[l], l = 1..order-1; crd[0] = root ids (nullptr: dense root)
+  const int32_t* pos[5];  // pos[l], l = 1..order-1 (pos[1] indexed by root position)
+  const int32_t* crd[5];  // crd[l], l = 1..order-1; crd[0] = root ids (nullptr: dense root)
   const void* vals;       // FP32 or BF16, padded
-  const void* fac[3];     // factors of modes 1..order-1, RP entries per row
+  const void* fac[4];     // factors of modes 1..order-1, RP entries per row
   const float* colscale;  // RP output scales (nullptr: all 1)
   float* out;             // output rows (row id = crd[0][ip] or ip), ldo floats apart
   const int32_t* part;    // (nblocks+1) x (order-1): root position, then fiber ids per level
@@ -59,7 +59,7 @@ struct alignas(64) WalkArgs {
   int32_t lgG;            // log2(G)
   int32_t nblocks;
   int32_t rp;             // factor row width the kernels were compiled for
-  int32_t fac_rows[3];    // rows of each factor (bounds for checked builds)
+  int32_t fac_rows[4];    // rows of each factor (bounds for checked builds)
   int32_t smem_bytes;     // dynamic shared memory of the launch (bounds for checked builds)
   int32_t accum;          // 1: add rows into out (slab passes), 0: overwrite
   int32_t gpol;           // L2 policy of the lean walk's factor-row gathers: 0 evict_last, 1 evict_normal
@@ -69,7 +69,8 @@ struct alignas(64) WalkArgs {
   int32_t wcap;           // staged kernels: window fibers per block the shared memory holds
   int32_t* err;           // staged kernels: set nonzero if a block's window exceeds wcap
   const int32_t* kexp;    // flat walk: the level-1 coordinate of every nonzero (padded)
-  const int32_t* kexp2;   // flat walk, four modes: the level-2 coordinate of every nonzero (padded)
+  const int32_t* kexp2;   // flat and strip walks, four or five modes: the level-2 coordinate of every nonzero (padded)
+  const int32_t* kexp3;   // strip walk, five modes: the level-3 coordinate of every nonzero (padded)
   const int32_t* rnz;     // flat and strip walks: first nonzero of every row (nrows + 1); null otherwise
 };
 
@@ -1380,7 +1381,7 @@ __global__ void __launch_bounds__(256) seg_chain_kernel(const __grid_constant__ 
     n1 = a.rnz[r + 1];
   } else {
     int64_t f1 = ORDER == 2 ? (int64_t)r + 1 : (int64_t)a.pos[1][r + 1];
-    if constexpr (ORDER == 4) f1 = a.pos[2][f1];
+    for (int l = 2; l < ORDER - 1; l++) f1 = a.pos[l][f1];
     n1 = a.pos[ORDER - 1][f1];
   }
   const int s1 = (int)((n1 - 1) / a.P) / kSeg;  // segment holding the row's last nonzero

@@ -131,9 +131,10 @@ int strip_default_variant(int order, int rank, int prec);
 
 int default_variant(int order, int rank, int prec, int64_t nnz) {
   (void)nnz;
-  // four modes and 16-bit fixed point: the strip rule (the fastest family on the
-  // 80M-nonzero 4-mode tensor in every storage precision)
-  if (order == 4 || prec == kFX16) {
+  // four and five modes and 16-bit fixed point: the strip rule (the fastest family
+  // on the 80M-nonzero 4-mode tensor in every storage precision; the only one for
+  // five modes)
+  if (order >= 4 || prec == kFX16) {
     const int id = strip_default_variant(order, rank, prec);
     if (id >= 0) return id;
   }
@@ -188,7 +189,7 @@ int strip_default_variant(int order, int rank, int prec) {
 // in slab-major order (virtual rows, summed afterwards); the lean, staged and TMA
 // walks run one pass per slab; the flat walk does not run on slab plans.
 int auto_slabs(int order, int64_t leaf_dim, int rp, int prec) {
-  (void)order;
+  if (order > 4) return 1;  // slab-major layouts are built for three and four modes
   const int64_t bytes = leaf_dim * (int64_t)rp * fac_bytes(prec);
   constexpr int64_t kMB = 1 << 20;
   if (bytes <= 48 * kMB) return 1;
@@ -415,8 +416,10 @@ int plan_default_variant(const tt_plan* p) {
 // slabs * (nroot + 1) virtual rows, row nroot of each slab covering its padding.
 // All or nothing: on failure no array is kept.
 tt_status build_slab_flat_arrays(tt_plan* p);
+tt_status build_flat_arrays5(tt_plan* p);
 tt_status build_flat_arrays(tt_plan* p) {
   if (p->slabs > 1) return build_slab_flat_arrays(p);
+  if (p->order == 5) return build_flat_arrays5(p);
   const size_t np = (size_t)pad16(p->nnz);
   int32_t *kexp = nullptr, *kexp2 = nullptr, *rnz = nullptr, *k1f2 = nullptr;
   auto undo = [&](tt_status s) {
@@ -457,6 +460,50 @@ tt_status build_flat_arrays(tt_plan* p) {
   dev_free(p, k1f2);
   p->d_kexp = kexp;
   p->d_kexp2 = kexp2;
+  p->d_rnz = rnz;
+  return TT_OK;
+}
+
+// Five modes (strip walk): the level-1, level-2 and level-3 coordinates of every
+// nonzero, each carried down the levels by launch_expand, and the row starts.
+tt_status build_flat_arrays5(tt_plan* p) {
+  const size_t np = (size_t)pad16(p->nnz);
+  int32_t *k1 = nullptr, *k2 = nullptr, *k3 = nullptr, *rnz = nullptr, *a2 = nullptr, *a31 = nullptr, *a32 = nullptr;
+  auto undo = [&](tt_status s) {
+    cudaStreamSynchronize(p->stream);
+    for (int32_t* d : {a32, a31, a2, rnz, k3, k2, k1}) dev_free(p, d);
+    return s;
+  };
+  auto ck = [&](cudaError_t e, const char* what) {
+    return e == cudaSuccess ? TT_OK
+                            : set_error(e == cudaErrorMemoryAllocation ? TT_ERR_OUT_OF_MEMORY : TT_ERR_CUDA,
+                                        "%s: %s", what, cudaGetErrorString(e));
+  };
+  tt_status s;
+  for (int32_t** d : {&k1, &k2, &k3}) {
+    if ((s = dev_alloc(p, d, np)) != TT_OK) return undo(s);
+    if ((s = ck(cudaMemsetAsync(*d, 0, sizeof(int32_t) * np, p->stream), "clear")) != TT_OK) return undo(s);
+  }
+  if ((s = dev_alloc(p, &rnz, (size_t)p->nroot + 1)) != TT_OK) return undo(s);
+  if ((s = dev_alloc(p, &a2, (size_t)p->count[2] + 1)) != TT_OK) return undo(s);
+  if ((s = dev_alloc(p, &a31, (size_t)p->count[3] + 1)) != TT_OK) return undo(s);
+  if ((s = dev_alloc(p, &a32, (size_t)p->count[3] + 1)) != TT_OK) return undo(s);
+  // a2: level-1 coordinate of each level-2 fiber; a31 / a32: level-1 / level-2
+  // coordinate of each level-3 fiber
+  if ((s = ck(launch_expand(p->d_crd[1], p->d_pos[2], p->count[1], p->count[2], a2, p->stream), "expand")) != TT_OK ||
+      (s = ck(launch_expand(a2, p->d_pos[3], p->count[2], p->count[3], a31, p->stream), "expand")) != TT_OK ||
+      (s = ck(launch_expand(p->d_crd[2], p->d_pos[3], p->count[2], p->count[3], a32, p->stream), "expand")) != TT_OK ||
+      (s = ck(launch_expand(a31, p->d_pos[4], p->count[3], p->nnz, k1, p->stream), "expand")) != TT_OK ||
+      (s = ck(launch_expand(a32, p->d_pos[4], p->count[3], p->nnz, k2, p->stream), "expand")) != TT_OK ||
+      (s = ck(launch_expand(p->d_crd[3], p->d_pos[4], p->count[3], p->nnz, k3, p->stream), "expand")) != TT_OK ||
+      (s = ck(launch_row_starts(p->d_pos[1], p->d_pos[2], p->d_pos[3], p->nroot, rnz, p->stream, 0, p->d_pos[4]),
+              "row starts")) != TT_OK)
+    return undo(s);
+  if ((s = ck(cudaStreamSynchronize(p->stream), "flat arrays")) != TT_OK) return undo(s);
+  for (int32_t* d : {a32, a31, a2}) dev_free(p, d);
+  p->d_kexp = k1;
+  p->d_kexp2 = k2;
+  p->d_kexp3 = k3;
   p->d_rnz = rnz;
   return TT_OK;
 }
@@ -586,7 +633,7 @@ WalkArgs walk_args(const tt_plan* p, float* A, int q) {
            (size_t)sl.off * (size_t)val_bytes(p->prec);
   a.accum = p->slabs > 1 ? 1 : 0;
   a.gpol = p->gpol;
-  for (int m = 0; m < 3; m++) a.fac[m] = p->fac[m];
+  for (int m = 0; m < 4; m++) a.fac[m] = p->fac[m];
   a.colscale = p->d_colscale;
   a.out = A;
   a.part = p->d_part;
@@ -608,9 +655,10 @@ WalkArgs walk_args(const tt_plan* p, float* A, int q) {
   a.err = p->d_err;
   a.kexp = p->d_kexp;
   a.kexp2 = p->d_kexp2;
+  a.kexp3 = p->d_kexp3;
   // rows through rnz only for the families that walk by it (the row merge uses it too)
   a.rnz = p->staged == 3 || p->staged == 4 ? p->d_rnz : nullptr;
-  for (int m = 0; m < 3; m++) a.fac_rows[m] = m + 1 < p->order ? (int32_t)p->dims[m + 1] : 0;
+  for (int m = 0; m < 4; m++) a.fac_rows[m] = m + 1 < p->order ? (int32_t)p->dims[m + 1] : 0;
   return a;
 }
 
@@ -623,7 +671,7 @@ WalkArgs strip_slab_args(const tt_plan* p) {
   a.vals = p->prec == kFX16 && p->d_vals_fx ? (const void*)p->d_vals_fx : p->d_vals;
   a.accum = 0;
   a.gpol = p->gpol;
-  for (int m = 0; m < 3; m++) a.fac[m] = p->fac[m];
+  for (int m = 0; m < 4; m++) a.fac[m] = p->fac[m];
   a.colscale = p->d_colscale;
   a.out = p->d_vrows;
   a.part = p->d_part;
@@ -644,8 +692,9 @@ WalkArgs strip_slab_args(const tt_plan* p) {
   a.err = p->d_err;
   a.kexp = p->d_kexp;
   a.kexp2 = p->d_kexp2;
+  a.kexp3 = p->d_kexp3;
   a.rnz = p->d_rnz;
-  for (int m = 0; m < 3; m++) a.fac_rows[m] = m + 1 < p->order ? (int32_t)p->dims[m + 1] : 0;
+  for (int m = 0; m < 4; m++) a.fac_rows[m] = m + 1 < p->order ? (int32_t)p->dims[m + 1] : 0;
   return a;
 }
 
@@ -877,7 +926,7 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
   // from the host arrays) and empty tensors, else on the device after upload
   if ((s = csf_check_root(v)) != TT_OK) return s;
   if (op == TT_OP_MTTKRP) {
-    if (v.order != 3 && v.order != 4) return set_error(TT_ERR_UNSUPPORTED, "MTTKRP needs order 3 or 4 (got %d)", v.order);
+    if (v.order < 3 || v.order > 5) return set_error(TT_ERR_UNSUPPORTED, "MTTKRP needs order 3, 4 or 5 (got %d)", v.order);
     if (rank < 1 || rank > TT_MAX_RANK) return set_error(TT_ERR_UNSUPPORTED, "rank %d (supported 1..%d)", rank, TT_MAX_RANK);
   } else if (op != TT_OP_TTV) {
     return set_error(TT_ERR_INVALID_ARGUMENT, "op %d", (int)op);
@@ -1151,7 +1200,7 @@ TT_EXPORT tt_status tt_plan_set_factors(tt_plan* p, const float* const* factors,
     if (!p->d_scales) {
       if ((s = dev_alloc(p, &p->d_scales, (size_t)(3 * nm + 1) * p->rp)) != TT_OK) return s;
     }
-    const float* inv[3] = {nullptr, nullptr, nullptr};
+    const float* inv[4] = {nullptr, nullptr, nullptr, nullptr};
     for (int m = 0; m < nm; m++) {
       const int64_t rows = p->dims[m + 1];
       if (p->prec == kFX16 && m < nm - 1) {
@@ -1304,7 +1353,7 @@ tt_status time_variants(tt_plan* p, cudaStream_t st, const std::vector<int>& can
     struct Scratch {
       tt_plan* p;
       cudaStream_t st;
-      const void* saved[3];
+      const void* saved[4];
       float* saved_scale;
       std::vector<void*> tmp;
       cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1313,10 +1362,10 @@ tt_status time_variants(tt_plan* p, cudaStream_t st, const std::vector<int>& can
         if (e1) cudaEventDestroy(e1);
         cudaStreamSynchronize(st);
         for (void* d : tmp) cudaFree(d);
-        for (int m = 0; m < 3; m++) p->fac[m] = saved[m];
+        for (int m = 0; m < 4; m++) p->fac[m] = saved[m];
         p->d_colscale = saved_scale;
       }
-    } sc{p, st, {p->fac[0], p->fac[1], p->fac[2]}, p->d_colscale, {}};
+    } sc{p, st, {p->fac[0], p->fac[1], p->fac[2], p->fac[3]}, p->d_colscale, {}};
     const int nm = p->order - 1;
     for (int m = 0; m < nm; m++) {
       // bytes per entry of factor m in this plan's storage (16-bit fixed point keeps
@@ -1405,7 +1454,7 @@ TT_EXPORT tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
   if (!A || !B || !factors || !A->vals || !A->dimensions || !B->dimensions)
     return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
   const int order = B->order;
-  if (order != 3 && order != 4) return set_error(TT_ERR_UNSUPPORTED, "MTTKRP needs order 3 or 4 (got %d)", order);
+  if (order < 3 || order > 5) return set_error(TT_ERR_UNSUPPORTED, "MTTKRP needs order 3, 4 or 5 (got %d)", order);
   const int rank = A->dimensions[1];
   if (A->dimensions[0] != B->dimensions[0]) return set_error(TT_ERR_INVALID_ARGUMENT, "A rows %d != B dims[0] %d", A->dimensions[0], B->dimensions[0]);
   for (int m = 0; m < order - 1; m++) {

@@ -44,8 +44,8 @@ struct tt_plan {
   float* d_vals_fx = nullptr;    // 16-bit fixed point: values times their leaf row's power of two
   int8_t* d_rowexp = nullptr;    // 16-bit fixed point: power of two of every leaf-factor row
   // factors in storage precision
-  const void* fac[3] = {nullptr, nullptr, nullptr};
-  void* fac_own[3] = {nullptr, nullptr, nullptr};
+  const void* fac[4] = {nullptr, nullptr, nullptr, nullptr};
+  void* fac_own[4] = {nullptr, nullptr, nullptr, nullptr};
   float* d_scales = nullptr;    // per factor: colmax, scale, inv (rp each); then the output scale
   float* d_colscale = nullptr;
   bool factors_set = false;
@@ -56,7 +56,8 @@ struct tt_plan {
   tt::WalkLauncher launcher = nullptr;
   int32_t* d_part = nullptr;
   int32_t* d_kexp = nullptr;  // flat walk: level-1 coordinate of every nonzero (padded)
-  int32_t* d_kexp2 = nullptr; // flat walk, four modes: level-2 coordinate of every nonzero (padded)
+  int32_t* d_kexp2 = nullptr; // flat and strip walks, four or five modes: level-2 coordinate of every nonzero (padded)
+  int32_t* d_kexp3 = nullptr; // strip walk, five modes: level-3 coordinate of every nonzero (padded)
   int32_t* d_rnz = nullptr;   // flat walk: first nonzero of every root position
   // the partition depends only on the CSF and the unit size: a single-slab plan
   // computes it once per variant (part_ready) and times it (part_ms)

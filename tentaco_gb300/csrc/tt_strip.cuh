@@ -1,13 +1,15 @@
 // tt_strip.cuh -- the strip walk (family 4): mode-0 MTTKRP over a CSF tensor whose
-// rows are long compared with a warp's step of nonzeros (3 or 4 modes).
+// rows are long compared with a warp's step of nonzeros (3, 4 or 5 modes).
 //
 //   A(i,:) = sum_{k,l}   B(i,k,l)   C(k,:) .* D(l,:)             (order 3)
 //   A(i,:) = sum_{k,l,m} B(i,k,l,m) C(k,:) .* D(l,:) .* E(m,:)    (order 4)
+//   A(i,:) = sum B(i,k,l,m,n) C(k,:) .* D(l,:) .* E(m,:) .* F(n,:)  (order 5)
 //
-// Every nonzero carries its upper coordinates (kexp, kexp2: built once per plan),
+// Every nonzero carries its upper coordinates (kexp, kexp2, kexp3: built once per plan),
 // so a nonzero is one independent product of gathered factor rows, the reference's
 // own loop arithmetic (tensor_kernels/mttkrp3_csf_cpu_taco.h:45,
-// mttkrp4_csf_cpu_taco.h:53).  The walk is warp-synchronous:
+// mttkrp4_csf_cpu_taco.h:53; five modes: the product of tensor_kernels/
+// mttkrp5_csf_cpu_taco.h:35-95, summed per nonzero instead of level by level).  The walk is warp-synchronous:
 //
 //   * a warp owns a tile of P consecutive nonzeros (the work unit of the partition
 //     and of the cross-unit row merge), staged into shared memory in order with
@@ -109,7 +111,8 @@ struct Strip {
   static constexpr int UB = CPT * (K::U == kF32 ? 4 : 2);  // bytes of a lane's upper-row piece
   static constexpr int LB = CPT * (K::L == kF32 ? 4 : 2);  // bytes of a lane's leaf-row piece
   static constexpr int UW = UB / 4, LW = LB / 4;
-  static constexpr int MW = ORDER == 4 ? UW : 1;
+  static constexpr int MW = ORDER >= 4 ? UW : 1;
+  static constexpr int EW = ORDER == 5 ? UW : 1;
   // bytes per factor row (the kernel is compiled for rows of RP = CPT * LPR entries)
   static constexpr uint32_t URB = (uint32_t)LPR * UB, LRB = (uint32_t)LPR * LB;
   static_assert(CPT >= 2 && CPT % 2 == 0, "the strip walk works on column pairs");
@@ -117,35 +120,45 @@ struct Strip {
   // gathered pieces of one step's U nonzeros of a team, and their values
   struct Batch {
     uint32_t c[U][UW];  // level-1 factor
-    uint32_t m[U][MW];  // level-2 factor (four modes)
+    uint32_t m[U][MW];  // level-2 factor (four and five modes)
+    uint32_t e[U][EW];  // level-3 factor (five modes)
     uint32_t d[U][LW];  // leaf factor
     uint32_t v[U * VB / 4 > 0 ? U * VB / 4 : 1];  // raw values (U * VB bytes)
   };
 
-  const unsigned char *fc, *fm, *fd;  // this lane's piece of row 0 of each factor
+  const unsigned char *fc, *fm, *fe, *fd;  // this lane's piece of row 0 of each factor
   uint64_t pol_u, pol_l;
 
   __device__ __forceinline__ void load(Batch& b, const int32_t* s_l, const int32_t* s_k, const int32_t* s_k2,
-                                       const unsigned char* s_v, int p0) const {
-    int32_t l[U], k[U], k2[U];
+                                       const int32_t* s_k3, const unsigned char* s_v, int p0) const {
+    int32_t l[U], k[U], k2[U], k3[U];
     if constexpr (U == 4) {
       const int4 a = *reinterpret_cast<const int4*>(s_l + p0), c = *reinterpret_cast<const int4*>(s_k + p0);
       l[0] = a.x; l[1] = a.y; l[2] = a.z; l[3] = a.w;
       k[0] = c.x; k[1] = c.y; k[2] = c.z; k[3] = c.w;
-      if constexpr (ORDER == 4) {
+      if constexpr (ORDER >= 4) {
         const int4 e = *reinterpret_cast<const int4*>(s_k2 + p0);
         k2[0] = e.x; k2[1] = e.y; k2[2] = e.z; k2[3] = e.w;
+      }
+      if constexpr (ORDER == 5) {
+        const int4 e = *reinterpret_cast<const int4*>(s_k3 + p0);
+        k3[0] = e.x; k3[1] = e.y; k3[2] = e.z; k3[3] = e.w;
       }
     } else if constexpr (U == 2) {
       const int2 a = *reinterpret_cast<const int2*>(s_l + p0), c = *reinterpret_cast<const int2*>(s_k + p0);
       l[0] = a.x; l[1] = a.y; k[0] = c.x; k[1] = c.y;
-      if constexpr (ORDER == 4) {
+      if constexpr (ORDER >= 4) {
         const int2 e = *reinterpret_cast<const int2*>(s_k2 + p0);
         k2[0] = e.x; k2[1] = e.y;
       }
+      if constexpr (ORDER == 5) {
+        const int2 e = *reinterpret_cast<const int2*>(s_k3 + p0);
+        k3[0] = e.x; k3[1] = e.y;
+      }
     } else {
       l[0] = s_l[p0]; k[0] = s_k[p0];
-      if constexpr (ORDER == 4) k2[0] = s_k2[p0];
+      if constexpr (ORDER >= 4) k2[0] = s_k2[p0];
+      if constexpr (ORDER == 5) k3[0] = s_k3[p0];
     }
     constexpr int NVW = U * VB / 4;
     if constexpr (NVW == 4) {
@@ -162,7 +175,8 @@ struct Strip {
 #pragma unroll
     for (int u = 0; u < U; u++) {
       strip_piece<UB, true>(fc + (uint64_t)(uint32_t)k[u] * URB, pol_u, b.c[u]);
-      if constexpr (ORDER == 4) strip_piece<UB, true>(fm + (uint64_t)(uint32_t)k2[u] * URB, pol_u, b.m[u]);
+      if constexpr (ORDER >= 4) strip_piece<UB, true>(fm + (uint64_t)(uint32_t)k2[u] * URB, pol_u, b.m[u]);
+      if constexpr (ORDER == 5) strip_piece<UB, true>(fe + (uint64_t)(uint32_t)k3[u] * URB, pol_u, b.e[u]);
       strip_piece<LB, false>(fd + (uint64_t)(uint32_t)l[u] * LRB, pol_l, b.d[u]);
     }
   }
@@ -186,7 +200,7 @@ struct Strip {
 #pragma unroll
       for (int j = 0; j < CPT / 2; j++) {
         const float2 p = hprod2<FK>(b.c[u][j], b.d[u][j]);
-        if constexpr (ORDER == 4) {
+        if constexpr (ORDER >= 4) {
           float2 t;
           if constexpr (K::V == FK) {
             const uint32_t w = b.v[u >> 1];
@@ -195,6 +209,10 @@ struct Strip {
           } else {
             const float2 mm = pair16<FK>(b.m[u][j]);
             t = fmul2(v, v, mm.x, mm.y);
+          }
+          if constexpr (ORDER == 5) {  // times the level-3 row (one rounding more)
+            const float2 ee = pair16<FK>(b.e[u][j]);
+            t = fmul2(t.x, t.y, ee.x, ee.y);
           }
           ffma2(acc[2 * j], acc[2 * j + 1], p.x, p.y, t.x, t.y);
         } else {
@@ -206,7 +224,8 @@ struct Strip {
 #pragma unroll
       for (int j = 0; j < CPT / 2; j++) {
         float2 t = fmul2(v, v, __uint_as_float(b.c[u][2 * j]), __uint_as_float(b.c[u][2 * j + 1]));
-        if constexpr (ORDER == 4) t = fmul2(t.x, t.y, __uint_as_float(b.m[u][2 * j]), __uint_as_float(b.m[u][2 * j + 1]));
+        if constexpr (ORDER >= 4) t = fmul2(t.x, t.y, __uint_as_float(b.m[u][2 * j]), __uint_as_float(b.m[u][2 * j + 1]));
+        if constexpr (ORDER == 5) t = fmul2(t.x, t.y, __uint_as_float(b.e[u][2 * j]), __uint_as_float(b.e[u][2 * j + 1]));
         float2 dd;
         if constexpr (K::L == kF32) dd = make_float2(__uint_as_float(b.d[u][2 * j]), __uint_as_float(b.d[u][2 * j + 1]));
         else dd = i16pair(b.d[u][j]);
@@ -294,7 +313,8 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_strip_kernel(const __grid_co
   unsigned char* ws = smem + (size_t)warp * strip_warp_bytes(P, VB, ORDER);
   int32_t* s_l = reinterpret_cast<int32_t*>(ws);
   int32_t* s_k = s_l + P;
-  int32_t* s_k2 = s_k + P;  // four modes only
+  int32_t* s_k2 = s_k + P;   // four and five modes
+  int32_t* s_k3 = s_k2 + P;  // five modes
   unsigned char* s_v = reinterpret_cast<unsigned char*>(s_l + (size_t)(ORDER - 1) * P);
   const int64_t ustart = (int64_t)unit * P;
   const int cnt = (int)min((int64_t)P, a.nnz - ustart);
@@ -303,14 +323,16 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_strip_kernel(const __grid_co
     const int n4 = (cnt + 3) >> 2;
     strip_stage(a.crd[ORDER - 1] + ustart, s_l, n4, lane, polF);
     strip_stage(a.kexp + ustart, s_k, n4, lane, polF);
-    if constexpr (ORDER == 4) strip_stage(a.kexp2 + ustart, s_k2, n4, lane, polF);
+    if constexpr (ORDER >= 4) strip_stage(a.kexp2 + ustart, s_k2, n4, lane, polF);
+    if constexpr (ORDER == 5) strip_stage(a.kexp3 + ustart, s_k3, n4, lane, polF);
     strip_stage(static_cast<const unsigned char*>(a.vals) + ustart * VB, s_v, (cnt * VB + 15) >> 4, lane, polF);
     // the tensor's last unit: the steps past its end still gather (masked out
     // later), so their coordinates must be valid rows
     for (int p = 4 * n4 + lane; p < (cnt + STEP - 1) / STEP * STEP; p += 32) {
       s_l[p] = 0;
       s_k[p] = 0;
-      if constexpr (ORDER == 4) s_k2[p] = 0;
+      if constexpr (ORDER >= 4) s_k2[p] = 0;
+      if constexpr (ORDER == 5) s_k3[p] = 0;
     }
   }
   __syncwarp();
@@ -320,6 +342,7 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_strip_kernel(const __grid_co
   ST st;
   st.fc = static_cast<const unsigned char*>(a.fac[0]) + q * ST::UB;
   st.fm = static_cast<const unsigned char*>(a.fac[1]) + q * ST::UB;
+  st.fe = static_cast<const unsigned char*>(a.fac[2]) + q * ST::UB;
   st.fd = static_cast<const unsigned char*>(a.fac[ORDER - 2]) + q * ST::LB;
   st.pol_u = policy_evict_last();
   st.pol_l = a.gpol == 1 ? policy_evict_normal() : policy_evict_last();
@@ -408,12 +431,12 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_strip_kernel(const __grid_co
   const int nsteps = (cnt + STEP - 1) / STEP;
   typename ST::Batch bA, bB;
   const int toff = team * U;
-  if (nsteps > 0) st.load(bA, s_l, s_k, s_k2, s_v, toff);
+  if (nsteps > 0) st.load(bA, s_l, s_k, s_k2, s_k3, s_v, toff);
   for (int s = 0; s < nsteps; s += 2) {
-    if (s + 1 < nsteps) st.load(bB, s_l, s_k, s_k2, s_v, (s + 1) * STEP + toff);
+    if (s + 1 < nsteps) st.load(bB, s_l, s_k, s_k2, s_k3, s_v, (s + 1) * STEP + toff);
     consume(bA, s);
     if (s + 1 < nsteps) {
-      if (s + 2 < nsteps) st.load(bA, s_l, s_k, s_k2, s_v, (s + 2) * STEP + toff);
+      if (s + 2 < nsteps) st.load(bA, s_l, s_k, s_k2, s_k3, s_v, (s + 2) * STEP + toff);
       consume(bB, s + 1);
     }
   }

@@ -73,7 +73,14 @@ def test_variant_table():
             # 16-bit fixed point runs on the strip family (ids 160..199) only
             assert not any(tt.variant_valid(x, order, rank, "fx16") for x in range(160))
             assert any(tt.variant_valid(x, order, rank, "fx16") for x in range(160, 200))
-    # the fixed heuristic: flat family for three modes, lean for four
+    # five modes: the strip family, FP32, FP16 and 16-bit fixed point
+    for rank in (1, 8, 16, 32, 64):
+        for prec in ("fp32", "fp16", "fx16"):
+            v = tt.default_variant(5, rank, prec)
+            assert tt.variant_info(v)["staged"] == 4 and tt.variant_valid(v, 5, rank, prec)
+            assert not any(tt.variant_valid(x, 5, rank, prec) for x in range(160))
+        assert not any(tt.variant_valid(x, 5, rank, "bf16") for x in range(200))
+    # the fixed heuristic: flat family for three modes, strip for four
     info = tt.variant_info(tt.default_variant(3, 32, "fp32"))
     assert info["threads"] == 256 and info["cols_per_lane"] == 4 and info["staged"] == 3
     assert info["name"] == "flat_b2_g64_c4"
@@ -119,7 +126,7 @@ def test_host_call_rejects_unsupported_orders_first():
     tensor's levels or the factor array (which has order - 1 entries)."""
     lv = [None, (np.array([0, 1, 1], np.int32), np.array([0], np.int32)),
           (np.array([0, 1], np.int32), np.array([1], np.int32))]
-    for order in (2, 5):
+    for order in (2, 6):
         B = tt.HostTaco((2, 2, 2), vals=np.ones(1, np.float32), levels=lv, order=order)
         with pytest.raises(tt.TTError) as e:
             tt.mttkrp_host(B, [np.ones((2, 8), np.float32), np.ones((2, 8), np.float32)])

@@ -19,7 +19,7 @@ def same(B, Oc):
 
 
 @pytest.mark.parametrize("dims,nnz", [((50, 40, 30), 5000), ((7, 5, 6, 9), 300), ((3, 1000, 1000), 2000),
-                                       ((1, 4, 4), 10), ((1000, 3, 3), 20)])
+                                       ((1, 4, 4), 10), ((1000, 3, 3), 20), ((6, 5, 4, 7, 9), 2000)])
 def test_builder_matches_oracle(dims, nnz):
     rng = np.random.default_rng(nnz)
     co = np.stack([rng.integers(0, d, nnz) for d in dims], 1)
@@ -98,11 +98,11 @@ def test_dense_generator():
     assert u.min() >= 0 and u.max() < 1
 
 
-@pytest.mark.parametrize("order", [3, 4])
+@pytest.mark.parametrize("order", [3, 4, 5])
 def test_reroot_matches_builder_on_permuted_coordinates(order):
     """tt_csf_reroot(B, m) is bit-identical to building the canonical CSF from B's
     coordinates permuted to (m, then the other modes in increasing order)."""
-    dims = (40, 30, 50) if order == 3 else (20, 15, 12, 30)
+    dims = {3: (40, 30, 50), 4: (20, 15, 12, 30), 5: (9, 8, 7, 6, 11)}[order]
     B = tt.gen_zipf(dims, (0.8,) * order, 4000, 11 + order)
     co = O.coords_of(to_oracle(B)).astype(np.int32)
     for m in range(order):

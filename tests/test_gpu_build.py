@@ -19,7 +19,8 @@ def same(a, b):
 
 
 @pytest.mark.parametrize("dims,nnz", [((7, 9), 40), ((50, 40, 30), 20_000), ((300, 200, 5000), 3_000_000),
-                                      ((12, 10, 9, 40), 30_000), ((3, 2, 2), 1), ((1000, 5, 5), 10)])
+                                      ((12, 10, 9, 40), 30_000), ((3, 2, 2), 1), ((1000, 5, 5), 10),
+                                      ((8, 7, 6, 5, 40), 20_000)])
 def test_gpu_builder_matches_host(dims, nnz):
     rng = np.random.default_rng(len(dims) * 7 + nnz % 97)
     co = np.stack([rng.integers(0, d, nnz) for d in dims], axis=1).astype(np.int32)

@@ -137,8 +137,6 @@ def test_four_modes(prec):
 def test_golden_vectors_strip(path):
     z = np.load(path)
     order = int(z["order"])
-    if order > 4:
-        pytest.skip("the C ABI runs orders 3 and 4")
     facs = [z[f"F{m}"].astype(np.float32) for m in range(1, order)]
     B = host_taco(golden_csf(z))
     R = facs[0].shape[1]
@@ -215,3 +213,21 @@ def test_slab_major_padded_ranks(zipf_rows, R):
     for prec in ("fp32", "fp16", "fx16"):
         v = strip_variants(3, R, prec)[0]
         close(run(B, facs, prec, v, slabs=3)[0], ref, prec)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp16", "fx16"])
+@pytest.mark.parametrize("R", [8, 32, 64])
+def test_five_modes(prec, R):
+    """Five modes (the reference's mttkrp5_csf_cpu_taco.h as the oracle): Zipf root
+    and leaf, long and short rows, a ragged nonzero count."""
+    dims = (400, 60, 50, 40, 3000)
+    B = tt.gen_zipf(dims, (1.1, 0.3, 0.0, 0.0, 1.0), 300_007, seed=9 + R)
+    facs = [tt.gen_dense(d, R, 1, 20 + m) for m, d in enumerate(dims[1:])]
+    ref = O.mttkrp(to_oracle(B), facs)
+    for v in strip_variants(5, R, prec)[::2]:
+        close(run(B, facs, prec, v)[0], ref, prec)
+    # the plan's own choice (the strip rule) and the one-shot host call
+    plan = tt.Plan(B, rank=R, prec=prec)
+    assert tt.variant_info(plan.variant)["staged"] == 4
+    if prec == "fp32":
+        close(tt.mttkrp_host(B, facs), ref, "fp32")
