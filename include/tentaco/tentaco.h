@@ -1,5 +1,5 @@
 /*
- * tentaco.h -- C ABI of libtentaco_gb300: sparse MTTKRP (3- and 4-mode, mode 0)
+ * tentaco.h -- C ABI of libtentaco_gb300: sparse MTTKRP (3- to 5-mode, any output mode)
  * and TTV over CSF tensors on one GB300 (sm_103a).
  *
  * Two layers:
@@ -48,8 +48,10 @@ typedef enum tt_status {
 } tt_status;
 
 typedef enum tt_op {
-  TT_OP_MTTKRP = 0, /* A(i,:) = sum B(i,k,l[,m]) C(k,:) .* D(l,:) [.* E(m,:)]      */
-  TT_OP_TTV = 1     /* y(fiber) = sum_l B(i,j,l) x(l), one output per (i,j) fiber */
+  TT_OP_MTTKRP = 0, /* A(i,:) = sum B(i,k,l[,m[,n]]) C(k,:) .* D(l,:) [.* E(m,:) [.* F(n,:)]] */
+  TT_OP_TTV = 1,    /* y(fiber) = sum_l B(i,j,l) x(l), one output per (i,j) fiber */
+  TT_OP_TTM = 2     /* Y(fiber,:) = sum_l B(i,j,l) U(:,l), U rank x dims[2]: COO plans
+                       (tt_plan_create_coo), as the reference's MATLAB interface    */
 } tt_op;
 
 typedef enum tt_precision {
@@ -164,6 +166,28 @@ tt_status tt_plan_mttkrp(tt_plan* plan, float* A, void* stream);
 /* TTV: x DEVICE FP32 of length dims[order-1]; y DEVICE FP32, one entry per
  * fiber of level order-2 (tt_plan_num_fibers), overwritten. */
 tt_status tt_plan_ttv(tt_plan* plan, const float* x, float* y, void* stream);
+
+/*
+ * Plans over sorted COO input, for the reference's MATLAB-interface kernels
+ * (tensor_kernels/fmtaco.cpp: compute_ttv 32-115, compute_ttm 117-223,
+ * compute_mttkrp 741-780).  coords: HOST, nnz x order int32, row-major, in
+ * lexicographic (non-decreasing) order -- duplicates are separate nonzeros, as
+ * there; vals: HOST FP32.  The plan uploads them once and walks the COO columns
+ * directly (no CSF is built): MTTKRP (order 3 to 5; rows are runs of the first
+ * coordinate) on the strip walk; TTV and TTM (order 3; fibers are runs of equal
+ * (i, j)) on the TTV walk and on the strip walk over the fibers.  Unsorted or
+ * out-of-range coordinates: TT_ERR_INVALID_ARGUMENT.  TTM: FP32 storage;
+ * tt_plan_set_factors takes U (DEVICE, rank x dims[2] row-major) and tt_plan_ttm
+ * writes Y (DEVICE, nfibers x rank); tt_plan_coo_fibers gives every fiber's (i, j)
+ * (HOST, 2 x nfibers int32); tt_plan_num_fibers(plan, 1) (TTV) or (plan, 0) (TTM)
+ * gives nfibers.  Variants: the strip family (MTTKRP, TTM); TT_SELECT_MODEL takes
+ * the strip rule.
+ */
+tt_status tt_plan_create_coo(int32_t order, const int32_t* dims, int64_t nnz, const int32_t* coords,
+                             const float* vals, tt_op op, int32_t rank, tt_precision prec, tt_select select,
+                             int32_t variant, void* stream, tt_plan** plan);
+tt_status tt_plan_ttm(tt_plan* plan, float* Y, void* stream);
+tt_status tt_plan_coo_fibers(const tt_plan* plan, int32_t* ij);
 
 /* Plans and one-shot calls take device memory from a stream-ordered pool per
  * device that keeps freed memory for the next plan; this returns what no live

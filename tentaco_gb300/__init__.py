@@ -25,7 +25,7 @@ TT_ERR_OUT_OF_MEMORY = 5
 TT_ERR_NO_DEVICE = 6
 TT_ERR_DEVICE_WAIT = 7
 
-OP_MTTKRP, OP_TTV = 0, 1
+OP_MTTKRP, OP_TTV, OP_TTM = 0, 1, 2
 PREC_FP32, PREC_BF16, PREC_BF16_FACTORS, PREC_FP16, PREC_FX16 = 0, 1, 2, 3, 4
 SELECT_DEFAULT, SELECT_MODEL, SELECT_SWEEP, SELECT_FIXED = 0, 1, 2, 3
 PRECISIONS = {"fp32": PREC_FP32, "bf16": PREC_BF16, "bf16f": PREC_BF16_FACTORS, "fp16": PREC_FP16, "fx16": PREC_FX16}
@@ -86,6 +86,10 @@ def lib():
         "tt_plan_set_factors": (S, [_P, C.POINTER(_P), _P]),
         "tt_plan_mttkrp": (S, [_P, _P, _P]),
         "tt_plan_ttv": (S, [_P, _P, _P, _P]),
+        "tt_plan_ttm": (S, [_P, _P, _P]),
+        "tt_plan_coo_fibers": (S, [_P, _P]),
+        "tt_plan_create_coo": (S, [C.c_int32, _P, C.c_int64, _P, _P, S, C.c_int32, S, S, C.c_int32, _P,
+                                   C.POINTER(_P)]),
         "tt_plan_set_timing": (S, [_P, C.c_int32]),
         "tt_plan_last_ms": (C.c_float, [_P]),
         "tt_plan_last_kernel_ms": (C.c_float, [_P]),
@@ -408,6 +412,37 @@ class Plan:
         self.mode = int(mode)
         check(lib().tt_plan_create_ex(_tensor_ptr(B), op, rank, PRECISIONS.get(prec, prec), select, variant,
                                       C.byref(opts), stream, C.byref(self.ptr)))
+
+    @classmethod
+    def from_coo(cls, dims, coords, vals, op=OP_MTTKRP, rank=32, prec="fp32", select=SELECT_DEFAULT, variant=0,
+                 stream=None):
+        """A plan over sorted COO input (tt_plan_create_coo): coords nnz x order int32
+        (lexicographically sorted), vals FP32.  MTTKRP (orders 3..5), TTV or TTM
+        (order 3; fibers are runs of equal (i, j))."""
+        self = cls.__new__(cls)
+        self.ptr = _P()
+        self.op = op
+        self.rank = rank
+        self.dims = tuple(int(x) for x in dims)
+        self.mode = 0
+        d = np.ascontiguousarray(dims, dtype=np.int32)
+        co = np.ascontiguousarray(coords, dtype=np.int32)
+        v = np.ascontiguousarray(vals, dtype=np.float32)
+        self._keep = (d, co, v)
+        check(lib().tt_plan_create_coo(len(d), d.ctypes.data, co.shape[0], co.ctypes.data, v.ctypes.data, op, rank,
+                                       PRECISIONS.get(prec, prec), select, variant, stream, C.byref(self.ptr)))
+        return self
+
+    def ttm(self, Y: "DeviceBuffer", stream=None) -> None:
+        check(lib().tt_plan_ttm(self.ptr, Y.ptr, stream))
+
+    def coo_fibers(self) -> np.ndarray:
+        """(i, j) of every fiber of a COO TTV or TTM plan (nfibers x 2)."""
+        n = self.num_fibers(1 if self.op == OP_TTV else 0)
+        out = np.empty((max(n, 0), 2), dtype=np.int32)
+        if n > 0:
+            check(lib().tt_plan_coo_fibers(self.ptr, out.ctypes.data))
+        return out
 
     @property
     def slabs(self) -> int:

@@ -279,6 +279,14 @@ cudaError_t exclusive_scan(const uint32_t* in, int64_t n, uint32_t* out, uint32_
 }
 
 }  // namespace
+
+// Exclusive scan of n uint32 on the device (out may alias in); *total (host) gets
+// the sum; sums: scratch of scan_scratch_entries(n) uint32.  Synchronises st.
+int64_t scan_scratch_entries(int64_t n) { return (n + kTile - 1) / kTile + 1; }
+cudaError_t device_exclusive_scan(const uint32_t* in, int64_t n, uint32_t* out, uint32_t* sums, uint32_t* total,
+                                  cudaStream_t st) {
+  return exclusive_scan(in, n, out, sums, total, st);
+}
 }  // namespace tt
 
 using namespace tt;

@@ -38,6 +38,7 @@ WalkLauncher walk_launcher_o4_fx16_strip(int cpt, int lpr, int fam);
 WalkLauncher walk_launcher_o5_fp32_strip(int cpt, int lpr, int fam);
 WalkLauncher walk_launcher_o5_fp16_strip(int cpt, int lpr, int fam);
 WalkLauncher walk_launcher_o5_fx16_strip(int cpt, int lpr, int fam);
+WalkLauncher walk_launcher_o2_fp32_strip(int cpt, int lpr, int fam);  // TTM: fibers times one matrix
 // Strip-walk partition: the row (through a.rnz) of every unit boundary, at stride order - 1.
 cudaError_t launch_partition_rows(int order, const WalkArgs& a, cudaStream_t s);
 // A(i, j) = sum over slabs k in order of V(k * vstride + i, j) for i < nrows, FP32 with
@@ -86,6 +87,29 @@ cudaError_t launch_pow2_scales(const float* colmax, int cols, int target_exp, fl
 // src (rows x cols) * scale[col], zero for cols <= j < rp.
 cudaError_t launch_to_16(const float* src, int64_t rows, int cols, int rp, const float* scale, int kind,
                          uint16_t* dst, cudaStream_t s);
+// Exclusive scan of n uint32 on the device (out may alias in); *total (host) gets the
+// sum; sums: scratch of scan_scratch_entries(n) uint32.  Synchronises st.
+int64_t scan_scratch_entries(int64_t n);
+cudaError_t device_exclusive_scan(const uint32_t* in, int64_t n, uint32_t* out, uint32_t* sums, uint32_t* total,
+                                  cudaStream_t st);
+// COO input (tt_coo.cu).  coords: nnz x order int32, row-major, on the device.
+// Check: every coordinate inside its mode and the nonzeros in lexicographic
+// (non-decreasing) order; *err (device, set to UINT64_MAX by the caller) keeps the
+// first violation as (index << 3) | code (1: coordinate out of range, 2: out of order).
+cudaError_t launch_coo_check(const int32_t* coords, int64_t nnz, int order, const int32_t* dims,
+                             unsigned long long* err, cudaStream_t s);
+// out[p] = coords[p * order + col] for p < nnz.
+cudaError_t launch_coo_column(const int32_t* coords, int64_t nnz, int order, int col, int32_t* out, cudaStream_t s);
+// rnz[r] = first nonzero whose mode-0 coordinate is >= r, r = 0..nrows (rows as runs).
+cudaError_t launch_coo_row_starts(const int32_t* coords, int64_t nnz, int order, int64_t nrows, int32_t* rnz,
+                                  cudaStream_t s);
+// flags[p] = 1 where a fiber (a run of equal (mode 0, mode 1) coordinates) starts.
+cudaError_t launch_coo_fiber_flags(const int32_t* coords, int64_t nnz, int order, uint32_t* flags, cudaStream_t s);
+// For fiber starts p (flags[p]): pos[fid[p]] = p, fcoords[2 fid[p] + {0, 1}] = (i, j).
+cudaError_t launch_coo_fibers(const int32_t* coords, int64_t nnz, int order, const uint32_t* flags,
+                              const uint32_t* fid, int32_t* pos, int32_t* fcoords, cudaStream_t s);
+// dst (K x rp, FP32, zero padded) = transpose of U (R x K, row-major).
+cudaError_t launch_transpose_pad(const float* U, int64_t R, int64_t K, int rp, float* dst, cudaStream_t s);
 // dst (rows x rp, FP32) = src (rows x cols), zero padded.
 cudaError_t launch_pad_fp32(const float* src, int64_t rows, int cols, int rp, float* dst, cudaStream_t s);
 // out[j] = prod_m inv_m[j] * vinv   (nm factor inverse-scale arrays, rp entries each)

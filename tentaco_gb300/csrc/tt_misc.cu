@@ -23,6 +23,8 @@ WalkLauncher walk_launcher(int order, int prec, int cpt, int lpr, int staged) {
       if (prec == kBF16F) return walk_launcher_o4_bf16f_strip(cpt, lpr, staged);
       if (prec == kFP16) return walk_launcher_o4_fp16_strip(cpt, lpr, staged);
       if (prec == kFX16) return walk_launcher_o4_fx16_strip(cpt, lpr, staged);
+    } else if (order == 2) {  // TTM (fibers times one matrix): FP32
+      if (prec == kFP32) return walk_launcher_o2_fp32_strip(cpt, lpr, staged);
     } else if (order == 5) {  // five modes: FP32, FP16 and 16-bit fixed point
       if (prec == kFP32) return walk_launcher_o5_fp32_strip(cpt, lpr, staged);
       if (prec == kFP16) return walk_launcher_o5_fp16_strip(cpt, lpr, staged);
@@ -30,7 +32,7 @@ WalkLauncher walk_launcher(int order, int prec, int cpt, int lpr, int staged) {
     }
     return nullptr;
   }
-  if (order > 4) return nullptr;  // five modes: strip walk only
+  if (order > 4 || order < 3) return nullptr;  // five modes and TTM: strip walk only
   if (prec == kFX16) return nullptr;  // 16-bit fixed point: strip walk only
   if (order == 3) {
     if (prec == kFP32) return walk_launcher_o3_fp32(cpt, lpr, staged);

@@ -582,7 +582,9 @@ tt_status set_variant(tt_plan* p, int id) {
   tt_status s = alloc_walk_scratch(p, p->P);
   if (s != TT_OK) return s;
   p->part_ready = false;
-  if ((v.staged == 3 || v.staged == 4) && !p->d_kexp && p->nnz > 0 && (s = build_flat_arrays(p)) != TT_OK) return s;
+  if (p->coo && v.staged != 4) return set_error(TT_ERR_UNSUPPORTED, "COO plans run the strip walk");
+  if ((v.staged == 3 || v.staged == 4) && !p->coo && !p->d_kexp && p->nnz > 0 && (s = build_flat_arrays(p)) != TT_OK)
+    return s;
   if (v.staged == 4 && p->slabs > 1 && !p->d_vrows && p->nnz > 0 &&
       (s = dev_alloc(p, &p->d_vrows, (size_t)p->slabs * (size_t)(p->nroot + 1) * (size_t)p->rp)) != TT_OK)
     return s;
@@ -825,53 +827,102 @@ tt_status run_ttv(tt_plan* p, const float* x, float* y, cudaStream_t st) {
 
 tt_status time_variants(tt_plan* p, cudaStream_t st, const std::vector<int>& cands, int max_timed, int extra);
 
+// Values on the device: FP32 as given, or 16-bit with one power-of-two scale
+// (max in [1,2) for BF16, [2^14,2^15) for FP16), found and applied on the device;
+// nvals_alloc - nvals entries of zero padding.
+tt_status upload_values(tt_plan* p, const float* hvals, int64_t nvals, size_t nvals_alloc, cudaStream_t st) {
+  tt_status s;
+  p->nvals_alloc = nvals_alloc;
+  const size_t n = nvals_alloc;
+  if (val_kind(p->prec) != kF32) {
+    // values: one power-of-two scale (max in [1,2) for BF16, [2^14,2^15) for FP16),
+    // found and applied on the device (absolute max, scale, round-to-nearest-even)
+    const bool h16 = p->prec == kFP16;
+    p->vinv = h16 ? 1.f / 16384.f : 1.f;  // (no values: never used)
+    uint16_t* d = nullptr;
+    if ((s = dev_alloc(p, &d, n)) != TT_OK) return s;
+    p->d_vals = d;
+    if (n > (size_t)nvals && cudaMemsetAsync(d + nvals, 0, (n - (size_t)nvals) * 2, st) != cudaSuccess)
+      return (set_error(TT_ERR_CUDA, "clear vals"));
+    if (nvals > 0) {
+      float* tmp = nullptr;
+      if (pool_alloc((void**)&tmp, (size_t)nvals * 4 + 64, st) != cudaSuccess)
+        return (set_error(TT_ERR_OUT_OF_MEMORY, "value staging"));
+      float* cmax = reinterpret_cast<float*>(((uintptr_t)(tmp + nvals) + 15) & ~(uintptr_t)15);
+      float* scl = cmax + 1;
+      float* inv = cmax + 2;
+      float vinv = 1.f;
+      cudaError_t e = cudaMemcpyAsync(tmp, hvals, (size_t)nvals * 4, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = launch_colmax(tmp, nvals, 1, cmax, st);
+      if (e == cudaSuccess) e = launch_pow2_scales(cmax, 1, h16 ? 14 : 0, scl, inv, st);
+      if (e == cudaSuccess) e = launch_to_16(tmp, nvals, 1, 1, scl, h16 ? 2 : 1, d, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&vinv, inv, 4, cudaMemcpyDeviceToHost, st);
+      cudaFreeAsync(tmp, st);
+      const cudaError_t e2 = cudaStreamSynchronize(st);
+      if (e != cudaSuccess || e2 != cudaSuccess)
+        return (set_error(TT_ERR_CUDA, "value conversion: %s", cudaGetErrorString(e != cudaSuccess ? e : e2)));
+      p->vinv = vinv;
+    }
+  } else {
+    float* d = nullptr;
+    if ((s = dev_alloc(p, &d, n)) != TT_OK) return s;
+    p->d_vals = d;
+    if (n > (size_t)nvals && cudaMemsetAsync(d + nvals, 0, (n - (size_t)nvals) * 4, st) != cudaSuccess)
+      return (set_error(TT_ERR_CUDA, "clear vals"));
+    if (nvals > 0 && cudaMemcpyAsync(d, hvals, (size_t)nvals * 4, cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return (set_error(TT_ERR_CUDA, "upload vals"));
+  }
+  return TT_OK;
+}
+
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
 // public API
 // ---------------------------------------------------------------------------
 TT_EXPORT const char* tt_status_string(tt_status s) {
-  switch (s) {
-    case TT_OK: return "TT_OK";
-    case TT_ERR_INVALID_ARGUMENT: return "TT_ERR_INVALID_ARGUMENT";
-    case TT_ERR_INVALID_CSF: return "TT_ERR_INVALID_CSF";
-    case TT_ERR_UNSUPPORTED: return "TT_ERR_UNSUPPORTED";
-    case TT_ERR_CUDA: return "TT_ERR_CUDA";
-    case TT_ERR_OUT_OF_MEMORY: return "TT_ERR_OUT_OF_MEMORY";
-    case TT_ERR_NO_DEVICE: return "TT_ERR_NO_DEVICE";
-    case TT_ERR_DEVICE_WAIT: return "TT_ERR_DEVICE_WAIT";
-  }
-  return "TT_ERR_UNKNOWN";
+switch (s) {
+  case TT_OK: return "TT_OK";
+  case TT_ERR_INVALID_ARGUMENT: return "TT_ERR_INVALID_ARGUMENT";
+  case TT_ERR_INVALID_CSF: return "TT_ERR_INVALID_CSF";
+  case TT_ERR_UNSUPPORTED: return "TT_ERR_UNSUPPORTED";
+  case TT_ERR_CUDA: return "TT_ERR_CUDA";
+  case TT_ERR_OUT_OF_MEMORY: return "TT_ERR_OUT_OF_MEMORY";
+  case TT_ERR_NO_DEVICE: return "TT_ERR_NO_DEVICE";
+  case TT_ERR_DEVICE_WAIT: return "TT_ERR_DEVICE_WAIT";
+}
+return "TT_ERR_UNKNOWN";
 }
 
 TT_EXPORT int32_t tt_abi_version(void) { return TT_ABI_VERSION; }
 TT_EXPORT int32_t tt_num_variants(void) { return kNumVariants; }
 
 TT_EXPORT tt_status tt_variant_get(int32_t id, tt_variant_info* info) {
-  clear_error();
-  if (!info || id < 0 || id >= kNumVariants) return set_error(TT_ERR_INVALID_ARGUMENT, "variant %d", id);
-  VariantSpec v = variant_spec(id);
-  std::memset(info, 0, sizeof(*info));
-  info->id = id;
-  info->threads = v.tb;
-  info->cols_per_lane = v.cpt;
-  info->nnz_per_team = v.G;
-  info->rank_pad = 32;
-  info->lanes_per_row = 32 / v.cpt;
-  info->nnz_per_block = v.tb / info->lanes_per_row * v.G;
-  info->staged = v.staged;
-  static const char* fam[kFamilies] = {"lean", "stage", "tma", "flat", "strip"};
-  if (v.staged == 0 || v.staged == 3 || v.staged == 4) {  // lean / flat / strip: 256-thread blocks, budget for b resident blocks per SM
-    info->threads = 256;
-    info->nnz_per_block = 256 / info->lanes_per_row * v.G;
-    std::snprintf(info->name, sizeof(info->name), "%s_b%d_g%d_c%d", fam[v.staged], lean_blocks(v), v.G, v.cpt);
-  } else if (v.staged == 2) {  // TMA gather: 256-thread blocks, s stages in flight per warp
-    info->threads = 256;
-    info->nnz_per_block = 256 / info->lanes_per_row * v.G;
-    std::snprintf(info->name, sizeof(info->name), "tma_s%d_g%d_c%d", tma_stages(v), v.G, v.cpt);
-  } else {
-    std::snprintf(info->name, sizeof(info->name), "%s_t%d_g%d_c%d", fam[v.staged], v.tb, v.G, v.cpt);
-  }
+clear_error();
+if (!info || id < 0 || id >= kNumVariants) return set_error(TT_ERR_INVALID_ARGUMENT, "variant %d", id);
+VariantSpec v = variant_spec(id);
+std::memset(info, 0, sizeof(*info));
+info->id = id;
+info->threads = v.tb;
+info->cols_per_lane = v.cpt;
+info->nnz_per_team = v.G;
+info->rank_pad = 32;
+info->lanes_per_row = 32 / v.cpt;
+info->nnz_per_block = v.tb / info->lanes_per_row * v.G;
+info->staged = v.staged;
+static const char* fam[kFamilies] = {"lean", "stage", "tma", "flat", "strip"};
+if (v.staged == 0 || v.staged == 3 || v.staged == 4) {  // lean / flat / strip: 256-thread blocks, budget for b resident blocks per SM
+  info->threads = 256;
+  info->nnz_per_block = 256 / info->lanes_per_row * v.G;
+  std::snprintf(info->name, sizeof(info->name), "%s_b%d_g%d_c%d", fam[v.staged], lean_blocks(v), v.G, v.cpt);
+} else if (v.staged == 2) {  // TMA gather: 256-thread blocks, s stages in flight per warp
+  info->threads = 256;
+  info->nnz_per_block = 256 / info->lanes_per_row * v.G;
+  std::snprintf(info->name, sizeof(info->name), "tma_s%d_g%d_c%d", tma_stages(v), v.G, v.cpt);
+} else {
+  std::snprintf(info->name, sizeof(info->name), "%s_t%d_g%d_c%d", fam[v.staged], v.tb, v.G, v.cpt);
+}
   return TT_OK;
 }
 
@@ -1034,48 +1085,7 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
       return fail(set_error(TT_ERR_CUDA, "upload root crd"));
     p->slab[0].crd[0] = p->d_crd[0];
   }
-  p->nvals_alloc = nvals_alloc;
-  {
-    const size_t n = nvals_alloc;
-    if (val_kind(p->prec) != kF32) {
-      // values: one power-of-two scale (max in [1,2) for BF16, [2^14,2^15) for FP16),
-      // found and applied on the device (absolute max, scale, round-to-nearest-even)
-      const bool h16 = p->prec == kFP16;
-      p->vinv = h16 ? 1.f / 16384.f : 1.f;  // (no values: never used)
-      uint16_t* d = nullptr;
-      if ((s = dev_alloc(p, &d, n)) != TT_OK) return fail(s);
-      p->d_vals = d;
-      if (n > (size_t)nvals && cudaMemsetAsync(d + nvals, 0, (n - (size_t)nvals) * 2, st) != cudaSuccess)
-        return fail(set_error(TT_ERR_CUDA, "clear vals"));
-      if (nvals > 0) {
-        float* tmp = nullptr;
-        if (pool_alloc((void**)&tmp, (size_t)nvals * 4 + 64, st) != cudaSuccess)
-          return fail(set_error(TT_ERR_OUT_OF_MEMORY, "value staging"));
-        float* cmax = reinterpret_cast<float*>(((uintptr_t)(tmp + nvals) + 15) & ~(uintptr_t)15);
-        float* scl = cmax + 1;
-        float* inv = cmax + 2;
-        float vinv = 1.f;
-        cudaError_t e = cudaMemcpyAsync(tmp, hvals, (size_t)nvals * 4, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = launch_colmax(tmp, nvals, 1, cmax, st);
-        if (e == cudaSuccess) e = launch_pow2_scales(cmax, 1, h16 ? 14 : 0, scl, inv, st);
-        if (e == cudaSuccess) e = launch_to_16(tmp, nvals, 1, 1, scl, h16 ? 2 : 1, d, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(&vinv, inv, 4, cudaMemcpyDeviceToHost, st);
-        cudaFreeAsync(tmp, st);
-        const cudaError_t e2 = cudaStreamSynchronize(st);
-        if (e != cudaSuccess || e2 != cudaSuccess)
-          return fail(set_error(TT_ERR_CUDA, "value conversion: %s", cudaGetErrorString(e != cudaSuccess ? e : e2)));
-        p->vinv = vinv;
-      }
-    } else {
-      float* d = nullptr;
-      if ((s = dev_alloc(p, &d, n)) != TT_OK) return fail(s);
-      p->d_vals = d;
-      if (n > (size_t)nvals && cudaMemsetAsync(d + nvals, 0, (n - (size_t)nvals) * 4, st) != cudaSuccess)
-        return fail(set_error(TT_ERR_CUDA, "clear vals"));
-      if (nvals > 0 && cudaMemcpyAsync(d, hvals, (size_t)nvals * 4, cudaMemcpyHostToDevice, st) != cudaSuccess)
-        return fail(set_error(TT_ERR_CUDA, "upload vals"));
-    }
-  }
+  if ((s = upload_values(p, hvals, nvals, nvals_alloc, st)) != TT_OK) return fail(s);
   // MTTKRP scratch is sized with the variant; TTV keeps one ticket per block, zeroed once here
   if (op == TT_OP_MTTKRP) {
     if ((s = dev_alloc(p, &p->d_err, 4)) != TT_OK) return fail(s);
@@ -1156,6 +1166,187 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
   return TT_OK;
 }
 
+// ---------------------------------------------------------------------------
+// plans over sorted COO input (the reference's MATLAB interface,
+// tensor_kernels/fmtaco.cpp: TTV 32-115, TTM 117-223, MTTKRP 741-780)
+// ---------------------------------------------------------------------------
+TT_EXPORT tt_status tt_plan_create_coo(int32_t order, const int32_t* dims, int64_t nnz, const int32_t* coords,
+                                       const float* vals, tt_op op, int32_t rank, tt_precision prec,
+                                       tt_select select, int32_t variant, void* stream, tt_plan** out) {
+  clear_error();
+  if (!out || !dims || (nnz > 0 && (!coords || !vals)) || nnz < 0)
+    return set_error(TT_ERR_INVALID_ARGUMENT, "null argument or negative nonzero count");
+  *out = nullptr;
+  if (op == TT_OP_MTTKRP) {
+    if (order < 3 || order > 5) return set_error(TT_ERR_UNSUPPORTED, "COO MTTKRP needs order 3, 4 or 5 (got %d)", order);
+  } else if (op == TT_OP_TTV || op == TT_OP_TTM) {
+    if (order != 3) return set_error(TT_ERR_UNSUPPORTED, "COO TTV and TTM take three-mode tensors (got order %d)", order);
+  } else {
+    return set_error(TT_ERR_INVALID_ARGUMENT, "op %d", (int)op);
+  }
+  if (op != TT_OP_TTV && (rank < 1 || rank > TT_MAX_RANK))
+    return set_error(TT_ERR_UNSUPPORTED, "rank %d (supported 1..%d)", rank, TT_MAX_RANK);
+  if (prec < TT_PREC_FP32 || prec > TT_PREC_FX16) return set_error(TT_ERR_INVALID_ARGUMENT, "precision %d", (int)prec);
+  if (op == TT_OP_TTM && prec != TT_PREC_FP32) return set_error(TT_ERR_UNSUPPORTED, "COO TTM runs in FP32 storage");
+  if (op == TT_OP_TTV && prec == TT_PREC_FX16)
+    return set_error(TT_ERR_UNSUPPORTED, "TTV does not take 16-bit fixed-point storage");
+  if (nnz >= INT32_MAX) return set_error(TT_ERR_UNSUPPORTED, "%lld nonzeros (at most 2^31 - 2)", (long long)nnz);
+  for (int m = 0; m < order; m++)
+    if (dims[m] < 1) return set_error(TT_ERR_INVALID_ARGUMENT, "dims[%d] = %d", m, dims[m]);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return set_error(TT_ERR_NO_DEVICE, "no CUDA device visible");
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  auto* p = new tt_plan();
+  auto fail = [&](tt_status s2) { tt_plan_destroy(p); return s2; };
+  cudaGetDevice(&p->device);
+  p->coo = true;
+  p->op = op;
+  p->order = order;
+  for (int m = 0; m < order; m++) p->dims[m] = dims[m];
+  p->nnz = nnz;
+  p->nroot = dims[0];
+  p->dense_root = true;
+  p->rank = op == TT_OP_TTV ? 1 : rank;
+  p->rp = op == TT_OP_TTV ? 1 : rank_pad(rank);
+  p->prec = (int)prec;
+  p->stream = st;
+  p->slabs = 1;
+  p->leaf_len = nnz;
+  tt_status s;
+  // coordinates and dims on the device, checked there (range and lexicographic order)
+  int32_t *dco = nullptr, *ddims = nullptr;
+  unsigned long long* derr = nullptr;
+  struct Tmp {
+    cudaStream_t st;
+    std::vector<void*> v;
+    ~Tmp() {
+      for (void* q : v) cudaFreeAsync(q, st);
+      cudaStreamSynchronize(st);
+    }
+  } tmp{st, {}};
+  auto talloc = [&](void** ptr, size_t bytes) -> tt_status {
+    if (pool_alloc(ptr, bytes < 16 ? 16 : bytes, st) != cudaSuccess)
+      return set_error(TT_ERR_OUT_OF_MEMORY, "COO staging of %zu bytes", bytes);
+    tmp.v.push_back(*ptr);
+    return TT_OK;
+  };
+  if ((s = talloc((void**)&dco, sizeof(int32_t) * (size_t)nnz * order)) != TT_OK) return fail(s);
+  if ((s = talloc((void**)&ddims, sizeof(int32_t) * TT_MAX_ORDER)) != TT_OK) return fail(s);
+  if ((s = talloc((void**)&derr, sizeof(unsigned long long))) != TT_OK) return fail(s);
+  unsigned long long herr = ~0ull;
+  if (nnz > 0 && cudaMemcpyAsync(dco, coords, sizeof(int32_t) * (size_t)nnz * order, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return fail(set_error(TT_ERR_CUDA, "upload coordinates"));
+  if (cudaMemcpyAsync(ddims, dims, sizeof(int32_t) * order, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(derr, &herr, sizeof(herr), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      launch_coo_check(dco, nnz, order, ddims, derr, st) != cudaSuccess ||
+      cudaMemcpyAsync(&herr, derr, sizeof(herr), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return fail(set_error(TT_ERR_CUDA, "COO check: %s", cudaGetErrorString(cudaGetLastError())));
+  if (herr != ~0ull)
+    return fail(set_error(TT_ERR_INVALID_ARGUMENT, "COO nonzero %llu: %s", herr >> 3,
+                          (herr & 7) == 1 ? "coordinate outside its mode"
+                                          : "out of lexicographic order (sort the coordinates)"));
+  if ((s = upload_values(p, vals, nnz, (size_t)pad16(nnz), st)) != TT_OK) return fail(s);
+  auto column = [&](int col, int32_t** dst) -> tt_status {
+    const size_t np = (size_t)pad16(nnz);
+    tt_status s2 = dev_alloc(p, dst, np);
+    if (s2 != TT_OK) return s2;
+    if (cudaMemsetAsync(*dst, 0, sizeof(int32_t) * np, st) != cudaSuccess ||
+        launch_coo_column(dco, nnz, order, col, *dst, st) != cudaSuccess)
+      return set_error(TT_ERR_CUDA, "COO column %d", col);
+    return TT_OK;
+  };
+  if (op == TT_OP_MTTKRP) {
+    // the leaf and upper coordinates are the COO columns; rows are runs of mode 0
+    const int L = order - 1;
+    if ((s = column(L, &p->d_crd[L])) != TT_OK) return fail(s);
+    if ((s = column(1, &p->d_kexp)) != TT_OK) return fail(s);
+    if (order >= 4 && (s = column(2, &p->d_kexp2)) != TT_OK) return fail(s);
+    if (order == 5 && (s = column(3, &p->d_kexp3)) != TT_OK) return fail(s);
+    if ((s = dev_alloc(p, &p->d_rnz, (size_t)dims[0] + 1)) != TT_OK) return fail(s);
+    if (launch_coo_row_starts(dco, nnz, order, dims[0], p->d_rnz, st) != cudaSuccess)
+      return fail(set_error(TT_ERR_CUDA, "COO rows"));
+  } else {
+    // fibers: runs of equal (i, j)
+    uint32_t *flags = nullptr, *sums = nullptr;
+    uint32_t nfib = 0;
+    if ((s = talloc((void**)&flags, sizeof(uint32_t) * ((size_t)nnz + 1))) != TT_OK) return fail(s);
+    if ((s = talloc((void**)&sums, sizeof(uint32_t) * (size_t)scan_scratch_entries(nnz + 1))) != TT_OK) return fail(s);
+    if (launch_coo_fiber_flags(dco, nnz, order, flags, st) != cudaSuccess)
+      return fail(set_error(TT_ERR_CUDA, "COO fiber flags"));
+    uint32_t* fid = nullptr;
+    if ((s = talloc((void**)&fid, sizeof(uint32_t) * ((size_t)nnz + 1))) != TT_OK) return fail(s);
+    if (nnz > 0 && device_exclusive_scan(flags, nnz, fid, sums, &nfib, st) != cudaSuccess)
+      return fail(set_error(TT_ERR_CUDA, "COO fiber scan"));
+    int32_t* fpos = nullptr;
+    if ((s = dev_alloc(p, &fpos, (size_t)nfib + 1)) != TT_OK) return fail(s);
+    if ((s = dev_alloc(p, &p->d_fcoords, (size_t)nfib * 2)) != TT_OK) return fail(s);
+    const int32_t end = (int32_t)nnz;
+    if (launch_coo_fibers(dco, nnz, order, flags, fid, fpos, p->d_fcoords, st) != cudaSuccess ||
+        cudaMemcpyAsync(fpos + nfib, &end, sizeof(int32_t), cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return fail(set_error(TT_ERR_CUDA, "COO fibers"));
+    int32_t* leaf = nullptr;
+    if ((s = column(2, &leaf)) != TT_OK) return fail(s);
+    if (op == TT_OP_TTV) {
+      p->d_pos[2] = fpos;
+      p->d_crd[2] = leaf;
+      p->nfib_last = nfib;
+      p->count[1] = nfib;
+      p->count[2] = nnz;
+    } else {
+      // TTM: a two-level walk, the fibers as rows and the leaf coordinates as its
+      // one factor's rows
+      p->order = 2;
+      p->dims[0] = (int32_t)nfib;
+      p->dims[1] = dims[2];
+      p->nroot = nfib;
+      p->d_rnz = fpos;
+      p->d_crd[1] = leaf;
+      p->count[0] = nfib;
+      p->count[1] = nnz;
+    }
+  }
+  for (int l = 0; l < TT_MAX_ORDER; l++) { p->slab[0].pos[l] = p->d_pos[l]; p->slab[0].crd[l] = p->d_crd[l]; }
+  p->slab[0].nnz = nnz;
+  if (op == TT_OP_TTV) {
+    p->tb = 256;
+    p->G = kTtvNpt;
+    p->P = 32 * kTtvNpt;
+    p->nblocks = (int)((p->nnz + p->P - 1) / p->P);
+    if ((s = alloc_walk_scratch(p, p->P)) != TT_OK) return fail(s);
+    if ((s = prepare_partition(p)) != TT_OK) return fail(s);
+  } else {
+    if ((s = dev_alloc(p, &p->d_err, 4)) != TT_OK) return fail(s);
+    if (cudaMemsetAsync(p->d_err, 0, 4 * sizeof(int32_t), st) != cudaSuccess)
+      return fail(set_error(TT_ERR_CUDA, "clear error word"));
+    // the strip family only (no CSF levels): the fixed variant, the strip rule, or
+    // a sweep over the strip variants (the learned network scores CSF plans)
+    int id;
+    if (select == TT_SELECT_FIXED) {
+      if (!variant_valid(variant, p->order, p->rank, p->prec) || variant_spec(variant).staged != 4)
+        return fail(set_error(TT_ERR_INVALID_ARGUMENT, "variant %d is not a strip variant valid here", variant));
+      id = variant;
+    } else {
+      id = strip_default_variant(p->order, p->rank, p->prec);
+    }
+    if (id < 0) return fail(set_error(TT_ERR_UNSUPPORTED, "no strip variant for order %d rank %d", p->order, p->rank));
+    if ((s = use_variant(p, id)) != TT_OK) return fail(s);
+    if (select == TT_SELECT_SWEEP) {
+      std::vector<int> all;
+      for (int v = 4 * kPerFamily; v < kNumVariants; v++)
+        if (variant_valid(v, p->order, p->rank, p->prec)) all.push_back(v);
+      if ((s = time_variants(p, st, all, kNumVariants, -1)) != TT_OK) return fail(s);
+      p->selected_by = 2;
+    }
+  }
+  if (cudaStreamSynchronize(st) != cudaSuccess) return fail(set_error(TT_ERR_CUDA, "COO plan: %s", cudaGetErrorString(cudaGetLastError())));
+  *out = p;
+  return TT_OK;
+}
+
 TT_EXPORT tt_status tt_plan_destroy(tt_plan* p) {
   if (!p) return TT_OK;
   if (p->ev0) cudaEventDestroy(p->ev0);
@@ -1174,9 +1365,26 @@ TT_EXPORT tt_status tt_plan_destroy(tt_plan* p) {
 TT_EXPORT tt_status tt_plan_set_factors(tt_plan* p, const float* const* factors, void* stream) {
   clear_error();
   if (!p || !factors) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
-  if (p->op != TT_OP_MTTKRP) return set_error(TT_ERR_INVALID_ARGUMENT, "plan is not an MTTKRP plan");
+  if (p->op != TT_OP_MTTKRP && p->op != TT_OP_TTM)
+    return set_error(TT_ERR_INVALID_ARGUMENT, "plan is not an MTTKRP or TTM plan");
   cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
   const int nm = p->order - 1;
+  if (p->op == TT_OP_TTM) {
+    // U is rank x K row-major (the reference's C, fmtaco.cpp:117-223): the walk
+    // gathers its columns as rows of U^T, K x RP, zero padded
+    if (!factors[0]) return set_error(TT_ERR_INVALID_ARGUMENT, "U is null");
+    tt_status s2;
+    if (!p->fac_own[0]) {
+      float* d = nullptr;
+      if ((s2 = dev_alloc(p, &d, (size_t)p->dims[1] * p->rp)) != TT_OK) return s2;
+      p->fac_own[0] = d;
+    }
+    CK(launch_transpose_pad(factors[0], p->rank, p->dims[1], p->rp, (float*)p->fac_own[0], st));
+    p->fac[0] = p->fac_own[0];
+    p->d_colscale = nullptr;
+    p->factors_set = true;
+    return TT_OK;
+  }
   for (int m = 0; m < nm; m++)
     if (!factors[m]) return set_error(TT_ERR_INVALID_ARGUMENT, "factor %d is null", m + 1);
   tt_status s;
@@ -1280,6 +1488,30 @@ TT_EXPORT tt_status tt_plan_mttkrp(tt_plan* p, float* A, void* stream) {
   if ((s = timed_begin(p, st)) != TT_OK) return s;
   if ((s = run_mttkrp(p, A, st)) != TT_OK) return s;
   return timed_end(p, st);
+}
+
+// TTM of a COO plan: Y (nfibers x rank, DEVICE) from the U last set.
+TT_EXPORT tt_status tt_plan_ttm(tt_plan* p, float* Y, void* stream) {
+  clear_error();
+  if (!p || !Y) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
+  if (p->op != TT_OP_TTM) return set_error(TT_ERR_INVALID_ARGUMENT, "plan is not a TTM plan");
+  if (!p->factors_set) return set_error(TT_ERR_INVALID_ARGUMENT, "U not set (tt_plan_set_factors)");
+  cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+  tt_status s;
+  if ((s = timed_begin(p, st)) != TT_OK) return s;
+  if ((s = run_mttkrp(p, Y, st)) != TT_OK) return s;
+  return timed_end(p, st);
+}
+
+// (i, j) of every fiber of a COO TTV or TTM plan, as 2 * nfibers int32 on the host.
+TT_EXPORT tt_status tt_plan_coo_fibers(const tt_plan* p, int32_t* ij) {
+  clear_error();
+  if (!p || !ij) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
+  if (!p->coo || (p->op != TT_OP_TTV && p->op != TT_OP_TTM))
+    return set_error(TT_ERR_INVALID_ARGUMENT, "not a COO TTV or TTM plan");
+  const int64_t nf = p->op == TT_OP_TTV ? p->nfib_last : p->nroot;
+  if (nf > 0) CK(cudaMemcpy(ij, p->d_fcoords, sizeof(int32_t) * 2 * (size_t)nf, cudaMemcpyDeviceToHost));
+  return TT_OK;
 }
 
 TT_EXPORT tt_status tt_plan_ttv(tt_plan* p, const float* x, float* y, void* stream) {

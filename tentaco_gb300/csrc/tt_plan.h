@@ -85,6 +85,10 @@ struct tt_plan {
   // slabs * (nroot + 1) virtual rows (row nroot of each slab holds its padding),
   // written here and summed into the output by launch_virtual_rows
   float* d_vrows = nullptr;
+  // plans over sorted COO input (tt_plan_create_coo): the walk streams the COO
+  // columns directly, rows (MTTKRP) or fibers (TTV, TTM) are runs of coordinates
+  bool coo = false;
+  int32_t* d_fcoords = nullptr;  // TTV / TTM: (i, j) of every fiber
   int slabs = 1;
   int mode = 0;  // output mode (the plan's tensor is re-rooted at it when not 0)
   int gpol = 0;  // WalkArgs::gpol

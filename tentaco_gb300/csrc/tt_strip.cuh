@@ -4,6 +4,8 @@
 //   A(i,:) = sum_{k,l}   B(i,k,l)   C(k,:) .* D(l,:)             (order 3)
 //   A(i,:) = sum_{k,l,m} B(i,k,l,m) C(k,:) .* D(l,:) .* E(m,:)    (order 4)
 //   A(i,:) = sum B(i,k,l,m,n) C(k,:) .* D(l,:) .* E(m,:) .* F(n,:)  (order 5)
+//   Y(f,:) = sum_l B(f,l) U(:,l)                                   (order 2: TTM,
+//            the rows being a 3-mode tensor's fibers and U^T the one factor)
 //
 // Every nonzero carries its upper coordinates (kexp, kexp2, kexp3: built once per plan),
 // so a nonzero is one independent product of gathered factor rows, the reference's
@@ -133,9 +135,12 @@ struct Strip {
                                        const int32_t* s_k3, const unsigned char* s_v, int p0) const {
     int32_t l[U], k[U], k2[U], k3[U];
     if constexpr (U == 4) {
-      const int4 a = *reinterpret_cast<const int4*>(s_l + p0), c = *reinterpret_cast<const int4*>(s_k + p0);
+      const int4 a = *reinterpret_cast<const int4*>(s_l + p0);
       l[0] = a.x; l[1] = a.y; l[2] = a.z; l[3] = a.w;
-      k[0] = c.x; k[1] = c.y; k[2] = c.z; k[3] = c.w;
+      if constexpr (ORDER >= 3) {
+        const int4 c = *reinterpret_cast<const int4*>(s_k + p0);
+        k[0] = c.x; k[1] = c.y; k[2] = c.z; k[3] = c.w;
+      }
       if constexpr (ORDER >= 4) {
         const int4 e = *reinterpret_cast<const int4*>(s_k2 + p0);
         k2[0] = e.x; k2[1] = e.y; k2[2] = e.z; k2[3] = e.w;
@@ -145,8 +150,12 @@ struct Strip {
         k3[0] = e.x; k3[1] = e.y; k3[2] = e.z; k3[3] = e.w;
       }
     } else if constexpr (U == 2) {
-      const int2 a = *reinterpret_cast<const int2*>(s_l + p0), c = *reinterpret_cast<const int2*>(s_k + p0);
-      l[0] = a.x; l[1] = a.y; k[0] = c.x; k[1] = c.y;
+      const int2 a = *reinterpret_cast<const int2*>(s_l + p0);
+      l[0] = a.x; l[1] = a.y;
+      if constexpr (ORDER >= 3) {
+        const int2 c = *reinterpret_cast<const int2*>(s_k + p0);
+        k[0] = c.x; k[1] = c.y;
+      }
       if constexpr (ORDER >= 4) {
         const int2 e = *reinterpret_cast<const int2*>(s_k2 + p0);
         k2[0] = e.x; k2[1] = e.y;
@@ -156,7 +165,8 @@ struct Strip {
         k3[0] = e.x; k3[1] = e.y;
       }
     } else {
-      l[0] = s_l[p0]; k[0] = s_k[p0];
+      l[0] = s_l[p0];
+      if constexpr (ORDER >= 3) k[0] = s_k[p0];
       if constexpr (ORDER >= 4) k2[0] = s_k2[p0];
       if constexpr (ORDER == 5) k3[0] = s_k3[p0];
     }
@@ -174,7 +184,7 @@ struct Strip {
     }
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      strip_piece<UB, true>(fc + (uint64_t)(uint32_t)k[u] * URB, pol_u, b.c[u]);
+      if constexpr (ORDER >= 3) strip_piece<UB, true>(fc + (uint64_t)(uint32_t)k[u] * URB, pol_u, b.c[u]);
       if constexpr (ORDER >= 4) strip_piece<UB, true>(fm + (uint64_t)(uint32_t)k2[u] * URB, pol_u, b.m[u]);
       if constexpr (ORDER == 5) strip_piece<UB, true>(fe + (uint64_t)(uint32_t)k3[u] * URB, pol_u, b.e[u]);
       strip_piece<LB, false>(fd + (uint64_t)(uint32_t)l[u] * LRB, pol_l, b.d[u]);
@@ -193,7 +203,13 @@ struct Strip {
   // acc += product of nonzero u of the batch
   __device__ __forceinline__ static void add(float (&acc)[CPT], const Batch& b, int u) {
     const float v = value(b, u);
-    if constexpr (K::U != kF32) {
+    if constexpr (ORDER == 2) {
+      // one factor: acc += v * d (FP32 storage)
+      static_assert(K::U == kF32 && K::L == kF32, "the two-level walk (TTM) is built for FP32 storage");
+#pragma unroll
+      for (int j = 0; j < CPT / 2; j++)
+        ffma2(acc[2 * j], acc[2 * j + 1], v, v, __uint_as_float(b.d[u][2 * j]), __uint_as_float(b.d[u][2 * j + 1]));
+    } else if constexpr (K::U != kF32) {
       // 16-bit upper and leaf rows of one kind: c * d (and v * m, or v converted
       // times m) exact in FP32, then one FMA per column
       constexpr int FK = K::U;
@@ -322,7 +338,7 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_strip_kernel(const __grid_co
     const uint64_t polF = policy_evict_first();
     const int n4 = (cnt + 3) >> 2;
     strip_stage(a.crd[ORDER - 1] + ustart, s_l, n4, lane, polF);
-    strip_stage(a.kexp + ustart, s_k, n4, lane, polF);
+    if constexpr (ORDER >= 3) strip_stage(a.kexp + ustart, s_k, n4, lane, polF);
     if constexpr (ORDER >= 4) strip_stage(a.kexp2 + ustart, s_k2, n4, lane, polF);
     if constexpr (ORDER == 5) strip_stage(a.kexp3 + ustart, s_k3, n4, lane, polF);
     strip_stage(static_cast<const unsigned char*>(a.vals) + ustart * VB, s_v, (cnt * VB + 15) >> 4, lane, polF);
@@ -330,7 +346,7 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_strip_kernel(const __grid_co
     // later), so their coordinates must be valid rows
     for (int p = 4 * n4 + lane; p < (cnt + STEP - 1) / STEP * STEP; p += 32) {
       s_l[p] = 0;
-      s_k[p] = 0;
+      if constexpr (ORDER >= 3) s_k[p] = 0;
       if constexpr (ORDER >= 4) s_k2[p] = 0;
       if constexpr (ORDER == 5) s_k3[p] = 0;
     }

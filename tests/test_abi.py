@@ -165,3 +165,16 @@ def test_last_error_is_per_thread():
     for th in threads:
         th.join()
     assert not errors, errors
+
+
+def test_coo_plan_argument_checks_before_the_device():
+    """COO plans refuse what they have no kernels for before touching a device."""
+    d = np.array([4, 4, 4, 4, 4, 4], np.int32)
+    co = np.zeros((1, 6), np.int32)
+    for order, op in ((2, tt.OP_MTTKRP), (6, tt.OP_MTTKRP), (4, tt.OP_TTV), (4, tt.OP_TTM)):
+        with pytest.raises(tt.TTError) as e:
+            tt.Plan.from_coo(d[:order], co[:, :order], np.ones(1, np.float32), op=op)
+        assert e.value.status == tt.TT_ERR_UNSUPPORTED
+    with pytest.raises(tt.TTError) as e:
+        tt.Plan.from_coo(d[:3], co[:, :3], np.ones(1, np.float32), op=tt.OP_TTM, prec="fp16")
+    assert e.value.status == tt.TT_ERR_UNSUPPORTED
