@@ -328,7 +328,9 @@ WalkArgs ttv_args(const tt_plan* p, const float* x, float* y);
 tt_status prepare_partition(tt_plan* p) {
   p->part_ready = false;
   p->part_ms = 0.f;
-  if ((p->slabs != 1 && !(p->op == TT_OP_MTTKRP && p->staged == 4)) || p->nnz == 0) return TT_OK;
+  // the strip walk (MTTKRP and COO TTM plans) partitions by rows through rnz
+  const bool strip = p->op != TT_OP_TTV && p->staged == 4;
+  if ((p->slabs != 1 && !strip) || p->nnz == 0) return TT_OK;
   const WalkArgs a = p->op == TT_OP_TTV ? ttv_args(p, nullptr, nullptr) : walk_args(p, nullptr, 0);
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
@@ -337,8 +339,8 @@ tt_status prepare_partition(tt_plan* p) {
     return set_error(TT_ERR_CUDA, "partition timer");
   }
   cudaError_t e = cudaEventRecord(e0, p->stream);
-  if (e == cudaSuccess) e = p->op == TT_OP_MTTKRP && p->staged == 4 ? launch_partition_rows(p->order, a, p->stream)
-                                                                     : launch_partition(p->op == TT_OP_TTV ? 2 : p->order, a, p->stream);
+  if (e == cudaSuccess) e = strip ? launch_partition_rows(p->order, a, p->stream)
+                                 : launch_partition(p->op == TT_OP_TTV ? 2 : p->order, a, p->stream);
   if (e == cudaSuccess) e = cudaEventRecord(e1, p->stream);
   if (e == cudaSuccess) e = cudaEventSynchronize(e1);
   float ms = 0.f;
