@@ -319,6 +319,24 @@ tt_status tt_csf_validate(const taco_tensor_t* B);
 tt_status tt_csf_reroot(const taco_tensor_t* B, int32_t mode, taco_tensor_t** out);
 void tt_tensor_free(taco_tensor_t* t);
 
+/* ---- Test hooks (process-wide; failure-detection tests, off by default) ----
+ * tt_debug_tma_wait: withhold != 0 makes the TMA walk (variant family 2) arm each
+ * stage's barrier without issuing the stage's copy, so that its first wait runs out
+ * after wait_ns nanoseconds (0: the default 5 ms; at most 10^9).  The call then
+ * records device error 301 (tt_plan_device_error; TT_ERR_DEVICE_WAIT from
+ * tt_mttkrp_host), leaves A incomplete and the context usable.  Applies to launches
+ * made after the call; tt_debug_tma_wait(0, 0) restores normal operation.
+ * tt_debug_fail_pool_alloc: the n-th device allocation of the library from now
+ * (n >= 1) fails once, as an out-of-memory condition; 0 disarms.  The environment
+ * variable TT_FAIL_POOL_ALLOC_AT=n arms the same before the library's first
+ * allocation.  A plan whose allocation failed after its creation refuses every later
+ * call but tt_plan_destroy (TT_ERR_INVALID_ARGUMENT).
+ * tt_debug_pool_live: device allocations the library holds right now (plans, their
+ * scratch and one-shot temporaries; not tt_device_malloc buffers). */
+tt_status tt_debug_tma_wait(int32_t withhold, int64_t wait_ns);
+tt_status tt_debug_fail_pool_alloc(int64_t n);
+int64_t tt_debug_pool_live(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -103,6 +103,9 @@ def lib():
         "tt_plan_device_error": (C.c_int32, [_P]),
         "tt_plan_use_variant": (S, [_P, C.c_int32]),
         "tt_plan_sweep_times": (S, [_P, C.POINTER(C.c_float), C.c_int32]),
+        "tt_debug_tma_wait": (S, [C.c_int32, C.c_int64]),
+        "tt_debug_fail_pool_alloc": (S, [C.c_int64]),
+        "tt_debug_pool_live": (C.c_int64, []),
         "tt_mttkrp_host": (S, [_TP, _TP, C.POINTER(_TP), S, S, C.c_int32]),
         "tt_ttv_host": (S, [_TP, _TP, _TP]),
         "tt_csf_from_coo": (S, [C.c_int32, C.POINTER(C.c_int32), C.c_int64, _P, _P, C.POINTER(_TP)]),

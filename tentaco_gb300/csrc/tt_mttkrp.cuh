@@ -72,6 +72,8 @@ struct alignas(64) WalkArgs {
   const int32_t* kexp2;   // flat and strip walks, four or five modes: the level-2 coordinate of every nonzero (padded)
   const int32_t* kexp3;   // strip walk, five modes: the level-3 coordinate of every nonzero (padded)
   const int32_t* rnz;     // flat and strip walks: first nonzero of every row (nrows + 1); null otherwise
+  uint32_t wait_ns;       // TMA walk: bound on each wait for a stage's barrier, ns (0: 5 ms)
+  int32_t tma_withhold;   // TMA walk, test hook: 1 arms every stage's barrier but issues no copy
 };
 
 constexpr int kEmpty = -2;  // summary of a team that owns no nonzeros
@@ -824,10 +826,11 @@ struct Walk {
   // this (teams without nonzeros pass n = 0) because the stage loop is warp-wide.
   //   s_lcw: the warp's coordinate runs (team t at t * (G + 4)); cnt: the warp
   //   tile's nonzeros; nst: stages (ceil(min(G, cnt) / U)); ring/bar_sa: the warp's
-  //   ring and barriers.  A barrier that does not complete within a bounded number
-  //   of probes sets the error word (301) and the warp stops walking.
+  //   ring and barriers.  A barrier that does not complete within a.wait_ns sets
+  //   the error word (301) and the warp stops walking: it waits (bounded again) for
+  //   the copies it has in flight and returns false (warp-uniform) without a summary.
   template <int U, int NS>
-  __device__ __forceinline__ void walk_tma(int s, int n, int team, int nst, const int32_t* s_lcw, int G, int cnt,
+  __device__ __forceinline__ bool walk_tma(int s, int n, int team, int nst, const int32_t* s_lcw, int G, int cnt,
                                            const unsigned char* vt, const int32_t* s_pos,
                                            const int32_t* s_fcrd, int W, int fs, const int32_t* pb,
                                            const int32_t* pn, const unsigned char* ring, uint32_t bar_sa,
@@ -900,7 +903,7 @@ struct Walk {
       const uint32_t bar = bar_sa + (uint32_t)slot * 8u;
       if (lane == 0) mbar_arrive_expect_tx(bar, (uint32_t)(SR * FRB));
       __syncwarp();
-      if (lane < SR / 4) {
+      if (lane < SR / 4 && !a.tma_withhold) {
         int r[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -959,7 +962,7 @@ struct Walk {
         }
       }
     };
-    constexpr uint64_t kWaitNs = 5000000;  // a stage normally lands within microseconds
+    const uint64_t kWaitNs = a.wait_ns ? a.wait_ns : 5000000u;  // a stage normally lands within microseconds
     bool ok = true;
     for (int k = 0; k < NS && k < nst; k++) issue(k);
     int k = 0;
@@ -982,9 +985,9 @@ struct Walk {
       // wait (bounded) for every copy still in flight before the warp leaves
       for (int kk = k; kk < nst && kk < k + NS; kk++)
         mbar_wait_bounded(bar_sa + (uint32_t)(kk % NS) * 8u, (uint32_t)((kk / NS) & 1), kWaitNs);
-      return;
+      return false;
     }
-    if (!active) return;
+    if (!active) return true;
     {
       float cw[CPT];
       piece_cvt(wc, cw);
@@ -1005,6 +1008,7 @@ struct Walk {
 #pragma unroll
       for (int c = 0; c < CPT; c++) X.ta[c] = ra[c];
     }
+    return true;
   }
 
   // Serial walk of nonzeros [s, e) reading only shared memory: values and the
@@ -1265,6 +1269,8 @@ __global__ void __launch_bounds__(256, 2) seg_fold_kernel(const __grid_constant_
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sg = blockIdx.x * (blockDim.x >> 5) + warp;
   if (sg >= num_segments(a.nblocks)) return;
+  // a walk that gave up (error word set) left some units' entries unwritten
+  if (a.err && *reinterpret_cast<volatile const int32_t*>(a.err) != 0) return;
   const int u0 = sg * kSeg, n = min(kSeg, a.nblocks - u0);
   const int rp = a.rp;
   int4 mine = make_int4(-1, -1, 0, 0);
@@ -1369,6 +1375,7 @@ __global__ void __launch_bounds__(256) seg_chain_kernel(const __grid_constant__ 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sg = blockIdx.x * (blockDim.x >> 5) + warp;
   if (sg >= num_segments(a.nblocks)) return;
+  if (a.err && *reinterpret_cast<volatile const int32_t*>(a.err) != 0) return;  // (as seg_fold_kernel)
   const int4 m = reinterpret_cast<const int4*>(a.segmeta)[sg];
   const bool before = m.z & 1, after = m.z & 2, single = m.z & 4;
   if (!after || (single && before)) return;  // warp-uniform: no crossing row starts here
@@ -1792,8 +1799,11 @@ __global__ void __launch_bounds__(256, 1) mttkrp_tma_kernel(const __grid_constan
   const int s = ustart + team * G;
   const int n = s < ustart + cnt ? min(G, ustart + cnt - s) : 0;
   const int nst = (min(G, cnt) + U - 1) / U;
-  wk.template walk_tma<U, NS>(s, n, team, nst, s_lc, G, cnt, s_val + (size_t)team * (G * VB + 16), s_pos, s_fcrd,
-                              W, fs, pb, pn, ring, bar_sa, X);
+  // a wait that ran out (error word 301): no summary, the unit's merge entries are
+  // left unwritten (the merge kernels skip once the error word is set)
+  if (!wk.template walk_tma<U, NS>(s, n, team, nst, s_lc, G, cnt, s_val + (size_t)team * (G * VB + 16), s_pos,
+                                   s_fcrd, W, fs, pb, pn, ring, bar_sa, X))
+    return;
   warp_tree(wk, X);
   if (lane < LPR) settle_unit(a, wk, X, head_ff, fs, s_pos[0], ustart64, pn[0], u, q);
 }

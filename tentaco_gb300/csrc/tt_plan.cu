@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -248,20 +249,59 @@ cudaError_t pool_of(cudaMemPool_t* out) {
   return cudaSuccess;
 }
 
+// Failure injection and accounting of the pool (tt_debug_fail_pool_alloc,
+// tt_debug_pool_live): g_fail_countdown > 0 counts allocations down to the one
+// that fails; g_pool_live counts the allocations held.
+std::atomic<int64_t> g_fail_countdown{0};
+std::atomic<int64_t> g_pool_live{0};
+std::atomic<int32_t> g_tma_withhold{0};
+std::atomic<int64_t> g_tma_wait_ns{0};
+
+tt_status broken_error() {
+  return set_error(TT_ERR_INVALID_ARGUMENT, "plan unusable: a device allocation failed in an earlier call (destroy it)");
+}
+
+bool injected_failure() {
+  static const bool env_read = [] {
+    const char* v = getenv("TT_FAIL_POOL_ALLOC_AT");
+    if (v && atoll(v) > 0) g_fail_countdown.store(atoll(v));
+    return true;
+  }();
+  (void)env_read;
+  int64_t c = g_fail_countdown.load();
+  while (c > 0 && !g_fail_countdown.compare_exchange_weak(c, c - 1)) {
+  }
+  return c == 1;
+}
+
 // Stream-ordered allocation from the pool: usable on `st` at once, on other
 // streams after `st` is synchronised.
 cudaError_t pool_alloc(void** ptr, size_t bytes, cudaStream_t st) {
+  *ptr = nullptr;
+  if (injected_failure()) return cudaErrorMemoryAllocation;
   cudaMemPool_t pool;
   cudaError_t e = pool_of(&pool);
   if (e != cudaSuccess) return e;
-  return cudaMallocFromPoolAsync(ptr, bytes, pool, st);
+  e = cudaMallocFromPoolAsync(ptr, bytes, pool, st);
+  if (e == cudaSuccess) g_pool_live.fetch_add(1);
+  return e;
+}
+
+void pool_free(void* ptr, cudaStream_t st) {
+  if (!ptr) return;
+  cudaFreeAsync(ptr, st);
+  g_pool_live.fetch_sub(1);
 }
 
 template <typename T>
 tt_status dev_alloc(tt_plan* p, T** ptr, size_t count) {
   *ptr = nullptr;
   if (count == 0) count = 1;
-  CK(pool_alloc((void**)ptr, count * sizeof(T), p->stream));
+  if (pool_alloc((void**)ptr, count * sizeof(T), p->stream) != cudaSuccess) {
+    // whatever the plan was building is incomplete: it refuses every later call
+    p->broken = true;
+    return set_error(TT_ERR_OUT_OF_MEMORY, "device allocation of %zu bytes", count * sizeof(T));
+  }
   p->allocs.push_back((void*)*ptr);
   p->device_bytes += (int64_t)(count * sizeof(T));
   return TT_OK;
@@ -273,7 +313,7 @@ void dev_free(tt_plan* p, void* ptr) {
   auto it = std::find(p->allocs.begin(), p->allocs.end(), ptr);
   if (it != p->allocs.end()) p->allocs.erase(it);
   cudaDeviceSynchronize();
-  cudaFreeAsync(ptr, p->stream);
+  pool_free(ptr, p->stream);
 }
 
 
@@ -369,8 +409,8 @@ tt_status device_csf_check(tt_plan* p, const CsfView& v, cudaStream_t st) {
     e = launch_csf_check(p->d_pos[l], v.count[l - 1], l >= 2 ? 1 : 0, p->d_crd[l], v.count[l], v.dims[l], starts,
                          err + 2 * (l - 1), st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(h, err, sizeof(unsigned long long) * 2 * (size_t)L, cudaMemcpyDeviceToHost, st);
-  if (err) cudaFreeAsync(err, st);
-  cudaFreeAsync(starts, st);
+  pool_free(err, st);
+  pool_free(starts, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return set_error(TT_ERR_CUDA, "structure check: %s", cudaGetErrorString(e));
   for (int l = 1; l <= L; l++) {
@@ -663,6 +703,8 @@ WalkArgs walk_args(const tt_plan* p, float* A, int q) {
   // rows through rnz only for the families that walk by it (the row merge uses it too)
   a.rnz = p->staged == 3 || p->staged == 4 ? p->d_rnz : nullptr;
   for (int m = 0; m < 4; m++) a.fac_rows[m] = m + 1 < p->order ? (int32_t)p->dims[m + 1] : 0;
+  a.wait_ns = (uint32_t)g_tma_wait_ns.load(std::memory_order_relaxed);
+  a.tma_withhold = g_tma_withhold.load(std::memory_order_relaxed);
   return a;
 }
 
@@ -859,7 +901,7 @@ tt_status upload_values(tt_plan* p, const float* hvals, int64_t nvals, size_t nv
       if (e == cudaSuccess) e = launch_pow2_scales(cmax, 1, h16 ? 14 : 0, scl, inv, st);
       if (e == cudaSuccess) e = launch_to_16(tmp, nvals, 1, 1, scl, h16 ? 2 : 1, d, st);
       if (e == cudaSuccess) e = cudaMemcpyAsync(&vinv, inv, 4, cudaMemcpyDeviceToHost, st);
-      cudaFreeAsync(tmp, st);
+      pool_free(tmp, st);
       const cudaError_t e2 = cudaStreamSynchronize(st);
       if (e != cudaSuccess || e2 != cudaSuccess)
         return (set_error(TT_ERR_CUDA, "value conversion: %s", cudaGetErrorString(e != cudaSuccess ? e : e2)));
@@ -1225,7 +1267,7 @@ TT_EXPORT tt_status tt_plan_create_coo(int32_t order, const int32_t* dims, int64
     cudaStream_t st;
     std::vector<void*> v;
     ~Tmp() {
-      for (void* q : v) cudaFreeAsync(q, st);
+      for (void* q : v) pool_free(q, st);
       cudaStreamSynchronize(st);
     }
   } tmp{st, {}};
@@ -1357,7 +1399,7 @@ TT_EXPORT tt_status tt_plan_destroy(tt_plan* p) {
   if (p->evk1) cudaEventDestroy(p->evk1);
   if (!p->allocs.empty()) {
     cudaDeviceSynchronize();  // as cudaFree would
-    for (void* a : p->allocs) cudaFreeAsync(a, p->stream);
+    for (void* a : p->allocs) pool_free(a, p->stream);
     cudaStreamSynchronize(p->stream);
   }
   delete p;
@@ -1369,6 +1411,7 @@ TT_EXPORT tt_status tt_plan_set_factors(tt_plan* p, const float* const* factors,
   if (!p || !factors) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
   if (p->op != TT_OP_MTTKRP && p->op != TT_OP_TTM)
     return set_error(TT_ERR_INVALID_ARGUMENT, "plan is not an MTTKRP or TTM plan");
+  if (p->broken) return broken_error();
   cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
   const int nm = p->order - 1;
   if (p->op == TT_OP_TTM) {
@@ -1484,6 +1527,7 @@ TT_EXPORT tt_status tt_plan_mttkrp(tt_plan* p, float* A, void* stream) {
   clear_error();
   if (!p || !A) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
   if (p->op != TT_OP_MTTKRP) return set_error(TT_ERR_INVALID_ARGUMENT, "plan is not an MTTKRP plan");
+  if (p->broken) return broken_error();
   if (!p->factors_set) return set_error(TT_ERR_INVALID_ARGUMENT, "factors not set (tt_plan_set_factors)");
   cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
   tt_status s;
@@ -1497,6 +1541,7 @@ TT_EXPORT tt_status tt_plan_ttm(tt_plan* p, float* Y, void* stream) {
   clear_error();
   if (!p || !Y) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
   if (p->op != TT_OP_TTM) return set_error(TT_ERR_INVALID_ARGUMENT, "plan is not a TTM plan");
+  if (p->broken) return broken_error();
   if (!p->factors_set) return set_error(TT_ERR_INVALID_ARGUMENT, "U not set (tt_plan_set_factors)");
   cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
   tt_status s;
@@ -1520,6 +1565,7 @@ TT_EXPORT tt_status tt_plan_ttv(tt_plan* p, const float* x, float* y, void* stre
   clear_error();
   if (!p || !x || !y) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
   if (p->op != TT_OP_TTV) return set_error(TT_ERR_INVALID_ARGUMENT, "plan is not a TTV plan");
+  if (p->broken) return broken_error();
   cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
   tt_status s;
   if ((s = timed_begin(p, st)) != TT_OK) return s;
@@ -1566,9 +1612,30 @@ TT_EXPORT int32_t tt_plan_device_error(tt_plan* p) {
 TT_EXPORT tt_status tt_plan_use_variant(tt_plan* p, int32_t id) {
   clear_error();
   if (!p || p->op != TT_OP_MTTKRP) return set_error(TT_ERR_INVALID_ARGUMENT, "need an MTTKRP plan");
+  if (p->broken) return broken_error();
   if (!variant_valid(id, p->order, p->rank, p->prec)) return set_error(TT_ERR_INVALID_ARGUMENT, "variant %d invalid here", id);
+  // a COO plan has no CSF levels: only the strip walk (rows through rnz) reads it
+  if (p->coo && variant_spec(id).staged != 4)
+    return set_error(TT_ERR_INVALID_ARGUMENT, "variant %d: a COO plan runs the strip family only", id);
   return use_variant(p, id);
 }
+
+TT_EXPORT tt_status tt_debug_tma_wait(int32_t withhold, int64_t wait_ns) {
+  clear_error();
+  if (wait_ns < 0 || wait_ns > 1000000000) return set_error(TT_ERR_INVALID_ARGUMENT, "wait_ns %lld", (long long)wait_ns);
+  g_tma_wait_ns.store(wait_ns);
+  g_tma_withhold.store(withhold ? 1 : 0);
+  return TT_OK;
+}
+
+TT_EXPORT tt_status tt_debug_fail_pool_alloc(int64_t n) {
+  clear_error();
+  if (n < 0) return set_error(TT_ERR_INVALID_ARGUMENT, "n %lld", (long long)n);
+  g_fail_countdown.store(n);
+  return TT_OK;
+}
+
+TT_EXPORT int64_t tt_debug_pool_live(void) { return g_pool_live.load(); }
 
 namespace {
 // Time variants (3 runs each after one warm-up) with placeholder factors and keep
@@ -1706,9 +1773,8 @@ TT_EXPORT tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
   std::vector<float*> dfac(order - 1, nullptr);
   float* dA = nullptr;
   auto cleanup = [&]() {
-    for (float* d : dfac)
-      if (d) cudaFreeAsync(d, 0);
-    if (dA) cudaFreeAsync(dA, 0);
+    for (float* d : dfac) pool_free(d, 0);
+    pool_free(dA, 0);
     tt_plan_destroy(p);
   };
   for (int m = 0; m < order - 1; m++) {
@@ -1752,8 +1818,8 @@ TT_EXPORT tt_status tt_ttv_host(taco_tensor_t* y, const taco_tensor_t* B, const 
   if (x->dimensions && x->dimensions[0] < nx) { tt_plan_destroy(p); return set_error(TT_ERR_INVALID_ARGUMENT, "x has %d entries, need %lld", x->dimensions[0], (long long)nx); }
   float *dx = nullptr, *dy = nullptr;
   auto cleanup = [&]() {
-    if (dx) cudaFreeAsync(dx, 0);
-    if (dy) cudaFreeAsync(dy, 0);
+    pool_free(dx, 0);
+    pool_free(dy, 0);
     tt_plan_destroy(p);
   };
   if (pool_alloc((void**)&dx, sizeof(float) * (size_t)std::max<int64_t>(1, nx), 0) != cudaSuccess ||

@@ -49,6 +49,7 @@ struct tt_plan {
   float* d_scales = nullptr;    // per factor: colmax, scale, inv (rp each); then the output scale
   float* d_colscale = nullptr;
   bool factors_set = false;
+  bool broken = false;  // a device allocation failed after creation: every later call is refused
   // variant and scratch
   int variant = -1, selected_by = 0;  // 0 heuristic/fixed, 1 model, 2 sweep, 3 model's top k timed
   int tb = 0, cpt = 0, lpr = 0, G = 0, P = 0, nblocks = 0, staged = 0, wcap = 1;

@@ -178,3 +178,13 @@ def test_coo_plan_argument_checks_before_the_device():
     with pytest.raises(tt.TTError) as e:
         tt.Plan.from_coo(d[:3], co[:, :3], np.ones(1, np.float32), op=tt.OP_TTM, prec="fp16")
     assert e.value.status == tt.TT_ERR_UNSUPPORTED
+
+
+def test_debug_hooks_check_arguments_without_a_device():
+    L = tt.lib()
+    assert L.tt_debug_tma_wait(1, -5) == tt.TT_ERR_INVALID_ARGUMENT
+    assert L.tt_debug_tma_wait(0, 0) == tt.TT_OK
+    assert L.tt_debug_fail_pool_alloc(-1) == tt.TT_ERR_INVALID_ARGUMENT
+    assert L.tt_debug_fail_pool_alloc(0) == tt.TT_OK
+    if tt.device_count() == 0:
+        assert L.tt_debug_pool_live() == 0
