@@ -1,6 +1,7 @@
 // tt_misc.cu -- partition, TTV and storage-conversion kernels of libtentaco_gb300.
 #include <cuda_bf16.h>
 #include <algorithm>
+#include <atomic>
 #include <cuda_fp16.h>
 #include "tt_kernels.h"
 #include "tt_mttkrp.cuh"
@@ -219,6 +220,51 @@ cudaError_t launch_row_starts(const int32_t* pos1, const int32_t* pos2, const in
                               int32_t* rnz, cudaStream_t s, int64_t off, const int32_t* pos4) {
   flat_rnz_kernel<<<flat_grid(nroot + 1), 256, 0, s>>>(pos1, pos2, pos3, pos4, nroot, rnz, off);
   return cudaGetLastError();
+}
+
+// Dynamic shared memory above 48 KB needs a per-kernel, per-device opt-in: recorded
+// per instantiation so that it is asked for once.
+template <int VK, bool XS>
+cudaError_t launch_ttv_range_k(const WalkArgs& a, size_t smem, int grid, cudaStream_t s) {
+  static std::atomic<size_t> allowed[64];
+  auto k = ttv_range_kernel<VK, XS>;
+  if (smem > 48 * 1024) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (allowed[dev].load(std::memory_order_acquire) < smem) {
+      e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      allowed[dev].store(smem, std::memory_order_release);
+    }
+  }
+  k<<<grid, 32 * kTtvWarps, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int VK>
+cudaError_t launch_ttv_range_vk(const WalkArgs& a, bool xs, size_t smem, int grid, cudaStream_t s) {
+  return xs ? launch_ttv_range_k<VK, true>(a, smem, grid, s) : launch_ttv_range_k<VK, false>(a, smem, grid, s);
+}
+
+// The range walk: a.nblocks ranges of a.wcap units, kTtvWarps ranges per block; x
+// goes to shared memory when it fits beside the flags.
+cudaError_t launch_ttv_ranges(const WalkArgs& a, int vals_kind, cudaStream_t s) {
+  if (a.nblocks == 0) return cudaSuccess;
+  if (a.wcap < 1 || a.wcap > kTtvMaxRU) return cudaErrorInvalidValue;
+  int dev = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  const size_t flags = (size_t)kTtvWarps * 32 * kTtvNpt;
+  const size_t with_x = flags + (size_t)a.fac_rows[0] * sizeof(float);
+  const bool xs = with_x <= (size_t)optin;
+  const size_t smem = xs ? with_x : flags;
+  const int grid = (a.nblocks + kTtvWarps - 1) / kTtvWarps;
+  if (vals_kind == kB16) return launch_ttv_range_vk<kB16>(a, xs, smem, grid, s);
+  if (vals_kind == kH16) return launch_ttv_range_vk<kH16>(a, xs, smem, grid, s);
+  return launch_ttv_range_vk<kF32>(a, xs, smem, grid, s);
 }
 
 cudaError_t launch_ttv(const WalkArgs& a, int vals_kind, cudaStream_t s) {

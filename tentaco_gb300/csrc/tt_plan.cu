@@ -852,7 +852,30 @@ WalkArgs ttv_args(const tt_plan* p, const float* x, float* y) {
   a.P = p->P;
   a.G = kTtvNpt;
   a.nblocks = p->nblocks;
+  a.fac_rows[0] = (int32_t)p->dims[p->order - 1];  // length of x
   return a;
+}
+
+// The range walk's view: the merge's units are ranges of ttv_ru partition units.
+WalkArgs ttv_range_args(const tt_plan* p, const float* x, float* y) {
+  WalkArgs a = ttv_args(p, x, y);
+  a.wcap = p->ttv_ru;
+  a.P = p->ttv_ru * p->P;
+  a.nblocks = p->ttv_ranges;
+  return a;
+}
+
+// Ranges for the TTV walk: one per resident warp (kTtvWarps per SM) while a range
+// holds at most kTtvMaxRU units, more ranges (in waves) beyond that.
+tt_status set_ttv_ranges(tt_plan* p) {
+  int dev = 0, sms = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t units = p->nblocks;
+  const int64_t warps = (int64_t)std::max(sms, 1) * kTtvWarps;
+  p->ttv_ru = (int32_t)std::min<int64_t>(kTtvMaxRU, std::max<int64_t>(1, (units + warps - 1) / warps));
+  p->ttv_ranges = (int32_t)((units + p->ttv_ru - 1) / p->ttv_ru);
+  return TT_OK;
 }
 
 tt_status run_ttv(tt_plan* p, const float* x, float* y, cudaStream_t st) {
@@ -860,10 +883,10 @@ tt_status run_ttv(tt_plan* p, const float* x, float* y, cudaStream_t st) {
     if (p->nfib_last > 0) CK(cudaMemsetAsync(y, 0, sizeof(float) * (size_t)p->nfib_last, st));
     return TT_OK;
   }
-  const WalkArgs a = ttv_args(p, x, y);
-  if (!p->part_ready) CK(launch_partition(2, a, st));
+  if (!p->part_ready) CK(launch_partition(2, ttv_args(p, x, y), st));
+  const WalkArgs a = ttv_range_args(p, x, y);
   if (p->timing) CK(cudaEventRecord(p->evk0, st));
-  CK(launch_ttv(a, val_kind(p->prec), st));
+  CK(launch_ttv_ranges(a, val_kind(p->prec), st));
   if (p->timing) CK(cudaEventRecord(p->evk1, st));
   CK(launch_chain_fixup(2, a, st));
   return TT_OK;
@@ -1202,6 +1225,7 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
     p->G = kTtvNpt;
     p->P = 32 * kTtvNpt;
     p->nblocks = (int)((p->nnz + p->P - 1) / p->P);
+    if ((s = set_ttv_ranges(p)) != TT_OK) return fail(s);
     if ((s = alloc_walk_scratch(p, p->P)) != TT_OK) return fail(s);
     if ((s = prepare_partition(p)) != TT_OK) return fail(s);
   }
@@ -1360,6 +1384,7 @@ TT_EXPORT tt_status tt_plan_create_coo(int32_t order, const int32_t* dims, int64
     p->G = kTtvNpt;
     p->P = 32 * kTtvNpt;
     p->nblocks = (int)((p->nnz + p->P - 1) / p->P);
+    if ((s = set_ttv_ranges(p)) != TT_OK) return fail(s);
     if ((s = alloc_walk_scratch(p, p->P)) != TT_OK) return fail(s);
     if ((s = prepare_partition(p)) != TT_OK) return fail(s);
   } else {

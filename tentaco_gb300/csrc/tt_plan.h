@@ -49,6 +49,7 @@ struct tt_plan {
   float* d_scales = nullptr;    // per factor: colmax, scale, inv (rp each); then the output scale
   float* d_colscale = nullptr;
   bool factors_set = false;
+  int32_t ttv_ru = 1, ttv_ranges = 0;  // TTV range walk: units per range, ranges
   bool broken = false;  // a device allocation failed after creation: every later call is refused
   // variant and scratch
   int variant = -1, selected_by = 0;  // 0 heuristic/fixed, 1 model, 2 sweep, 3 model's top k timed

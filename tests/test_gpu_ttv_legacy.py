@@ -114,3 +114,17 @@ def test_reference_ttv_entry_point():
     tt.lib().ttv_csf_gpu_taco(y.ptr, B.ptr, x.ptr)
     close(y.vals, z["y"])
     assert tt.gpu_timer_ms() > 0
+
+
+@pytest.mark.parametrize("leaf,long_min", [(40_000, 30_000), (1_000_000, 400_000)])
+def test_ttv_ranges_with_fibers_across_ranges(leaf, long_min):
+    """12M nonzeros: ranges of several units each, with fibers longer than a range
+    (crossing several ranges) among short ones; x in shared memory (40,000 entries)
+    and in global memory (1,000,000 entries)."""
+    B = tt.gen_lognormal_fibers((3000, 2000, leaf), 12_000_000, 2.5, 1.5, 6, long_min, 31)
+    x = tt.gen_dense(leaf, 1, 2, 6).ravel()
+    ref = O.ttv(to_oracle(B), x)
+    got = run_ttv(B, x)
+    close(got, ref)
+    assert np.array_equal(got, run_ttv(B, x))
+    close(run_ttv(B, x, prec="bf16"), ref, mx=2e-2, fr=8e-3)
