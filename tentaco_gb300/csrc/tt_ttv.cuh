@@ -31,8 +31,8 @@ namespace tt {
 
 constexpr int kTtvNpt = 16;  // nonzeros per lane (the mask holds 16 bits per lane)
 // range walk (ttv_range_kernel)
-constexpr int kTtvWarps = 16;  // warps per block
-constexpr int kTtvPre = 8;     // fiber starts per lane loaded ahead (256 per unit)
+constexpr int kTtvWarps = 24;  // warps per block
+constexpr int kTtvPre = 8;     // fiber starts per lane loaded with the unit (256 per unit)
 constexpr int kTtvMaxRU = 62;  // units per range (the partition entries fit two per lane)
 
 #ifndef TT_ARGS_ONLY
@@ -210,19 +210,24 @@ __global__ void __launch_bounds__(256, 4) ttv_stream_kernel(const __grid_constan
 // units, a "range", and walks them in order, so a fiber crossing a unit boundary
 // inside the range is carried in registers and only the range's first and last
 // fibers go through the two-level merge (over ranges: about 2,400 on 50M nonzeros
-// instead of 98,000 units).  One 512-thread block per SM.
+// instead of 98,000 units).  One block of kTtvWarps warps per SM (80 registers a
+// thread).
 //   * x sits in shared memory when it fits (XS): the 16 gathers per lane and unit
 //     are shared-memory loads instead of L1 tag lookups (the unit walk above spends
 //     72% of the L1's throughput on them);
-//   * the next unit's coordinates, values and first 256 fiber starts are loaded into
-//     a second register set while the current unit is walked (the range's unit
-//     boundaries come from one load of its partition entries per lane);
+//   * the range's unit boundaries come from one load of its partition entries per
+//     lane; a unit's coordinates, values and first 256 fiber starts are loaded
+//     together (16-byte loads), the first unit's while x is being staged;
 //   * per unit, the fiber-end mask, lane merge and emission are the unit walk's.
+// Measured on 50M nonzeros (x of 30,000 entries): 24 warps per SM without loads
+// ahead, 16 warps with the next unit's loads in a second register set, and 32
+// warps (spilling) take 139, 139 and 162 us; with the loads coalesced in chunks of
+// 128 nonzeros (four lane merges per unit) 195 us.
 // a.P = RU * 512 and a.nblocks = ranges (the merge's units), a.wcap = RU,
 // a.part = the 512-nonzero partition, a.fac_rows[0] = length of x.
 
 template <int VK, bool XS>
-__global__ void __launch_bounds__(512, 1) ttv_range_kernel(const __grid_constant__ WalkArgs a) {
+__global__ void __launch_bounds__(32 * kTtvWarps, 1) ttv_range_kernel(const __grid_constant__ WalkArgs a) {
   constexpr int NPT = kTtvNpt;
   constexpr int UN = 32 * NPT;                    // nonzeros per unit
   constexpr int NW = VK == kF32 ? NPT : NPT / 2;  // value words per lane
@@ -285,7 +290,7 @@ __global__ void __launch_bounds__(512, 1) ttv_range_kernel(const __grid_constant
     }
   };
 
-  Set A, B;
+  Set A;
   if (ub < ue) issue(ub, A);
   if constexpr (XS) {
     // x into shared memory (all threads of the block; overlaps the first unit's loads)
@@ -425,14 +430,10 @@ __global__ void __launch_bounds__(512, 1) ttv_range_kernel(const __grid_constant
     }
   };
 
-  int u = ub;
-  for (;;) {
-    if (u + 1 < ue) issue(u + 1, B);
+  walk(ub, A);
+  for (int u = ub + 1; u < ue; u++) {
+    issue(u, A);
     walk(u, A);
-    if (++u >= ue) break;
-    if (u + 1 < ue) issue(u + 1, A);
-    walk(u, B);
-    if (++u >= ue) break;
   }
   if (lane == 0) {
     // the range's summary: its head fiber and, if different, the fiber open at its end
