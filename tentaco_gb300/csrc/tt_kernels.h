@@ -69,7 +69,6 @@ cudaError_t launch_row_starts(const int32_t* pos1, const int32_t* pos2, const in
 // FP64 merge of the rows the walk left in the carry buffer (after the walk kernel).
 cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s);
 // TTV walk over units of 32 * kTtvNpt nonzeros (a: the 2-level view, see tt_ttv.cuh).
-cudaError_t launch_ttv(const WalkArgs& a, int vals_kind, cudaStream_t s);
 cudaError_t launch_ttv_ranges(const WalkArgs& a, int vals_kind, cudaStream_t s);
 
 // Column max |x| of a rows x cols FP32 row-major matrix into colmax (cols floats, zeroed here).

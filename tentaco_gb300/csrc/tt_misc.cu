@@ -257,7 +257,7 @@ cudaError_t launch_ttv_ranges(const WalkArgs& a, int vals_kind, cudaStream_t s) 
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
-  const size_t flags = (size_t)kTtvWarps * 32 * kTtvNpt;
+  const size_t flags = (size_t)kTtvWarps * (32 * kTtvNpt + kTtvYStage * sizeof(float));  // flags and fiber stages
   const size_t with_x = flags + (size_t)a.fac_rows[0] * sizeof(float);
   const bool xs = with_x <= (size_t)optin;
   const size_t smem = xs ? with_x : flags;
@@ -267,14 +267,6 @@ cudaError_t launch_ttv_ranges(const WalkArgs& a, int vals_kind, cudaStream_t s) 
   return launch_ttv_range_vk<kF32>(a, xs, smem, grid, s);
 }
 
-cudaError_t launch_ttv(const WalkArgs& a, int vals_kind, cudaStream_t s) {
-  if (a.nblocks == 0) return cudaSuccess;
-  const int grid = (a.nblocks + 7) / 8;  // one warp per unit, 8 warps per block
-  if (vals_kind == kB16) ttv_stream_kernel<kB16><<<grid, 256, 0, s>>>(a);
-  else if (vals_kind == kH16) ttv_stream_kernel<kH16><<<grid, 256, 0, s>>>(a);
-  else ttv_stream_kernel<kF32><<<grid, 256, 0, s>>>(a);
-  return cudaGetLastError();
-}
 
 // ---------------------------------------------------------------------------
 // CSF structure check of one level on the plan's device copies (after upload;

@@ -1278,6 +1278,14 @@ __global__ void __launch_bounds__(256, 2) seg_fold_kernel(const __grid_constant_
   double* sc0 = a.segcarry + (size_t)(2 * sg) * rp;
   double* sc1 = sc0 + rp;
   int sfirst = -1, slast = -1, sflags = 0, nruns = 0;
+  // one column (TTV): every lane loads its own unit's two carries at once, and the
+  // fold takes them by shuffle (no load waits inside the fold)
+  const bool one_col = rp == 1;
+  float lane_c0 = 0.f, lane_c1 = 0.f;
+  if (one_col && lane < n) {
+    lane_c0 = a.carry[(size_t)(2 * (u0 + lane))];
+    lane_c1 = a.carry[(size_t)(2 * (u0 + lane)) + 1];
+  }
   // one pass per 32 columns (lane = column); the run structure is the same in every pass
   for (int c0 = 0; c0 < rp; c0 += 32) {
     const int col = c0 + lane;
@@ -1327,7 +1335,11 @@ __global__ void __launch_bounds__(256, 2) seg_fold_kernel(const __grid_constant_
         const int uu = g * kG + k;
         w0[k] = 0.f;
         w1[k] = 0.f;
-        if (uu < n && live) {
+        if (one_col) {  // warp-uniform
+          const float x0 = __shfl_sync(0xffffffffu, lane_c0, uu & 31);
+          const float x1 = __shfl_sync(0xffffffffu, lane_c1, uu & 31);
+          if (uu < n && live) { w0[k] = x0; w1[k] = x1; }
+        } else if (uu < n && live) {
           const float* c = a.carry + (size_t)(2 * (u0 + uu)) * rp + col;
           w0[k] = c[0];
           w1[k] = c[rp];

@@ -8,21 +8,22 @@
 // levels are read: the kernel sees a 2-level CSF (WalkArgs with pos[1] = fiber
 // starts, crd[1] = last-mode coordinates, nrows = fibers, one output column).
 // Unlike the reference, every output is written exactly once (no memset, no
-// float atomics):
-//   * a warp owns kTtvNpt * 32 consecutive nonzeros (its work unit) and lane L
-//     the kTtvNpt nonzeros from 16 L; the lane loads its coordinates and values
-//     straight into registers (16-byte loads, issued first: they depend on
-//     nothing), then its x entries;
-//   * the unit's fiber ends are byte flags in shared memory (flag e: nonzero e
-//     ends a fiber), set by plain byte stores from the fiber starts of the unit's
-//     window (no atomics), then packed into a 16-bit mask per lane; a lane's
-//     first fiber is fs + the ends before it (a warp prefix sum of popcounts);
-//   * the per-nonzero loop has no branches: an FMA, a predicated store of a fiber
-//     that starts and ends in the lane, and selects;
+// float atomics).  Work: 512-nonzero units (the partition's), grouped into ranges
+// of RU consecutive units; warp w of the grid walks range w in order.
+//   * per unit, lane L owns the 16 nonzeros from 16 L and loads its coordinates,
+//     values and (XS) x entries; the unit's fiber ends are byte flags in shared
+//     memory (flag e: nonzero e ends a fiber), set by plain byte stores from the
+//     fiber starts of the unit's window, then packed into a 16-bit mask per lane;
+//     a lane's first fiber is fs + the ends before it (a warp prefix sum);
+//   * the per-nonzero loop has no branches: an FMA, a predicated shared-memory
+//     store of a fiber that starts and ends in the lane, and selects;
 //   * the lanes are merged by a segmented scan of their open tail sums (a lane
-//     where a fiber ends starts a segment); fibers shared between warps go
-//     through the unit carry slots and the two-level merge of tt_mttkrp.cuh
-//     (FP32 Kahan inside a segment of units, FP64 across).
+//     where a fiber ends starts a segment); the unit's finished fibers, staged in
+//     shared memory, leave in one coalesced store (not one 32-byte sector write
+//     per fiber);
+//   * a fiber crossing a unit boundary inside the range is carried in registers;
+//     the range's first and last fibers go through the carry slots and the
+//     two-level merge of tt_mttkrp.cuh (FP32 Kahan inside a segment, FP64 across).
 // Fibers are never empty (canonical CSF), so a nonzero ends at most one fiber.
 #pragma once
 #include "tt_mttkrp.cuh"
@@ -32,197 +33,23 @@ namespace tt {
 constexpr int kTtvNpt = 16;  // nonzeros per lane (the mask holds 16 bits per lane)
 // range walk (ttv_range_kernel)
 constexpr int kTtvWarps = 24;  // warps per block
+constexpr int kTtvYStage = 520;  // floats per warp staging a unit's finished fibers (at most 512)
 constexpr int kTtvPre = 8;     // fiber starts per lane loaded with the unit (256 per unit)
 constexpr int kTtvMaxRU = 62;  // units per range (the partition entries fit two per lane)
 
 #ifndef TT_ARGS_ONLY
-template <int VK>
-__global__ void __launch_bounds__(256, 4) ttv_stream_kernel(const __grid_constant__ WalkArgs a) {
-  constexpr int NPT = kTtvNpt;
-  static_assert(NPT == 16, "a lane's fiber-end bits are half a mask word");
-  constexpr int NW = VK == kF32 ? NPT : NPT / 2;  // value words per lane
-  using WK = Walk<3, kFP32, 1, 1>;                // the merge helpers for one output column
-  __shared__ __align__(16) uint8_t s_end[8][32 * NPT];  // per warp: one flag per nonzero
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int u = blockIdx.x * (blockDim.x >> 5) + warp;
-  if (u >= a.nblocks) return;  // whole warp
-  const int PU = a.P;          // 32 * NPT
-  const int64_t ustart64 = (int64_t)u * PU;
-  const int cnt = (int)min((int64_t)PU, a.nnz - ustart64);
-  const int n = max(0, min(NPT, cnt - lane * NPT));
-  const int64_t s64 = ustart64 + (int64_t)lane * NPT;
-
-  // the lane's streams (runs start 64-byte aligned; the arrays are padded past
-  // the last 16-entry run, so a run that starts before nnz stays in bounds)
-  int32_t lc[NPT];
-  uint32_t vw[NW];
-  {
-    const uint64_t polF = policy_evict_first();
-    const int32_t* gl = a.crd[1] + s64;
-    if (n > 0) {
-#pragma unroll
-      for (int k = 0; k < NPT / 4; k++) {
-        const uint4 c4 = ld_stream_l1_u4(gl + 4 * k, polF);
-        lc[4 * k] = (int32_t)c4.x; lc[4 * k + 1] = (int32_t)c4.y; lc[4 * k + 2] = (int32_t)c4.z; lc[4 * k + 3] = (int32_t)c4.w;
-      }
-      const unsigned char* gv = static_cast<const unsigned char*>(a.vals) + s64 * (VK == kF32 ? 4 : 2);
-#pragma unroll
-      for (int k = 0; k < NW / 4; k++) {
-        const uint4 w = ld_stream_l1_u4(gv + 16 * k, polF);
-        vw[4 * k] = w.x; vw[4 * k + 1] = w.y; vw[4 * k + 2] = w.z; vw[4 * k + 3] = w.w;
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < NPT; k++) lc[k] = 0;
-#pragma unroll
-      for (int k = 0; k < NW; k++) vw[k] = 0u;
-    }
-  }
-
-  // the lane's x entries (x is small and stays in L1/L2); the coordinates are dead after this
-  float xv[NPT];
-  {
-    const float* xg = static_cast<const float*>(a.fac[0]);
-#pragma unroll
-    for (int k = 0; k < NPT; k++) xv[k] = __ldg(xg + lc[k]);
-  }
-
-  // fiber window: fibers fs .. fs + W - 1; fiber fs + x ends at nonzero pos[fs + x + 1] - 1
-  const int fs = a.part[u];
-  const int fnext = a.part[u + 1];
-  const int W = fnext - fs + 1;
-  const int32_t* gpos = a.pos[1] + fs;
-  reinterpret_cast<uint4*>(s_end[warp])[lane] = make_uint4(0u, 0u, 0u, 0u);  // 32 x 16 bytes
-  __syncwarp();
-  const int ustart = (int)ustart64;
-  for (int x0 = lane + 1; x0 <= W; x0 += 32 * 4) {
-    int e[4];
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-      const int x = x0 + 32 * r;
-      e[r] = x <= W ? gpos[x] - 1 - ustart : -1;
-    }
-#pragma unroll
-    for (int r = 0; r < 4; r++)
-      if (e[r] >= 0 && e[r] < cnt) s_end[warp][e[r]] = 1;
-  }
-  const int win0 = lane == 0 ? gpos[0] : 0;  // start of the unit's first fiber
-  __syncwarp();
-  uint32_t m = 0u;
-  {
-    // the lane's 16 flags (bytes 0 or 1) as bits 0..15
-    const uint4 b = reinterpret_cast<const uint4*>(s_end[warp])[lane];
-    const uint32_t w[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-    for (int k = 0; k < 4; k++)
-      m |= ((w[k] & 1u) | ((w[k] >> 7) & 2u) | ((w[k] >> 14) & 4u) | ((w[k] >> 21) & 8u)) << (4 * k);
-  }
-  int incl = __popc(m);
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const int t = __shfl_up_sync(0xffffffffu, incl, d);
-    if (lane >= d) incl += t;
-  }
-  const int f0 = fs + incl - __popc(m);  // fiber of the lane's first nonzero
-
-  float v[NPT];
-  if constexpr (VK == kF32) {
-#pragma unroll
-    for (int k = 0; k < NPT; k++) v[k] = __uint_as_float(vw[k]);
-  } else {
-#pragma unroll
-    for (int k = 0; k < NPT / 2; k++) {
-      const float2 p = pair16<VK>(vw[k]);
-      v[2 * k] = p.x * a.vscale;
-      v[2 * k + 1] = p.y * a.vscale;
-    }
-  }
-
-  float acc = 0.f, hacc = 0.f;
-  bool hset = false;
-  int f = f0;
-  auto step = [&](int k) {
-    acc = fmaf(v[k], xv[k], acc);
-    const bool e = (m >> k) & 1u;
-    if (e && hset) a.out[f] = acc;  // a fiber that started and ended in this lane
-    hacc = (e && !hset) ? acc : hacc;
-    hset = hset || e;
-    f += e ? 1 : 0;
-    acc = e ? 0.f : acc;
-  };
-  if (cnt == PU) {  // every lane full (all units but the tensor's last)
-#pragma unroll
-    for (int k = 0; k < NPT; k++) step(k);
-  } else {
-#pragma unroll
-    for (int k = 0; k < NPT; k++)
-      if (k < n) step(k);
-  }
-  // Merge the lanes: a segmented inclusive scan of the lanes' open tail sums
-  // (a lane where a fiber ends starts a segment) gives the carry leaving each
-  // lane; the carry into lane L plus its sum up to its first fiber end is that
-  // fiber's total in the unit.  Fixed order, so deterministic.
-  const bool active = n > 0;
-  float val = active ? acc : 0.f;
-  bool head = active && hset;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const float vu = __shfl_up_sync(0xffffffffu, val, d);
-    const int hu = __shfl_up_sync(0xffffffffu, head ? 1 : 0, d);
-    if (lane >= d) {
-      if (!head) val = vu + val;
-      head = head || hu;
-    }
-  }
-  float cin = __shfl_up_sync(0xffffffffu, val, 1);
-  if (lane == 0) cin = 0.f;
-  const float total = cin + hacc;  // the lane's first fiber, when it ends in the lane
-  const unsigned ends = __ballot_sync(0xffffffffu, active && hset);
-  const int lstar = ends ? __ffs((int)ends) - 1 : -1;  // first lane where a fiber ends
-  // later lanes' first fibers started and ended inside the unit: final
-  if (active && hset && lane != lstar) a.out[f0] = total;
-  const int la = (cnt - 1) / NPT;  // last lane with nonzeros
-  const float tot_first = __shfl_sync(0xffffffffu, total, lstar < 0 ? 0 : lstar);
-  const float out_last = __shfl_sync(0xffffffffu, val, la);
-  const int f_last = __shfl_sync(0xffffffffu, f, la);
-  const uint32_t m_last = __shfl_sync(0xffffffffu, m, la);
-  const bool open = !((m_last >> (cnt - la * NPT - 1)) & 1u);  // the unit's last fiber continues
-  if (lane == 0) {
-    // the unit's summary: its first fiber fs and, if different, the fiber open at its end
-    Summ<1> X;
-    X.h = fs;
-    X.t = kNone;
-    if (lstar < 0) {
-      X.ha[0] = out_last;  // the whole unit lies in fiber fs
-    } else {
-      X.ha[0] = tot_first;
-      if (open) {
-        X.t = f_last;
-        X.ta[0] = out_last;
-      }
-    }
-    WK wk(a, 0);
-    settle_unit(a, wk, X, (int64_t)fs, (int64_t)fs, (int64_t)win0, ustart64, fnext, u, 0);
-  }
-}
-
-// Range walk (the default): warp w of the grid owns RU consecutive 512-nonzero
-// units, a "range", and walks them in order, so a fiber crossing a unit boundary
-// inside the range is carried in registers and only the range's first and last
-// fibers go through the two-level merge (over ranges: about 2,400 on 50M nonzeros
-// instead of 98,000 units).  One block of kTtvWarps warps per SM (80 registers a
-// thread).
-//   * x sits in shared memory when it fits (XS): the 16 gathers per lane and unit
-//     are shared-memory loads instead of L1 tag lookups (the unit walk above spends
-//     72% of the L1's throughput on them);
-//   * the range's unit boundaries come from one load of its partition entries per
-//     lane; a unit's coordinates, values and first 256 fiber starts are loaded
-//     together (16-byte loads), the first unit's while x is being staged;
-//   * per unit, the fiber-end mask, lane merge and emission are the unit walk's.
+// The range walk.  Ranges instead of single units cut the merge's work units from
+// about 98,000 to 3,600 on 50M nonzeros.  One block of kTtvWarps warps per SM (80
+// registers a thread).  x sits in shared memory when it fits (XS): the 16 gathers
+// per lane and unit are then shared-memory loads instead of L1 tag lookups (a
+// walk gathering x through L1 spent 72% of the L1's throughput on them).  The
+// range's unit boundaries come from one load of its partition entries per lane; a
+// unit's coordinates, values and first 256 fiber starts are loaded together, the
+// first unit's while x is being staged.
 // Measured on 50M nonzeros (x of 30,000 entries): 24 warps per SM without loads
 // ahead, 16 warps with the next unit's loads in a second register set, and 32
 // warps (spilling) take 139, 139 and 162 us; with the loads coalesced in chunks of
-// 128 nonzeros (four lane merges per unit) 195 us.
+// 128 nonzeros (four lane merges per unit) 195 us; the staged fiber stores, 134 us.
 // a.P = RU * 512 and a.nblocks = ranges (the merge's units), a.wcap = RU,
 // a.part = the 512-nonzero partition, a.fac_rows[0] = length of x.
 
@@ -235,7 +62,8 @@ __global__ void __launch_bounds__(32 * kTtvWarps, 1) ttv_range_kernel(const __gr
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint8_t* s_end = smem + warp * UN;  // one flag per nonzero of the unit
-  float* s_x = reinterpret_cast<float*>(smem + kTtvWarps * UN);
+  float* s_y = reinterpret_cast<float*>(smem + kTtvWarps * UN) + warp * kTtvYStage;  // the unit's finished fibers
+  float* s_x = reinterpret_cast<float*>(smem + kTtvWarps * UN) + kTtvWarps * kTtvYStage;
   const int nunits = (int)((a.nnz + UN - 1) / UN);
   const int RU = a.wcap;
   const int r = blockIdx.x * kTtvWarps + warp;
@@ -371,7 +199,7 @@ __global__ void __launch_bounds__(32 * kTtvWarps, 1) ttv_range_kernel(const __gr
     auto step = [&](int k) {
       acc = fmaf(v[k], xv[k], acc);
       const bool e = (m >> k) & 1u;
-      if (e && hset) a.out[f] = acc;  // a fiber that started and ended in this lane
+      if (e && hset) s_y[f - fs] = acc;  // a fiber that started and ended in this lane
       hacc = (e && !hset) ? acc : hacc;
       hset = hset || e;
       f += e ? 1 : 0;
@@ -404,7 +232,11 @@ __global__ void __launch_bounds__(32 * kTtvWarps, 1) ttv_range_kernel(const __gr
     const float total = cin + hacc;
     const unsigned ends = __ballot_sync(0xffffffffu, active && hset);
     const int lstar = ends ? __ffs((int)ends) - 1 : -1;
-    if (active && hset && lane != lstar) a.out[f0] = total;
+    if (active && hset && lane != lstar) s_y[f0 - fs] = total;
+    // fibers fs + 1 .. fs + E - 1 start and end in the unit: one coalesced store
+    __syncwarp();
+    const int E = __shfl_sync(0xffffffffu, incl, 31);  // fiber ends in the unit
+    for (int i = 1 + lane; i < E; i += 32) a.out[fs + i] = s_y[i];
     const int la = (cnt - 1) / NPT;
     const float tot_first = __shfl_sync(0xffffffffu, total, lstar < 0 ? 0 : lstar);
     const float out_last = __shfl_sync(0xffffffffu, val, la);
