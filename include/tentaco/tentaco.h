@@ -233,6 +233,11 @@ int32_t tt_plan_device_error(tt_plan* plan);
 
 tt_status tt_device_malloc(int64_t bytes, void** ptr);
 tt_status tt_device_free(void* ptr);
+/* Page-lock (and release) a caller's host buffer: copies from and to it then run
+ * as direct DMA, e.g. the one-shot calls' uploads of a tensor kept in pinned
+ * memory.  Registering an already registered range succeeds. */
+tt_status tt_host_register(void* ptr, int64_t bytes);
+tt_status tt_host_unregister(void* ptr);
 tt_status tt_memcpy_htod(void* dst, const void* src, int64_t bytes);
 tt_status tt_memcpy_dtoh(void* dst, const void* src, int64_t bytes);
 tt_status tt_device_synchronize(void);

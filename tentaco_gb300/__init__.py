@@ -122,6 +122,8 @@ def lib():
         "tt_read_tns": (S, [C.c_char_p, C.c_int32, C.POINTER(_TP)]),
         "tt_device_malloc": (S, [C.c_int64, C.POINTER(_P)]),
         "tt_device_free": (S, [_P]),
+        "tt_host_register": (S, [_P, C.c_int64]),
+        "tt_host_unregister": (S, [_P]),
         "tt_memcpy_htod": (S, [_P, _P, C.c_int64]),
         "tt_memcpy_dtoh": (S, [_P, _P, C.c_int64]),
         "tt_device_synchronize": (S, []),
@@ -221,6 +223,11 @@ class Tensor:
         if n == 0:
             return np.zeros(0, dtype=np.float32)
         return np.ctypeslib.as_array(self.ptr.contents.vals, shape=(n,))
+
+    def host_arrays(self) -> list:
+        """The tensor's host arrays (every level's pos and crd, and the values)."""
+        out = [self.pos(l) for l in range(1, self.order)] + [self.crd(l) for l in range(1, self.order)]
+        return [a for a in out + [self.vals] if a.size]
 
     def features(self, rank: int) -> np.ndarray:
         f = np.zeros(12, dtype=np.float32)
@@ -335,10 +342,28 @@ def _tensor_ptr(B):
     return B.ptr
 
 
-def mttkrp_host(B, factors, prec="fp32", select=SELECT_DEFAULT, variant=0) -> np.ndarray:
-    """One-shot MTTKRP through tt_mttkrp_host: host in, host out."""
+def pin(arrays) -> None:
+    """Page-lock host arrays (tt_host_register): copies from and to them become DMA."""
+    for a in arrays:
+        if a.size:
+            check(lib().tt_host_register(a.ctypes.data, a.nbytes))
+
+
+def unpin(arrays) -> None:
+    for a in arrays:
+        if a.size:
+            check(lib().tt_host_unregister(a.ctypes.data))
+
+
+def mttkrp_host(B, factors, prec="fp32", select=SELECT_DEFAULT, variant=0, out=None) -> np.ndarray:
+    """One-shot MTTKRP through tt_mttkrp_host: host in, host out (into `out`, a
+    C-contiguous FP32 dims[0] x R array, when given)."""
     R = factors[0].shape[1]
-    A = np.zeros((B.dims[0], R), dtype=np.float32)
+    if out is not None:
+        assert out.dtype == np.float32 and out.shape == (B.dims[0], R) and out.flags.c_contiguous
+        A = out
+    else:
+        A = np.zeros((B.dims[0], R), dtype=np.float32)
     Ah = dense(A)
     Fh = [dense(f) for f in factors]
     arr = (_TP * len(Fh))(*[f.ptr for f in Fh])

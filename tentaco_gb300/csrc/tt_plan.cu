@@ -1882,6 +1882,31 @@ TT_EXPORT tt_status tt_device_free(void* ptr) {
   CK(cudaFree(ptr));
   return TT_OK;
 }
+// Page-lock a caller's host buffer so that copies from and to it are direct DMA
+// (what a caller keeping its inputs in pinned memory gets); already registered
+// memory is accepted.
+TT_EXPORT tt_status tt_host_register(void* ptr, int64_t bytes) {
+  clear_error();
+  if (!ptr || bytes <= 0) return set_error(TT_ERR_INVALID_ARGUMENT, "bad host range");
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return set_error(TT_ERR_NO_DEVICE, "no CUDA device visible");
+  }
+  const cudaError_t e = cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault);
+  if (e == cudaErrorHostMemoryAlreadyRegistered) {
+    cudaGetLastError();
+    return TT_OK;
+  }
+  if (e != cudaSuccess) return set_error(TT_ERR_CUDA, "host register: %s", cudaGetErrorString(e));
+  return TT_OK;
+}
+TT_EXPORT tt_status tt_host_unregister(void* ptr) {
+  clear_error();
+  if (!ptr) return set_error(TT_ERR_INVALID_ARGUMENT, "null pointer");
+  CK(cudaHostUnregister(ptr));
+  return TT_OK;
+}
 TT_EXPORT tt_status tt_memcpy_htod(void* dst, const void* src, int64_t bytes) {
   clear_error();
   CK(cudaMemcpy(dst, src, (size_t)bytes, cudaMemcpyHostToDevice));

@@ -356,3 +356,22 @@ def test_other_output_modes(order, prec):
         tt.Plan(B, rank=R, mode=order)
     with pytest.raises(tt.TTError):
         tt.Plan(B, op=tt.OP_TTV, mode=1)
+
+
+def test_one_shot_from_pinned_memory():
+    """The one-shot call with the tensor, factors and output page-locked
+    (tt_host_register): same result as from pageable memory."""
+    B = tt.gen_zipf((3000, 800, 5000), (1.1, 0.5, 0.8), 400_000, seed=12)
+    C, D = tt.gen_dense(800, 32, 1, 1), tt.gen_dense(5000, 32, 1, 2)
+    ref = tt.mttkrp_host(B, [C, D])
+    A = np.zeros((3000, 32), np.float32)
+    arrays = B.host_arrays() + [C, D, A]
+    tt.pin(arrays)
+    tt.pin(arrays)  # registering twice is accepted
+    try:
+        got = tt.mttkrp_host(B, [C, D], out=A)
+        assert got is A or np.shares_memory(got, A)
+        assert np.array_equal(A, ref)
+    finally:
+        tt.unpin(arrays)
+    close(A, O.mttkrp(to_oracle(B), [C, D]))
