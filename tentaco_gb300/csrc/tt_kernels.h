@@ -78,6 +78,14 @@ cudaError_t launch_ttv_ranges(const WalkArgs& a, int vals_kind, cudaStream_t s);
 // UINT64_MAX by the caller (see tt_misc.cu).
 cudaError_t launch_csf_check(const int32_t* pos, int64_t nf, int inner, const int32_t* crd, int64_t n, int32_t dim,
                              uint32_t* starts, unsigned long long* err, cudaStream_t s);
+// The same check in two parts, for a level whose coordinates arrive in pieces: the
+// pos pass (err[0]; marks the fiber starts in `starts`), then the crd pass over
+// positions [p0, p1) (err: the crd violation word), in increasing ranges on one
+// stream.  clamp != 0: out-of-range coordinates are also overwritten with 0.
+cudaError_t launch_csf_pos_check(const int32_t* pos, int64_t nf, int inner, int64_t n, uint32_t* starts,
+                                 unsigned long long* err, cudaStream_t s);
+cudaError_t launch_csf_crd_check_range(int32_t* crd, int64_t p0, int64_t p1, int32_t dim, const uint32_t* starts,
+                                       unsigned long long* err, int clamp, cudaStream_t s);
 cudaError_t launch_colmax(const float* x, int64_t rows, int cols, float* colmax, cudaStream_t s);
 // scale[j] = 2^(target_exp - floor(log2(colmax[j]))) (1 where colmax is 0 or not finite);
 // inv[j] = 1/scale[j].  Both exact powers of two.

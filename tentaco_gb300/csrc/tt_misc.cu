@@ -301,13 +301,47 @@ __global__ void csf_crd_check_kernel(const int32_t* __restrict__ crd, int64_t n,
   }
 }
 
-cudaError_t launch_csf_check(const int32_t* pos, int64_t nf, int inner, const int32_t* crd, int64_t n, int32_t dim,
-                             uint32_t* starts, unsigned long long* err, cudaStream_t s) {
+// The crd pass over positions [p0, p1) of a level that arrives in pieces (the
+// one-shot call's leaf coordinates): the same checks, and with `clamp` an
+// out-of-range coordinate is also overwritten with 0, so that a walk launched
+// after this pass on the same stream gathers only rows inside the factor (the
+// call then reports the recorded violation and discards its result).  Position
+// p0 - 1 must have arrived (and been checked) before.
+__global__ void csf_crd_check_range_kernel(int32_t* __restrict__ crd, int64_t p0, int64_t p1, int32_t dim,
+                                           const uint32_t* __restrict__ starts, unsigned long long* __restrict__ err,
+                                           int clamp) {
+  for (int64_t p = p0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < p1; p += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t c = crd[p];
+    if (c < 0 || c >= dim) {
+      atomicMin(err, ((unsigned long long)p << 3) | 3ull);
+      if (clamp) crd[p] = 0;
+    } else if (p > 0 && !((starts[p >> 5] >> (p & 31)) & 1u) && c <= crd[p - 1]) {
+      atomicMin(err, ((unsigned long long)p << 3) | 4ull);
+    }
+  }
+}
+
+static int check_grid(int64_t m) { return (int)std::min<int64_t>((m + 255) / 256, 152 * 16); }
+
+cudaError_t launch_csf_pos_check(const int32_t* pos, int64_t nf, int inner, int64_t n, uint32_t* starts,
+                                 unsigned long long* err, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(starts, 0, sizeof(uint32_t) * (size_t)((n + 31) / 32 + 1), s);
   if (e != cudaSuccess) return e;
-  auto grid = [](int64_t m) { return (int)std::min<int64_t>((m + 255) / 256, 152 * 16); };
-  if (nf > 0) csf_pos_check_kernel<<<grid(nf), 256, 0, s>>>(pos, nf, n, inner, starts, err);
-  if (n > 0) csf_crd_check_kernel<<<grid(n), 256, 0, s>>>(crd, n, dim, starts, err + 1);
+  if (nf > 0) csf_pos_check_kernel<<<check_grid(nf), 256, 0, s>>>(pos, nf, n, inner, starts, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_csf_crd_check_range(int32_t* crd, int64_t p0, int64_t p1, int32_t dim, const uint32_t* starts,
+                                       unsigned long long* err, int clamp, cudaStream_t s) {
+  if (p1 > p0) csf_crd_check_range_kernel<<<check_grid(p1 - p0), 256, 0, s>>>(crd, p0, p1, dim, starts, err, clamp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_csf_check(const int32_t* pos, int64_t nf, int inner, const int32_t* crd, int64_t n, int32_t dim,
+                             uint32_t* starts, unsigned long long* err, cudaStream_t s) {
+  cudaError_t e = launch_csf_pos_check(pos, nf, inner, n, starts, err, s);
+  if (e != cudaSuccess) return e;
+  if (n > 0) csf_crd_check_kernel<<<check_grid(n), 256, 0, s>>>(crd, n, dim, starts, err + 1);
   return cudaGetLastError();
 }
 

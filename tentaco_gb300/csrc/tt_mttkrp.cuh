@@ -74,6 +74,8 @@ struct alignas(64) WalkArgs {
   const int32_t* rnz;     // flat and strip walks: first nonzero of every row (nrows + 1); null otherwise
   uint32_t wait_ns;       // TMA walk: bound on each wait for a stage's barrier, ns (0: 5 ms)
   int32_t tma_withhold;   // TMA walk, test hook: 1 arms every stage's barrier but issues no copy
+  int32_t unit_lo;        // strip walk: first unit of this launch (units arriving in chunks)
+  int32_t unit_hi;        // strip walk: end of this launch's units (0: nblocks)
 };
 
 constexpr int kEmpty = -2;  // summary of a team that owns no nonzeros

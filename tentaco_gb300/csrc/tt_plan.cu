@@ -1773,6 +1773,267 @@ TT_EXPORT tt_status tt_plan_sweep_times(const tt_plan* p, float* ms, int32_t n) 
 // ---------------------------------------------------------------------------
 // one-shot host calls
 // ---------------------------------------------------------------------------
+namespace {
+
+// Page-locked (registered or pinned-allocated) host memory: copies from it are DMA
+// and return at once, so a call can queue all of them before its device work.
+bool host_pinned(const void* ptr) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
+// Nonzeros per chunk of the leaf coordinates in the overlapped one-shot call:
+// whole work units, at most 16 chunks, at least 64 units each.
+int64_t oneshot_chunk(int64_t nnz, int P) {
+  const int64_t c = std::max<int64_t>((int64_t)P * 64, (nnz + 15) / 16);
+  return (c + P - 1) / P * P;
+}
+
+// The one-shot MTTKRP of a strip-walk variant over page-locked host buffers, with
+// the host-to-device copies overlapped with the device work.  The copies bound the
+// call (a GB300 moves host data at about 200 GB/s, from one stream as from
+// several), so the rest runs under them:
+//   copy stream  the fiber structure, the values, the factors, then the leaf
+//                coordinates in chunks of whole work units;
+//   work stream  the structure check (the host waits for its verdict before
+//                anything indexes through pos), kexp / rnz / the partition (the
+//                structure alone), the value and factor conversion, then per chunk
+//                the check of its leaf coordinates and the walk of every unit whose
+//                nonzeros have all arrived; the row merge, and A.
+// Results are bit-identical to the serial path: the same conversions, the same walk
+// of every unit and the same fixed-order merge.  A chunk's check overwrites an
+// out-of-range leaf coordinate with 0 before the chunk's walk runs; the call then
+// reports the first violation and leaves A untouched.
+tt_status oneshot_overlapped(taco_tensor_t* A, const CsfView& v, const taco_tensor_t* const* factors, int prec,
+                             int variant, int rank) {
+  tt_status s = csf_check_root(v);
+  if (s != TT_OK) return s;
+  const int L = v.order - 1, nm = v.order - 1;
+  const int64_t nnz = v.nnz;
+  cudaStream_t cs = nullptr, xs = nullptr;
+  std::vector<cudaEvent_t> evs;
+  std::vector<float*> dfac(nm, nullptr);
+  float *dA = nullptr, *tmp = nullptr;
+  uint32_t *starts_up = nullptr, *starts_leaf = nullptr;
+  unsigned long long* err = nullptr;
+  tt_plan* p = nullptr;
+  auto cleanup = [&](tt_status st2) {
+    // copies still in flight land in buffers that go back to the pool
+    if (xs) cudaStreamSynchronize(xs);
+    if (cs) cudaStreamSynchronize(cs);
+    for (float* d : dfac) pool_free(d, cs);
+    pool_free(dA, cs);
+    pool_free(tmp, cs);
+    pool_free(starts_up, cs);
+    pool_free(starts_leaf, cs);
+    pool_free(err, cs);
+    tt_plan_destroy(p);
+    if (cs) cudaStreamSynchronize(cs);
+    for (cudaEvent_t e : evs) cudaEventDestroy(e);
+    if (xs) cudaStreamDestroy(xs);
+    if (cs) cudaStreamDestroy(cs);
+    return st2;
+  };
+  auto cuda_fail = [&](cudaError_t e, const char* what) {
+    return cleanup(set_error(e == cudaErrorMemoryAllocation ? TT_ERR_OUT_OF_MEMORY : TT_ERR_CUDA, "%s: %s", what,
+                             cudaGetErrorString(e)));
+  };
+  auto event = [&](cudaEvent_t* e, bool timing) {
+    const cudaError_t r = cudaEventCreateWithFlags(e, timing ? cudaEventDefault : cudaEventDisableTiming);
+    if (r == cudaSuccess) evs.push_back(*e);
+    return r;
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&xs, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(e, "streams");
+
+  p = new tt_plan();
+  cudaGetDevice(&p->device);
+  p->op = TT_OP_MTTKRP;
+  p->order = v.order;
+  for (int i = 0; i < v.order; i++) p->dims[i] = v.dims[i];
+  p->nnz = nnz;
+  p->nroot = v.nroot;
+  p->dense_root = true;
+  p->rank = rank;
+  p->rp = rank_pad(rank);
+  p->prec = prec;
+  p->stream = cs;
+  for (int l = 0; l < v.order; l++) p->count[l] = v.count[l];
+  p->nfib_last = v.count[v.order - 2];
+  p->slabs = 1;
+  p->leaf_len = nnz;
+
+  // device buffers (stream-ordered on the work stream; the copy stream waits)
+  for (int l = 1; l <= L; l++) {
+    if ((s = dev_alloc(p, &p->d_pos[l], (size_t)v.count[l - 1] + 1)) != TT_OK) return cleanup(s);
+    if ((s = dev_alloc(p, &p->d_crd[l], l == L ? (size_t)pad16(nnz) : (size_t)v.count[l])) != TT_OK) return cleanup(s);
+  }
+  e = cudaMemsetAsync(p->d_crd[L] + nnz, 0, sizeof(int32_t) * (size_t)(pad16(nnz) - nnz), cs);
+  for (int l = 0; l < TT_MAX_ORDER; l++) { p->slab[0].pos[l] = p->d_pos[l]; p->slab[0].crd[l] = p->d_crd[l]; }
+  for (int l = 0; l < v.order; l++) p->slab[0].count[l] = v.count[l];
+  p->slab[0].nnz = nnz;
+  p->slab[0].off = 0;
+  const bool v16 = val_kind(prec) != kF32;
+  p->nvals_alloc = (size_t)pad16(nnz);
+  if (v16) {
+    uint16_t* d = nullptr;
+    if ((s = dev_alloc(p, &d, p->nvals_alloc)) != TT_OK) return cleanup(s);
+    p->d_vals = d;
+    if (e == cudaSuccess) e = cudaMemsetAsync(d + nnz, 0, (p->nvals_alloc - (size_t)nnz) * 2, cs);
+    if (e == cudaSuccess) e = pool_alloc((void**)&tmp, (size_t)nnz * 4 + 64, cs);
+  } else {
+    float* d = nullptr;
+    if ((s = dev_alloc(p, &d, p->nvals_alloc)) != TT_OK) return cleanup(s);
+    p->d_vals = d;
+    if (e == cudaSuccess) e = cudaMemsetAsync(d + nnz, 0, (p->nvals_alloc - (size_t)nnz) * 4, cs);
+  }
+  if ((s = dev_alloc(p, &p->d_err, 4)) != TT_OK) return cleanup(s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(p->d_err, 0, 4 * sizeof(int32_t), cs);
+  for (int m = 0; m < nm && e == cudaSuccess; m++)
+    e = pool_alloc((void**)&dfac[m], (size_t)v.dims[m + 1] * rank * sizeof(float), cs);
+  const size_t abytes = (size_t)v.dims[0] * rank * sizeof(float);
+  if (e == cudaSuccess) e = pool_alloc((void**)&dA, abytes, cs);
+  int64_t upmax = 1;
+  for (int l = 1; l < L; l++) upmax = std::max<int64_t>(upmax, v.count[l]);
+  if (e == cudaSuccess) e = pool_alloc((void**)&starts_up, sizeof(uint32_t) * (size_t)((upmax + 31) / 32 + 1), cs);
+  if (e == cudaSuccess) e = pool_alloc((void**)&starts_leaf, sizeof(uint32_t) * (size_t)((nnz + 31) / 32 + 1), cs);
+  if (e == cudaSuccess) e = pool_alloc((void**)&err, sizeof(unsigned long long) * 2 * (size_t)L, cs);
+  if (e == cudaSuccess) e = cudaMemsetAsync(err, 0xff, sizeof(unsigned long long) * 2 * (size_t)L, cs);
+  cudaEvent_t ev_alloc, ev_struct, ev_vals, ev_fac;
+  if (e == cudaSuccess) e = event(&ev_alloc, false);
+  if (e == cudaSuccess) e = event(&ev_struct, false);
+  if (e == cudaSuccess) e = event(&ev_vals, false);
+  if (e == cudaSuccess) e = event(&ev_fac, false);
+  if (e == cudaSuccess) e = cudaEventRecord(ev_alloc, cs);
+  if (e != cudaSuccess) return cuda_fail(e, "one-shot setup");
+
+  // copy stream, first part: the fiber structure, then the values
+  e = cudaStreamWaitEvent(xs, ev_alloc, 0);
+  for (int l = 1; l <= L && e == cudaSuccess; l++) {
+    e = cudaMemcpyAsync(p->d_pos[l], v.pos[l], sizeof(int32_t) * (size_t)(v.count[l - 1] + 1), cudaMemcpyHostToDevice, xs);
+    if (e == cudaSuccess && l < L)
+      e = cudaMemcpyAsync(p->d_crd[l], v.crd[l], sizeof(int32_t) * (size_t)v.count[l], cudaMemcpyHostToDevice, xs);
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(ev_struct, xs);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(v16 ? (void*)tmp : p->d_vals, v.vals, (size_t)nnz * 4, cudaMemcpyHostToDevice, xs);
+  if (e == cudaSuccess) e = cudaEventRecord(ev_vals, xs);
+  if (e != cudaSuccess) return cuda_fail(e, "upload");
+
+  // structure check: every pos, the upper levels' crd; the leaf fiber starts are
+  // kept for the leaf chunks' checks
+  e = cudaStreamWaitEvent(cs, ev_struct, 0);
+  for (int l = 1; l <= L && e == cudaSuccess; l++) {
+    e = launch_csf_pos_check(p->d_pos[l], v.count[l - 1], l >= 2 ? 1 : 0, v.count[l], l == L ? starts_leaf : starts_up,
+                             err + 2 * (l - 1), cs);
+    if (e == cudaSuccess && l < L)
+      e = launch_csf_crd_check_range(p->d_crd[l], 0, v.count[l], v.dims[l], starts_up, err + 2 * (l - 1) + 1, 0, cs);
+  }
+  unsigned long long h[2 * TT_MAX_ORDER];
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, err, sizeof(unsigned long long) * 2 * (size_t)L, cudaMemcpyDeviceToHost, cs);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+  if (e != cudaSuccess) return cuda_fail(e, "structure check");
+  for (int l = 1; l <= L; l++) {
+    s = csf_check_error(l, h[2 * (l - 1)]);
+    if (s == TT_OK && l < L) s = csf_check_error(l, h[2 * (l - 1) + 1]);
+    if (s != TT_OK) return cleanup(s);
+  }
+  // the variant: scratch, kexp / rnz, the partition (structure only)
+  if ((s = use_variant(p, variant)) != TT_OK) return cleanup(s);
+
+  // copy stream, second part: the factors, then the leaf coordinates in chunks
+  const int64_t chunk = oneshot_chunk(nnz, p->P);
+  const int K = (int)((nnz + chunk - 1) / chunk);
+  std::vector<cudaEvent_t> ev_chunk(K), ev_w0(K), ev_w1(K);
+  e = cudaSuccess;
+  for (int i = 0; i < K && e == cudaSuccess; i++) {
+    e = event(&ev_chunk[i], false);
+    if (e == cudaSuccess) e = event(&ev_w0[i], true);
+    if (e == cudaSuccess) e = event(&ev_w1[i], true);
+  }
+  for (int m = 0; m < nm && e == cudaSuccess; m++)
+    e = cudaMemcpyAsync(dfac[m], factors[m]->vals, (size_t)v.dims[m + 1] * rank * sizeof(float), cudaMemcpyHostToDevice, xs);
+  if (e == cudaSuccess) e = cudaEventRecord(ev_fac, xs);
+  for (int i = 0; i < K && e == cudaSuccess; i++) {
+    const int64_t c0 = i * chunk, c1 = std::min(nnz, c0 + chunk);
+    e = cudaMemcpyAsync(p->d_crd[L] + c0, v.crd[L] + c0, sizeof(int32_t) * (size_t)(c1 - c0), cudaMemcpyHostToDevice, xs);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_chunk[i], xs);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "upload");
+
+  // values: one power-of-two scale for 16-bit storage (the factors' output scale
+  // needs it on the host)
+  e = cudaStreamWaitEvent(cs, ev_vals, 0);
+  if (e == cudaSuccess && v16) {
+    const bool h16 = prec == kFP16;
+    float* cmax = reinterpret_cast<float*>(((uintptr_t)(tmp + nnz) + 15) & ~(uintptr_t)15);
+    float vinv = 1.f;
+    e = launch_colmax(tmp, nnz, 1, cmax, cs);
+    if (e == cudaSuccess) e = launch_pow2_scales(cmax, 1, h16 ? 14 : 0, cmax + 1, cmax + 2, cs);
+    if (e == cudaSuccess) e = launch_to_16(tmp, nnz, 1, 1, cmax + 1, h16 ? 2 : 1, (uint16_t*)p->d_vals, cs);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&vinv, cmax + 2, 4, cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+    p->vinv = vinv;
+  }
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev_fac, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "value conversion");
+  if ((s = tt_plan_set_factors(p, (const float* const*)dfac.data(), cs)) != TT_OK) return cleanup(s);
+
+  // per chunk: check its leaf coordinates, walk the units that have arrived
+  const size_t smem = variant_smem(variant_spec(p->variant), p->rp, p->prec, p->wcap, p->order);
+  WalkArgs a = walk_args(p, dA, 0);
+  a.smem_bytes = (int32_t)smem;
+  cudaEvent_t ev_m0, ev_m1;
+  e = event(&ev_m0, true);
+  if (e == cudaSuccess) e = event(&ev_m1, true);
+  if (e == cudaSuccess) e = cudaMemsetAsync(dA, 0, abytes, cs);
+  int32_t ulo = 0;
+  for (int i = 0; i < K && e == cudaSuccess; i++) {
+    const int64_t c0 = i * chunk, c1 = std::min(nnz, c0 + chunk);
+    e = cudaStreamWaitEvent(cs, ev_chunk[i], 0);
+    if (e == cudaSuccess)
+      e = launch_csf_crd_check_range(p->d_crd[L], c0, c1, v.dims[L], starts_leaf, err + 2 * (L - 1) + 1, 1, cs);
+    const int32_t uhi = i == K - 1 ? a.nblocks : (int32_t)(c1 / p->P);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_w0[i], cs);
+    if (e == cudaSuccess && uhi > ulo) {
+      a.unit_lo = ulo;
+      a.unit_hi = uhi;
+      e = p->launcher(a, uhi - ulo, p->tb, smem, cs);
+      ulo = uhi;
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(ev_w1[i], cs);
+  }
+  a.unit_lo = 0;
+  a.unit_hi = 0;
+  if (e == cudaSuccess) e = cudaEventRecord(ev_m0, cs);
+  if (e == cudaSuccess) e = launch_chain_fixup(p->order, a, cs);
+  if (e == cudaSuccess) e = cudaEventRecord(ev_m1, cs);
+  int32_t derr = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, err + 2 * (L - 1) + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, cs);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&derr, p->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, cs);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+  if (e != cudaSuccess) return cuda_fail(e, "walk");
+  if ((s = csf_check_error(L, h[0])) != TT_OK) return cleanup(s);
+  if (derr != 0)
+    return cleanup(set_error(derr == 301 ? TT_ERR_DEVICE_WAIT : TT_ERR_CUDA, "device error word %d", (int)derr));
+  e = cudaMemcpyAsync(A->vals, dA, abytes, cudaMemcpyDeviceToHost, cs);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+  if (e != cudaSuccess) return cuda_fail(e, "download A");
+  // the legacy timer: the walks, the merge and the partition (kernel time, not the copies)
+  float ms = 0.f, t = 0.f;
+  for (int i = 0; i < K; i++)
+    if (cudaEventElapsedTime(&t, ev_w0[i], ev_w1[i]) == cudaSuccess) ms += t;
+  if (cudaEventElapsedTime(&t, ev_m0, ev_m1) == cudaSuccess) ms += t;
+  g_legacy_ms.store(ms + (p->part_ready ? p->part_ms : 0.f));
+  return cleanup(TT_OK);
+}
+
+}  // namespace
+
 TT_EXPORT tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
                                    const taco_tensor_t* const* factors, tt_precision prec,
                                    tt_select select, int32_t variant) {
@@ -1788,6 +2049,21 @@ TT_EXPORT tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
     if (!F || !F->vals || !F->dimensions) return set_error(TT_ERR_INVALID_ARGUMENT, "factor %d missing", m + 1);
     if (F->dimensions[1] != rank || F->dimensions[0] != B->dimensions[m + 1])
       return set_error(TT_ERR_INVALID_ARGUMENT, "factor %d is %dx%d, expected %dx%d", m + 1, F->dimensions[0], F->dimensions[1], B->dimensions[m + 1], rank);
+  }
+  // a strip-walk variant over page-locked host buffers: the copies overlapped
+  if (select == TT_SELECT_FIXED || select == TT_SELECT_DEFAULT) {
+    CsfView v;
+    int ndev = 0;
+    if (csf_view(B, &v) == TT_OK && v.dense_root && v.nnz > 0 && prec != TT_PREC_FX16 && rank >= 1 && rank <= TT_MAX_RANK &&
+        cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0) {
+      const int id = select == TT_SELECT_FIXED ? variant : default_variant(order, rank, (int)prec, v.nnz);
+      bool pinned = variant_valid(id, order, rank, (int)prec) && variant_spec(id).staged == 4 && host_pinned(v.vals);
+      for (int l = 1; pinned && l < order; l++) pinned = host_pinned(v.pos[l]) && host_pinned(v.crd[l]);
+      for (int m = 0; pinned && m < order - 1; m++) pinned = host_pinned(factors[m]->vals);
+      if (pinned) return oneshot_overlapped(A, v, factors, (int)prec, id, rank);
+    }
+    cudaGetLastError();
+    clear_error();
   }
   // one call cannot repay the slab-major layout's one-time host build: no slabs
   tt_plan_options opts{};

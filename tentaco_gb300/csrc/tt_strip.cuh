@@ -314,7 +314,9 @@ struct TeamScatter {
   }
 };
 
-// Strip kernel: one work unit (P = TW * G nonzeros) per warp, 256-thread blocks.
+// Strip kernel: one work unit (P = TW * G nonzeros) per warp, 256-thread blocks;
+// a launch covers units [unit_lo, unit_hi) of the nblocks (the one-shot call walks
+// the units whose nonzeros have arrived while later ones are still being copied).
 // part[u * (ORDER - 1)]: the row holding unit u's first nonzero (launch_partition_rows).
 template <int ORDER, int PREC, int CPT, int LPR, int U, int MINB>
 __global__ void __launch_bounds__(256, MINB) mttkrp_strip_kernel(const __grid_constant__ WalkArgs a) {
@@ -323,8 +325,8 @@ __global__ void __launch_bounds__(256, MINB) mttkrp_strip_kernel(const __grid_co
   constexpr int STEP = ST::STEP, VB = ST::VB;
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int unit = blockIdx.x * (blockDim.x >> 5) + warp;
-  if (unit >= a.nblocks) return;  // whole warp: nothing below synchronises the block
+  const int unit = a.unit_lo + blockIdx.x * (blockDim.x >> 5) + warp;
+  if (unit >= (a.unit_hi > 0 ? a.unit_hi : a.nblocks)) return;  // whole warp: nothing below synchronises the block
   const int P = a.P;
   unsigned char* ws = smem + (size_t)warp * strip_warp_bytes(P, VB, ORDER);
   int32_t* s_l = reinterpret_cast<int32_t*>(ws);
