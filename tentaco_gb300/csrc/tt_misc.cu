@@ -84,27 +84,38 @@ cudaError_t launch_partition_rows(int order, const WalkArgs& a, cudaStream_t s) 
 // V is allocated for every virtual row).  ldv: row stride of V, a multiple of 4;
 // lda: row stride of A.
 constexpr int kVirtMaxSlabs = 16;
-__global__ void virtual_rows_kernel(const float* __restrict__ V, const int32_t* __restrict__ rnz, int S,
-                                    int64_t nrows, int64_t vstride, int ldv, int lda, int R, float* __restrict__ A) {
+// One instance per slab count S (registers for S rows, not for the maximum): with
+// four slabs a thread holds 16 loaded words and the SMs stay fully occupied.
+template <int S>
+__global__ void __launch_bounds__(256) virtual_rows_kernel(const float* __restrict__ V, const int32_t* __restrict__ rnz,
+                                                           int64_t nrows, int64_t vstride, int ldv, int lda, int R,
+                                                           float* __restrict__ A) {
   const int q4 = (R + 3) >> 2;  // 4-column groups per row
   const int64_t n = nrows * q4;
+  const bool narrow = n <= 0x7fffffff;  // 32-bit index arithmetic
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = e / q4;
-    const int j = (int)(e - i * q4) * 4;
-    float4 v[kVirtMaxSlabs];
-    bool live[kVirtMaxSlabs];
+    int64_t i;
+    int j;
+    if (narrow) {
+      const int i32 = (int)e / q4;
+      i = i32;
+      j = ((int)e - i32 * q4) * 4;
+    } else {
+      i = e / q4;
+      j = (int)(e - i * q4) * 4;
+    }
+    float4 v[S];
+    bool live[S];
 #pragma unroll
-    for (int k = 0; k < kVirtMaxSlabs; k++) {
-      if (k < S) {
-        const int64_t r = (int64_t)k * vstride + i;
-        live[k] = rnz[r + 1] > rnz[r];
-        v[k] = *reinterpret_cast<const float4*>(V + r * ldv + j);
-      }
+    for (int k = 0; k < S; k++) {
+      const int64_t r = (int64_t)k * vstride + i;
+      live[k] = rnz[r + 1] > rnz[r];
+      v[k] = *reinterpret_cast<const float4*>(V + r * ldv + j);
     }
     float sum[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-    for (int k = 0; k < kVirtMaxSlabs; k++) {
-      if (k < S && live[k]) {
+    for (int k = 0; k < S; k++) {
+      if (live[k]) {
         const float x[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
 #pragma unroll
         for (int c = 0; c < 4; c++) {  // Kahan: cmp holds the low part lost so far
@@ -124,14 +135,26 @@ __global__ void virtual_rows_kernel(const float* __restrict__ V, const int32_t* 
   }
 }
 
+template <int S>
+cudaError_t launch_virtual_rows_s(const float* V, const int32_t* rnz, int64_t nrows, int64_t vstride, int ldv, int lda,
+                                  int R, float* A, int grid, cudaStream_t s) {
+  virtual_rows_kernel<S><<<grid, 256, 0, s>>>(V, rnz, nrows, vstride, ldv, lda, R, A);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_virtual_rows(const float* V, const int32_t* rnz, int S, int64_t nrows, int64_t vstride, int ldv,
                                 int lda, int R, float* A, cudaStream_t s) {
   if (nrows == 0 || R == 0) return cudaSuccess;
   if (S < 1 || S > kVirtMaxSlabs || (ldv & 3) != 0 || ldv < ((R + 3) & ~3) || lda < R) return cudaErrorInvalidValue;
   const int64_t n = nrows * ((R + 3) / 4);
-  const int64_t grid = std::min<int64_t>((n + 255) / 256, 152 * 16);
-  virtual_rows_kernel<<<(int)grid, 256, 0, s>>>(V, rnz, S, nrows, vstride, ldv, lda, R, A);
-  return cudaGetLastError();
+  const int grid = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+  using L = cudaError_t (*)(const float*, const int32_t*, int64_t, int64_t, int, int, int, float*, int, cudaStream_t);
+  static const L table[kVirtMaxSlabs] = {
+      launch_virtual_rows_s<1>,  launch_virtual_rows_s<2>,  launch_virtual_rows_s<3>,  launch_virtual_rows_s<4>,
+      launch_virtual_rows_s<5>,  launch_virtual_rows_s<6>,  launch_virtual_rows_s<7>,  launch_virtual_rows_s<8>,
+      launch_virtual_rows_s<9>,  launch_virtual_rows_s<10>, launch_virtual_rows_s<11>, launch_virtual_rows_s<12>,
+      launch_virtual_rows_s<13>, launch_virtual_rows_s<14>, launch_virtual_rows_s<15>, launch_virtual_rows_s<16>};
+  return table[S - 1](V, rnz, nrows, vstride, ldv, lda, R, A, grid, s);
 }
 
 __global__ void window_max_kernel(const __grid_constant__ WalkArgs a, int lvl, int stride, int* out) {
