@@ -249,7 +249,13 @@ tt_status tt_l2_flush(void* stream);
 
 /* A->vals (host, dims[0] x rank) = MTTKRP(B, factors[0..order-2]) (host dense).
  * Returns TT_ERR_DEVICE_WAIT if a walk's bounded wait ran out (A is then
- * incomplete), like any nonzero device error word of the call. */
+ * incomplete), like any nonzero device error word of the call.
+ * With every host array of B and of the factors page-locked (tt_host_register)
+ * and a strip-walk variant (TT_SELECT_FIXED with a strip id, or TT_SELECT_DEFAULT
+ * where the default is one), the copies to the device overlap the device work:
+ * the leaf coordinates arrive in chunks, each checked and walked as it lands.  The
+ * results are the same bits as without the overlap; a malformed CSF is reported
+ * (TT_ERR_INVALID_CSF) with A left untouched. */
 tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
                          const taco_tensor_t* const* factors, tt_precision prec,
                          tt_select select, int32_t variant);
