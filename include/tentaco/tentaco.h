@@ -124,7 +124,7 @@ typedef struct tt_plan_options {
    * slab-major order (one output row per slab and row, summed into A in FP32 with Kahan compensation in
    * slab order); the lean, staged and TMA families run one pass per slab, each
    * adding into A; the flat family runs without slabs.  0: automatic (slabs of at
-   * most 32 MB of the last factor as stored, when it exceeds 48 MB); 1: no slabs;
+   * most 44 MB of the last factor as stored, when it exceeds 48 MB); 1: no slabs;
    * at most 16.  One-shot calls (tt_mttkrp_host) use no slabs. */
   int32_t slabs;
   /* L2 policy of factor-row gathers in the lean walk: 0 automatic (evict_last
