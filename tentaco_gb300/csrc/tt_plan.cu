@@ -15,6 +15,7 @@
 #include <cstring>
 #include <mutex>
 #include <vector>
+#include <nvtx3/nvToolsExt.h>
 #include "tt_internal.h"
 #include "tt_kernels.h"
 #define TT_ARGS_ONLY
@@ -217,6 +218,15 @@ int auto_slabs(int order, int64_t leaf_dim, int rp, int prec) {
   } while (0)
 
 namespace {
+
+// NVTX range over a public entry point (or a phase of one): shows in Nsight
+// Systems / Nsight Compute (--nvtx) when a tool is attached, a no-op otherwise.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 std::atomic<float> g_legacy_ms{-1.0f};
 
@@ -1029,6 +1039,7 @@ TT_EXPORT tt_status tt_plan_create(const taco_tensor_t* B, tt_op op, int32_t ran
 TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t rank, tt_precision prec,
                                       tt_select select, int32_t variant, const tt_plan_options* opts,
                                       void* stream, tt_plan** out) {
+  NvtxRange nvtx_range("tt_plan_create");
   clear_error();
   if (opts && (opts->slabs < 0 || opts->slabs > kMaxSlabs))
     return set_error(TT_ERR_INVALID_ARGUMENT, "slabs %d (0 = automatic, at most %d)", opts->slabs, kMaxSlabs);
@@ -1261,6 +1272,7 @@ TT_EXPORT tt_status tt_plan_create_ex(const taco_tensor_t* B, tt_op op, int32_t 
 TT_EXPORT tt_status tt_plan_create_coo(int32_t order, const int32_t* dims, int64_t nnz, const int32_t* coords,
                                        const float* vals, tt_op op, int32_t rank, tt_precision prec,
                                        tt_select select, int32_t variant, void* stream, tt_plan** out) {
+  NvtxRange nvtx_range("tt_plan_create_coo");
   clear_error();
   if (!out || !dims || (nnz > 0 && (!coords || !vals)) || nnz < 0)
     return set_error(TT_ERR_INVALID_ARGUMENT, "null argument or negative nonzero count");
@@ -1452,6 +1464,7 @@ TT_EXPORT tt_status tt_plan_destroy(tt_plan* p) {
 }
 
 TT_EXPORT tt_status tt_plan_set_factors(tt_plan* p, const float* const* factors, void* stream) {
+  NvtxRange nvtx_range("tt_plan_set_factors");
   clear_error();
   if (!p || !factors) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
   if (p->op != TT_OP_MTTKRP && p->op != TT_OP_TTM)
@@ -1569,6 +1582,7 @@ static tt_status timed_end(tt_plan* p, cudaStream_t st) {
 }
 
 TT_EXPORT tt_status tt_plan_mttkrp(tt_plan* p, float* A, void* stream) {
+  NvtxRange nvtx_range("tt_plan_mttkrp");
   clear_error();
   if (!p || !A) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
   if (p->op != TT_OP_MTTKRP) return set_error(TT_ERR_INVALID_ARGUMENT, "plan is not an MTTKRP plan");
@@ -1583,6 +1597,7 @@ TT_EXPORT tt_status tt_plan_mttkrp(tt_plan* p, float* A, void* stream) {
 
 // TTM of a COO plan: Y (nfibers x rank, DEVICE) from the U last set.
 TT_EXPORT tt_status tt_plan_ttm(tt_plan* p, float* Y, void* stream) {
+  NvtxRange nvtx_range("tt_plan_ttm");
   clear_error();
   if (!p || !Y) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
   if (p->op != TT_OP_TTM) return set_error(TT_ERR_INVALID_ARGUMENT, "plan is not a TTM plan");
@@ -1607,6 +1622,7 @@ TT_EXPORT tt_status tt_plan_coo_fibers(const tt_plan* p, int32_t* ij) {
 }
 
 TT_EXPORT tt_status tt_plan_ttv(tt_plan* p, const float* x, float* y, void* stream) {
+  NvtxRange nvtx_range("tt_plan_ttv");
   clear_error();
   if (!p || !x || !y) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
   if (p->op != TT_OP_TTV) return set_error(TT_ERR_INVALID_ARGUMENT, "plan is not a TTV plan");
@@ -1833,6 +1849,7 @@ int64_t oneshot_chunk(int64_t nnz, int P) {
 // reports the first violation and leaves A untouched.
 tt_status oneshot_overlapped(taco_tensor_t* A, const CsfView& v, const taco_tensor_t* const* factors, int prec,
                              int variant, int rank) {
+  NvtxRange nvtx_range("tt_mttkrp_host: overlapped");
   tt_status s = csf_check_root(v);
   if (s != TT_OK) return s;
   const int L = v.order - 1, nm = v.order - 1;
@@ -2081,6 +2098,7 @@ tt_status oneshot_overlapped(taco_tensor_t* A, const CsfView& v, const taco_tens
 TT_EXPORT tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
                                    const taco_tensor_t* const* factors, tt_precision prec,
                                    tt_select select, int32_t variant) {
+  NvtxRange nvtx_range("tt_mttkrp_host");
   clear_error();
   if (!A || !B || !factors || !A->vals || !A->dimensions || !B->dimensions)
     return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
@@ -2152,6 +2170,7 @@ TT_EXPORT tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
 }
 
 TT_EXPORT tt_status tt_ttv_host(taco_tensor_t* y, const taco_tensor_t* B, const taco_tensor_t* x) {
+  NvtxRange nvtx_range("tt_ttv_host");
   clear_error();
   if (!y || !B || !x || !y->vals || !x->vals) return set_error(TT_ERR_INVALID_ARGUMENT, "null argument");
   tt_plan* p = nullptr;
