@@ -235,3 +235,22 @@ def test_five_modes(prec, R):
     assert tt.variant_info(plan.variant)["staged"] == 4
     if prec == "fp32":
         close(tt.mttkrp_host(B, facs), ref, "fp32")
+
+
+def test_headline_code_path():
+    """The headline's exact code path on a 4M-nonzero tensor of its shape class: a
+    leaf mode of 2,000,000 (so the automatic rule gives the headline's 3 slabs of
+    the 128 MB FP16 leaf factor), lognormal(1.5, 1.8) fiber lengths with long
+    fibers, N(0,1) factors; variant strip_b2_g128_c8 with FP16 storage, and 16-bit
+    fixed point, against the FP64 oracle on every row, twice (bit-equal)."""
+    B = tt.gen_lognormal_fibers((20_000, 10_000, 2_000_000), 4_000_003, 1.5, 1.8, 2, 200_000, 5)
+    facs = [tt.gen_dense(10_000, 32, 1, 41), tt.gen_dense(2_000_000, 32, 1, 42)]
+    ref = O.mttkrp(to_oracle(B), facs)
+    v = next(i for i in range(tt.num_variants()) if tt.variant_info(i)["name"] == "strip_b2_g128_c8")
+    for prec in ("fp16", "fx16"):
+        plan = tt.Plan(B, rank=32, prec=prec, select=tt.SELECT_FIXED, variant=v)
+        assert plan.slabs == 3
+        del plan
+        outs = run(B, facs, prec, v, reps=2)
+        close(outs[0], ref, prec)
+        assert np.array_equal(outs[0], outs[1])
