@@ -506,8 +506,8 @@ def secondary_ttv(args):
 def secondary_mttkrp4(args):
     """MTTKRP on the 80M-nonzero 4-mode tensor: 5,000 x 3,000 x 2,000 x 100,000, 80M nonzeros, Zipf(1.2) on
     modes 0 and 3, rank 32 N(0,1) factors; 16-bit storage against plain FP32, each on the fastest variant of
-    an exhaustive sweep (the learned network covers three modes); every output row checked against the FP64
-    oracle."""
+    an exhaustive sweep, and FP16 with the learned selector's four-mode model (``fp16_model``: its regret
+    against the sweep's pick); every output row checked against the FP64 oracle."""
     import tentaco_gb300 as tt
     from oracle import oracle as O
 
@@ -519,8 +519,11 @@ def secondary_mttkrp4(args):
     res = {"nnz": B.nnz}
     sub = argparse.Namespace(**vars(args))
     sub.steps = max(3, args.steps // 2)
+    sweep_ms = None
     for prec in ("fp16", "fx16", "fp32"):
         plan, A, info = timed_plan(tt, B, facs, prec, tt.SELECT_SWEEP, sub)
+        if prec == "fp16":
+            sweep_ms = plan.sweep_times()
         info["gflops"] = round(4.0 * B.nnz * RANK / (info["ms_per_step"] * 1e-3) / 1e9, 2)
         s_v, s_u, s_l = prec_bytes(prec)
         U = [int(np.count_nonzero(np.bincount(B.crd(l), minlength=dims[l]))) for l in (1, 2, 3)]
@@ -532,6 +535,17 @@ def secondary_mttkrp4(args):
         del plan
     for prec in ("fp16", "fx16"):
         res[f"speedup_{prec}_vs_fp32"] = round(res["fp32"]["ms_per_step"] / res[prec]["ms_per_step"], 3)
+    # the learned selector (the four-mode model) on the same tensor, FP16: its pick
+    # against the sweep's, and the speed-up over plain FP32
+    plan, A, info = timed_plan(tt, B, facs, "fp16", tt.SELECT_MODEL, sub)
+    info["gflops"] = round(4.0 * B.nnz * RANK / (info["ms_per_step"] * 1e-3) / 1e9, 2)
+    info["error_vs_fp64"] = errors(A, ref)
+    # regret from the sweep's own timings of both picks (one timing context)
+    info["same_variant_as_sweep"] = info["variant"] == res["fp16"]["variant"]
+    info["regret_vs_sweep"] = round(float(sweep_ms[info["variant"]] / sweep_ms[res["fp16"]["variant"]]) - 1.0, 4)
+    info["speedup_vs_fp32"] = round(res["fp32"]["ms_per_step"] / info["ms_per_step"], 3)
+    res["fp16_model"] = info
+    del plan
     return res
 
 

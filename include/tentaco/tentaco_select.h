@@ -56,23 +56,29 @@ tt_status tt_mlp_adam(float* params, const float* grads, float* m, float* v, int
 
 /*
  * Selector model file ("TTSEL001"): header {magic[8], int32 version, n_in,
- * hidden, nout, n_models}, then per model {int32 storage class (0: FP32
- * storage, 1: 16-bit storage), float mean[12], float std[12], float
- * params[tt_mlp_num_params(nout)]}.  Little-endian.
+ * hidden, nout, n_models}, (version 3) int32 tensor order, then per model
+ * {int32 storage class (0: FP32 storage, 1: 16-bit storage), float mean[12],
+ * float std[12], (versions 2 and 3) float lo[12], float hi[12] (the training
+ * tensors' feature range), float params[tt_mlp_num_params(nout)]}.
+ * Little-endian.  Versions 1 and 2 hold three-mode models; a version 3 file
+ * names its order (3 or 4) and replaces that order's models.
  *
- * path NULL: selector_model.bin in the directory of this library (loaded on
- * first use by TT_SELECT_MODEL as well).  Returns TT_ERR_INVALID_ARGUMENT for a
- * missing or malformed file; the previously loaded model, if any, is kept.
+ * path NULL: selector_model.bin in the directory of this library.  Each order's
+ * default file (selector_model.bin, selector_model_o4.bin) is loaded on first use
+ * by TT_SELECT_MODEL.  Returns TT_ERR_INVALID_ARGUMENT for a missing or malformed
+ * file; the previously loaded models, if any, are kept.
  */
 tt_status tt_selector_load(const char* path);
-/* Number of models loaded (0: TT_SELECT_MODEL falls back to the heuristic). */
+/* Number of three-mode models loaded (0: TT_SELECT_MODEL falls back to the heuristic). */
 int32_t tt_selector_models(void);
+/* Number of models loaded for tensors of this order (3 or 4; 0 otherwise). */
+int32_t tt_selector_models_for_order(int32_t order);
 
 /*
  * Run the network (on the current device) for tensor B at the given rank and
  * storage precision: scores[v] for v < n (n <= tt_num_variants()), lower
  * meaning predicted faster; variants not valid for the shape get +inf.
- * TT_ERR_UNSUPPORTED when no model covers the shape (order 3 only).
+ * TT_ERR_UNSUPPORTED when no model covers the shape (orders 3 and 4).
  */
 tt_status tt_selector_scores(const taco_tensor_t* B, int32_t rank, tt_precision prec, float* scores,
                              int32_t n);

@@ -139,6 +139,7 @@ def lib():
         "tt_selector_load": (S, [C.c_char_p]),
         "tt_release_cached_memory": (S, []),
         "tt_selector_models": (C.c_int32, []),
+        "tt_selector_models_for_order": (C.c_int32, [C.c_int32]),
         "tt_selector_scores": (S, [_TP, C.c_int32, S, C.POINTER(C.c_float), C.c_int32]),
         "ttv_csf_gpu_taco": (None, [_TP, _TP, _TP]),
     }
@@ -649,8 +650,9 @@ def selector_load(path=None) -> None:
     check(lib().tt_selector_load(None if path is None else os.fsencode(path)))
 
 
-def selector_models() -> int:
-    return int(lib().tt_selector_models())
+def selector_models(order: int = 3) -> int:
+    """Models loaded for tensors of this order (3 or 4)."""
+    return int(lib().tt_selector_models_for_order(order))
 
 
 def selector_scores(B, rank: int, prec="fp32") -> np.ndarray:

@@ -26,34 +26,44 @@ struct Model {
   std::vector<float> params;
 };
 
+// One model set per tensor order (three and four modes), each with its own
+// default file beside the library.
+struct ModelSet {
+  std::vector<Model> models;
+  int nout = 0;
+  bool tried_default = false;
+};
 std::mutex g_mu;
-std::vector<Model> g_models;
-int g_nout = 0;
-bool g_tried_default = false;
+ModelSet g_sets[2];  // [0]: three modes, [1]: four modes
+int set_index(int order) { return order == 4 ? 1 : order == 3 ? 0 : -1; }
 
-std::string default_model_path() {
+std::string default_model_path(int order = 3) {
+  const char* name = order == 4 ? "/selector_model_o4.bin" : "/selector_model.bin";
   Dl_info info;
   if (dladdr((void*)&tt_selector_models, &info) && info.dli_fname) {
     std::string p(info.dli_fname);
     const size_t k = p.rfind('/');
-    return (k == std::string::npos ? std::string(".") : p.substr(0, k)) + "/selector_model.bin";
+    return (k == std::string::npos ? std::string(".") : p.substr(0, k)) + name;
   }
-  return "selector_model.bin";
+  return name + 1;
 }
 
 // File layout (little-endian): "TTSEL001", int32 {version, inputs, hidden, outputs,
-// models}, then per model: int32 storage, float mean[inputs], sd[inputs], (version
-// 2 only) lo[inputs], hi[inputs], params.  Version 1 files carry no training range
-// and count every tensor as inside it.
-tt_status load_file(const std::string& path, std::vector<Model>& out, int& nout) {
+// models}, (version 3) int32 tensor order, then per model: int32 storage, float
+// mean[inputs], sd[inputs], (versions 2 and 3) lo[inputs], hi[inputs], params.
+// Version 1 files carry no training range and count every tensor as inside it;
+// versions 1 and 2 hold three-mode models.
+tt_status load_file(const std::string& path, std::vector<Model>& out, int& nout, int& order) {
   FILE* f = std::fopen(path.c_str(), "rb");
   if (!f) return set_error(TT_ERR_INVALID_ARGUMENT, "selector model %s: cannot open", path.c_str());
   auto rd = [&](void* p, size_t n) { return std::fread(p, 1, n, f) == n; };
   char magic[8];
   int32_t hdr[5];
   bool ok = rd(magic, 8) && std::memcmp(magic, "TTSEL001", 8) == 0 && rd(hdr, sizeof(hdr));
-  ok = ok && (hdr[0] == 1 || hdr[0] == 2) && hdr[1] == TT_MLP_IN && hdr[2] == TT_MLP_HIDDEN && hdr[3] > 0 && hdr[3] <= 4096 &&
-       hdr[4] > 0 && hdr[4] <= 8;
+  ok = ok && hdr[0] >= 1 && hdr[0] <= 3 && hdr[1] == TT_MLP_IN && hdr[2] == TT_MLP_HIDDEN && hdr[3] > 0 &&
+       hdr[3] <= 4096 && hdr[4] > 0 && hdr[4] <= 8;
+  int32_t ord = 3;
+  if (ok && hdr[0] == 3) ok = rd(&ord, 4) && set_index(ord) >= 0;
   std::vector<Model> ms;
   if (ok) {
     const int64_t np = tt_mlp_num_params(hdr[3]);
@@ -62,7 +72,7 @@ tt_status load_file(const std::string& path, std::vector<Model>& out, int& nout)
       int32_t storage = 0;
       m.params.resize((size_t)np);
       ok = rd(&storage, 4) && rd(m.mean, sizeof(m.mean)) && rd(m.sd, sizeof(m.sd));
-      if (hdr[0] == 2) {
+      if (hdr[0] >= 2) {
         ok = ok && rd(m.lo, sizeof(m.lo)) && rd(m.hi, sizeof(m.hi));
       } else {
         std::fill(m.lo, m.lo + TT_MLP_IN, -std::numeric_limits<float>::infinity());
@@ -80,21 +90,29 @@ tt_status load_file(const std::string& path, std::vector<Model>& out, int& nout)
   if (!ok) return set_error(TT_ERR_INVALID_ARGUMENT, "selector model %s: malformed", path.c_str());
   out = std::move(ms);
   nout = hdr[3];
+  order = ord;
   return TT_OK;
 }
 
-// The model for a storage class, loading the default file on first use.
-const Model* model_for(int storage, int& nout) {
+// The model for a storage class and tensor order, loading that order's default
+// file on first use.
+const Model* model_for(int storage, int order, int& nout) {
+  const int si = set_index(order);
+  if (si < 0) return nullptr;
   std::lock_guard<std::mutex> lk(g_mu);
-  if (g_models.empty() && !g_tried_default) {
-    g_tried_default = true;
+  ModelSet& set = g_sets[si];
+  if (set.models.empty() && !set.tried_default) {
+    set.tried_default = true;
     std::vector<Model> ms;
-    int n = 0;
-    if (load_file(default_model_path(), ms, n) == TT_OK) { g_models = std::move(ms); g_nout = n; }
+    int n = 0, ord = 0;
+    if (load_file(default_model_path(order), ms, n, ord) == TT_OK && ord == order) {
+      set.models = std::move(ms);
+      set.nout = n;
+    }
     clear_error();
   }
-  for (const Model& m : g_models)
-    if (m.storage == storage) { nout = g_nout; return &m; }
+  for (const Model& m : set.models)
+    if (m.storage == storage) { nout = set.nout; return &m; }
   return nullptr;
 }
 
@@ -104,9 +122,9 @@ int storage_class(int prec) { return prec == (int)TT_PREC_FP32 ? 0 : 1; }
 // in_range (optional): whether every feature lies inside the training range.
 tt_status scores_for(const taco_tensor_t* B, int order, int rank, int prec, std::vector<float>& scores,
                      bool* in_range = nullptr) {
-  if (order != 3) return set_error(TT_ERR_UNSUPPORTED, "the selector covers 3-mode tensors");
+  if (order != 3 && order != 4) return set_error(TT_ERR_UNSUPPORTED, "the selector covers 3- and 4-mode tensors");
   int nout = 0;
-  const Model* m = model_for(storage_class(prec), nout);
+  const Model* m = model_for(storage_class(prec), order, nout);
   if (!m) return set_error(TT_ERR_UNSUPPORTED, "no selector model for this storage precision");
   float f[TT_MLP_IN];
   tt_status s = tt_csf_features(B, rank, f);
@@ -165,21 +183,26 @@ using namespace tt;
 TT_EXPORT tt_status tt_selector_load(const char* path) {
   clear_error();
   std::vector<Model> ms;
-  int n = 0;
-  tt_status s = load_file(path ? std::string(path) : default_model_path(), ms, n);
+  int n = 0, ord = 3;
+  tt_status s = load_file(path ? std::string(path) : default_model_path(), ms, n, ord);
   if (s != TT_OK) return s;
   std::lock_guard<std::mutex> lk(g_mu);
-  g_models = std::move(ms);
-  g_nout = n;
-  g_tried_default = true;
+  ModelSet& set = g_sets[set_index(ord)];
+  set.models = std::move(ms);
+  set.nout = n;
+  set.tried_default = true;
   return TT_OK;
 }
 
-TT_EXPORT int32_t tt_selector_models(void) {
+TT_EXPORT int32_t tt_selector_models(void) { return tt_selector_models_for_order(3); }
+
+TT_EXPORT int32_t tt_selector_models_for_order(int32_t order) {
+  const int si = set_index(order);
+  if (si < 0) return 0;
   int n = 0;
-  model_for(0, n);  // triggers the default load
+  model_for(0, order, n);  // triggers the default load
   std::lock_guard<std::mutex> lk(g_mu);
-  return (int32_t)g_models.size();
+  return (int32_t)g_sets[si].models.size();
 }
 
 TT_EXPORT tt_status tt_selector_scores(const taco_tensor_t* B, int32_t rank, tt_precision prec, float* scores,

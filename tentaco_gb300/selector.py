@@ -40,6 +40,7 @@ NIN = 12
 HIDDEN = 64
 MAGIC = b"TTSEL001"
 CORPUS_SEED = 4000
+CORPUS_SEED_O4 = 5000  # four-mode corpus: tensor t uses seed 5000 + t
 PRECS = ("fp16", "fp32")  # storage classes 1 and 0
 
 
@@ -62,13 +63,38 @@ def corpus_params(t: int) -> dict:
     return {"t": t, "seed": CORPUS_SEED + t, "dims": dims, "nnz_target": min(nnz, cap), "zipf": zipf, "rank": rank}
 
 
+def corpus_params_o4(t: int) -> dict:
+    """Parameters of four-mode corpus tensor t (config 5's family: four modes of
+    10^3-10^5, Zipf skew per mode, rank 8-64; at most 2*10^7 nonzeros so that a
+    sweep of every variant stays short)."""
+    rng = np.random.default_rng(CORPUS_SEED_O4 + t)
+    # the CSF builder packs a nonzero's coordinates into one 64-bit key: mode sizes
+    # are redrawn until their bits fit in 62 (config 5's 5,000 x 3,000 x 2,000 x
+    # 100,000 needs 53)
+    while True:
+        dims = [int(round(10 ** rng.uniform(3, 5))) for _ in range(4)]
+        if sum(int(np.ceil(np.log2(d))) for d in dims) <= 62:
+            break
+    nnz = int(round(10 ** rng.uniform(5, np.log10(2e7))))
+    zipf = [float(rng.uniform(0, 1.5)) for _ in range(4)]
+    rank = int(rng.choice([8, 16, 32, 64]))
+    cap = dims[0] * dims[1] * dims[2] * dims[3] // 4
+    return {"t": t, "seed": CORPUS_SEED_O4 + t, "dims": dims, "nnz_target": min(nnz, cap), "zipf": zipf,
+            "rank": rank, "order": 4}
+
+
+def params_for(t: int, order: int) -> dict:
+    return corpus_params(t) if order == 3 else corpus_params_o4(t)
+
+
 def corpus_tensor(r: dict):
     import tentaco_gb300 as tt
     return tt.gen_zipf(r["dims"], r["zipf"], r["nnz_target"], r["seed"], 0.0, 1.0, 8)
 
 
-def run_corpus(out_path: str, n: int = 400, start: int = 0, precs=PRECS, log=sys.stdout) -> None:
-    """Sweep every variant on corpus tensors start..n-1; one JSON line per (tensor, precision)."""
+def run_corpus(out_path: str, n: int = 400, start: int = 0, precs=PRECS, log=sys.stdout, order: int = 3) -> None:
+    """Sweep every variant on corpus tensors start..n-1 (three or four modes); one
+    JSON line per (tensor, precision)."""
     import tentaco_gb300 as tt
     done = set()
     if os.path.exists(out_path):
@@ -81,7 +107,7 @@ def run_corpus(out_path: str, n: int = 400, start: int = 0, precs=PRECS, log=sys
         for t in range(start, n):
             if all((t, p) in done for p in precs):
                 continue
-            r0 = corpus_params(t)
+            r0 = params_for(t, order)
             t0 = time.time()
             B = corpus_tensor(r0)
             feats = B.features(r0["rank"])
@@ -93,7 +119,7 @@ def run_corpus(out_path: str, n: int = 400, start: int = 0, precs=PRECS, log=sys
                 valid = [m if m > 0 else np.inf for m in ms]
                 rec = dict(r0, nnz=int(B.nnz), prec=prec, features=[float(x) for x in feats], ms=ms,
                            best=int(np.argmin(valid)),
-                           default=int(tt.default_variant(3, r0["rank"], prec, int(B.nnz))))
+                           default=int(tt.default_variant(order, r0["rank"], prec, int(B.nnz))))
                 del plan
                 f.write(json.dumps(rec) + "\n")
                 f.flush()
@@ -114,11 +140,15 @@ def dataset(recs: list, storage: int, split: str | None):
     return rs, X, T, valid.astype(np.float64)
 
 
-def write_model(path: str, models: list) -> None:
-    """Version 2: per model storage, mean, sd, lo, hi (training feature range), params."""
+def write_model(path: str, models: list, order: int = 3) -> None:
+    """Version 2 (three modes) or 3 (the tensor order recorded after the model
+    count): per model storage, mean, sd, lo, hi (training feature range), params."""
     with open(path, "wb") as f:
         f.write(MAGIC)
-        f.write(struct.pack("<5i", 2, NIN, HIDDEN, models[0]["nout"], len(models)))
+        if order == 3:
+            f.write(struct.pack("<5i", 2, NIN, HIDDEN, models[0]["nout"], len(models)))
+        else:
+            f.write(struct.pack("<6i", 3, NIN, HIDDEN, models[0]["nout"], len(models), order))
         for m in models:
             f.write(struct.pack("<i", m["storage"]))
             for key in ("mean", "sd", "lo", "hi"):
@@ -131,16 +161,20 @@ def read_model(path: str) -> list:
         data = f.read()
     assert data[:8] == MAGIC, "not a selector model file"
     ver, nin, hid, nout, nm = struct.unpack_from("<5i", data, 8)
-    assert ver in (1, 2) and nin == NIN and hid == HIDDEN
+    assert ver in (1, 2, 3) and nin == NIN and hid == HIDDEN
     np_ = NIN * HIDDEN + HIDDEN + 2 * (HIDDEN * HIDDEN + HIDDEN) + HIDDEN * nout + nout
     off = 28
+    order = 3
+    if ver == 3:
+        (order,) = struct.unpack_from("<i", data, off)
+        off += 4
     out = []
     for _ in range(nm):
         (storage,) = struct.unpack_from("<i", data, off)
         off += 4
         mean = np.frombuffer(data, "<f4", NIN, off); off += 4 * NIN
         sd = np.frombuffer(data, "<f4", NIN, off); off += 4 * NIN
-        if ver == 2:
+        if ver >= 2:
             lo = np.frombuffer(data, "<f4", NIN, off).copy(); off += 4 * NIN
             hi = np.frombuffer(data, "<f4", NIN, off).copy(); off += 4 * NIN
         else:  # no recorded range: every tensor counts as inside it
@@ -148,7 +182,7 @@ def read_model(path: str) -> list:
             hi = np.full(NIN, np.inf, np.float32)
         params = np.frombuffer(data, "<f4", np_, off); off += 4 * np_
         out.append({"storage": storage, "nout": nout, "mean": mean.copy(), "sd": sd.copy(), "lo": lo, "hi": hi,
-                    "params": params.copy()})
+                    "params": params.copy(), "order": order})
     assert off == len(data)
     return out
 
@@ -208,7 +242,7 @@ def heuristic_pick(r: dict) -> int:
     """The fixed heuristic's variant for a corpus record (the library's current rule)."""
     try:
         import tentaco_gb300 as tt
-        return int(tt.default_variant(3, r["rank"], r["prec"], r["nnz"]))
+        return int(tt.default_variant(r.get("order", 3), r["rank"], r["prec"], r["nnz"]))
     except Exception:  # library not built: the rule recorded with the sweep
         return int(r["default"])
 
@@ -248,6 +282,7 @@ def main(argv=None) -> int:
     c.add_argument("--out", required=True)
     c.add_argument("--n", type=int, default=400)
     c.add_argument("--start", type=int, default=0)
+    c.add_argument("--order", type=int, default=3, choices=[3, 4])
     t = sub.add_parser("train")
     t.add_argument("--corpus", required=True)
     t.add_argument("--out", required=True)
@@ -256,16 +291,17 @@ def main(argv=None) -> int:
     t.add_argument("--wd", type=float, default=3e-3, help="decoupled weight decay")
     t.add_argument("--seed", type=int, default=0, help="seed of the initial weights")
     t.add_argument("--report", default=None, help="write the held-out regret report (JSON) here")
+    t.add_argument("--order", type=int, default=3, choices=[3, 4], help="tensor order of the corpus")
     a = ap.parse_args(argv)
     if a.cmd == "corpus":
-        run_corpus(a.out, a.n, a.start)
+        run_corpus(a.out, a.n, a.start, order=a.order)
         return 0
     import tentaco_gb300 as tt
     with open(a.corpus) as f:
         recs = [json.loads(l) for l in f if l.strip()]
     nout = len(recs[0]["ms"])
     models = [train(recs, s, nout, steps=a.steps, lr=a.lr, wd=a.wd, seed=a.seed) for s in (0, 1)]
-    write_model(a.out, models)
+    write_model(a.out, models, order=a.order)
     net = tt.Mlp(nout, 1024)
     rep = evaluate(recs, {m["storage"]: m for m in models},
                    forward=lambda p, X: net.forward(p.astype(np.float32), X.astype(np.float32)).astype(np.float64))
