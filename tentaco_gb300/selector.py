@@ -212,7 +212,7 @@ def init_params(nout: int, seed: int) -> np.ndarray:
     return np.concatenate(parts).astype(np.float32)
 
 
-def train(recs: list, storage: int, nout: int, steps: int = 3000, lr: float = 1e-3, wd: float = 3e-3,
+def train(recs: list, storage: int, nout: int, steps: int = 3000, lr: float = 3e-4, wd: float = 3e-3,
           seed: int = 0, log=sys.stdout) -> dict:
     import tentaco_gb300 as tt
     _, X, T, M = dataset(recs, storage, "train")
@@ -287,7 +287,7 @@ def main(argv=None) -> int:
     t.add_argument("--corpus", required=True)
     t.add_argument("--out", required=True)
     t.add_argument("--steps", type=int, default=3000)
-    t.add_argument("--lr", type=float, default=1e-3)
+    t.add_argument("--lr", type=float, default=3e-4)
     t.add_argument("--wd", type=float, default=3e-3, help="decoupled weight decay")
     t.add_argument("--seed", type=int, default=0, help="seed of the initial weights")
     t.add_argument("--report", default=None, help="write the held-out regret report (JSON) here")
