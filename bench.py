@@ -447,8 +447,9 @@ def run_gpu_arm(args, rank, world, d):
                       "ms_per_step": round(float(np.mean(e2e_ms)), 2), "h2d_bytes_per_step": int(h2d),
                       "d2h_bytes_per_step": int(Ahost.nbytes),
                       "host_memory": "pinned (tt_host_register)",
-                      "api": "tt_mttkrp_host (plan create + upload + factor conversion + run + download; "
-                             "no slabs: one call cannot repay the slab layout's host build)"}
+                      "api": "tt_mttkrp_host (plan create + upload + factor conversion + run + download, "
+                             "the uploads overlapped with the device work; no slabs: one call cannot repay "
+                             "the slab layout's host build)"}
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(oracle_csf(B), C, D, budget_s=12.0)
