@@ -15,6 +15,13 @@
 
 namespace tt {
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization starts (its blocks become resident) once every block of the
+// previous kernel on the stream has exited, without the launch gap, and waits here
+// until that kernel's memory operations are visible.  Launched without the
+// attribute, it returns at once.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Storage precisions: which of values / factors are held in 16 bits.
 //   kFP32  values FP32, factors FP32
 //   kBF16  values BF16, factors BF16 (power-of-two per-column scales)

@@ -2,6 +2,7 @@
 #include <cuda_bf16.h>
 #include <algorithm>
 #include <atomic>
+#include <utility>
 #include <cuda_fp16.h>
 #include "tt_kernels.h"
 #include "tt_mttkrp.cuh"
@@ -9,6 +10,25 @@
 #include "tt_strip.cuh"
 
 namespace tt {
+
+// A launch of a kernel that begins with grid_dependency_wait(): with programmatic
+// stream serialization, so it starts as the previous kernel's blocks finish instead
+// of after a launch gap.
+template <typename... P, typename... A>
+cudaError_t launch_dependent(void (*k)(P...), int grid, int block, cudaStream_t s, A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...);
+}
+
 
 WalkLauncher walk_launcher(int order, int prec, int cpt, int lpr, int staged) {
   if (staged == 8 || staged == 9) {  // strip walk (U = 4 / 2 nonzeros per team and step)
@@ -90,6 +110,7 @@ template <int S>
 __global__ void __launch_bounds__(256) virtual_rows_kernel(const float* __restrict__ V, const int32_t* __restrict__ rnz,
                                                            int64_t nrows, int64_t vstride, int ldv, int lda, int R,
                                                            float* __restrict__ A) {
+  grid_dependency_wait();       // the walk's and the merge's virtual rows
   const int q4 = (R + 3) >> 2;  // 4-column groups per row
   const int64_t n = nrows * q4;
   const bool narrow = n <= 0x7fffffff;  // 32-bit index arithmetic
@@ -138,8 +159,8 @@ __global__ void __launch_bounds__(256) virtual_rows_kernel(const float* __restri
 template <int S>
 cudaError_t launch_virtual_rows_s(const float* V, const int32_t* rnz, int64_t nrows, int64_t vstride, int ldv, int lda,
                                   int R, float* A, int grid, cudaStream_t s) {
-  virtual_rows_kernel<S><<<grid, 256, 0, s>>>(V, rnz, nrows, vstride, ldv, lda, R, A);
-  return cudaGetLastError();
+  const cudaError_t e = launch_dependent(virtual_rows_kernel<S>, grid, 256, s, V, rnz, nrows, vstride, ldv, lda, R, A);
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_virtual_rows(const float* V, const int32_t* rnz, int S, int64_t nrows, int64_t vstride, int ldv,
@@ -172,22 +193,22 @@ cudaError_t launch_window_max(int order, const WalkArgs& a, int* out, cudaStream
   return cudaGetLastError();
 }
 
+template <int ORDER>
+cudaError_t launch_fold_chain(const WalkArgs& a, int grid, cudaStream_t s) {
+  cudaError_t e = launch_dependent(seg_fold_kernel<ORDER>, grid, 256, s, a);
+  if (e == cudaSuccess) e = launch_dependent(seg_chain_kernel<ORDER>, grid, 256, s, a);
+  return e;
+}
+
 cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s) {
   if (a.nblocks == 0) return cudaSuccess;
   const int grid = (num_segments(a.nblocks) + 7) / 8;  // one warp per segment
-  if (order == 2) {
-    seg_fold_kernel<2><<<grid, 256, 0, s>>>(a);
-    seg_chain_kernel<2><<<grid, 256, 0, s>>>(a);
-  } else if (order == 3) {
-    seg_fold_kernel<3><<<grid, 256, 0, s>>>(a);
-    seg_chain_kernel<3><<<grid, 256, 0, s>>>(a);
-  } else if (order == 4) {
-    seg_fold_kernel<4><<<grid, 256, 0, s>>>(a);
-    seg_chain_kernel<4><<<grid, 256, 0, s>>>(a);
-  } else {
-    seg_fold_kernel<5><<<grid, 256, 0, s>>>(a);
-    seg_chain_kernel<5><<<grid, 256, 0, s>>>(a);
-  }
+  cudaError_t e;
+  if (order == 2) e = launch_fold_chain<2>(a, grid, s);
+  else if (order == 3) e = launch_fold_chain<3>(a, grid, s);
+  else if (order == 4) e = launch_fold_chain<4>(a, grid, s);
+  else e = launch_fold_chain<5>(a, grid, s);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 

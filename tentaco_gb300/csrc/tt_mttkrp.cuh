@@ -1268,6 +1268,7 @@ __device__ __forceinline__ void put_row_pair(const WalkArgs& a, int r, int j, fl
 
 template <int ORDER>  // (the fold itself does not depend on the order)
 __global__ void __launch_bounds__(256, 2) seg_fold_kernel(const __grid_constant__ WalkArgs a) {
+  grid_dependency_wait();  // the walk's carries and metadata
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sg = blockIdx.x * (blockDim.x >> 5) + warp;
   if (sg >= num_segments(a.nblocks)) return;
@@ -1385,6 +1386,7 @@ __global__ void __launch_bounds__(256, 2) seg_fold_kernel(const __grid_constant_
 
 template <int ORDER>
 __global__ void __launch_bounds__(256) seg_chain_kernel(const __grid_constant__ WalkArgs a) {
+  grid_dependency_wait();  // the fold's segment partials
   constexpr int kShort = 16;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sg = blockIdx.x * (blockDim.x >> 5) + warp;
