@@ -543,7 +543,8 @@ def secondary_mttkrp4(args):
     info["error_vs_fp64"] = errors(A, ref)
     # regret from the sweep's own timings of both picks (one timing context)
     info["same_variant_as_sweep"] = info["variant"] == res["fp16"]["variant"]
-    info["regret_vs_sweep"] = round(float(sweep_ms[info["variant"]] / sweep_ms[res["fp16"]["variant"]]) - 1.0, 4)
+    mv, sv = float(sweep_ms[info["variant"]]), float(sweep_ms[res["fp16"]["variant"]])
+    info["regret_vs_sweep"] = round(mv / sv - 1.0, 4) if mv > 0 and sv > 0 else None
     info["speedup_vs_fp32"] = round(res["fp32"]["ms_per_step"] / info["ms_per_step"], 3)
     res["fp16_model"] = info
     del plan
