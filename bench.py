@@ -327,6 +327,7 @@ def timed_plan(tt, B, facs, prec, select, args, clk=None, variant=0, rank=RANK, 
         clk.stop()
     assert plan.device_error() == 0
     info = {"ms_per_step": float(np.mean(step_ms)), "kernel_ms": float(np.mean(kern_ms)),
+            "ms_median": round(float(np.median(step_ms)), 4), "ms_min": round(float(np.min(step_ms)), 4),
             "variant": plan.variant, "variant_name": tt.variant_info(plan.variant)["name"], "slabs": plan.slabs,
             "selected_by": "fixed" if select == tt.SELECT_FIXED else
             ["heuristic", "model", "sweep", "model top-k timed"][plan.selected_by],
@@ -369,6 +370,7 @@ def run_gpu_arm(args, rank, world, d):
         oi["gflops"] = flops / (oi["ms_per_step"] * 1e-3) / 1e9
         cb, _, _ = compulsory_bytes(B, prec)
         oi["gbs_compulsory"] = round(cb / (oi["ms_per_step"] * 1e-3) / 1e9, 1)
+        oi["gbs_fp32_equivalent"] = round(compulsory_bytes(B, "fp32")[0] / (oi["ms_per_step"] * 1e-3) / 1e9, 1)
         oi["_A"] = Ao
         others[prec] = oi
         del po
@@ -387,6 +389,8 @@ def run_gpu_arm(args, rank, world, d):
         "config": workload_config(B.nnz, B.count(1), world),
         "plan": dict(info, precision=args.prec, select=args.select, gen_s=round(gen_s, 1)),
         "gbs_compulsory": round(cbytes / (ms * 1e-3) / 1e9, 1),
+        # the same work counted in FP32 bytes (the 16-bit speed-ups on equal work)
+        "gbs_fp32_equivalent": round(compulsory_bytes(B, "fp32")[0] / (ms * 1e-3) / 1e9, 1),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": prof.get("dram_bytes_per_launch") if prof else None,
                      "l2_hit_rate_pct": prof.get("l2_hit_rate_pct") if prof else None,
@@ -500,6 +504,8 @@ def secondary_ttv(args):
             "partition_ms": round(plan.partition_ms(), 4),
             "gflops": round(2.0 * B.nnz / (ms * 1e-3) / 1e9, 2),
             "gbs_compulsory": round(cbytes / (ms * 1e-3) / 1e9, 1),
+        # the same work counted in FP32 bytes (the 16-bit speed-ups on equal work)
+        "gbs_fp32_equivalent": round(compulsory_bytes(B, "fp32")[0] / (ms * 1e-3) / 1e9, 1),
             "roofline_frac": round(cbytes / (ms * 1e-3) / 1e9 / peak, 4),
             "error_vs_fp64": errors(y, ref)}
 
