@@ -89,6 +89,12 @@ __device__ __forceinline__ uint4 ld_stream_l1_u4(const void* p, uint64_t pol) {
                : "l"(p), "l"(pol));
   return r;
 }
+// 32 bytes of a stream (p 32-byte aligned): one 256-bit load (sm_100 and later).
+__device__ __forceinline__ void ld_stream_l1_v8(const void* p, uint64_t pol, uint32_t (&r)[8]) {
+  asm volatile("ld.global.nc.L2::cache_hint.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "l"(p), "l"(pol));
+}
 __device__ __forceinline__ uint2 ld_stream_u2(const void* p, uint64_t pol) {
   uint2 r;
   asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0,%1}, [%2], %3;"

@@ -268,10 +268,10 @@ cudaError_t launch_row_starts(const int32_t* pos1, const int32_t* pos2, const in
 
 // Dynamic shared memory above 48 KB needs a per-kernel, per-device opt-in: recorded
 // per instantiation so that it is asked for once.
-template <int VK, bool XS>
+template <int VK, bool XS, bool V8>
 cudaError_t launch_ttv_range_k(const WalkArgs& a, size_t smem, int grid, cudaStream_t s) {
   static std::atomic<size_t> allowed[64];
-  auto k = ttv_range_kernel<VK, XS>;
+  auto k = ttv_range_kernel<VK, XS, V8>;
   if (smem > 48 * 1024) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -289,7 +289,11 @@ cudaError_t launch_ttv_range_k(const WalkArgs& a, size_t smem, int grid, cudaStr
 
 template <int VK>
 cudaError_t launch_ttv_range_vk(const WalkArgs& a, bool xs, size_t smem, int grid, cudaStream_t s) {
-  return xs ? launch_ttv_range_k<VK, true>(a, smem, grid, s) : launch_ttv_range_k<VK, false>(a, smem, grid, s);
+  // 32-byte stream loads when both streams start on 32-byte boundaries (every
+  // lane's run then does: it begins a multiple of 16 entries in)
+  const bool v8 = ((uintptr_t)a.crd[1] & 31) == 0 && ((uintptr_t)a.vals & 31) == 0;
+  if (v8) return xs ? launch_ttv_range_k<VK, true, true>(a, smem, grid, s) : launch_ttv_range_k<VK, false, true>(a, smem, grid, s);
+  return xs ? launch_ttv_range_k<VK, true, false>(a, smem, grid, s) : launch_ttv_range_k<VK, false, false>(a, smem, grid, s);
 }
 
 // The range walk: a.nblocks ranges of a.wcap units, kTtvWarps ranges per block; x

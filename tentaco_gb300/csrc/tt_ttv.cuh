@@ -53,7 +53,10 @@ constexpr int kTtvMaxRU = 62;  // units per range (the partition entries fit two
 // a.P = RU * 512 and a.nblocks = ranges (the merge's units), a.wcap = RU,
 // a.part = the 512-nonzero partition, a.fac_rows[0] = length of x.
 
-template <int VK, bool XS>
+// V8: the lane's 64 bytes of coordinates (and of values) as 32-byte loads, half the
+// load instructions and L1 wavefronts of 16-byte ones (the streams must be 32-byte
+// aligned; the launcher checks).
+template <int VK, bool XS, bool V8>
 __global__ void __launch_bounds__(32 * kTtvWarps, 1) ttv_range_kernel(const __grid_constant__ WalkArgs a) {
   constexpr int NPT = kTtvNpt;
   constexpr int UN = 32 * NPT;                    // nonzeros per unit
@@ -90,17 +93,34 @@ __global__ void __launch_bounds__(32 * kTtvWarps, 1) ttv_range_kernel(const __gr
     const int64_t s64 = (int64_t)u * UN + (int64_t)lane * NPT;
     if (s64 < a.nnz) {  // runs are padded past the last 16-entry run
       const int32_t* gl = a.crd[1] + s64;
-#pragma unroll
-      for (int k = 0; k < NPT / 4; k++) {
-        const uint4 c4 = ld_stream_l1_u4(gl + 4 * k, polF);
-        S.lc[4 * k] = (int32_t)c4.x; S.lc[4 * k + 1] = (int32_t)c4.y;
-        S.lc[4 * k + 2] = (int32_t)c4.z; S.lc[4 * k + 3] = (int32_t)c4.w;
-      }
       const unsigned char* gv = static_cast<const unsigned char*>(a.vals) + s64 * (VK == kF32 ? 4 : 2);
+      if constexpr (V8) {
 #pragma unroll
-      for (int k = 0; k < NW / 4; k++) {
-        const uint4 w = ld_stream_l1_u4(gv + 16 * k, polF);
-        S.vw[4 * k] = w.x; S.vw[4 * k + 1] = w.y; S.vw[4 * k + 2] = w.z; S.vw[4 * k + 3] = w.w;
+        for (int k = 0; k < NPT / 8; k++) {
+          uint32_t w[8];
+          ld_stream_l1_v8(gl + 8 * k, polF, w);
+#pragma unroll
+          for (int j = 0; j < 8; j++) S.lc[8 * k + j] = (int32_t)w[j];
+        }
+#pragma unroll
+        for (int k = 0; k < NW / 8; k++) {
+          uint32_t w[8];
+          ld_stream_l1_v8(gv + 32 * k, polF, w);
+#pragma unroll
+          for (int j = 0; j < 8; j++) S.vw[8 * k + j] = w[j];
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < NPT / 4; k++) {
+          const uint4 c4 = ld_stream_l1_u4(gl + 4 * k, polF);
+          S.lc[4 * k] = (int32_t)c4.x; S.lc[4 * k + 1] = (int32_t)c4.y;
+          S.lc[4 * k + 2] = (int32_t)c4.z; S.lc[4 * k + 3] = (int32_t)c4.w;
+        }
+#pragma unroll
+        for (int k = 0; k < NW / 4; k++) {
+          const uint4 w = ld_stream_l1_u4(gv + 16 * k, polF);
+          S.vw[4 * k] = w.x; S.vw[4 * k + 1] = w.y; S.vw[4 * k + 2] = w.z; S.vw[4 * k + 3] = w.w;
+        }
       }
     } else {
 #pragma unroll
