@@ -1836,7 +1836,7 @@ int64_t oneshot_chunk(int64_t nnz, int P) {
 //   copy stream  the fiber structure, the values, the factors, then the leaf
 //                coordinates in chunks (starting on 128-byte host boundaries);
 //   check stream each chunk's leaf coordinates as the chunk lands;
-//   work stream  the structure check (the host waits for its verdict before
+//   work stream  the structure check (the host waits for its result before
 //                anything indexes through pos), kexp / rnz / the partition (the
 //                structure alone), the value and factor conversion, then per
 //                checked chunk the walk of every unit whose nonzeros have all
