@@ -71,9 +71,34 @@ def parse():
     return ap.parse_args()
 
 
+def physical_gpu_index() -> int:
+    """NVML's index of the GPU this process computes on (NVML ignores
+    CUDA_VISIBLE_DEVICES): its first entry when numeric, else 0."""
+    first = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0].strip()
+    return int(first) if first.isdigit() else 0
+
+
+def rank_visible_devices(env) -> str | None:
+    """CUDA_VISIBLE_DEVICES for this rank of a multi-process run (one GPU per rank):
+    the LOCAL_RANK-th entry of a list the launcher set, else the LOCAL_RANK-th GPU;
+    None for a single process."""
+    if int(env.get("WORLD_SIZE", "1")) <= 1:
+        return None
+    local = int(env.get("LOCAL_RANK", env.get("RANK", "0")))
+    given = [d for d in env.get("CUDA_VISIBLE_DEVICES", "").split(",") if d.strip()]
+    if given:
+        return given[local % len(given)].strip()
+    return str(local)
+
+
 def dist_setup(n):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    # each replica on its own GPU: the library works on the current device, so the
+    # rank sees only its GPU (set before anything initialises CUDA in this process)
+    vis = rank_visible_devices(os.environ)
+    if vis is not None:
+        os.environ["CUDA_VISIBLE_DEVICES"] = vis
     if world > 1:
         import torch.distributed as dist
 
@@ -155,7 +180,10 @@ class Clocks:
         if lib.nvmlInit_v2() != 0:
             return None
         h = ctypes.c_void_p()
-        if lib.nvmlDeviceGetHandleByIndex_v2(0, ctypes.byref(h)) != 0:
+        # the process's own GPU; index 0 when NVML numbers the GPUs differently (a
+        # container that shows one GPU under a host index)
+        if lib.nvmlDeviceGetHandleByIndex_v2(physical_gpu_index(), ctypes.byref(h)) != 0 and \
+                lib.nvmlDeviceGetHandleByIndex_v2(0, ctypes.byref(h)) != 0:
             return None
         mx = ctypes.c_uint()
         lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))  # NVML_CLOCK_SM
@@ -191,8 +219,11 @@ class Clocks:
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            n = subprocess.run(["nvidia-smi", "-L"], capture_output=True, text=True).stdout.count("GPU ")
+            idx = physical_gpu_index() if physical_gpu_index() < n else 0
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(idx), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
 

@@ -71,3 +71,27 @@ def test_reference_arm_loads_no_product_code():
     res = json.loads(r.stdout.strip().splitlines()[-1])
     assert res["mods"] == []
     assert res["keys"] == res["want"]
+
+
+def test_each_rank_computes_on_its_own_gpu():
+    """Under torchrun every replica sees one GPU: its LOCAL_RANK-th (of the list the
+    launcher set, if any), chosen before CUDA starts; a single process keeps the
+    environment as it is.  The clock sampler reads the same physical GPU."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert bench.rank_visible_devices({"WORLD_SIZE": "1"}) is None
+    assert bench.rank_visible_devices({"WORLD_SIZE": "4", "LOCAL_RANK": "3"}) == "3"
+    assert bench.rank_visible_devices({"WORLD_SIZE": "2", "LOCAL_RANK": "1", "CUDA_VISIBLE_DEVICES": "4,6"}) == "6"
+    assert bench.rank_visible_devices({"WORLD_SIZE": "2", "RANK": "1"}) == "1"
+    old = os.environ.get("CUDA_VISIBLE_DEVICES")
+    try:
+        os.environ["CUDA_VISIBLE_DEVICES"] = "6"
+        assert bench.physical_gpu_index() == 6
+        os.environ["CUDA_VISIBLE_DEVICES"] = "GPU-1234"
+        assert bench.physical_gpu_index() == 0
+    finally:
+        if old is None:
+            os.environ.pop("CUDA_VISIBLE_DEVICES", None)
+        else:
+            os.environ["CUDA_VISIBLE_DEVICES"] = old
