@@ -394,8 +394,11 @@ def run_gpu_arm(args, rank, world, d):
     del plan
 
     # other storage precisions on the same tensor (plain FP32 gives the 16-bit speed-ups)
+    # only rank 0 reports: the other replicas skip what is not timed across ranks
+    # (the other storage modes, the FP64 error checks, the secondary workloads)
+    lead = rank == 0
     others = {}
-    for prec in [x for x in args.compare.split(",") if x and x != args.prec]:
+    for prec in [x for x in args.compare.split(",") if x and x != args.prec and lead]:
         po, Ao, oi = timed_plan(tt, B, [C, D], prec, tt.SELECT_SWEEP if args.select != "default" else
                                 tt.SELECT_DEFAULT, args)
         oi["gflops"] = flops / (oi["ms_per_step"] * 1e-3) / 1e9
@@ -441,7 +444,7 @@ def run_gpu_arm(args, rank, world, d):
         for prec, o in others.items():
             if prec != "fp32":
                 o["speedup_vs_fp32"] = round(others["fp32"]["ms_per_step"] / o["ms_per_step"], 3)
-    if not args.no_errors:
+    if not args.no_errors and lead:
         ref = O.mttkrp(oracle_csf(B), [C.astype(np.float64), D.astype(np.float64)])
         out["error_vs_fp64"] = errors(Ah, ref)
         for o in others.values():
@@ -461,6 +464,9 @@ def run_gpu_arm(args, rank, world, d):
                            "ms_by_precision": {c[1]: round(c[0], 4) for c in cands}}
 
     if not args.no_e2e:
+        # every replica at once (a barrier first); the job's throughput over the
+        # slowest rank's mean call
+        barrier(d)
         prec_map = {"fp32": 0, "bf16": 1, "bf16f": 2, "fp16": 3, "fx16": 4}
         e2e_ms = []
         # the inputs and the output live in pinned (page-locked) host memory, as a
@@ -478,8 +484,9 @@ def run_gpu_arm(args, rank, world, d):
                 e2e_ms.append((time.perf_counter() - t) * 1e3)
         tt.unpin(pinned)
         h2d = B.nnz * 8 + (B.dims[0] + 1 + 2 * B.count(1) + 1) * 4 + (C.size + D.size) * 4
-        out["e2e"] = {"value": round(flops / (np.mean(e2e_ms) * 1e-3) / 1e9, 2), "unit": "GFLOP/s",
-                      "ms_per_step": round(float(np.mean(e2e_ms)), 2), "h2d_bytes_per_step": int(h2d),
+        e2e_mean = allmax(d, float(np.mean(e2e_ms)))
+        out["e2e"] = {"value": round(world * flops / (e2e_mean * 1e-3) / 1e9, 2), "unit": "GFLOP/s",
+                      "ms_per_step": round(e2e_mean, 2), "h2d_bytes_per_step": int(h2d),
                       "d2h_bytes_per_step": int(Ahost.nbytes),
                       "host_memory": "pinned (tt_host_register)",
                       "api": "tt_mttkrp_host (plan create + upload + factor conversion + run + download, "
@@ -488,7 +495,7 @@ def run_gpu_arm(args, rank, world, d):
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(oracle_csf(B), C, D, budget_s=12.0)
-    if not args.no_secondary:
+    if not args.no_secondary and lead:
         del B, C, D, Ah
         import gc
         import tentaco_gb300 as tt
