@@ -1723,7 +1723,8 @@ tt_status time_variants(tt_plan* p, cudaStream_t st, const std::vector<int>& can
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
         cudaStreamSynchronize(st);
-        for (void* d : tmp) cudaFree(d);
+        for (void* d : tmp) pool_free(d, st);
+        cudaStreamSynchronize(st);
         for (int m = 0; m < 4; m++) p->fac[m] = saved[m];
         p->d_colscale = saved_scale;
       }
@@ -1734,14 +1735,14 @@ tt_status time_variants(tt_plan* p, cudaStream_t st, const std::vector<int>& can
       // the upper-level factors in FP32)
       const size_t esz = p->prec == kFP32 || (p->prec == kFX16 && m < nm - 1) ? 4 : 2;
       void* d = nullptr;
-      CK(cudaMalloc(&d, (size_t)p->dims[m + 1] * p->rp * esz));
+      CK(pool_alloc(&d, (size_t)p->dims[m + 1] * p->rp * esz, st));
       sc.tmp.push_back(d);
       CK(cudaMemsetAsync(d, 0, (size_t)p->dims[m + 1] * p->rp * esz, st));
       p->fac[m] = d;
     }
     p->d_colscale = nullptr;
     float* A = nullptr;
-    CK(cudaMalloc(&A, (size_t)p->dims[0] * p->rank * sizeof(float)));
+    CK(pool_alloc((void**)&A, (size_t)p->dims[0] * p->rank * sizeof(float), st));
     sc.tmp.push_back(A);
     CK(cudaEventCreate(&sc.e0));
     CK(cudaEventCreate(&sc.e1));
