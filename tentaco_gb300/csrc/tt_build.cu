@@ -15,6 +15,7 @@
 #include <cstring>
 #include <vector>
 #include "tt_internal.h"
+#include "tt_kernels.h"
 
 namespace tt {
 namespace {
@@ -251,18 +252,22 @@ __global__ void root_pos_kernel(const int32_t* __restrict__ frow, int64_t nf, in
   }
 }
 
-// Device buffers freed at scope exit.
+// Device buffers from the library's pool (on the legacy default stream, which the
+// builder works on), handed back at scope exit, like all of the library's device
+// memory: driver-level allocation and release between plans (measured on the
+// candidate timing's placeholders) slowed the kernels of a later plan.
 struct DevBufs {
   std::vector<void*> p;
   template <typename T>
   cudaError_t get(T** out, size_t count) {
     *out = nullptr;
-    cudaError_t e = cudaMalloc((void**)out, std::max<size_t>(count, 1) * sizeof(T));
+    cudaError_t e = device_pool_alloc((void**)out, std::max<size_t>(count, 1) * sizeof(T), nullptr);
     if (e == cudaSuccess) p.push_back((void*)*out);
     return e;
   }
   ~DevBufs() {
-    for (void* q : p) cudaFree(q);
+    for (void* q : p) device_pool_free(q, nullptr);
+    cudaStreamSynchronize(nullptr);
   }
 };
 

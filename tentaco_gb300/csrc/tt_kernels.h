@@ -68,6 +68,10 @@ cudaError_t launch_row_starts(const int32_t* pos1, const int32_t* pos2, const in
                               int32_t* rnz, cudaStream_t s, int64_t off = 0, const int32_t* pos4 = nullptr);
 // FP64 merge of the rows the walk left in the carry buffer (after the walk kernel).
 cudaError_t launch_chain_fixup(int order, const WalkArgs& a, cudaStream_t s);
+// Allocation from the library's stream-ordered device memory pool (usable on `st` at
+// once, elsewhere after `st` is synchronised), and its release on `st`.
+cudaError_t device_pool_alloc(void** ptr, size_t bytes, cudaStream_t st);
+void device_pool_free(void* ptr, cudaStream_t st);
 // TTV walk over units of 32 * kTtvNpt nonzeros (a: the 2-level view, see tt_ttv.cuh).
 cudaError_t launch_ttv_ranges(const WalkArgs& a, int vals_kind, cudaStream_t s);
 

@@ -1807,6 +1807,13 @@ TT_EXPORT tt_status tt_plan_sweep_times(const tt_plan* p, float* ms, int32_t n) 
   return TT_OK;
 }
 
+// The library's stream-ordered device memory pool for the other translation units
+// (the GPU CSF builder's scratch): the same accounting and failure injection.
+namespace tt {
+cudaError_t device_pool_alloc(void** ptr, size_t bytes, cudaStream_t st) { return pool_alloc(ptr, bytes, st); }
+void device_pool_free(void* ptr, cudaStream_t st) { pool_free(ptr, st); }
+}  // namespace tt
+
 // ---------------------------------------------------------------------------
 // one-shot host calls
 // ---------------------------------------------------------------------------
