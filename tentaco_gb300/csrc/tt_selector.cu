@@ -138,7 +138,7 @@ tt_status scores_for(const taco_tensor_t* B, int order, int rank, int prec, std:
   const int64_t ns = tt_mlp_scratch_floats(1, nout);
   float* d = nullptr;
   const size_t total = (size_t)(np + TT_MLP_IN + ns + nout);
-  if (cudaMalloc((void**)&d, total * sizeof(float)) != cudaSuccess)
+  if (device_pool_alloc((void**)&d, total * sizeof(float), nullptr) != cudaSuccess)
     return set_error(TT_ERR_OUT_OF_MEMORY, "selector inference buffers");
   float* dp = d;
   float* dx = dp + np;
@@ -151,7 +151,8 @@ tt_status scores_for(const taco_tensor_t* B, int order, int rank, int prec, std:
     s = tt_mlp_forward(dp, nout, dx, 1, dsc, dout, nullptr);
     if (s == TT_OK) e = cudaMemcpy(out.data(), dout, sizeof(float) * (size_t)nout, cudaMemcpyDeviceToHost);
   }
-  cudaFree(d);
+  device_pool_free(d, nullptr);
+  cudaStreamSynchronize(nullptr);
   if (s != TT_OK) return s;
   if (e != cudaSuccess) return set_error(TT_ERR_CUDA, "selector inference: %s", cudaGetErrorString(e));
   const int nv = tt_num_variants();
