@@ -329,6 +329,35 @@ def oracle_csf(B):
                  [None] + [B.crd(l).astype(np.int64) for l in range(1, B.order)], B.vals.astype(np.float64))
 
 
+def _call_and_kernel_ms(tt, call, plan, steps, warmup, clk=None):
+    """Per-call ms of `steps` timed calls (the L2 flushed before each; CUDA events around each whole call on
+    the plan's stream), then the walk kernel's own ms over a second pass of `steps` calls with events around
+    the walk.  The first pass records no event between the walk and the merge kernels: one there holds back
+    the merge's programmatic dependent launch (about 6 us per call on a GB300)."""
+    plan.set_timing(2)
+    for _ in range(warmup):
+        tt.l2_flush()
+        call()
+    tt.synchronize()
+    step_ms, kern_ms = [], []
+    if clk:
+        clk.start()
+    for _ in range(steps):
+        tt.l2_flush()
+        call()
+        step_ms.append(plan.last_ms())
+    tt.synchronize()
+    if clk:
+        clk.stop()
+    plan.set_timing(1)
+    for _ in range(steps):
+        tt.l2_flush()
+        call()
+        kern_ms.append(plan.last_kernel_ms())
+    tt.synchronize()
+    return step_ms, kern_ms
+
+
 def timed_plan(tt, B, facs, prec, select, args, clk=None, variant=0, rank=RANK, steps=None, mode=0):
     """A plan on device-resident inputs: setup timed on the host; W warm-up calls,
     then K timed calls with the L2 flushed before each (CUDA events)."""
@@ -340,22 +369,7 @@ def timed_plan(tt, B, facs, prec, select, args, clk=None, variant=0, rank=RANK, 
     plan.set_factors(bufs)
     rows = B.dims[mode]
     A = tt.DeviceBuffer(rows * rank * 4)
-    plan.set_timing(True)
-    for _ in range(args.warmup):
-        tt.l2_flush()
-        plan.mttkrp(A)
-    tt.synchronize()
-    step_ms, kern_ms = [], []
-    if clk:
-        clk.start()
-    for _ in range(steps):
-        tt.l2_flush()
-        plan.mttkrp(A)
-        step_ms.append(plan.last_ms())
-        kern_ms.append(plan.last_kernel_ms())
-    tt.synchronize()
-    if clk:
-        clk.stop()
+    step_ms, kern_ms = _call_and_kernel_ms(tt, lambda: plan.mttkrp(A), plan, steps, args.warmup, clk)
     assert plan.device_error() == 0
     info = {"ms_per_step": float(np.mean(step_ms)), "kernel_ms": float(np.mean(kern_ms)),
             "ms_median": round(float(np.median(step_ms)), 4), "ms_min": round(float(np.min(step_ms)), 4),
@@ -515,19 +529,12 @@ def run_gpu_arm(args, rank, world, d):
 
 
 def _timed(call, plan, steps, warmup):
-    """Mean ms of a plan call over `steps` (L2 flushed before each), CUDA events."""
+    """Mean ms of a plan call and of its walk kernel over `steps` calls each (L2 flushed before each call),
+    CUDA events."""
     import tentaco_gb300 as tt
 
-    plan.set_timing(True)
-    for _ in range(warmup):
-        tt.l2_flush()
-        call()
-    ms = []
-    for _ in range(steps):
-        tt.l2_flush()
-        call()
-        ms.append(plan.last_ms())
-    return float(np.mean(ms))
+    step_ms, kern_ms = _call_and_kernel_ms(tt, call, plan, steps, warmup)
+    return float(np.mean(step_ms)), float(np.mean(kern_ms))
 
 
 def secondary_ttv(args):
@@ -542,8 +549,7 @@ def secondary_ttv(args):
     nfib = B.count(1)
     dx = tt.DeviceBuffer.from_array(x)
     dy = tt.DeviceBuffer(nfib * 4)
-    ms = _timed(lambda: plan.ttv(dx, dy), plan, max(3, args.steps), args.warmup)
-    kern = plan.last_kernel_ms()
+    ms, kern = _timed(lambda: plan.ttv(dx, dy), plan, max(3, args.steps), args.warmup)
     y = dy.to_array((nfib,))
     ref = O.ttv(oracle_csf(B), x.astype(np.float64))
     U = int(np.count_nonzero(np.bincount(B.crd(2), minlength=B.dims[2])))

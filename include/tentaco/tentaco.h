@@ -194,7 +194,12 @@ tt_status tt_plan_coo_fibers(const tt_plan* plan, int32_t* ij);
  * plan holds to the driver. */
 tt_status tt_release_cached_memory(void);
 
-/* Time every subsequent call's device work with CUDA events (default off). */
+/* Time every subsequent call's device work with CUDA events (default 0, off).
+ * 1: the whole call and its walk kernel(s) (tt_plan_last_ms, tt_plan_last_kernel_ms);
+ * 2: the whole call only.  Mode 1 records an event between the walk and the row
+ * merge, which holds back the merge kernels' early (programmatic dependent) launch:
+ * on a GB300 a call timed that way takes about 6 us longer than in mode 0 or 2.
+ * Other values: TT_ERR_INVALID_ARGUMENT. */
 tt_status tt_plan_set_timing(tt_plan* plan, int32_t enabled);
 /* Milliseconds of the last timed call (clear + kernels); waits for it.  The
  * work-unit partition of a single-slab plan depends only on the tensor and runs
@@ -223,7 +228,8 @@ tt_status tt_plan_use_variant(tt_plan* plan, int32_t variant);
  * TT_SELECT_MODEL's top-k candidates (negative: not timed); n entries. */
 tt_status tt_plan_sweep_times(const tt_plan* plan, float* ms, int32_t n);
 /* Milliseconds of the walk kernel(s) alone in the last timed call (first slab's
- * walk to the last slab's), without partition, clear and row merge. */
+ * walk to the last slab's), without partition, clear and row merge; -1 when that
+ * call was not timed in mode 1. */
 float tt_plan_last_kernel_ms(tt_plan* plan);
 /* Device error word of the plan's kernels (0: none; -1: could not be read);
  * waits for the plan's stream. */

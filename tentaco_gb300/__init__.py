@@ -494,8 +494,10 @@ class Plan:
     def ttv(self, x: DeviceBuffer, y: DeviceBuffer, stream=None) -> None:
         check(lib().tt_plan_ttv(self.ptr, x.ptr, y.ptr, stream))
 
-    def set_timing(self, on: bool) -> None:
-        check(lib().tt_plan_set_timing(self.ptr, 1 if on else 0))
+    def set_timing(self, on) -> None:
+        """False/0: off; True/1: the call and its walk kernels; 2: the call only (no event between the
+        walk and the merge kernels, which would hold back their dependent launch)."""
+        check(lib().tt_plan_set_timing(self.ptr, int(on)))
 
     def last_ms(self) -> float:
         return float(lib().tt_plan_last_ms(self.ptr))

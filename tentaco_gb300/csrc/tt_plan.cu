@@ -827,9 +827,9 @@ tt_status run_mttkrp(tt_plan* p, float* A, cudaStream_t st) {
     const size_t smem = variant_smem(variant_spec(p->variant), p->rp, p->prec, p->wcap, p->order);
     a.smem_bytes = (int32_t)smem;
     if (!p->part_ready) CK(launch_partition_rows(p->order, a, st));
-    if (p->timing) CK(cudaEventRecord(p->evk0, st));
+    if (p->timing == 1) CK(cudaEventRecord(p->evk0, st));
     CK(p->launcher(a, a.nblocks, p->tb, smem, st));
-    if (p->timing) CK(cudaEventRecord(p->evk1, st));
+    if (p->timing == 1) CK(cudaEventRecord(p->evk1, st));
     CK(launch_chain_fixup(p->order, a, st));
     CK(launch_virtual_rows(p->d_vrows, p->d_rnz, p->slabs, p->nroot, p->nroot + 1, p->rp, p->rank, p->rank, A, st));
     return TT_OK;
@@ -851,9 +851,9 @@ tt_status run_mttkrp(tt_plan* p, float* A, cudaStream_t st) {
       if (s2 != TT_OK) return s2;
     }
     if (!p->part_ready) CK(p->staged == 4 ? launch_partition_rows(p->order, a, st) : launch_partition(p->order, a, st));
-    if (p->timing && q == first) CK(cudaEventRecord(p->evk0, st));
+    if (p->timing == 1 && q == first) CK(cudaEventRecord(p->evk0, st));
     CK(p->launcher(a, a.nblocks, p->tb, smem, st));
-    if (p->timing && q == last) CK(cudaEventRecord(p->evk1, st));
+    if (p->timing == 1 && q == last) CK(cudaEventRecord(p->evk1, st));
     CK(launch_chain_fixup(p->order, a, st));
   }
   return TT_OK;
@@ -915,9 +915,9 @@ tt_status run_ttv(tt_plan* p, const float* x, float* y, cudaStream_t st) {
   }
   if (!p->part_ready) CK(launch_partition(2, ttv_args(p, x, y), st));
   const WalkArgs a = ttv_range_args(p, x, y);
-  if (p->timing) CK(cudaEventRecord(p->evk0, st));
+  if (p->timing == 1) CK(cudaEventRecord(p->evk0, st));
   CK(launch_ttv_ranges(a, val_kind(p->prec), st));
-  if (p->timing) CK(cudaEventRecord(p->evk1, st));
+  if (p->timing == 1) CK(cudaEventRecord(p->evk1, st));
   CK(launch_chain_fixup(2, a, st));
   return TT_OK;
 }
@@ -1578,6 +1578,7 @@ static tt_status timed_end(tt_plan* p, cudaStream_t st) {
   if (!p->timing) return TT_OK;
   CK(cudaEventRecord(p->ev1, st));
   p->timed_pending = true;
+  p->kernel_timed = p->timing == 1;
   return TT_OK;
 }
 
@@ -1636,7 +1637,8 @@ TT_EXPORT tt_status tt_plan_ttv(tt_plan* p, const float* x, float* y, void* stre
 
 TT_EXPORT tt_status tt_plan_set_timing(tt_plan* p, int32_t enabled) {
   if (!p) return set_error(TT_ERR_INVALID_ARGUMENT, "null plan");
-  p->timing = enabled != 0;
+  if (enabled < 0 || enabled > 2) return set_error(TT_ERR_INVALID_ARGUMENT, "timing mode %d (0, 1 or 2)", (int)enabled);
+  p->timing = enabled;
   return TT_OK;
 }
 
@@ -2155,7 +2157,7 @@ TT_EXPORT tt_status tt_mttkrp_host(taco_tensor_t* A, const taco_tensor_t* B,
   }
   const size_t abytes = (size_t)A->dimensions[0] * rank * sizeof(float);
   if (pool_alloc((void**)&dA, abytes, 0) != cudaSuccess) { cleanup(); return set_error(TT_ERR_OUT_OF_MEMORY, "output"); }
-  tt_plan_set_timing(p, 1);
+  tt_plan_set_timing(p, 2);  // the whole call (no event between the walk and the merge)
   if ((s = tt_plan_set_factors(p, (const float* const*)dfac.data(), nullptr)) != TT_OK) { cleanup(); return s; }
   if ((s = tt_plan_mttkrp(p, dA, nullptr)) != TT_OK) { cleanup(); return s; }
   // the reference times partition + clear + kernel per call; the plan ran its
@@ -2200,7 +2202,7 @@ TT_EXPORT tt_status tt_ttv_host(taco_tensor_t* y, const taco_tensor_t* B, const 
     return set_error(TT_ERR_OUT_OF_MEMORY, "ttv buffers");
   }
   if (cudaMemcpy(dx, x->vals, sizeof(float) * (size_t)nx, cudaMemcpyHostToDevice) != cudaSuccess) { cleanup(); return set_error(TT_ERR_CUDA, "upload x"); }
-  tt_plan_set_timing(p, 1);
+  tt_plan_set_timing(p, 2);  // the whole call (no event between the walk and the merge)
   if ((s = tt_plan_ttv(p, dx, dy, nullptr)) != TT_OK) { cleanup(); return s; }
   g_legacy_ms.store(tt_plan_last_ms(p) + (p->part_ready ? p->part_ms : 0.f));
   if (cudaMemcpy(y->vals, dy, sizeof(float) * (size_t)ny, cudaMemcpyDeviceToHost) != cudaSuccess) { cleanup(); return set_error(TT_ERR_CUDA, "download y"); }
@@ -2292,7 +2294,7 @@ TT_EXPORT tt_status tt_l2_flush(void* stream) {
 
 // Milliseconds of the walk kernel alone in the last timed call (no partition, no clear).
 TT_EXPORT float tt_plan_last_kernel_ms(tt_plan* p) {
-  if (!p || !p->timed_pending || !p->evk0) return -1.f;
+  if (!p || !p->timed_pending || !p->kernel_timed || !p->evk0) return -1.f;
   if (cudaEventSynchronize(p->ev1) != cudaSuccess) return -1.f;
   float ms = -1.f;
   cudaEventElapsedTime(&ms, p->evk0, p->evk1);

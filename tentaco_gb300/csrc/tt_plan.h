@@ -95,8 +95,10 @@ struct tt_plan {
   int mode = 0;  // output mode (the plan's tensor is re-rooted at it when not 0)
   int gpol = 0;  // WalkArgs::gpol
   SlabDev slab[tt::kMaxSlabs];
-  // timing
-  bool timing = false, timed_pending = false;
+  // timing: 0 off, 1 the call and its walk kernels, 2 the call only (no event
+  // between the walk and the merge kernels, whose dependent launch it would hold back)
+  int timing = 0;
+  bool timed_pending = false, kernel_timed = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
   // bookkeeping
   std::vector<void*> allocs;

@@ -237,6 +237,34 @@ def test_slabs_parity(skewed, slabs):
                 close(outs[0], ref, prec)
 
 
+def test_timing_modes(skewed):
+    """Timing mode 1 times the call and its walk kernel, mode 2 the call only (no event between the walk
+    and the merge kernels); the results are the same bits in every mode."""
+    B, Oc = skewed
+    facs = [tt.gen_dense(2000, 32, 1, 81), tt.gen_dense(5000, 32, 1, 82)]
+    ref = O.mttkrp(Oc, facs)
+    v = next(v for v in range(tt.num_variants())
+             if tt.variant_valid(v, 3, 32, "fp16") and tt.variant_info(v)["staged"] == 4)
+    plan = tt.Plan(B, rank=32, prec="fp16", select=tt.SELECT_FIXED, variant=v, slabs=3)
+    plan.set_factors([tt.DeviceBuffer.from_array(f) for f in facs])
+    A = tt.DeviceBuffer(B.dims[0] * 32 * 4)
+    outs = []
+    for mode in (0, 1, 2, 1):
+        plan.set_timing(mode)
+        plan.mttkrp(A)
+        outs.append(A.to_array((B.dims[0], 32)))
+        if mode == 1:
+            assert 0 < plan.last_kernel_ms() <= plan.last_ms()
+        if mode == 2:
+            assert plan.last_ms() > 0 and plan.last_kernel_ms() == -1
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+    close(outs[0], ref, "fp16")
+    with pytest.raises(tt.TTError) as e:
+        plan.set_timing(3)
+    assert e.value.status == tt.TT_ERR_INVALID_ARGUMENT
+
+
 def test_failed_variant_switch_blocks_calls(skewed):
     """A failed switch (the flat family on a slab plan) leaves the plan without a
     variant: a call reports an error instead of launching, until a switch succeeds."""
