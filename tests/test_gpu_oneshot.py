@@ -12,7 +12,8 @@ chunk's check and the walk of the units that have arrived.  These tests check:
   * the FP64 oracle within the tolerances of the other MTTKRP tests
     (FP32: max|x-y| <= 2e-5 max|y|, ||x-y||_F <= 1e-5 ||y||_F; FP16: 3e-3 / 1e-3;
     BF16: 2e-2 / 8e-3);
-  * one chunk, two chunks with a ragged end, and a tensor smaller than one unit;
+  * one chunk, two chunks with a ragged end, a tensor smaller than one unit, and
+    16 chunks of 1.25M nonzeros;
   * a leaf coordinate out of range, or out of order, in a late chunk: the call
     reports TT_ERR_INVALID_CSF and leaves the output untouched, and the next call
     is correct.
@@ -108,6 +109,20 @@ def test_chunk_edges(nnz, rows):
         got = one_shot(B, facs, "fp16", vid, pinned=True)
         assert np.array_equal(got, one_shot(B, facs, "fp16", vid, pinned=False))
         close(got, ref, "fp16")
+
+
+def test_sixteen_chunks_20m_nonzeros():
+    """20,000,003 nonzeros: 16 leaf chunks of 1.25M nonzeros, each checked and
+    walked as it lands, the last one ragged."""
+    B = tt.gen_zipf((20_000, 3_000, 400_000), (1.1, 0.6, 0.0), 20_000_003, seed=91)
+    facs = [tt.gen_dense(3_000, 32, 1, 9), tt.gen_dense(400_000, 32, 1, 10)]
+    ref = O.mttkrp(to_oracle(B), facs)
+    v = tt.default_variant(3, 32, "fp16", B.nnz)
+    if tt.variant_info(v)["staged"] != 4:
+        v = strip_variants(3, 32, "fp16")[0]
+    got = one_shot(B, facs, "fp16", v, pinned=True)
+    assert np.array_equal(got, one_shot(B, facs, "fp16", v, pinned=False))
+    close(got, ref, "fp16")
 
 
 @pytest.mark.parametrize("bad", ["range", "order"])
